@@ -1,0 +1,414 @@
+"""GB300-native Helmholtz boundary-element hot path (ctypes host layer).
+
+The compute runs in ``libbemgpu.so`` (CUDA, sm_103a) behind the C ABI declared
+in ``include/bemgpu.h``.  This module loads that library and mirrors the call
+surface of KG93/3d_BEM's H-matrix solve:
+
+* :class:`BoundaryElementSolver` -- ``calculateBoundarySolution`` /
+  ``hMatrixSolve`` (boundaryelementsolver.cpp:12, :526-744),
+* :class:`HMatrix` with :meth:`HArithm.MVM` (HMatrix/harithm.cpp:3-28),
+* :meth:`GMRES.gmresSolve` (HMatrix/gmres.h:170-180),
+
+plus :class:`Solver`, a thin handle wrapper used by the tests and the benchmark.
+There is no CPU fallback: if the library is missing or no CUDA device is
+present, every call raises :class:`BemError`.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libbemgpu.so")
+
+BEM_OK, BEM_EINVAL, BEM_ENOMEM, BEM_ENONFINITE, BEM_EMAXIT = 0, 1, 2, 3, 4
+BEM_EBREAKDOWN, BEM_ETIMEOUT, BEM_ECUDA, BEM_ERANK = 5, 6, 7, 8
+STATUS_NAMES = {0: "OK", 1: "EINVAL", 2: "ENOMEM", 3: "ENONFINITE", 4: "EMAXIT",
+                5: "EBREAKDOWN", 6: "ETIMEOUT", 7: "ECUDA", 8: "ERANK"}
+
+# the C-ABI symbols declared in include/bemgpu.h
+EXPORTS = [
+    "bem_config_default", "bem_create", "bem_destroy", "bem_last_error", "bem_set_mesh",
+    "bem_plan_mesh",
+    "bem_get_permutation", "bem_get_partition", "bem_set_bc", "bem_operators",
+    "bem_assemble", "bem_hmatvec", "bem_hmatvec_device", "bem_get_block", "bem_get_ranks",
+    "bem_gmres", "bem_solve", "bem_solve_device", "bem_sweep", "bem_points_assemble",
+    "bem_launch_count",
+]
+
+
+class BemError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Config(ct.Structure):
+    _fields_ = [("leaf_size", ct.c_int64), ("eta", ct.c_double), ("aca_tol", ct.c_double),
+                ("aca_max_rank", ct.c_int64), ("rank_reserve", ct.c_int64),
+                ("gmres_tol", ct.c_double), ("gmres_restart", ct.c_int64),
+                ("gmres_maxit", ct.c_int64), ("coupling", ct.c_int32),
+                ("precision", ct.c_int32), ("wave_speed", ct.c_double),
+                ("density", ct.c_double), ("seed", ct.c_uint64)]
+
+
+class SolveInfo(ct.Structure):
+    _fields_ = [("iterations", ct.c_int64), ("rel_residual", ct.c_double),
+                ("true_residual", ct.c_double), ("max_rank", ct.c_int64),
+                ("capped_blocks", ct.c_int64), ("t_nearfield", ct.c_double),
+                ("t_aca", ct.c_double), ("t_rhs", ct.c_double), ("t_gmres", ct.c_double),
+                ("t_total", ct.c_double), ("status", ct.c_int32), ("pad", ct.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile libbemgpu.so in-tree (nvcc, sm_103a)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_bemgpu_build", os.path.join(_HERE, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(force=force)
+
+
+def lib():
+    """Load libbemgpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise BemError(BEM_EINVAL, f"{LIB_PATH} is missing: build the CUDA library first "
+                                   "(python 3d_bem_gb300/build.py)")
+    L = ct.CDLL(LIB_PATH)
+    vp, i64, i32, dbl = ct.c_void_p, ct.c_int64, ct.c_int32, ct.c_double
+    P = ct.POINTER
+    L.bem_config_default.argtypes = [P(Config)]
+    L.bem_config_default.restype = None
+    L.bem_create.argtypes = [P(Config), P(vp)]
+    L.bem_destroy.argtypes = [vp]
+    L.bem_destroy.restype = None
+    L.bem_last_error.argtypes = [vp]
+    L.bem_last_error.restype = ct.c_char_p
+    L.bem_set_mesh.argtypes = [vp, vp, i64]
+    L.bem_plan_mesh.argtypes = [P(Config), vp, i64, vp, P(i64), vp]
+    L.bem_get_permutation.argtypes = [vp, vp]
+    L.bem_get_partition.argtypes = [vp, P(i64), vp]
+    L.bem_set_bc.argtypes = [vp, vp, vp]
+    L.bem_operators.argtypes = [vp, dbl, vp, vp, i64, vp]
+    L.bem_assemble.argtypes = [vp, dbl]
+    L.bem_hmatvec.argtypes = [vp, i32, vp, vp, i64, i32]
+    L.bem_hmatvec_device.argtypes = [vp, i32, vp, vp, i64, i32]
+    L.bem_get_block.argtypes = [vp, i32, i64, P(i64), vp, vp, vp, vp]
+    L.bem_get_ranks.argtypes = [vp, i32, vp]
+    L.bem_gmres.argtypes = [vp, vp, vp, i64, P(SolveInfo)]
+    L.bem_solve.argtypes = [vp, dbl, vp, i64, vp, vp, vp, P(SolveInfo)]
+    L.bem_solve_device.argtypes = [vp, dbl, vp, i64, vp, vp, vp, P(SolveInfo)]
+    L.bem_sweep.argtypes = [vp, vp, i64, vp, i64, vp, vp]
+    L.bem_points_assemble.argtypes = [vp, vp, i64, vp, i64, dbl, vp, vp]
+    L.bem_launch_count.argtypes = [vp]
+    L.bem_launch_count.restype = i64
+    for name in EXPORTS:
+        f = getattr(L, name)
+        if f.restype is ct.c_int:  # default restype: status codes are int32
+            f.restype = ct.c_int32
+    _lib = L
+    return L
+
+
+def default_config(**overrides) -> Config:
+    c = Config()
+    lib().bem_config_default(ct.byref(c))
+    for k, v in overrides.items():
+        setattr(c, k, v)
+    return c
+
+
+def plan_mesh(tri, config: Config | None = None):
+    """Host-only cluster-tree permutation and partition (no GPU needed)."""
+    tri = np.ascontiguousarray(tri, dtype=np.float64).reshape(-1, 9)
+    cfg = config if config is not None else default_config()
+    n = tri.shape[0]
+    perm = np.zeros(n, np.int64)
+    nb = ct.c_int64()
+    st = lib().bem_plan_mesh(ct.byref(cfg), _ptr(tri), n, _ptr(perm), ct.byref(nb), None)
+    if st != BEM_OK:
+        raise BemError(st, "bem_plan_mesh failed")
+    info = np.zeros((nb.value, 5), np.int64)
+    st = lib().bem_plan_mesh(ct.byref(cfg), _ptr(tri), n, _ptr(perm), ct.byref(nb), _ptr(info))
+    if st != BEM_OK:
+        raise BemError(st, "bem_plan_mesh failed")
+    return perm, info
+
+
+def _ptr(a: np.ndarray):
+    return ct.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def _c128(a, n=None):
+    a = np.asarray(a, dtype=np.complex128)
+    return np.asfortranarray(a) if a.ndim == 2 else np.ascontiguousarray(a)
+
+
+class Solver:
+    """One GPU solver handle (mesh, BCs, assembled H-matrices, GMRES state)."""
+
+    def __init__(self, config: Config | None = None, **overrides):
+        L = lib()
+        self.config = config if config is not None else default_config(**overrides)
+        h = ct.c_void_p()
+        st = L.bem_create(ct.byref(self.config), ct.byref(h))
+        if st != BEM_OK:
+            raise BemError(st, "bem_create failed (is a CUDA device visible?)")
+        self._h = h
+        self.n = 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().bem_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, st, what=""):
+        if st != BEM_OK:
+            msg = lib().bem_last_error(self._h)
+            raise BemError(st, f"{what}: {msg.decode() if msg else ''}")
+        return st
+
+    # ---- mesh / BC ----
+    def set_mesh(self, tri: np.ndarray):
+        tri = np.ascontiguousarray(tri, dtype=np.float64).reshape(-1, 9)
+        self._check(lib().bem_set_mesh(self._h, _ptr(tri), tri.shape[0]), "bem_set_mesh")
+        self.n = tri.shape[0]
+
+    @property
+    def permutation(self) -> np.ndarray:
+        p = np.zeros(self.n, np.int64)
+        self._check(lib().bem_get_permutation(self._h, _ptr(p)), "bem_get_permutation")
+        return p
+
+    def partition(self) -> np.ndarray:
+        nb = ct.c_int64()
+        self._check(lib().bem_get_partition(self._h, ct.byref(nb), None), "bem_get_partition")
+        info = np.zeros((nb.value, 5), np.int64)
+        self._check(lib().bem_get_partition(self._h, ct.byref(nb), _ptr(info)), "bem_get_partition")
+        return info
+
+    def set_bc(self, a, b):
+        a = _c128(a)
+        b = _c128(b)
+        self._check(lib().bem_set_bc(self._h, _ptr(a), _ptr(b)), "bem_set_bc")
+
+    # ---- operators / matrices ----
+    def operators(self, k, rows, cols) -> np.ndarray:
+        rows = np.ascontiguousarray(rows, np.int64)
+        cols = np.ascontiguousarray(cols, np.int64)
+        out = np.zeros((rows.size, 4), np.complex128)
+        self._check(lib().bem_operators(self._h, k, _ptr(rows), _ptr(cols), rows.size, _ptr(out)),
+                    "bem_operators")
+        return out
+
+    def assemble(self, freq: float):
+        self._check(lib().bem_assemble(self._h, freq), "bem_assemble")
+
+    def hmatvec(self, which: int, x, y=None, accumulate: bool = False) -> np.ndarray:
+        x = _c128(x)
+        R = 1 if x.ndim == 1 else x.shape[1]
+        nrows = x.shape[0] if y is None else np.asarray(y).shape[0]
+        out = np.zeros(x.shape if y is None else np.asarray(y).shape, np.complex128,
+                       order="F") if y is None else _c128(y).copy(order="F")
+        self._check(lib().bem_hmatvec(self._h, which, _ptr(x), _ptr(out), R, int(accumulate)),
+                    "bem_hmatvec")
+        return out
+
+    def ranks(self, which: int) -> np.ndarray:
+        r = np.zeros(self.partition().shape[0], np.int64)
+        self._check(lib().bem_get_ranks(self._h, which, _ptr(r)), "bem_get_ranks")
+        return r
+
+    def block(self, which: int, i: int, info_row):
+        r0, m, c0, n, adm = [int(v) for v in info_row]
+        rank = ct.c_int64()
+        if adm:
+            self._check(lib().bem_get_block(self._h, which, i, ct.byref(rank), None, None, None,
+                                            None), "bem_get_block")
+            k = rank.value
+            U = np.zeros((k, m), np.complex128)
+            s = np.zeros(k, np.complex128)
+            V = np.zeros((k, n), np.complex128)
+            self._check(lib().bem_get_block(self._h, which, i, ct.byref(rank), _ptr(U), _ptr(s),
+                                            _ptr(V), None), "bem_get_block")
+            return U.T.copy(), s, V
+        F = np.zeros((n, m), np.complex128)
+        self._check(lib().bem_get_block(self._h, which, i, ct.byref(rank), None, None, None,
+                                        _ptr(F)), "bem_get_block")
+        return F.T.copy()
+
+    def dense(self, which: int, info=None) -> np.ndarray:
+        """Expand the assembled H-matrix (tests only; O(N^2) memory)."""
+        info = self.partition() if info is None else info
+        nr = int((info[:, 0] + info[:, 1]).max())
+        nc = int((info[:, 2] + info[:, 3]).max())
+        D = np.zeros((nr, nc), np.complex128)
+        for i, row in enumerate(info):
+            r0, m, c0, n, adm = [int(v) for v in row]
+            blk = self.block(which, i, row)
+            if adm:
+                U, s, V = blk
+                D[r0:r0 + m, c0:c0 + n] = (U * s) @ V
+            else:
+                D[r0:r0 + m, c0:c0 + n] = blk
+        return D
+
+    def gmres(self, b, x0=None):
+        b = _c128(b)
+        R = 1 if b.ndim == 1 else b.shape[1]
+        x = np.zeros_like(b) if x0 is None else _c128(x0).copy()
+        info = SolveInfo()
+        st = lib().bem_gmres(self._h, _ptr(b), _ptr(x), R, ct.byref(info))
+        if st not in (BEM_OK, BEM_EMAXIT):
+            self._check(st, "bem_gmres")
+        return x, info.as_dict()
+
+    def solve(self, freq: float, g, want=("phi", "dphi", "p")):
+        g = np.asfortranarray(np.asarray(g, np.complex128).reshape(self.n, -1))
+        R = g.shape[1]
+        outs = {k: (np.zeros((self.n, R), np.complex128, order="F") if k in want else None)
+                for k in ("phi", "dphi", "p")}
+        info = SolveInfo()
+        st = lib().bem_solve(self._h, freq, _ptr(g), R, _ptr(outs["phi"]), _ptr(outs["dphi"]),
+                             _ptr(outs["p"]), ct.byref(info))
+        if st not in (BEM_OK, BEM_EMAXIT):
+            self._check(st, "bem_solve")
+        return outs["phi"], outs["dphi"], outs["p"], info.as_dict()
+
+    def solve_device(self, freq: float, g_ptr: int, R: int, phi_ptr=0, dphi_ptr=0, p_ptr=0):
+        info = SolveInfo()
+        st = lib().bem_solve_device(self._h, freq, ct.c_void_p(g_ptr), R,
+                                    ct.c_void_p(phi_ptr) if phi_ptr else None,
+                                    ct.c_void_p(dphi_ptr) if dphi_ptr else None,
+                                    ct.c_void_p(p_ptr) if p_ptr else None, ct.byref(info))
+        if st not in (BEM_OK, BEM_EMAXIT):
+            self._check(st, "bem_solve_device")
+        return info.as_dict()
+
+    def sweep(self, freqs, g):
+        freqs = np.ascontiguousarray(freqs, np.float64)
+        g = np.asfortranarray(np.asarray(g, np.complex128).reshape(self.n, -1))
+        R = g.shape[1]
+        p = np.zeros((self.n, R, freqs.size), np.complex128, order="F")
+        infos = (SolveInfo * freqs.size)()
+        st = lib().bem_sweep(self._h, _ptr(freqs), freqs.size, _ptr(g), R, _ptr(p), infos)
+        if st not in (BEM_OK, BEM_EMAXIT):
+            self._check(st, "bem_sweep")
+        return p, [i.as_dict() for i in infos]
+
+    def points_assemble(self, rowpts, colpts, k):
+        rowpts = np.ascontiguousarray(rowpts, np.float64)
+        colpts = np.ascontiguousarray(colpts, np.float64)
+        rp = np.zeros(rowpts.shape[0], np.int64)
+        cp = np.zeros(colpts.shape[0], np.int64)
+        self._check(lib().bem_points_assemble(self._h, _ptr(rowpts), rowpts.shape[0],
+                                              _ptr(colpts), colpts.shape[0], k, _ptr(rp),
+                                              _ptr(cp)), "bem_points_assemble")
+        return rp, cp
+
+    def launch_count(self) -> int:
+        return int(lib().bem_launch_count(self._h))
+
+
+# ---------------------------------------------------------------------------
+# Reference-named facade
+# ---------------------------------------------------------------------------
+@dataclass
+class BemSolverParameters:
+    """bemparameters.h:21-34 (+ the constants the reference hard-wires)."""
+    hMatSolving: bool = True
+    acaRelativeError: float = 0.01
+    acaMaxRank: int = 0
+    coupling: int = 2  # KirkupCoupling
+    leafSize: int = 32
+    eta: float = 2.0
+    gmresTolerance: float | None = None  # None: 1e-3 * acaRelativeError as the reference
+    gmresRestart: int = 300
+    gmresMaxIterations: int = 1000
+
+
+@dataclass
+class BoundaryElements:
+    """Triangles (N x 9) and their Robin data a*phi + b*dphi/dn = g."""
+    triangles: np.ndarray
+    a: np.ndarray
+    b: np.ndarray
+    g: np.ndarray
+    phiSolution: np.ndarray | None = None
+    dPhiSolution: np.ndarray | None = None
+    soundPressure: np.ndarray | None = None
+
+
+@dataclass
+class BoundaryElementSolver:
+    """Mirror of BoundaryElementSolver (boundaryelementsolver.h) for the
+    H-matrix path: set ``boundaryElements``, ``frequency``, ``waveSpeed``,
+    ``airDensity`` and call :meth:`calculateBoundarySolution`."""
+    boundaryElements: BoundaryElements
+    frequency: float
+    waveSpeed: float = 343.0
+    airDensity: float = 1.2041
+    bemSolverParameters: BemSolverParameters = field(default_factory=BemSolverParameters)
+    info: dict | None = None
+
+    def _solver(self) -> Solver:
+        p = self.bemSolverParameters
+        if not p.hMatSolving:
+            raise BemError(BEM_EINVAL, "only the H-matrix path is accelerated")
+        tol = p.gmresTolerance if p.gmresTolerance is not None else 1e-3 * p.acaRelativeError
+        s = Solver(leaf_size=p.leafSize, eta=p.eta, aca_tol=p.acaRelativeError,
+                   aca_max_rank=p.acaMaxRank, gmres_tol=tol, gmres_restart=p.gmresRestart,
+                   gmres_maxit=p.gmresMaxIterations, coupling=p.coupling,
+                   wave_speed=self.waveSpeed, density=self.airDensity)
+        s.set_mesh(self.boundaryElements.triangles)
+        s.set_bc(self.boundaryElements.a, self.boundaryElements.b)
+        return s
+
+    def calculateBoundarySolution(self):
+        s = self._solver()
+        phi, dphi, p, info = s.solve(self.frequency, self.boundaryElements.g)
+        be = self.boundaryElements
+        be.phiSolution, be.dPhiSolution, be.soundPressure = phi[:, 0], dphi[:, 0], p[:, 0]
+        self.info = info
+        s.close()
+        return info
+
+    hMatrixSolve = calculateBoundarySolution
+
+
+class HMatrix:
+    """An assembled H-matrix living on the GPU (``which`` 0 = phi, 1 = dPhi)."""
+
+    def __init__(self, solver: Solver, which: int):
+        self.solver, self.which = solver, which
+
+
+class HArithm:
+    @staticmethod
+    def MVM(y: np.ndarray, hmatrix: HMatrix, x: np.ndarray) -> np.ndarray:
+        """y += H x (harithm.cpp:3-28); returns the updated y."""
+        return hmatrix.solver.hmatvec(hmatrix.which, x, y, accumulate=True)
+
+
+class GMRES:
+    @staticmethod
+    def gmresSolve(A: HMatrix, xGuess, b):
+        """GMRES on the assembled system matrix (gmres.h:170-180); the
+        tolerance and restart come from the solver configuration."""
+        x, info = A.solver.gmres(b, xGuess)
+        return x

@@ -1,0 +1,115 @@
+// bem_kernels.h -- launch interfaces of the CUDA kernels (host <-> device).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bem_types.h"
+
+namespace bemgpu {
+
+constexpr int ACA_MAX_KCAP = 512;  // largest per-block rank reservation
+
+// Seeded stand-in for the reference's QRandomGenerator picks
+// (hmatrix.cpp:508, boundaryelementsolver.cpp:2156-2158): splitmix64 finaliser.
+__host__ __device__ inline uint64_t pivot_hash(uint64_t seed, uint64_t a, uint64_t b) {
+  uint64_t z = seed ^ (a * 0x9E3779B97F4A7C15ull) ^ (b * 0xC2B2AE3D27D4EB4Full);
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+#ifdef __CUDACC__
+__device__ __forceinline__ double2 load_c(const double2* p) { return __ldg(p); }
+__device__ __forceinline__ double2 load_c(const float2* p) {
+  float2 v = __ldg(p);
+  return make_double2((double)v.x, (double)v.y);
+}
+#endif
+
+struct LeafRows {
+  int64_t start;
+  int32_t size;
+  int32_t pad;
+};
+
+struct NearfieldArgs {
+  const Elem* E;
+  const BcCoef* bc;
+  const NearBlock* blocks;
+  const NearTile* tiles;
+  int64_t ntiles;
+  const uint32_t* special_bits;
+  const int64_t* sp_entry;
+  const int32_t* sp_row;
+  const int32_t* sp_col;
+  int64_t nspecial;
+  double k;
+  double2 alpha;
+  double2* phi;
+  double2* dphi;
+};
+
+struct AcaArgs {
+  int mode;  // 0 = BEM entries, 1 = point-cloud Helmholtz kernel (tests)
+  const Elem* E;
+  const BcCoef* bc;
+  double k;
+  double near_r;
+  double2 alpha;
+  int which;  // 0 phi, 1 dphi
+  const double* rowpts;
+  const double* colpts;
+  const FarBlock* far;
+  const int32_t* order;
+  int64_t nfar;
+  double2* U;
+  double2* V;
+  double2* S;
+  int32_t* rank;
+  int32_t* flags;
+  double tol;
+  int max_rank;
+  uint64_t seed;
+  int extra;
+  const int64_t* piv_off;
+  const int32_t* piv_cnt;
+  const int32_t* piv_rc;
+};
+
+struct HmvArgs {
+  int precision;  // 0: double2 storage, 1: float2 storage
+  int nrhs;
+  const FarBlock* far;
+  const int32_t* rank;
+  int64_t nfar;
+  const NearBlock* nearb;
+  const LeafRows* leaves;
+  int64_t nleaves;
+  const int32_t* list_off;
+  const int32_t* list;
+  const void* U;
+  const void* V;
+  const void* S;
+  const void* F;
+  const double2* x;
+  int64_t ldx;
+  double2* t;
+  int64_t ldt;
+  double2* y;
+  int64_t ldy;
+  int accumulate;
+};
+
+void nearfield_upload_rules(const QuadRules& r, cudaStream_t s);
+void aca_upload_rules(const QuadRules& r, cudaStream_t s);
+void launch_nearfield(const NearfieldArgs& a, cudaStream_t s);
+void launch_operators(const Elem* E, const int64_t* rows, const int64_t* cols, int64_t count,
+                      double k, double near_r, double2* out, cudaStream_t s);
+void launch_points_nearfield(const NearBlock* blocks, int64_t nblocks, const NearTile* tiles,
+                             int64_t ntiles, const double* rp, const double* cp, double k,
+                             double2* F, cudaStream_t s);
+void launch_aca(const AcaArgs& a, cudaStream_t s);
+void launch_hmatvec(const HmvArgs& a, cudaStream_t s);
+
+}  // namespace bemgpu

@@ -1,0 +1,905 @@
+// capi.cpp -- the solver handle and the extern "C" entry points of bemgpu.h.
+//
+// Host orchestration of one frequency follows BoundaryElementSolver::
+// hMatrixSolve (boundaryelementsolver.cpp:526-744): BC set-up, phi assembly,
+// rhs = phi g, dPhi assembly, GMRES, BC back-substitution, p = i rho omega phi.
+// Everything after bem_set_mesh runs on the GPU; the host only sequences
+// kernels and reads back convergence flags.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/bemgpu.h"
+#include "bem_kernels.h"
+#include "host_tree.h"
+#include "krylov.h"
+#include "post.h"
+
+using namespace bemgpu;
+using cplx = std::complex<double>;
+
+namespace {
+
+struct BemError {
+  bem_status st;
+  std::string msg;
+};
+
+#define CK(x)                                                                             \
+  do {                                                                                    \
+    cudaError_t e_ = (x);                                                                 \
+    if (e_ != cudaSuccess)                                                                \
+      throw BemError{e_ == cudaErrorMemoryAllocation ? BEM_ENOMEM : BEM_ECUDA,            \
+                     std::string(#x) + ": " + cudaGetErrorString(e_)};                    \
+  } while (0)
+
+void require(bool ok, bem_status st, const char* msg) {
+  if (!ok) throw BemError{st, msg};
+}
+
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void ensure(size_t cnt) {
+    if (cnt <= n && p) return;
+    release();
+    size_t c = std::max<size_t>(cnt, 1);
+    CK(cudaMalloc((void**)&p, c * sizeof(T)));
+    n = c;
+  }
+  void upload(const std::vector<T>& v, cudaStream_t s) {
+    ensure(v.size());
+    if (!v.empty()) CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+};
+
+struct DevHM {
+  DBuf<double2> F, U, V, S;
+  DBuf<int32_t> rank, flags;
+  std::vector<int32_t> h_rank, h_flags;
+  bool assembled = false;
+};
+
+struct GmresWS {
+  int64_t N = 0;
+  int R = 0, m = 0;
+  DBuf<double2> Vb, w, H, g, cs, sn, h, y, cpart, bcopy;
+  DBuf<double> npart, hnorm;
+  DBuf<GmresState> st;
+  std::vector<GmresState> hst;
+};
+
+}  // namespace
+
+struct bem_handle {
+  bem_config cfg{};
+  std::string err;
+  cudaStream_t stream = nullptr;
+  int64_t launches = 0;
+  // mesh
+  int64_t N = 0;
+  bool have_mesh = false, points_mode = false;
+  HTree rows, cols;
+  std::vector<Elem> E;
+  double avgdim = 0, near_r = 0;
+  Layout L;
+  DBuf<Elem> dE;
+  DBuf<NearBlock> dNear;
+  DBuf<FarBlock> dFar;
+  DBuf<int32_t> dOrder, dSpRow, dSpCol, dListOff, dList, dPivCnt, dPivRc;
+  DBuf<NearTile> dTiles;
+  DBuf<uint32_t> dBits;
+  DBuf<int64_t> dSpEntry, dPivOff, dPerm;
+  DBuf<LeafRows> dLeaves;
+  DBuf<double> dRowPts, dColPts;
+  // boundary conditions (cluster order)
+  bool have_bc = false;
+  std::vector<cplx> a, b;
+  DBuf<BcCoef> dBc;
+  DBuf<double2> dA, dB;
+  double k = 0;
+  DevHM hm[2];
+  DBuf<double2> dT;
+  GmresWS gw;
+  DBuf<double2> dG, dX, dRhs, dIn, dOut1, dOut2, dOut3;
+  DBuf<int> dBad;
+  QuadRules rules{};
+  cudaEvent_t ev[10]{};
+};
+
+namespace {
+
+bem_status fail(bem_handle* h, const BemError& e) {
+  if (h) h->err = e.msg;
+  return e.st;
+}
+
+template <typename F>
+bem_status guarded(bem_handle* h, F&& f) {
+  try {
+    f();
+    if (h) h->err.clear();
+    return BEM_OK;
+  } catch (const BemError& e) {
+    return fail(h, e);
+  } catch (const std::bad_alloc&) {
+    return fail(h, BemError{BEM_ENOMEM, "host allocation failed"});
+  } catch (const std::exception& e) {
+    return fail(h, BemError{BEM_EINVAL, e.what()});
+  }
+}
+
+double elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms * 1e-3;
+}
+
+cplx coupling_parameter(int kind, double k) {
+  const cplx I(0.0, 1.0);
+  const double tiny = 10.0 * 2.220446049250313080847263336181640625e-16;
+  if (kind == 0) return 0.0;
+  if (kind == 1) return std::fabs(k) < tiny ? I : I / k;
+  return I / (k + 1.0);
+}
+
+void upload_layout(bem_handle* h) {
+  cudaStream_t s = h->stream;
+  const Layout& L = h->L;
+  h->dNear.upload(L.near, s);
+  h->dFar.upload(L.far, s);
+  h->dOrder.upload(L.far_order, s);
+  h->dTiles.upload(L.tiles, s);
+  h->dBits.upload(L.special_bits, s);
+  h->dSpEntry.upload(L.sp_entry, s);
+  h->dSpRow.upload(L.sp_row, s);
+  h->dSpCol.upload(L.sp_col, s);
+  h->dLeaves.upload(L.leaves, s);
+  h->dListOff.upload(L.list_off, s);
+  h->dList.upload(L.list, s);
+  h->dPivOff.upload(L.piv_off, s);
+  h->dPivCnt.upload(L.piv_cnt, s);
+  h->dPivRc.upload(L.piv_rc, s);
+  for (auto& m : h->hm) m.assembled = false;
+}
+
+void alloc_hm(bem_handle* h, DevHM& m) {
+  const Layout& L = h->L;
+  m.F.ensure(L.near_entries);
+  m.U.ensure(L.u_size);
+  m.V.ensure(L.v_size);
+  m.S.ensure(L.s_size);
+  m.rank.ensure(L.far.size());
+  m.flags.ensure(L.far.size());
+}
+
+void set_frequency(bem_handle* h, double k) {
+  require(h->have_bc, BEM_EINVAL, "boundary conditions not set (bem_set_bc)");
+  const int64_t N = h->N;
+  std::vector<BcCoef> bc(N);
+  std::vector<double2> av(N), bv(N);
+  for (int64_t i = 0; i < N; i++) {
+    const cplx a = h->a[i], b = h->b[i];
+    BcCoef c{};
+    c.subst = std::abs(a) < std::abs(b) ? 1 : 0;
+    cplx inv = c.subst ? 1.0 / b : 1.0 / a;
+    cplx ratio = c.subst ? a / b : b / a;
+    c.inv_main = make_double2(inv.real(), inv.imag());
+    c.ratio = make_double2(ratio.real(), ratio.imag());
+    bc[i] = c;
+    av[i] = make_double2(a.real(), a.imag());
+    bv[i] = make_double2(b.real(), b.imag());
+  }
+  h->dBc.upload(bc, h->stream);
+  h->dA.upload(av, h->stream);
+  h->dB.upload(bv, h->stream);
+  h->k = k;
+}
+
+void sync(bem_handle* h) { CK(cudaStreamSynchronize(h->stream)); }
+
+void fetch_ranks(bem_handle* h, DevHM& m) {
+  const size_t nf = h->L.far.size();
+  m.h_rank.resize(nf);
+  m.h_flags.resize(nf);
+  if (nf) {
+    CK(cudaMemcpyAsync(m.h_rank.data(), m.rank.p, nf * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(m.h_flags.data(), m.flags.p, nf * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+  }
+  sync(h);
+  m.assembled = true;
+}
+
+AcaArgs aca_args(bem_handle* h, DevHM& m, int which, int extra) {
+  AcaArgs a{};
+  a.mode = h->points_mode ? 1 : 0;
+  a.E = h->dE.p;
+  a.bc = h->dBc.p;
+  a.k = h->k;
+  a.near_r = h->near_r;
+  cplx al = coupling_parameter(h->cfg.coupling, h->k);
+  a.alpha = make_double2(al.real(), al.imag());
+  a.which = which;
+  a.rowpts = h->dRowPts.p;
+  a.colpts = h->dColPts.p;
+  a.far = h->dFar.p;
+  a.order = h->dOrder.p;
+  a.nfar = (int64_t)h->L.far.size();
+  a.U = m.U.p;
+  a.V = m.V.p;
+  a.S = m.S.p;
+  a.rank = m.rank.p;
+  a.flags = m.flags.p;
+  a.tol = h->cfg.aca_tol;
+  a.max_rank = (int)h->cfg.aca_max_rank;
+  a.seed = h->cfg.seed;
+  a.extra = extra;
+  a.piv_off = h->dPivOff.p;
+  a.piv_cnt = h->dPivCnt.p;
+  a.piv_rc = h->dPivRc.p;
+  return a;
+}
+
+// both H-matrices at wavenumber k; optional timing events
+void assemble(bem_handle* h, double freq, double* t_near, double* t_aca) {
+  require(h->have_mesh && !h->points_mode, BEM_EINVAL, "mesh not set (bem_set_mesh)");
+  const double k = 2.0 * M_PI * freq / h->cfg.wave_speed;
+  require(k > 0 && std::isfinite(k), BEM_EINVAL, "frequency must be positive and finite");
+  set_frequency(h, k);
+  for (auto& m : h->hm) alloc_hm(h, m);
+  cudaStream_t s = h->stream;
+  cplx al = coupling_parameter(h->cfg.coupling, k);
+  NearfieldArgs na{};
+  na.E = h->dE.p;
+  na.bc = h->dBc.p;
+  na.blocks = h->dNear.p;
+  na.tiles = h->dTiles.p;
+  na.ntiles = (int64_t)h->L.tiles.size();
+  na.special_bits = h->dBits.p;
+  na.sp_entry = h->dSpEntry.p;
+  na.sp_row = h->dSpRow.p;
+  na.sp_col = h->dSpCol.p;
+  na.nspecial = (int64_t)h->L.sp_entry.size();
+  na.k = k;
+  na.alpha = make_double2(al.real(), al.imag());
+  na.phi = h->hm[0].F.p;
+  na.dphi = h->hm[1].F.p;
+  CK(cudaEventRecord(h->ev[0], s));
+  launch_nearfield(na, s);
+  h->launches += (na.ntiles > 0) + (na.nspecial > 0);
+  CK(cudaEventRecord(h->ev[1], s));
+  launch_aca(aca_args(h, h->hm[0], 0, 0), s);
+  launch_aca(aca_args(h, h->hm[1], 1, 1), s);
+  h->launches += 2;
+  CK(cudaEventRecord(h->ev[2], s));
+  CK(cudaGetLastError());
+  fetch_ranks(h, h->hm[0]);
+  fetch_ranks(h, h->hm[1]);
+  if (t_near) *t_near = elapsed(h->ev[0], h->ev[1]);
+  if (t_aca) *t_aca = elapsed(h->ev[1], h->ev[2]);
+}
+
+void hmatvec_dev(bem_handle* h, int which, const double2* x, double2* y, int64_t R, int acc) {
+  require(which == 0 || which == 1, BEM_EINVAL, "which must be 0 (phi) or 1 (dPhi)");
+  DevHM& m = h->hm[which];
+  require(m.assembled, BEM_EINVAL, "matrix not assembled");
+  const int64_t nrows = h->points_mode ? (int64_t)h->rows.perm.size() : h->N;
+  const int64_t ncols = h->points_mode ? (int64_t)h->cols.perm.size() : h->N;
+  h->dT.ensure(std::max<int64_t>(h->L.s_size, 1) * 8);
+  for (int64_t r0 = 0; r0 < R; r0 += 8) {
+    HmvArgs a{};
+    a.precision = 0;
+    a.nrhs = (int)std::min<int64_t>(8, R - r0);
+    a.far = h->dFar.p;
+    a.rank = m.rank.p;
+    a.nfar = (int64_t)h->L.far.size();
+    a.nearb = h->dNear.p;
+    a.leaves = h->dLeaves.p;
+    a.nleaves = (int64_t)h->L.leaves.size();
+    a.list_off = h->dListOff.p;
+    a.list = h->dList.p;
+    a.U = m.U.p;
+    a.V = m.V.p;
+    a.S = m.S.p;
+    a.F = m.F.p;
+    a.x = x + r0 * ncols;
+    a.ldx = ncols;
+    a.t = h->dT.p;
+    a.ldt = std::max<int64_t>(h->L.s_size, 1);
+    a.y = y + r0 * nrows;
+    a.ldy = nrows;
+    a.accumulate = acc;
+    launch_hmatvec(a, h->stream);
+    h->launches += (a.nfar > 0) + (a.nleaves > 0);
+  }
+}
+
+void ensure_gmres(bem_handle* h, int R) {
+  GmresWS& g = h->gw;
+  const int m = (int)std::max<int64_t>(1, std::min(h->cfg.gmres_restart, h->cfg.gmres_maxit));
+  if (g.N == h->N && g.R == R && g.m == m) return;
+  const int64_t N = h->N;
+  const int nct = krylov_num_ctas(N);
+  g.Vb.ensure((size_t)(m + 1) * R * N);
+  g.w.ensure((size_t)R * N);
+  g.bcopy.ensure((size_t)R * N);
+  g.H.ensure((size_t)R * m * (m + 1));
+  g.g.ensure((size_t)R * (m + 1));
+  g.cs.ensure((size_t)R * m);
+  g.sn.ensure((size_t)R * m);
+  g.h.ensure((size_t)R * (m + 1));
+  g.y.ensure((size_t)R * m);
+  g.cpart.ensure((size_t)nct * R * (m + 1));
+  g.npart.ensure((size_t)nct * R);
+  g.hnorm.ensure(R);
+  g.st.ensure(R);
+  g.hst.resize(R);
+  g.N = N;
+  g.R = R;
+  g.m = m;
+}
+
+KrylovArgs krylov_args(bem_handle* h, double2* x) {
+  GmresWS& g = h->gw;
+  KrylovArgs a{};
+  a.N = g.N;
+  a.R = g.R;
+  a.m = g.m;
+  a.tol = h->cfg.gmres_tol;
+  a.Vb = g.Vb.p;
+  a.w = g.w.p;
+  a.x = x;
+  a.H = g.H.p;
+  a.g = g.g.p;
+  a.cs = g.cs.p;
+  a.sn = g.sn.p;
+  a.h = g.h.p;
+  a.y = g.y.p;
+  a.cpart = g.cpart.p;
+  a.npart = g.npart.p;
+  a.hnorm = g.hnorm.p;
+  a.st = g.st.p;
+  return a;
+}
+
+bool read_states(bem_handle* h) {
+  GmresWS& g = h->gw;
+  CK(cudaMemcpyAsync(g.hst.data(), g.st.p, g.R * sizeof(GmresState), cudaMemcpyDeviceToHost, h->stream));
+  sync(h);
+  for (const auto& s : g.hst)
+    if (!s.done) return false;
+  return true;
+}
+
+// Restarted GMRES for R right-hand sides on the dPhi matrix (device b, x).
+void gmres_dev(bem_handle* h, const double2* b, double2* x, int R, bem_solve_info* info) {
+  require(h->hm[1].assembled, BEM_EINVAL, "system matrix not assembled");
+  ensure_gmres(h, R);
+  GmresWS& g = h->gw;
+  const int64_t N = h->N;
+  cudaStream_t s = h->stream;
+  KrylovArgs a = krylov_args(h, x);
+  CK(cudaMemcpyAsync(g.bcopy.p, b, (size_t)R * N * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(g.w.p, b, (size_t)R * N * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+  krylov_restart(a, 1, s);  // measures ||b||
+  h->launches += 2;
+  int64_t total = 0;
+  const int64_t maxit = h->cfg.gmres_maxit;
+  while (true) {
+    hmatvec_dev(h, 1, x, g.w.p, R, 0);
+    krylov_residual(g.bcopy.p, g.w.p, (int64_t)R * N, s);
+    krylov_restart(a, 0, s);
+    h->launches += 3;
+    if (read_states(h) || total >= maxit) break;
+    for (int j = 0; j < g.m; j++) {
+      hmatvec_dev(h, 1, g.Vb.p + (int64_t)j * R * N, g.w.p, R, 0);
+      krylov_orthogonalize(a, j, s);
+      h->launches += 9;
+      total++;
+      const bool last = (j == g.m - 1) || total >= maxit;
+      if (((j + 1) % 8 == 0) || last) {
+        if (read_states(h)) break;
+      }
+      if (total >= maxit) break;
+    }
+    krylov_update(a, s);
+    h->launches += 2;
+  }
+  CK(cudaGetLastError());
+  if (info) {
+    int64_t it = 0;
+    double res = 0;
+    bool all = true;
+    for (const auto& st : g.hst) {
+      it = std::max<int64_t>(it, st.iters);
+      res = std::max(res, st.resid);
+      all = all && st.done;
+    }
+    info->iterations = it;
+    info->rel_residual = res;
+    info->true_residual = res;  // the loop exits right after a true-residual restart
+    info->status = all ? BEM_OK : BEM_EMAXIT;
+  }
+}
+
+void fill_rank_info(bem_handle* h, bem_solve_info* info) {
+  if (!info) return;
+  int64_t mr = 0, capped = 0;
+  for (int w = 0; w < 2; w++) {
+    const DevHM& m = h->hm[w];
+    for (size_t i = 0; i < m.h_rank.size(); i++) {
+      if (w == 1) mr = std::max<int64_t>(mr, m.h_rank[i]);
+      capped += m.h_flags[i] ? 1 : 0;
+    }
+  }
+  info->max_rank = mr;
+  info->capped_blocks = capped;
+}
+
+// One frequency, all R right-hand sides; g / outputs are device pointers in
+// caller order.
+void solve_dev(bem_handle* h, double freq, const double2* g_caller, int64_t R, double2* phi,
+               double2* dphi, double2* p, bem_solve_info* info) {
+  require(R >= 1, BEM_EINVAL, "nrhs must be >= 1");
+  const int64_t N = h->N;
+  cudaStream_t s = h->stream;
+  auto t0 = std::chrono::steady_clock::now();
+  bem_solve_info loc{};
+  assemble(h, freq, &loc.t_nearfield, &loc.t_aca);
+  h->dG.ensure((size_t)R * N);
+  h->dRhs.ensure((size_t)R * N);
+  h->dX.ensure((size_t)R * N);
+  launch_gather(g_caller, h->dG.p, h->dPerm.p, N, (int)R, s);
+  h->launches++;
+  CK(cudaEventRecord(h->ev[3], s));
+  // rhs = source term (none) + phi * g  (boundaryelementsolver.cpp:578-579)
+  hmatvec_dev(h, 0, h->dG.p, h->dRhs.p, R, 0);
+  CK(cudaEventRecord(h->ev[4], s));
+  CK(cudaMemsetAsync(h->dX.p, 0, (size_t)R * N * sizeof(double2), s));
+  gmres_dev(h, h->dRhs.p, h->dX.p, (int)R, &loc);
+  CK(cudaEventRecord(h->ev[5], s));
+  const double omega = 2.0 * M_PI * freq;
+  double2 pfac = make_double2(0.0, h->cfg.density * omega);
+  launch_backsub(h->dX.p, h->dG.p, h->dA.p, h->dB.p, h->dBc.p, h->dPerm.p, N, (int)R, pfac, phi,
+                 dphi, p, s);
+  h->launches++;
+  h->dBad.ensure(1);
+  CK(cudaMemsetAsync(h->dBad.p, 0, sizeof(int), s));
+  h->launches += launch_finite_check(h->dX.p, R * N, h->dBad.p, s);
+  int bad = 0;
+  CK(cudaMemcpyAsync(&bad, h->dBad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  sync(h);
+  loc.t_rhs = elapsed(h->ev[3], h->ev[4]);
+  loc.t_gmres = elapsed(h->ev[4], h->ev[5]);
+  loc.t_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  fill_rank_info(h, &loc);
+  if (bad) loc.status = BEM_ENONFINITE;
+  if (info) *info = loc;
+  if (bad) throw BemError{BEM_ENONFINITE, "non-finite values in the solution"};
+}
+
+void copy_in(bem_handle* h, DBuf<double2>& d, const double* src, size_t cnt) {
+  d.ensure(cnt);
+  CK(cudaMemcpyAsync(d.p, src, cnt * sizeof(double2), cudaMemcpyHostToDevice, h->stream));
+}
+
+void copy_out(bem_handle* h, double* dst, const double2* src, size_t cnt) {
+  if (!dst) return;
+  CK(cudaMemcpyAsync(dst, src, cnt * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+}
+
+}  // namespace
+
+extern "C" {
+
+void bem_config_default(bem_config* c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->leaf_size = 32;
+  c->eta = 2.0;
+  c->aca_tol = 1e-4;
+  c->aca_max_rank = 0;
+  c->rank_reserve = 96;
+  c->gmres_tol = 1e-8;
+  c->gmres_restart = 300;
+  c->gmres_maxit = 1000;
+  c->coupling = 2;
+  c->precision = 0;
+  c->wave_speed = 343.0;
+  c->density = 1.2;
+  c->seed = 1234;
+}
+
+bem_status bem_create(const bem_config* cfg, bem_handle** out) {
+  if (!out) return BEM_EINVAL;
+  *out = nullptr;
+  bem_handle* h = new (std::nothrow) bem_handle();
+  if (!h) return BEM_ENOMEM;
+  bem_status st = guarded(h, [&] {
+    if (cfg) h->cfg = *cfg;
+    else bem_config_default(&h->cfg);
+    require(h->cfg.leaf_size >= 2, BEM_EINVAL, "leaf_size must be >= 2");
+    require(h->cfg.eta > 0, BEM_EINVAL, "eta must be positive");
+    require(h->cfg.aca_tol >= 0, BEM_EINVAL, "aca_tol must be >= 0");
+    require(h->cfg.rank_reserve >= 1 && h->cfg.rank_reserve <= ACA_MAX_KCAP, BEM_EINVAL,
+            "rank_reserve must be in [1, 512]");
+    require(h->cfg.gmres_restart >= 1 && h->cfg.gmres_maxit >= 1, BEM_EINVAL,
+            "gmres_restart and gmres_maxit must be >= 1");
+    require(h->cfg.coupling >= 0 && h->cfg.coupling <= 2, BEM_EINVAL, "coupling must be 0, 1 or 2");
+    require(h->cfg.precision == 0, BEM_EINVAL, "precision must be 0 (complex FP64)");
+    require(h->cfg.wave_speed > 0, BEM_EINVAL, "wave_speed must be positive");
+    CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    for (auto& e : h->ev) CK(cudaEventCreate(&e));
+    h->rules = make_rules();
+    nearfield_upload_rules(h->rules, h->stream);
+    aca_upload_rules(h->rules, h->stream);
+    CK(cudaGetLastError());
+    sync(h);
+  });
+  if (st != BEM_OK) {
+    bem_destroy(h);
+    return st;
+  }
+  *out = h;
+  return BEM_OK;
+}
+
+void bem_destroy(bem_handle* h) {
+  if (!h) return;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (auto& e : h->ev)
+    if (e) cudaEventDestroy(e);
+  cudaStream_t s = h->stream;
+  delete h;  // device buffers are released by their destructors
+  if (s) cudaStreamDestroy(s);
+}
+
+const char* bem_last_error(const bem_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+bem_status bem_set_mesh(bem_handle* h, const double* tri, int64_t n) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] {
+    require(tri != nullptr && n >= 1, BEM_EINVAL, "mesh needs at least one triangle");
+    for (int64_t i = 0; i < 9 * n; i++)
+      require(std::isfinite(tri[i]), BEM_ENONFINITE, "non-finite vertex coordinate");
+    std::vector<double> mids(3 * n);
+    for (int64_t i = 0; i < n; i++)
+      for (int d = 0; d < 3; d++)
+        mids[3 * i + d] = ((tri[9 * i + d] + tri[9 * i + 3 + d]) + tri[9 * i + 6 + d]) / 3.0;
+    h->rows = build_tree(mids, h->cfg.leaf_size);
+    h->cols = h->rows;
+    h->N = n;
+    prepare_elements(tri, h->rows.perm, h->E, h->avgdim);
+    for (const Elem& e : h->E)
+      require(e.area > 0 && std::isfinite(e.nrm[0]), BEM_EINVAL, "degenerate (zero-area) triangle");
+    h->near_r = 4.0 * h->avgdim;
+    build_layout(h->rows, h->cols, &h->E, h->near_r, h->cfg.eta, h->cfg.rank_reserve,
+                 h->cfg.aca_max_rank, true, h->cfg.seed, h->L);
+    h->points_mode = false;
+    h->dE.upload(h->E, h->stream);
+    h->dPerm.upload(h->rows.perm, h->stream);
+    upload_layout(h);
+    h->have_mesh = true;
+    h->have_bc = false;
+    sync(h);
+  });
+}
+
+bem_status bem_plan_mesh(const bem_config* cfg, const double* tri, int64_t n, int64_t* perm,
+                         int64_t* nblocks, int64_t* info) {
+  return guarded(nullptr, [&] {
+    bem_config c;
+    if (cfg) c = *cfg;
+    else bem_config_default(&c);
+    require(tri != nullptr && n >= 1 && nblocks != nullptr, BEM_EINVAL, "bad arguments");
+    require(c.leaf_size >= 2 && c.eta > 0, BEM_EINVAL, "bad configuration");
+    std::vector<double> mids(3 * n);
+    for (int64_t i = 0; i < n; i++)
+      for (int d = 0; d < 3; d++)
+        mids[3 * i + d] = ((tri[9 * i + d] + tri[9 * i + 3 + d]) + tri[9 * i + 6 + d]) / 3.0;
+    HTree t = build_tree(mids, c.leaf_size);
+    std::vector<HBlockDesc> blocks = build_blocks(t, t, c.eta);
+    if (perm) std::memcpy(perm, t.perm.data(), n * sizeof(int64_t));
+    if (info)
+      for (size_t i = 0; i < blocks.size(); i++) {
+        int64_t* o = info + 5 * i;
+        o[0] = blocks[i].r0;
+        o[1] = blocks[i].m;
+        o[2] = blocks[i].c0;
+        o[3] = blocks[i].n;
+        o[4] = blocks[i].adm ? 1 : 0;
+      }
+    *nblocks = (int64_t)blocks.size();
+  });
+}
+
+bem_status bem_get_permutation(const bem_handle* h, int64_t* perm) {
+  if (!h || !perm || !h->have_mesh) return BEM_EINVAL;
+  std::memcpy(perm, h->rows.perm.data(), h->rows.perm.size() * sizeof(int64_t));
+  return BEM_OK;
+}
+
+bem_status bem_get_partition(const bem_handle* h, int64_t* nblocks, int64_t* info) {
+  if (!h || !nblocks || !(h->have_mesh || h->points_mode)) return BEM_EINVAL;
+  *nblocks = (int64_t)h->L.blocks.size();
+  if (info)
+    for (size_t i = 0; i < h->L.blocks.size(); i++) {
+      const HBlockDesc& b = h->L.blocks[i];
+      int64_t* o = info + 5 * i;
+      o[0] = b.r0;
+      o[1] = b.m;
+      o[2] = b.c0;
+      o[3] = b.n;
+      o[4] = b.adm ? 1 : 0;
+    }
+  return BEM_OK;
+}
+
+bem_status bem_set_bc(bem_handle* h, const double* a, const double* b) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] {
+    require(h->have_mesh && !h->points_mode, BEM_EINVAL, "mesh not set (bem_set_mesh)");
+    require(a && b, BEM_EINVAL, "a and b are required");
+    const int64_t N = h->N;
+    h->a.resize(N);
+    h->b.resize(N);
+    for (int64_t i = 0; i < N; i++) {
+      const int64_t o = h->rows.perm[i];
+      cplx av(a[2 * o], a[2 * o + 1]), bv(b[2 * o], b[2 * o + 1]);
+      require(std::isfinite(av.real()) && std::isfinite(av.imag()) && std::isfinite(bv.real()) &&
+                  std::isfinite(bv.imag()),
+              BEM_ENONFINITE, "non-finite Robin coefficient");
+      // the reference only warns when both are tiny (:3425-3428); dividing by
+      // them would produce NaN, so reject it
+      const double tiny = 10.0 * 2.220446049250313080847263336181640625e-16;
+      require(!(std::abs(av) < tiny && std::abs(bv) < tiny), BEM_EINVAL,
+              "Robin coefficients a and b are both zero for an element");
+      h->a[i] = av;
+      h->b[i] = bv;
+    }
+    h->have_bc = true;
+  });
+}
+
+bem_status bem_operators(bem_handle* h, double k, const int64_t* rows, const int64_t* cols,
+                         int64_t count, double* out) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] {
+    require(h->have_mesh && !h->points_mode, BEM_EINVAL, "mesh not set");
+    require(count >= 0 && (count == 0 || (rows && cols && out)), BEM_EINVAL, "bad arguments");
+    for (int64_t i = 0; i < count; i++)
+      require(rows[i] >= 0 && rows[i] < h->N && cols[i] >= 0 && cols[i] < h->N, BEM_EINVAL,
+              "index out of range");
+    if (count == 0) return;
+    DBuf<int64_t> dr, dc;
+    DBuf<double2> dout;
+    dr.ensure(count);
+    dc.ensure(count);
+    dout.ensure(4 * count);
+    CK(cudaMemcpyAsync(dr.p, rows, count * 8, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(dc.p, cols, count * 8, cudaMemcpyHostToDevice, h->stream));
+    launch_operators(h->dE.p, dr.p, dc.p, count, k, h->near_r, dout.p, h->stream);
+    h->launches++;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, dout.p, 4 * count * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+    sync(h);
+  });
+}
+
+bem_status bem_assemble(bem_handle* h, double freq) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] { assemble(h, freq, nullptr, nullptr); });
+}
+
+bem_status bem_hmatvec(bem_handle* h, int32_t which, const double* x, double* y, int64_t nrhs,
+                       int32_t accumulate) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] {
+    require(x && y && nrhs >= 1, BEM_EINVAL, "bad arguments");
+    const int64_t nr = h->points_mode ? (int64_t)h->rows.perm.size() : h->N;
+    const int64_t nc = h->points_mode ? (int64_t)h->cols.perm.size() : h->N;
+    copy_in(h, h->dIn, x, (size_t)nc * nrhs);
+    h->dOut1.ensure((size_t)nr * nrhs);
+    if (accumulate)
+      CK(cudaMemcpyAsync(h->dOut1.p, y, (size_t)nr * nrhs * sizeof(double2), cudaMemcpyHostToDevice, h->stream));
+    hmatvec_dev(h, which, h->dIn.p, h->dOut1.p, nrhs, accumulate);
+    CK(cudaGetLastError());
+    copy_out(h, y, h->dOut1.p, (size_t)nr * nrhs);
+    sync(h);
+  });
+}
+
+bem_status bem_hmatvec_device(bem_handle* h, int32_t which, const void* x, void* y, int64_t nrhs,
+                              int32_t accumulate) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] {
+    require(x && y && nrhs >= 1, BEM_EINVAL, "bad arguments");
+    hmatvec_dev(h, which, (const double2*)x, (double2*)y, nrhs, accumulate);
+    CK(cudaGetLastError());
+  });
+}
+
+bem_status bem_get_block(bem_handle* h, int32_t which, int64_t block, int64_t* rank, double* U,
+                         double* s, double* V, double* F) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] {
+    require(which == 0 || which == 1, BEM_EINVAL, "which must be 0 or 1");
+    DevHM& m = h->hm[which];
+    require(m.assembled, BEM_EINVAL, "matrix not assembled");
+    require(block >= 0 && block < (int64_t)h->L.blocks.size(), BEM_EINVAL, "block out of range");
+    // map partition index -> near / far index
+    int64_t nearI = 0, farI = 0;
+    for (int64_t i = 0; i < block; i++) (h->L.blocks[i].adm ? farI : nearI)++;
+    const HBlockDesc& b = h->L.blocks[block];
+    if (b.adm) {
+      const FarBlock& fb = h->L.far[farI];
+      const int k = m.h_rank[farI];
+      if (rank) *rank = k;
+      for (int l = 0; l < k; l++) {
+        if (U)
+          CK(cudaMemcpyAsync(U + 2 * (int64_t)l * b.m, m.U.p + fb.uoff + (int64_t)l * b.m,
+                             b.m * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+        if (V)
+          CK(cudaMemcpyAsync(V + 2 * (int64_t)l * b.n, m.V.p + fb.voff + (int64_t)l * b.n,
+                             b.n * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+      }
+      if (s && k > 0)
+        CK(cudaMemcpyAsync(s, m.S.p + fb.soff, k * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+    } else {
+      const NearBlock& nb = h->L.near[nearI];
+      if (rank) *rank = -1;
+      if (F)
+        CK(cudaMemcpyAsync(F, m.F.p + nb.off, (size_t)b.m * b.n * sizeof(double2),
+                           cudaMemcpyDeviceToHost, h->stream));
+    }
+    sync(h);
+  });
+}
+
+bem_status bem_get_ranks(bem_handle* h, int32_t which, int64_t* ranks) {
+  if (!h || !ranks) return BEM_EINVAL;
+  return guarded(h, [&] {
+    require(which == 0 || which == 1, BEM_EINVAL, "which must be 0 or 1");
+    DevHM& m = h->hm[which];
+    require(m.assembled, BEM_EINVAL, "matrix not assembled");
+    int64_t fi = 0;
+    for (size_t i = 0; i < h->L.blocks.size(); i++)
+      ranks[i] = h->L.blocks[i].adm ? m.h_rank[fi++] : -1;
+  });
+}
+
+bem_status bem_gmres(bem_handle* h, const double* b, double* x, int64_t nrhs, bem_solve_info* info) {
+  if (!h) return BEM_EINVAL;
+  bem_solve_info loc{};
+  bem_status st = guarded(h, [&] {
+    require(b && x && nrhs >= 1, BEM_EINVAL, "bad arguments");
+    require(!h->points_mode, BEM_EINVAL, "GMRES needs the BEM system matrix");
+    const int64_t N = h->N;
+    copy_in(h, h->dRhs, b, (size_t)N * nrhs);
+    copy_in(h, h->dX, x, (size_t)N * nrhs);
+    gmres_dev(h, h->dRhs.p, h->dX.p, (int)nrhs, &loc);
+    copy_out(h, x, h->dX.p, (size_t)N * nrhs);
+    sync(h);
+  });
+  if (info) *info = loc;
+  return st != BEM_OK ? st : loc.status;
+}
+
+bem_status bem_solve_device(bem_handle* h, double freq, const void* g, int64_t nrhs, void* phi,
+                            void* dphi, void* p, bem_solve_info* info) {
+  if (!h) return BEM_EINVAL;
+  bem_solve_info loc{};
+  bem_status st = guarded(h, [&] {
+    require(g != nullptr, BEM_EINVAL, "g is required");
+    solve_dev(h, freq, (const double2*)g, nrhs, (double2*)phi, (double2*)dphi, (double2*)p, &loc);
+  });
+  if (info) *info = loc;
+  return st != BEM_OK ? st : loc.status;
+}
+
+bem_status bem_solve(bem_handle* h, double freq, const double* g, int64_t nrhs, double* phi,
+                     double* dphi, double* p, bem_solve_info* info) {
+  if (!h) return BEM_EINVAL;
+  bem_solve_info loc{};
+  bem_status st = guarded(h, [&] {
+    require(h->have_mesh && !h->points_mode, BEM_EINVAL, "mesh not set");
+    require(g != nullptr && nrhs >= 1, BEM_EINVAL, "bad arguments");
+    const int64_t N = h->N;
+    const size_t cnt = (size_t)N * nrhs;
+    copy_in(h, h->dIn, g, cnt);
+    h->dOut1.ensure(cnt);
+    h->dOut2.ensure(cnt);
+    h->dOut3.ensure(cnt);
+    solve_dev(h, freq, h->dIn.p, nrhs, phi ? h->dOut1.p : nullptr, dphi ? h->dOut2.p : nullptr,
+              p ? h->dOut3.p : nullptr, &loc);
+    copy_out(h, phi, h->dOut1.p, cnt);
+    copy_out(h, dphi, h->dOut2.p, cnt);
+    copy_out(h, p, h->dOut3.p, cnt);
+    sync(h);
+  });
+  if (info) *info = loc;
+  return st != BEM_OK ? st : loc.status;
+}
+
+bem_status bem_sweep(bem_handle* h, const double* freqs, int64_t nf, const double* g, int64_t nrhs,
+                     double* p, bem_solve_info* info) {
+  if (!h) return BEM_EINVAL;
+  bem_status worst = BEM_OK;
+  bem_status st = guarded(h, [&] {
+    require(freqs && g && p && nf >= 1 && nrhs >= 1, BEM_EINVAL, "bad arguments");
+    const int64_t N = h->N;
+    const size_t cnt = (size_t)N * nrhs;
+    copy_in(h, h->dIn, g, cnt);
+    h->dOut3.ensure(cnt);
+    for (int64_t f = 0; f < nf; f++) {
+      bem_solve_info loc{};
+      solve_dev(h, freqs[f], h->dIn.p, nrhs, nullptr, nullptr, h->dOut3.p, &loc);
+      copy_out(h, p + 2 * cnt * f, h->dOut3.p, cnt);
+      if (info) info[f] = loc;
+      if (loc.status != BEM_OK) worst = loc.status;
+    }
+    sync(h);
+  });
+  return st != BEM_OK ? st : worst;
+}
+
+bem_status bem_points_assemble(bem_handle* h, const double* rowpts, int64_t nr,
+                               const double* colpts, int64_t nc, double k, int64_t* rowperm,
+                               int64_t* colperm) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] {
+    require(rowpts && colpts && nr >= 1 && nc >= 1, BEM_EINVAL, "bad arguments");
+    std::vector<double> rp(rowpts, rowpts + 3 * nr), cp(colpts, colpts + 3 * nc);
+    h->rows = build_tree(rp, h->cfg.leaf_size);
+    h->cols = build_tree(cp, h->cfg.leaf_size);
+    build_layout(h->rows, h->cols, nullptr, 0.0, h->cfg.eta, h->cfg.rank_reserve,
+                 h->cfg.aca_max_rank, false, h->cfg.seed, h->L);
+    std::vector<double> rps(3 * nr), cps(3 * nc);
+    for (int64_t i = 0; i < nr; i++)
+      for (int d = 0; d < 3; d++) rps[3 * i + d] = rp[3 * h->rows.perm[i] + d];
+    for (int64_t i = 0; i < nc; i++)
+      for (int d = 0; d < 3; d++) cps[3 * i + d] = cp[3 * h->cols.perm[i] + d];
+    h->dRowPts.upload(rps, h->stream);
+    h->dColPts.upload(cps, h->stream);
+    upload_layout(h);
+    h->points_mode = true;
+    h->have_mesh = false;
+    h->N = nr;
+    h->k = k;
+    DevHM& m = h->hm[0];
+    alloc_hm(h, m);
+    launch_points_nearfield(h->dNear.p, (int64_t)h->L.near.size(), h->dTiles.p,
+                            (int64_t)h->L.tiles.size(), h->dRowPts.p, h->dColPts.p, k, m.F.p,
+                            h->stream);
+    AcaArgs a = aca_args(h, m, 0, 0);
+    a.mode = 1;
+    launch_aca(a, h->stream);
+    h->launches += 2;
+    CK(cudaGetLastError());
+    fetch_ranks(h, m);
+    h->hm[1].assembled = false;
+    if (rowperm) std::memcpy(rowperm, h->rows.perm.data(), nr * sizeof(int64_t));
+    if (colperm) std::memcpy(colperm, h->cols.perm.data(), nc * sizeof(int64_t));
+  });
+}
+
+int64_t bem_launch_count(const bem_handle* h) { return h ? h->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,165 @@
+// hmatvec.cu -- K5: H-matrix times a block of R vectors, y = beta*y + H x.
+//
+// Reference: HArithm::MVM (HMatrix/harithm.cpp:3-28) loops over the partition
+// and scatters each block's U(s o (V^T x)) or F x into y under an omp critical.
+// Here the product runs in two passes with no atomics and a fixed summation
+// order:
+//   pass V: t_b = s_b o (V_b x_C) for every admissible block (one CTA each);
+//   pass U: one CTA per leaf row cluster sums, for its rows, every block whose
+//           row range contains them (U_b rows . t_b and dense F_b rows . x_C).
+// Every stored matrix entry is read once per call for all R vectors.
+#include "bem_kernels.h"
+#include "quadrature.cuh"
+
+namespace bemgpu {
+namespace {
+
+constexpr int VT = 128;  // threads of a pass-V CTA
+constexpr int UT = 128;  // threads of a pass-U CTA
+
+// t[r][soff + l] = s_l * sum_j V[l, j] x[c0 + j, r]
+template <typename T, int R>
+__global__ void __launch_bounds__(VT) hmv_vpass(const FarBlock* __restrict__ far,
+                                                const int32_t* __restrict__ rank,
+                                                const T* __restrict__ Vp,
+                                                const T* __restrict__ Sp,
+                                                const double2* __restrict__ x, int64_t ldx,
+                                                double2* __restrict__ t, int64_t ldt) {
+  const FarBlock fb = far[blockIdx.x];
+  const int k = rank[blockIdx.x];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int l = w; l < k; l += VT / 32) {
+    const T* Vl = Vp + fb.voff + (int64_t)l * fb.n;
+    double ax[R], ay[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) ax[r] = ay[r] = 0.0;
+    for (int j = lane; j < fb.n; j += 32) {
+      double2 v = load_c(Vl + j);
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        double2 xv = x[r * ldx + fb.c0 + j];
+        ax[r] += v.x * xv.x - v.y * xv.y;
+        ay[r] += v.x * xv.y + v.y * xv.x;
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        ax[r] += __shfl_xor_sync(0xffffffffu, ax[r], o);
+        ay[r] += __shfl_xor_sync(0xffffffffu, ay[r], o);
+      }
+    }
+    if (lane == 0) {
+      double2 s = load_c(Sp + fb.soff + l);
+#pragma unroll
+      for (int r = 0; r < R; r++) t[r * ldt + fb.soff + l] = cmul(s, make_double2(ax[r], ay[r]));
+    }
+  }
+}
+
+// One CTA per leaf row cluster; warps split the leaf's block list, lanes own
+// rows (32 rows per pass).
+template <typename T, int R>
+__global__ void __launch_bounds__(UT) hmv_upass(
+    const LeafRows* __restrict__ leaves, const int32_t* __restrict__ list_off,
+    const int32_t* __restrict__ list, const FarBlock* __restrict__ far,
+    const int32_t* __restrict__ rank, const NearBlock* __restrict__ nearb,
+    const T* __restrict__ Up, const T* __restrict__ F, const double2* __restrict__ x,
+    int64_t ldx, const double2* __restrict__ t, int64_t ldt, double2* __restrict__ y,
+    int64_t ldy, int accumulate) {
+  __shared__ double2 part[UT / 32][32][R];
+  const LeafRows lf = leaves[blockIdx.x];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int beg = list_off[blockIdx.x], end = list_off[blockIdx.x + 1];
+  for (int base = 0; base < lf.size; base += 32) {
+    const int ri = base + lane;  // row inside the leaf
+    const bool active = ri < lf.size;
+    const int64_t grow = lf.start + ri;
+    double ax[R], ay[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) ax[r] = ay[r] = 0.0;
+    for (int e = beg + w; e < end; e += UT / 32) {
+      const int32_t code = list[e];
+      if (code >= 0) {  // admissible block
+        const FarBlock fb = far[code];
+        const int k = rank[code];
+        const int64_t li = grow - fb.r0;
+        const T* U = Up + fb.uoff + li;
+        if (active) {
+          for (int l = 0; l < k; l++) {
+            double2 u = load_c(U + (int64_t)l * fb.m);
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+              double2 tv = t[r * ldt + fb.soff + l];
+              ax[r] += u.x * tv.x - u.y * tv.y;
+              ay[r] += u.x * tv.y + u.y * tv.x;
+            }
+          }
+        }
+      } else {  // dense near-field block
+        const NearBlock nb = nearb[-code - 1];
+        const int64_t li = grow - nb.r0;
+        const T* Fb = F + nb.off + li;
+        if (active) {
+          for (int j = 0; j < nb.n; j++) {
+            double2 f = load_c(Fb + (int64_t)j * nb.m);
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+              double2 xv = x[r * ldx + nb.c0 + j];
+              ax[r] += f.x * xv.x - f.y * xv.y;
+              ay[r] += f.x * xv.y + f.y * xv.x;
+            }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++) part[w][lane][r] = make_double2(ax[r], ay[r]);
+    __syncthreads();
+    if (w == 0 && active) {
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        double2 s = part[0][lane][r];
+#pragma unroll
+        for (int q = 1; q < UT / 32; q++) s = cadd(s, part[q][lane][r]);
+        double2* yp = y + r * ldy + grow;
+        *yp = accumulate ? cadd(*yp, s) : s;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T, int R>
+void launch_r(const HmvArgs& a, cudaStream_t s) {
+  if (a.nfar > 0)
+    hmv_vpass<T, R><<<(unsigned)a.nfar, VT, 0, s>>>(a.far, a.rank, (const T*)a.V, (const T*)a.S,
+                                                    a.x, a.ldx, a.t, a.ldt);
+  if (a.nleaves > 0)
+    hmv_upass<T, R><<<(unsigned)a.nleaves, UT, 0, s>>>(
+        a.leaves, a.list_off, a.list, a.far, a.rank, a.nearb, (const T*)a.U, (const T*)a.F, a.x,
+        a.ldx, a.t, a.ldt, a.y, a.ldy, a.accumulate);
+}
+
+template <typename T>
+void launch_t(const HmvArgs& a, cudaStream_t s) {
+  switch (a.nrhs) {
+    case 1: launch_r<T, 1>(a, s); break;
+    case 2: launch_r<T, 2>(a, s); break;
+    case 3: launch_r<T, 3>(a, s); break;
+    case 4: launch_r<T, 4>(a, s); break;
+    case 5: launch_r<T, 5>(a, s); break;
+    case 6: launch_r<T, 6>(a, s); break;
+    case 7: launch_r<T, 7>(a, s); break;
+    default: launch_r<T, 8>(a, s); break;  // the runtime splits R > 8 into chunks of 8
+  }
+}
+}  // namespace
+
+void launch_hmatvec(const HmvArgs& a, cudaStream_t s) {
+  if (a.precision == 0) launch_t<double2>(a, s);
+  else launch_t<float2>(a, s);
+}
+
+}  // namespace bemgpu

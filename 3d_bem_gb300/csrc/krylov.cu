@@ -1,0 +1,302 @@
+// krylov.cu -- K6: restarted GMRES building blocks in FP64 for R independent
+// right-hand sides that share each operator application.
+//
+// Reference: GMRES::gmresSolve / gmresLUPreconditionedSolve
+// (HMatrix/gmres.h:170-207) call Eigen's GMRES (Householder Arnoldi, Givens
+// rotations, restart 300, tolerance on ||b - A x|| / ||b||). This is the same
+// Krylov method (Saad & Schultz 1986) with classical Gram-Schmidt applied
+// twice (CGS2) for the Arnoldi step, which maps to two dense passes over the
+// basis instead of a sequence of dependent Householder reflections.
+//
+// Basis layout: V[q][r][i] (q = basis index, r = right-hand side), so the
+// R vectors of one basis index are one N x R column-major panel.
+// Hessenberg column j of RHS r: H[(r * m + j) * (m + 1) + i].
+#include "bem_kernels.h"
+#include "krylov.h"
+#include "quadrature.cuh"
+
+namespace bemgpu {
+namespace {
+
+constexpr int DT = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// partial[cta][r][q] = sum_{i in chunk} conj(V[q][r][i]) w[r][i]
+__global__ void __launch_bounds__(DT) dot_partial_kernel(const double2* __restrict__ Vb,
+                                                         const double2* __restrict__ w, int64_t N,
+                                                         int R, int nq, int64_t chunk,
+                                                         const GmresState* __restrict__ st,
+                                                         double2* __restrict__ partial) {
+  const int64_t i0 = (int64_t)blockIdx.x * chunk;
+  const int64_t i1 = min(N, i0 + chunk);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int task = warp; task < nq * R; task += DT / 32) {
+    const int q = task / R, r = task % R;
+    double sx = 0, sy = 0;
+    if (!st[r].done) {
+      const double2* v = Vb + ((int64_t)q * R + r) * N;
+      const double2* ww = w + (int64_t)r * N;
+      for (int64_t i = i0 + lane; i < i1; i += 32) {
+        double2 a = v[i], b = ww[i];
+        sx += a.x * b.x + a.y * b.y;
+        sy += a.x * b.y - a.y * b.x;
+      }
+      sx = warp_sum(sx);
+      sy = warp_sum(sy);
+    }
+    if (lane == 0) partial[((int64_t)blockIdx.x * R + r) * nq + q] = make_double2(sx, sy);
+  }
+}
+
+// h[r][q] = sum over CTAs (fixed order); H column j += h (first pass sets it)
+__global__ void dot_reduce_kernel(const double2* __restrict__ partial, int nct, int R, int nq,
+                                  int m, int j, int first, const GmresState* __restrict__ st,
+                                  double2* __restrict__ h, double2* __restrict__ H) {
+  const int task = blockIdx.x * blockDim.x + threadIdx.x;
+  if (task >= R * nq) return;
+  const int r = task / nq, q = task % nq;
+  if (st[r].done) return;
+  double2 s = make_double2(0, 0);
+  for (int c = 0; c < nct; c++) s = cadd(s, partial[((int64_t)c * R + r) * nq + q]);
+  h[r * nq + q] = s;
+  double2* Hc = H + ((int64_t)r * m + j) * (m + 1);
+  Hc[q] = first ? s : cadd(Hc[q], s);
+}
+
+// w[r][i] -= sum_q h[r][q] V[q][r][i]
+__global__ void __launch_bounds__(DT) axpy_kernel(const double2* __restrict__ Vb,
+                                                  double2* __restrict__ w, int64_t N, int R,
+                                                  int nq, const double2* __restrict__ h,
+                                                  const GmresState* __restrict__ st) {
+  const int r = blockIdx.y;
+  if (st[r].done) return;
+  const int64_t i = (int64_t)blockIdx.x * DT + threadIdx.x;
+  if (i >= N) return;
+  double2 acc = w[(int64_t)r * N + i];
+  for (int q = 0; q < nq; q++) {
+    double2 hv = h[r * nq + q];
+    double2 v = Vb[((int64_t)q * R + r) * N + i];
+    acc = csub(acc, cmul(hv, v));
+  }
+  w[(int64_t)r * N + i] = acc;
+}
+
+// partial squared norms of R vectors: partial[cta][r]
+__global__ void __launch_bounds__(DT) nrm_partial_kernel(const double2* __restrict__ w, int64_t N,
+                                                         int R, int64_t chunk,
+                                                         double* __restrict__ partial) {
+  __shared__ double red[DT / 32];
+  const int64_t i0 = (int64_t)blockIdx.x * chunk;
+  const int64_t i1 = min(N, i0 + chunk);
+  for (int r = 0; r < R; r++) {
+    double s = 0;
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += DT) s += cabs2(w[(int64_t)r * N + i]);
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0;
+      for (int q = 0; q < DT / 32; q++) t += red[q];
+      partial[(int64_t)blockIdx.x * R + r] = t;
+    }
+    __syncthreads();
+  }
+}
+
+// One thread per RHS: finish Arnoldi step j (subdiagonal, previous and new
+// Givens rotations, residual estimate, convergence flag).
+__global__ void finish_step_kernel(const double* __restrict__ partial, int nct, int R, int m,
+                                   int j, double tol, GmresState* __restrict__ st,
+                                   double2* __restrict__ H, double2* __restrict__ g,
+                                   double2* __restrict__ cs, double2* __restrict__ sn,
+                                   double* __restrict__ hnorm) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= R) return;
+  GmresState s = st[r];
+  if (s.done) return;
+  double n2 = 0;
+  for (int c = 0; c < nct; c++) n2 += partial[(int64_t)c * R + r];
+  const double hn = sqrt(n2);
+  hnorm[r] = hn;
+  double2* Hc = H + ((int64_t)r * m + j) * (m + 1);
+  double2* cr = cs + (int64_t)r * m;
+  double2* sr = sn + (int64_t)r * m;
+  double2* gr = g + (int64_t)r * (m + 1);
+  Hc[j + 1] = make_double2(hn, 0.0);
+  for (int q = 0; q < j; q++) {
+    double2 a = Hc[q], b = Hc[q + 1];
+    Hc[q] = cadd(cmul(cr[q], a), cmul(sr[q], b));
+    Hc[q + 1] = cadd(cscale(-1.0, cmul(cconj(sr[q]), a)), cmul(cr[q], b));
+  }
+  double2 a = Hc[j], b = Hc[j + 1];
+  double aa = sqrt(cabs2(a));
+  double rho = sqrt(cabs2(a) + cabs2(b));
+  double2 c, sv;
+  if (aa == 0.0) {
+    c = make_double2(0, 0);
+    sv = make_double2(1, 0);
+  } else {
+    c = make_double2(aa / rho, 0.0);
+    sv = cscale(1.0 / (aa * rho), cmul(a, cconj(b)));
+  }
+  cr[j] = c;
+  sr[j] = sv;
+  Hc[j] = cadd(cmul(c, a), cmul(sv, b));
+  Hc[j + 1] = make_double2(0, 0);
+  double2 gj = gr[j];
+  gr[j + 1] = cscale(-1.0, cmul(cconj(sv), gj));
+  gr[j] = cmul(c, gj);
+  s.jcount = j + 1;
+  s.iters += 1;
+  s.resid = sqrt(cabs2(gr[j + 1])) / s.bnorm;
+  if (s.resid < tol || hn == 0.0) s.done = 1;
+  st[r] = s;
+}
+
+// V[j+1][r] = w[r] / hnorm[r]
+__global__ void __launch_bounds__(DT) scale_kernel(const double2* __restrict__ w,
+                                                   double2* __restrict__ vnext, int64_t N,
+                                                   const double* __restrict__ hnorm,
+                                                   const GmresState* __restrict__ st,
+                                                   int j) {
+  const int r = blockIdx.y;
+  // a RHS that converged at this very step (jcount == j+1) still gets its
+  // vector; it is not used afterwards
+  if (st[r].done && st[r].jcount != j + 1) return;
+  const int64_t i = (int64_t)blockIdx.x * DT + threadIdx.x;
+  if (i >= N) return;
+  const double hn = hnorm[r];
+  double2 v = w[(int64_t)r * N + i];
+  vnext[(int64_t)r * N + i] = hn > 0 ? cscale(1.0 / hn, v) : make_double2(0, 0);
+}
+
+// One thread per RHS: solve the jcount x jcount triangular system H y = g.
+__global__ void trisolve_kernel(int R, int m, const GmresState* __restrict__ st,
+                                const double2* __restrict__ H, const double2* __restrict__ g,
+                                double2* __restrict__ y) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= R) return;
+  const int kk = st[r].jcount;
+  double2* yr = y + (int64_t)r * m;
+  for (int q = kk - 1; q >= 0; q--) {
+    double2 s = g[(int64_t)r * (m + 1) + q];
+    for (int t = q + 1; t < kk; t++) s = csub(s, cmul(H[((int64_t)r * m + t) * (m + 1) + q], yr[t]));
+    yr[q] = cdiv(s, H[((int64_t)r * m + q) * (m + 1) + q]);
+  }
+  for (int q = kk; q < m; q++) yr[q] = make_double2(0, 0);
+}
+
+// x[r] += sum_q y[r][q] V[q][r]
+__global__ void __launch_bounds__(DT) update_x_kernel(const double2* __restrict__ Vb,
+                                                      double2* __restrict__ x, int64_t N, int R,
+                                                      int m, const double2* __restrict__ y,
+                                                      const GmresState* __restrict__ st) {
+  const int r = blockIdx.y;
+  const int kk = st[r].jcount;
+  const int64_t i = (int64_t)blockIdx.x * DT + threadIdx.x;
+  if (i >= N) return;
+  double2 acc = x[(int64_t)r * N + i];
+  for (int q = 0; q < kk; q++) acc = cadd(acc, cmul(y[(int64_t)r * m + q], Vb[((int64_t)q * R + r) * N + i]));
+  x[(int64_t)r * N + i] = acc;
+}
+
+// r = b - w (stored into w), per RHS
+__global__ void __launch_bounds__(DT) residual_kernel(const double2* __restrict__ b,
+                                                      double2* __restrict__ w, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * DT + threadIdx.x;
+  if (i >= n) return;
+  w[i] = csub(b[i], w[i]);
+}
+
+// restart: beta = ||r||, V[0] = r / beta, g = [beta, 0, ...], jcount = 0
+__global__ void restart_kernel(const double* __restrict__ partial, int nct, int R, int m,
+                               double tol, int init, GmresState* __restrict__ st,
+                               double2* __restrict__ g, double* __restrict__ hnorm) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= R) return;
+  double n2 = 0;
+  for (int c = 0; c < nct; c++) n2 += partial[(int64_t)c * R + r];
+  double beta = sqrt(n2);
+  GmresState s = st[r];
+  if (init) {
+    s.bnorm = beta;  // first call measures ||b|| (w holds b)
+    s.iters = 0;
+    s.done = 0;
+  }
+  s.beta = beta;
+  s.jcount = 0;
+  s.resid = s.bnorm > 0 ? beta / s.bnorm : 0.0;
+  if (!init) {
+    if (s.bnorm == 0.0 || s.resid < tol) s.done = 1;
+    else s.done = 0;
+  }
+  st[r] = s;
+  hnorm[r] = beta;
+  for (int q = 0; q <= m; q++) g[(int64_t)r * (m + 1) + q] = make_double2(q == 0 ? beta : 0.0, 0.0);
+}
+
+__global__ void __launch_bounds__(DT) copy_scale_kernel(const double2* __restrict__ w,
+                                                        double2* __restrict__ v0, int64_t N,
+                                                        const double* __restrict__ hnorm) {
+  const int r = blockIdx.y;
+  const int64_t i = (int64_t)blockIdx.x * DT + threadIdx.x;
+  if (i >= N) return;
+  const double hn = hnorm[r];
+  v0[(int64_t)r * N + i] = hn > 0 ? cscale(1.0 / hn, w[(int64_t)r * N + i]) : make_double2(0, 0);
+}
+
+}  // namespace
+
+int krylov_num_ctas(int64_t N) {
+  int64_t c = (N + 4095) / 4096;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(c, 304));
+}
+
+void krylov_orthogonalize(const KrylovArgs& a, int j, cudaStream_t s) {
+  const int nq = j + 1;
+  const int nct = krylov_num_ctas(a.N);
+  const int64_t chunk = (a.N + nct - 1) / nct;
+  for (int pass = 0; pass < 2; pass++) {
+    dot_partial_kernel<<<nct, DT, 0, s>>>(a.Vb, a.w, a.N, a.R, nq, chunk, a.st, a.cpart);
+    int tasks = a.R * nq;
+    dot_reduce_kernel<<<(tasks + 127) / 128, 128, 0, s>>>(a.cpart, nct, a.R, nq, a.m, j,
+                                                          pass == 0, a.st, a.h, a.H);
+    dim3 g((unsigned)((a.N + DT - 1) / DT), (unsigned)a.R);
+    axpy_kernel<<<g, DT, 0, s>>>(a.Vb, a.w, a.N, a.R, nq, a.h, a.st);
+  }
+  nrm_partial_kernel<<<nct, DT, 0, s>>>(a.w, a.N, a.R, chunk, a.npart);
+  finish_step_kernel<<<(a.R + 31) / 32, 32, 0, s>>>(a.npart, nct, a.R, a.m, j, a.tol, a.st, a.H,
+                                                   a.g, a.cs, a.sn, a.hnorm);
+  dim3 g((unsigned)((a.N + DT - 1) / DT), (unsigned)a.R);
+  scale_kernel<<<g, DT, 0, s>>>(a.w, a.Vb + (int64_t)(j + 1) * a.R * a.N, a.N, a.hnorm, a.st, j);
+}
+
+void krylov_restart(const KrylovArgs& a, int init, cudaStream_t s) {
+  // w holds r (or b when init); writes V[0] = r / ||r||
+  const int nct = krylov_num_ctas(a.N);
+  const int64_t chunk = (a.N + nct - 1) / nct;
+  nrm_partial_kernel<<<nct, DT, 0, s>>>(a.w, a.N, a.R, chunk, a.npart);
+  restart_kernel<<<(a.R + 31) / 32, 32, 0, s>>>(a.npart, nct, a.R, a.m, a.tol, init, a.st, a.g,
+                                               a.hnorm);
+  if (!init) {
+    dim3 g((unsigned)((a.N + DT - 1) / DT), (unsigned)a.R);
+    copy_scale_kernel<<<g, DT, 0, s>>>(a.w, a.Vb, a.N, a.hnorm);
+  }
+}
+
+void krylov_residual(const double2* b, double2* w, int64_t n, cudaStream_t s) {
+  residual_kernel<<<(unsigned)((n + DT - 1) / DT), DT, 0, s>>>(b, w, n);
+}
+
+void krylov_update(const KrylovArgs& a, cudaStream_t s) {
+  trisolve_kernel<<<(a.R + 31) / 32, 32, 0, s>>>(a.R, a.m, a.st, a.H, a.g, a.y);
+  dim3 g((unsigned)((a.N + DT - 1) / DT), (unsigned)a.R);
+  update_x_kernel<<<g, DT, 0, s>>>(a.Vb, a.x, a.N, a.R, a.m, a.y, a.st);
+}
+
+}  // namespace bemgpu

@@ -1,0 +1,133 @@
+// nearfield.cu -- K1/K2: dense near-field blocks of both BC-substituted
+// matrices (phi = right-hand-side operator, dPhi = system operator) from one
+// operator evaluation per entry.
+//
+// The reference fills every inadmissible leaf entry by entry and evaluates the
+// operators twice, once per matrix (BlockCluster::fullRankAssembly,
+// HMatrix/hmatrix.cpp:350-374, called from assembleBlocks / assembleBlocksExtra
+// :793-846 with implicitPhiMatrix2 / implicitDPhiMatrix2,
+// boundaryelementsolver.cpp:2004-2040). Here one thread owns one entry and
+// writes both matrices. Regular pairs (16-point rule) and special pairs
+// (i == j singular rule, near-singular split-polar rule) run in separate
+// kernels so every warp follows one rule.
+#include "bem_kernels.h"
+#include "quadrature.cuh"
+
+namespace bemgpu {
+
+static __constant__ QuadRules c_rules;
+
+void nearfield_upload_rules(const QuadRules& r, cudaStream_t s) {
+  cudaMemcpyToSymbolAsync(c_rules, &r, sizeof(QuadRules), 0, cudaMemcpyHostToDevice, s);
+}
+
+// Regular entries of all near-field blocks; entries the host classified as
+// special (flag bit set) are left to nearfield_special.
+__global__ void __launch_bounds__(256) nearfield_regular_kernel(
+    const Elem* __restrict__ E, const BcCoef* __restrict__ bc,
+    const NearBlock* __restrict__ blocks, const NearTile* __restrict__ tiles,
+    const uint32_t* __restrict__ special_bits, double k, double2 alpha,
+    double2* __restrict__ phi, double2* __restrict__ dphi) {
+  const NearTile t = tiles[blockIdx.x];
+  if ((int)threadIdx.x >= t.count) return;
+  const NearBlock b = blocks[t.block];
+  const int e = t.first + threadIdx.x;
+  const int64_t g = b.off + e;
+  if (special_bits[g >> 5] & (1u << (g & 31))) return;
+  const int r = e % b.m, c = e / b.m;
+  const int64_t row = b.r0 + r, col = b.c0 + c;
+  Ops o = ops_regular(E[row], E[col], k, c_rules);
+  double2 p, d;
+  substitute(o, false, bc[col], alpha, p, d);
+  phi[g] = p;
+  dphi[g] = d;
+}
+
+// Special entries: (global entry index, row, col) triples sorted so that the
+// singular (row == col) ones come first.
+__global__ void __launch_bounds__(128) nearfield_special_kernel(
+    const Elem* __restrict__ E, const BcCoef* __restrict__ bc,
+    const int64_t* __restrict__ sp_entry, const int32_t* __restrict__ sp_row,
+    const int32_t* __restrict__ sp_col, int64_t count, double k, double2 alpha,
+    double2* __restrict__ phi, double2* __restrict__ dphi) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const int64_t row = sp_row[i], col = sp_col[i];
+  Ops o = (row == col) ? ops_singular(E[row], k, c_rules)
+                       : ops_nearsing(E[row], E[col], k, c_rules);
+  double2 p, d;
+  substitute(o, row == col, bc[col], alpha, p, d);
+  const int64_t g = sp_entry[i];
+  phi[g] = p;
+  dphi[g] = d;
+}
+
+// Raw operators L, M, Mt, N for arbitrary pairs (reference BemOperatorsConst,
+// boundaryelementsolver.cpp:844-894), used by bem_operators().
+__global__ void operators_kernel(const Elem* __restrict__ E, const int64_t* __restrict__ rows,
+                                 const int64_t* __restrict__ cols, int64_t count, double k,
+                                 double near_r, double2* __restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const int64_t row = rows[i], col = cols[i];
+  Ops o;
+  if (row == col) o = ops_singular(E[row], k, c_rules);
+  else if (near_pair(E[row], E[col], near_r)) o = ops_nearsing(E[row], E[col], k, c_rules);
+  else o = ops_regular(E[row], E[col], k, c_rules);
+  out[4 * i + 0] = o.L;
+  out[4 * i + 1] = o.M;
+  out[4 * i + 2] = o.Mt;
+  out[4 * i + 3] = o.N;
+}
+
+// Dense blocks of the point-cloud test kernel exp(ikr)/(4 pi r), 1 at r = 0
+// (Tests/tests.h:30-42).
+__global__ void __launch_bounds__(256) points_nearfield_kernel(
+    const NearBlock* __restrict__ blocks, const NearTile* __restrict__ tiles,
+    const double* __restrict__ rp, const double* __restrict__ cp, double k,
+    double2* __restrict__ F) {
+  const NearTile t = tiles[blockIdx.x];
+  if ((int)threadIdx.x >= t.count) return;
+  const NearBlock b = blocks[t.block];
+  const int e = t.first + threadIdx.x;
+  const int r = e % b.m, c = e / b.m;
+  const double* x = rp + 3 * (b.r0 + r);
+  const double* y = cp + 3 * (b.c0 + c);
+  double dx = x[0] - y[0], dy = x[1] - y[1], dz = x[2] - y[2];
+  double d = sqrt(dx * dx + dy * dy + dz * dz);
+  double2 v = make_double2(1.0, 0.0);
+  if (d != 0.0) {
+    double sn, cs;
+    sincos(k * d, &sn, &cs);
+    double g = 1.0 / (4.0 * 3.14159265358979323846 * d);
+    v = make_double2(cs * g, sn * g);
+  }
+  F[b.off + e] = v;
+}
+
+void launch_points_nearfield(const NearBlock* blocks, int64_t nblocks, const NearTile* tiles,
+                             int64_t ntiles, const double* rp, const double* cp, double k,
+                             double2* F, cudaStream_t s) {
+  (void)nblocks;
+  if (ntiles > 0) points_nearfield_kernel<<<(unsigned)ntiles, 256, 0, s>>>(blocks, tiles, rp, cp, k, F);
+}
+
+void launch_nearfield(const NearfieldArgs& a, cudaStream_t s) {
+  if (a.ntiles > 0)
+    nearfield_regular_kernel<<<(unsigned)a.ntiles, 256, 0, s>>>(
+        a.E, a.bc, a.blocks, a.tiles, a.special_bits, a.k, a.alpha, a.phi, a.dphi);
+  if (a.nspecial > 0) {
+    unsigned g = (unsigned)((a.nspecial + 127) / 128);
+    nearfield_special_kernel<<<g, 128, 0, s>>>(a.E, a.bc, a.sp_entry, a.sp_row, a.sp_col,
+                                               a.nspecial, a.k, a.alpha, a.phi, a.dphi);
+  }
+}
+
+void launch_operators(const Elem* E, const int64_t* rows, const int64_t* cols, int64_t count,
+                      double k, double near_r, double2* out, cudaStream_t s) {
+  if (count <= 0) return;
+  operators_kernel<<<(unsigned)((count + 127) / 128), 128, 0, s>>>(E, rows, cols, count, k,
+                                                                   near_r, out);
+}
+
+}  // namespace bemgpu

@@ -1,0 +1,165 @@
+/*
+ * bemgpu.h -- C ABI of the GB300 (sm_103a) Helmholtz BEM hot path.
+ *
+ * Drop-in boundary for the H-matrix solve of KG93/3d_BEM
+ * (BoundaryElementSolver::hMatrixSolve, boundaryelementsolver.cpp:526-744).
+ * Every entry point takes plain pointers and sizes, returns a bem_status and
+ * never aborts; complex numbers are interleaved (re, im) doubles. Unless
+ * stated otherwise, pointers are host pointers and the call copies in / out.
+ *
+ * Index order: the library renumbers elements by its cluster tree exactly as
+ * the reference's ClusterTree constructor reorders the triangles in place
+ * (HMatrix/clustertree.h:77-86, clustertree.cpp:265-283); instead of
+ * reordering the caller's arrays it returns the permutation
+ * (bem_get_permutation). Per-element inputs and outputs of bem_set_bc,
+ * bem_solve and bem_sweep are in the caller's order; the matrix-level calls
+ * (bem_operators, bem_hmatvec, bem_gmres, bem_get_block) use cluster order,
+ * like the reference's HMatrix / HArithm calls.
+ */
+#ifndef BEMGPU_H
+#define BEMGPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t bem_status;
+#define BEM_OK 0
+#define BEM_EINVAL 1     /* bad argument or call order */
+#define BEM_ENOMEM 2     /* device allocation failed */
+#define BEM_ENONFINITE 3 /* NaN / Inf detected in inputs or results */
+#define BEM_EMAXIT 4     /* iteration cap reached before the tolerance */
+#define BEM_EBREAKDOWN 5 /* Krylov breakdown */
+#define BEM_ETIMEOUT 6   /* a bounded device wait gave up */
+#define BEM_ECUDA 7      /* CUDA runtime error */
+#define BEM_ERANK 8      /* an ACA block reached its rank reservation */
+
+typedef struct bem_handle bem_handle;
+
+/* Solver parameters (BemSolverParameters, bemparameters.h:21-34, plus the
+ * constants the reference hard-wires: leaf size clustertree.h:146,
+ * admissibility constant hmatrix.h:240, GMRES tolerance and restart
+ * boundaryelementsolver.cpp:670/692 and gmres.h:170). */
+typedef struct bem_config {
+  int64_t leaf_size;       /* a cluster is a leaf when size < leaf_size (ref: 50) */
+  double eta;              /* admissible iff min(diam)/dist < eta (ref: 3) */
+  double aca_tol;          /* acaRelativeError */
+  int64_t aca_max_rank;    /* acaMaxRank, 0 = unlimited */
+  int64_t rank_reserve;    /* device rank reservation per admissible block */
+  double gmres_tol;        /* relative residual (ref: 1e-3 * aca_tol) */
+  int64_t gmres_restart;   /* ref: 300 */
+  int64_t gmres_maxit;     /* total Arnoldi steps allowed */
+  int32_t coupling;        /* 0 none, 1 Burton-Miller, 2 Kirkup (BemCoupling) */
+  int32_t precision;       /* 0 complex FP64 throughout */
+  double wave_speed;       /* c */
+  double density;          /* rho (p = i rho omega phi) */
+  uint64_t seed;           /* seeds the ACA start columns / pivot members */
+} bem_config;
+
+typedef struct bem_solve_info {
+  int64_t iterations;      /* max GMRES steps over right-hand sides */
+  double rel_residual;     /* max GMRES residual estimate */
+  double true_residual;    /* max ||b - A x|| / ||b|| after the solve */
+  int64_t max_rank;        /* largest ACA rank of the system matrix */
+  int64_t capped_blocks;   /* blocks that hit their rank reservation */
+  double t_nearfield;      /* seconds, device-timed */
+  double t_aca;
+  double t_rhs;
+  double t_gmres;
+  double t_total;
+  int32_t status;
+  int32_t pad;
+} bem_solve_info;
+
+void bem_config_default(bem_config* cfg);
+
+/* Create / destroy a solver handle on the current CUDA device. */
+bem_status bem_create(const bem_config* cfg, bem_handle** out);
+void bem_destroy(bem_handle* h);
+const char* bem_last_error(const bem_handle* h);
+
+/* Mesh: n triangles, 9 doubles each (node1, node2, node3). Builds the cluster
+ * tree, the block partition and every frequency-independent index table
+ * (ClusterTree(BoundaryElements*) clustertree.h:77-86,
+ * HMatrix::populateBlockClusterTree hmatrix.cpp:922,
+ * prepareBoundaryElements boundaryelementsolver.cpp:3463). */
+bem_status bem_set_mesh(bem_handle* h, const double* tri, int64_t n);
+bem_status bem_get_permutation(const bem_handle* h, int64_t* perm /* n, perm[new] = caller */);
+/* Partition in the reference's minPartition order: per block r0, m, c0, n,
+ * admissible. Pass info = NULL to query the count. */
+bem_status bem_get_partition(const bem_handle* h, int64_t* nblocks, int64_t* info);
+
+/* Host-only planning (no GPU needed): the cluster-tree permutation and the
+ * partition bem_set_mesh would build for this mesh and configuration
+ * (perm: n entries; info: 5 per block, NULL to query *nblocks). */
+bem_status bem_plan_mesh(const bem_config* cfg, const double* tri, int64_t n, int64_t* perm,
+                         int64_t* nblocks, int64_t* info);
+
+/* Robin coefficients a, b per element, caller order
+ * (calculateBoundaryConditionAndSourceTermVector, :3386-3429). */
+bem_status bem_set_bc(bem_handle* h, const double* a, const double* b);
+
+/* Collocation operators L, M, Mt, N for (row, col) pairs in cluster order
+ * (BemOperatorsConst, boundaryelementsolver.cpp:844-894); out: count x 4
+ * complex. */
+bem_status bem_operators(bem_handle* h, double k, const int64_t* rows, const int64_t* cols,
+                         int64_t count, double* out);
+
+/* Assemble both BC-substituted H-matrices at one frequency:
+ * phi via ACA (HMatrix::assembleBlocks, hmatrix.cpp:793) and dPhi via the
+ * seeded ACA (assembleBlocksExtra, hmatrix.cpp:825). */
+bem_status bem_assemble(bem_handle* h, double freq);
+
+/* y = (accumulate ? y : 0) + H x for nrhs vectors (N x nrhs, column-major,
+ * cluster order); which = 0 phi, 1 dPhi (HArithm::MVM, harithm.cpp:3-28).
+ * bem_hmatvec_device takes device pointers and runs on the handle's stream. */
+bem_status bem_hmatvec(bem_handle* h, int32_t which, const double* x, double* y, int64_t nrhs,
+                       int32_t accumulate);
+bem_status bem_hmatvec_device(bem_handle* h, int32_t which, const void* x, void* y,
+                              int64_t nrhs, int32_t accumulate);
+
+/* Block data of the assembled matrix `which`, block index in partition
+ * order. Admissible: rank returned, U (m x k col-major), s (k), V (k x n
+ * row-major) written when non-NULL. Full: *rank = -1, F (m x n col-major). */
+bem_status bem_get_block(bem_handle* h, int32_t which, int64_t block, int64_t* rank, double* U,
+                         double* s, double* V, double* F);
+/* Ranks of all blocks (-1 for full blocks). */
+bem_status bem_get_ranks(bem_handle* h, int32_t which, int64_t* ranks);
+
+/* GMRES on the assembled dPhi matrix, nrhs right-hand sides, cluster order
+ * (GMRES::gmresSolve, gmres.h:170-180; x0 = the content of x). */
+bem_status bem_gmres(bem_handle* h, const double* b, double* x, int64_t nrhs,
+                     bem_solve_info* info);
+
+/* Whole frequency solve (calculateBoundarySolution -> hMatrixSolve ->
+ * phiSolutionToSoundPressure): g is n x nrhs (caller order); phi, dphi and p
+ * (n x nrhs, caller order) may be NULL. */
+bem_status bem_solve(bem_handle* h, double freq, const double* g, int64_t nrhs, double* phi,
+                     double* dphi, double* p, bem_solve_info* info);
+/* Same with device pointers (inputs already resident in GPU memory). */
+bem_status bem_solve_device(bem_handle* h, double freq, const void* g, int64_t nrhs, void* phi,
+                            void* dphi, void* p, bem_solve_info* info);
+
+/* Frequency sweep (BemSolverController::run, bemsolvercontroller.cpp:49-109):
+ * nf frequencies x nrhs right-hand sides; p is n x nrhs x nf (caller order).
+ * info may be NULL or hold nf records. */
+bem_status bem_sweep(bem_handle* h, const double* freqs, int64_t nf, const double* g,
+                     int64_t nrhs, double* p, bem_solve_info* info);
+
+/* Point-cloud H-matrix with the reference's test kernel exp(ikr)/(4 pi r)
+ * (Tests/tests.h:30-42): rows and columns get their own cluster trees.
+ * Afterwards which = 0 addresses this matrix in bem_hmatvec / bem_get_block
+ * (indices in the two cluster orders, returned through rowperm / colperm). */
+bem_status bem_points_assemble(bem_handle* h, const double* rowpts, int64_t nr,
+                               const double* colpts, int64_t nc, double k, int64_t* rowperm,
+                               int64_t* colperm);
+
+/* Number of kernel launches issued by the library since the handle was
+ * created (instrumentation for benchmarks). */
+int64_t bem_launch_count(const bem_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -34,7 +34,8 @@ orc_problem* orc_create(const double* tri, int64_t n, int64_t leaf, double eta) 
   std::vector<V3> mids(n);
   for (int64_t i = 0; i < n; i++) {
     const double* t = tri + 9 * i;
-    mids[i] = (1.0 / 3.0) * (V3(t[0], t[1], t[2]) + V3(t[3], t[4], t[5]) + V3(t[6], t[7], t[8]));
+    V3 s = (V3(t[0], t[1], t[2]) + V3(t[3], t[4], t[5])) + V3(t[6], t[7], t[8]);
+    mids[i] = V3(s.x / 3.0, s.y / 3.0, s.z / 3.0);
   }
   p->tree = build_cluster_tree(mids, leaf);
   p->mesh.tri.resize(n);

@@ -265,8 +265,9 @@ void mesh_prepare(Mesh& m) {
     const Tri& t = m.tri[i];
     V3 c = cross(t.n2 - t.n1, t.n3 - t.n1);
     double cn = norm(c);
-    m.normal[i] = (1.0 / cn) * c;
-    m.colloc[i] = (1.0 / 3.0) * (t.n1 + t.n2 + t.n3);
+    m.normal[i] = V3(c.x / cn, c.y / cn, c.z / cn);
+    V3 s = (t.n1 + t.n2) + t.n3;
+    m.colloc[i] = V3(s.x / 3.0, s.y / 3.0, s.z / 3.0);
     m.area[i] = norm(cross(t.n1 - t.n2, t.n1 - t.n3)) / 2.0;
     acc += std::sqrt(m.area[i]);
   }

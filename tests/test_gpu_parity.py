@@ -1,0 +1,224 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle on the
+same seeded inputs. Complex FP64 throughout, so operators and dense near-field
+entries must agree to 1e-12 relative; H-matrix quantities carry the ACA
+tolerance."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "operators.npz")
+TIGHT = 1e-12  # FP64 kernels vs FP64 oracle, same quadrature rules
+
+
+def sphere_setup(bem, meshes, sub=3, **cfg):
+    tri = meshes.icosphere(sub, 1.0)
+    s = bem.Solver(**{"aca_tol": 1e-4, "gmres_tol": 1e-8, **cfg})
+    s.set_mesh(tri)
+    n = tri.shape[0]
+    s.set_bc(np.zeros(n), np.ones(n))
+    return tri, s
+
+
+def test_operators_vs_oracle_and_golden(bem, orc):
+    z = np.load(GOLDEN)
+    tri = z["tri"]
+    s = bem.Solver()
+    s.set_mesh(tri)
+    P = orc.Problem(tri, 32, 2.0)
+    assert np.array_equal(s.permutation, P.perm)
+    inv = np.argsort(P.perm)
+    rng = np.random.default_rng(1)
+    n = tri.shape[0]
+    rows = np.concatenate([inv[z["pairs"][:, 0]], rng.integers(0, n, 400), np.arange(n)])
+    cols = np.concatenate([inv[z["pairs"][:, 1]], rng.integers(0, n, 400), np.arange(n)])
+    for k in (0.5, 3.66, 27.5):
+        g = s.operators(k, rows, cols)
+        o = P.operators(k, rows, cols)
+        scale = np.abs(o).max(axis=0)
+        assert (np.abs(g - o) / scale).max() < TIGHT, k
+
+
+def test_nearfield_blocks_vs_oracle(bem, meshes, orc):
+    tri, s = sphere_setup(bem, meshes, 3)
+    P = orc.Problem(tri, 32, 2.0)
+    k = 2 * np.pi * 200 / 343
+    s.assemble(200.0)
+    info = s.partition()
+    n = tri.shape[0]
+    a, b = np.zeros(n), np.ones(n)
+    for which in (0, 1):
+        errs = []
+        for i, row in enumerate(info):
+            r0, m, c0, nn, adm = row
+            if adm:
+                continue
+            F = s.block(which, i, row)
+            rr, cc = np.meshgrid(np.arange(r0, r0 + m), np.arange(c0, c0 + nn), indexing="ij")
+            phi, dphi = P.entries(k, 2, a, b, rr.ravel(), cc.ravel())
+            ref = (phi if which == 0 else dphi).reshape(m, nn)
+            errs.append(np.abs(F - ref).max() / np.abs(ref).max())
+        assert max(errs) < TIGHT
+
+
+def test_aca_accuracy_and_ranks(bem, meshes, orc):
+    tri, s = sphere_setup(bem, meshes, 3, aca_tol=1e-4)
+    P = orc.Problem(tri, 32, 2.0)
+    k = 2 * np.pi * 200 / 343
+    n = tri.shape[0]
+    a, b = np.zeros(n), np.ones(n)
+    s.assemble(200.0)
+    exact_phi, exact_dphi = P.dense(k, 2, a, b)
+    for which, exact in ((0, exact_phi), (1, exact_dphi)):
+        D = s.dense(which)
+        # Tests/tests.cpp:27-43 design: ||A - A_H|| / ||A|| < 2 * tol
+        assert rel(D, exact) < 2e-4
+        H = P.hassemble(k, 2, a, b, which, 1e-4, seed=s.config.seed)
+        # identical deterministic pivots -> the same ranks and blocks
+        rg, ro = s.ranks(which), H.ranks()
+        assert np.mean(rg == ro) > 0.98
+        assert rel(D, H.dense()) < 1e-6
+
+
+def test_hmatvec_exact_for_its_blocks(bem, meshes):
+    tri, s = sphere_setup(bem, meshes, 3)
+    s.assemble(200.0)
+    rng = np.random.default_rng(2)
+    n = tri.shape[0]
+    D = s.dense(1)
+    for R in (1, 3, 9):
+        x = rng.standard_normal((n, R)) + 1j * rng.standard_normal((n, R))
+        y = s.hmatvec(1, x)
+        assert rel(y, D @ x) < 1e-13
+    y0 = rng.standard_normal(n) + 0j
+    x = rng.standard_normal(n) + 0j
+    y = s.hmatvec(1, x, y0, accumulate=True)
+    assert rel(y, y0 + D @ x) < 1e-13
+
+
+def test_solve_vs_oracle_and_analytic(bem, meshes, orc):
+    tri, s = sphere_setup(bem, meshes, 3, aca_tol=1e-4, gmres_tol=1e-8)
+    n = tri.shape[0]
+    f, c, rho = 200.0, 343.0, 1.2
+    g = np.ones(n)
+    phi, dphi, p, info = s.solve(f, g)
+    assert info["status"] == 0 and info["true_residual"] < 1e-8
+    P = orc.Problem(tri, 32, 2.0)
+    _, _, po, st = P.solve(f, c, rho, 2, np.zeros(n), np.ones(n), g, 1e-4, 1e-8,
+                           seed=s.config.seed)
+    assert rel(p[:, 0], po[:, 0]) < 1e-6
+    k = 2 * np.pi * f / c
+    pa = rho * c * (1j * k) / (1j * k - 1)
+    assert np.abs(p[:, 0] - pa).max() / abs(pa) < 0.03
+    assert np.allclose(dphi[:, 0], 1.0)
+
+
+def test_robin_mixed_bc_box_vs_oracle(bem, meshes, orc):
+    """Both substitution branches (|a| < |b| and |a| >= |b|) on a box."""
+    tri = meshes.box(n_target=1200, seed=11)
+    n = tri.shape[0]
+    rng = np.random.default_rng(5)
+    a = np.where(rng.random(n) < 0.3, 2.0 + 1j * rng.random(n), 0.3j * rng.random(n))
+    b = np.ones(n, complex)
+    g = rng.uniform(-1, 1, n) + 0j
+    s = bem.Solver(aca_tol=1e-5, gmres_tol=1e-9)
+    s.set_mesh(tri)
+    s.set_bc(a, b)
+    phi, dphi, p, info = s.solve(800.0, g)
+    P = orc.Problem(tri, 32, 2.0)
+    po, dpo, ppo, st = P.solve(800.0, 343.0, 1.2, 2, a, b, g, 1e-5, 1e-9, seed=s.config.seed)
+    assert rel(phi[:, 0], po[:, 0]) < 1e-6
+    assert rel(dphi[:, 0], dpo[:, 0]) < 1e-6
+
+
+def test_multi_rhs_and_sweep(bem, meshes):
+    tri = meshes.icosphere(3)
+    n = tri.shape[0]
+    G = meshes.random_patches(tri, 3, 0.05, seed=9)
+    G[:, 0] = 1.0
+    s = bem.Solver(aca_tol=1e-5, gmres_tol=1e-9)
+    s.set_mesh(tri)
+    s.set_bc(np.zeros(n), np.ones(n))
+    freqs = np.array([150.0, 300.0])
+    P, infos = s.sweep(freqs, G)
+    for fi, f in enumerate(freqs):
+        for r in range(3):
+            _, _, p1, _ = s.solve(f, G[:, r])
+            assert rel(P[:, r, fi], p1[:, 0]) < 1e-9
+    assert all(i["status"] == 0 for i in infos)
+
+
+def test_point_cloud_reference_design(bem, orc):
+    """Tests/tests.cpp:27-106 design on the GPU: ACA within 2 tol, MVM exact
+    to ~10 eps for the stored blocks."""
+    rng = np.random.default_rng(7)
+    X = rng.uniform(-1, 1, (300, 3))
+    Y = rng.uniform(-1, 1, (300, 3))
+    s = bem.Solver(aca_tol=1e-3, eta=3.0)
+    rp, cp = s.points_assemble(X, Y, 150.0)
+    Xs, Ys = X[rp], Y[cp]
+    d = np.linalg.norm(Xs[:, None] - Ys[None], axis=2)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        A = np.where(d == 0, 1.0, np.exp(1j * 150 * d) / (4 * np.pi * d))
+    D = s.dense(0)
+    assert rel(D, A) < 2e-3
+    x = rng.standard_normal(300) + 1j * rng.standard_normal(300)
+    assert rel(s.hmatvec(0, x), D @ x) < 100 * np.finfo(float).eps
+
+
+def test_single_triangle_and_error_paths(bem):
+    tri = np.array([[0, 0, 0, 0.1, 0, 0, 0, 0.1, 0]], float)
+    s = bem.Solver()
+    s.set_mesh(tri)
+    s.set_bc(np.zeros(1), np.ones(1))
+    phi, dphi, p, info = s.solve(500.0, np.ones(1))
+    assert np.isfinite(p).all() and info["status"] == 0
+    # invalid inputs fail loudly with a status, the handle stays usable
+    with pytest.raises(bem.BemError) as e:
+        s.set_bc(np.zeros(1), np.zeros(1))
+    assert e.value.status == bem.BEM_EINVAL
+    bad = tri.copy()
+    bad[0, 0] = np.nan
+    with pytest.raises(bem.BemError) as e:
+        s.set_mesh(bad)
+    assert e.value.status == bem.BEM_ENONFINITE
+    degenerate = np.array([[0, 0, 0, 1, 0, 0, 2, 0, 0]], float)
+    with pytest.raises(bem.BemError) as e:
+        s.set_mesh(degenerate)
+    assert e.value.status == bem.BEM_EINVAL
+    s2 = bem.Solver()
+    with pytest.raises(bem.BemError):
+        s2.solve(100.0, np.ones(1))
+    s.set_mesh(tri)
+    s.set_bc(np.zeros(1), np.ones(1))
+    _, _, p2, _ = s.solve(500.0, np.ones(1))
+    assert np.allclose(p, p2)
+
+
+def test_large_sphere_properties(bem, meshes, orc):
+    """20,480-element sphere at 1.5 kHz (the benchmark workload): size-
+    independent checks -- converged true residual, sampled entries against the
+    oracle, and the analytic monopole within the discretisation error."""
+    tri = meshes.icosphere(5, 1.0)
+    n = tri.shape[0]
+    s = bem.Solver(aca_tol=1e-5, gmres_tol=1e-10)
+    s.set_mesh(tri)
+    s.set_bc(np.zeros(n), np.ones(n))
+    f, c, rho = 1500.0, 343.0, 1.2
+    phi, dphi, p, info = s.solve(f, np.ones(n))
+    assert info["status"] == 0 and info["true_residual"] < 1e-10
+    assert info["capped_blocks"] == 0
+    k = 2 * np.pi * f / c
+    pa = rho * c * (1j * k) / (1j * k - 1)
+    assert np.abs(p[:, 0] - pa).max() / abs(pa) < 0.02
+    # sampled operator entries against the oracle at full size
+    P = orc.Problem(tri, 32, 2.0)
+    rng = np.random.default_rng(4)
+    rows = rng.integers(0, n, 3000)
+    cols = np.concatenate([rng.integers(0, n, 2000), rows[2000:]])
+    go = s.operators(k, rows, cols)
+    oo = P.operators(k, rows, cols)
+    assert (np.abs(go - oo) / np.abs(oo).max(axis=0)).max() < TIGHT

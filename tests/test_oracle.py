@@ -1,0 +1,181 @@
+"""CPU tests of the oracle: it is pinned against independent known answers
+before it is trusted as the checker of the GPU kernels."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "operators.npz")
+
+
+def test_triangle_rules_exact_for_polynomials(orc):
+    # Dunavant degree-8 rule (16 pts): exact for x^a y^b, a + b <= 8, on the
+    # reference triangle (area 1/2): int x^a y^b = a! b! / (a + b + 2)!
+    from math import factorial
+    for order, deg in [(1, 1), (2, 2), (5, 5), (7, 7), (8, 8), (10, 10), (15, 14)]:
+        r = orc.triangle_rule(order)
+        assert abs(r[:, 2].sum() - 1.0) < 1e-12, order
+        for a in range(deg + 1):
+            for b in range(deg + 1 - a):
+                exact = factorial(a) * factorial(b) / factorial(a + b + 2)
+                approx = 0.5 * np.sum(r[:, 2] * r[:, 0] ** a * r[:, 1] ** b)
+                assert abs(approx - exact) < 2e-12 + 1e-9 * exact, (order, a, b)
+
+
+def test_line_rules(orc):
+    for n in (1, 2, 3, 4, 5, 32):
+        r = orc.line_rule(n)
+        x, w = np.polynomial.legendre.leggauss(n)
+        assert np.allclose(r[:, 0], x, atol=1e-15) and np.allclose(r[:, 1], w, atol=1e-15)
+
+
+def test_operators_against_golden(orc):
+    z = np.load(GOLDEN)
+    P = orc.Problem(z["tri"], 32, 2.0)
+    inv = np.argsort(P.perm)
+    pairs, kinds = z["pairs"], z["kinds"]
+    for a, k in enumerate(z["ks"]):
+        ops = P.operators(k, inv[pairs[:, 0]], inv[pairs[:, 1]])
+        ref = z["vals"][a]
+        scale = np.abs(ref).max(axis=0)
+        reg = kinds == 0
+        # 16-point rule at distance >= 4 * averageTriangleDim
+        assert (np.abs(ops[reg] - ref[reg]) / scale).max() < 1e-6
+        # the reference's 5 x 5 split-polar rule on adjacent panels
+        assert (np.abs(ops[~reg] - ref[~reg]) / scale).max() < 5e-2
+    idx = z["self_idx"]
+    ops = P.operators(1e-5, inv[idx], inv[idx])
+    assert np.abs(ops[:, 0].real - z["self_laplace"]).max() < 1e-9
+    assert np.all(ops[:, 1] == 0) and np.all(ops[:, 2] == 0)  # flat panel: M = Mt = 0
+
+
+def test_pulsating_sphere_analytic(orc, meshes):
+    """Uniform normal velocity on a sphere: p = rho c v ika / (ika - 1)."""
+    tri = meshes.icosphere(3, 1.0)
+    P = orc.Problem(tri, 32, 2.0)
+    n = P.n
+    f, c, rho = 200.0, 343.0, 1.2
+    k = 2 * np.pi * f / c
+    a, b, g = np.zeros(n), np.ones(n), np.ones(n)
+    phi, dphi, p, st = P.solve(f, c, rho, 2, a, b, g, 1e-4, 1e-8)
+    pa = rho * c * (1j * k) / (1j * k - 1)
+    assert st["rel_resid"] < 1e-8
+    assert np.abs(p[:, 0] - pa).max() / abs(pa) < 0.03  # O(h^2) discretisation error
+    assert np.allclose(dphi[:, 0], 1.0)
+
+
+def test_hmatrix_vs_dense_solution(orc, meshes):
+    tri = meshes.icosphere(3, 1.0)
+    P = orc.Problem(tri, 32, 2.0)
+    n = P.n
+    f, c, rho = 200.0, 343.0, 1.2
+    k = 2 * np.pi * f / c
+    a, b, g = np.zeros(n), np.ones(n), np.ones(n)
+    perm = P.perm
+    Dphi, Ddphi = P.dense(k, 2, a[perm], b[perm])
+    x = np.linalg.solve(Ddphi, Dphi @ g[perm])
+    pd = np.zeros(n, complex)
+    pd[perm] = 1j * rho * 2 * np.pi * f * x
+    for tol in (1e-4, 1e-6):
+        _, _, p, st = P.solve(f, c, rho, 2, a, b, g, tol, 1e-3 * tol)
+        assert rel(p[:, 0], pd) < 20 * tol
+
+
+def test_point_cloud_aca_reference_design(orc):
+    """Tests/tests.cpp:27-43 design: 300 random points, k = 150, tol 1e-3."""
+    rng = np.random.default_rng(7)
+    X = rng.uniform(-1, 1, (300, 3))
+    Y = rng.uniform(-1, 1, (300, 3))
+    H, rp, cp = orc.hassemble_points(X, Y, 150.0, 32, 3.0, 1e-3)
+    Xs, Ys = X[rp], Y[cp]
+    d = np.linalg.norm(Xs[:, None] - Ys[None], axis=2)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        A = np.where(d == 0, 1.0, np.exp(1j * 150 * d) / (4 * np.pi * d))
+    D = H.dense()
+    assert rel(D, A) < 2e-3
+    x = rng.standard_normal(300) + 1j * rng.standard_normal(300)
+    tiny = 10 * np.finfo(float).eps
+    assert rel(H.matvec(x), D @ x) < tiny * 10
+
+
+def test_recompression_truncates(orc, meshes):
+    tri = meshes.icosphere(3, 1.0)
+    P = orc.Problem(tri, 32, 2.0)
+    n = P.n
+    k = 2 * np.pi * 200 / 343
+    a, b = np.zeros(n), np.ones(n)
+    H = P.hassemble(k, 2, a, b, 1, 1e-6)
+    D0 = H.dense()
+    r0 = H.ranks()
+    H.recompress(0, 1e-4)
+    r1 = H.ranks()
+    assert np.all(r1[r0 >= 0] <= r0[r0 >= 0])
+    assert rel(H.dense(), D0) < 1e-3
+    H.recompress(2, 0.0)
+    assert r1.max() >= 2 and H.ranks().max() <= 2
+
+
+def _random_block_triangular(n, leaf, rng, lower):
+    """Flat leaf lists of a random block-triangular matrix on a binary
+    cluster split (diag leaves Q (unitary) or R (upper), off-diagonal full or
+    low-rank), plus its dense form."""
+    blocks, data = [], []
+    D = np.zeros((n, n), complex)
+
+    def add(r0, m, c0, nn, kind, arr):
+        off = sum(x.size for x in data)
+        rank = 0
+        if kind == 1:
+            U, V = arr
+            rank = U.shape[1]
+            data.append(np.asfortranarray(U).ravel(order="F"))
+            data.append(np.ascontiguousarray(V).ravel())
+            D[r0:r0 + m, c0:c0 + nn] = U @ V
+        else:
+            data.append(np.asfortranarray(arr).ravel(order="F"))
+            D[r0:r0 + m, c0:c0 + nn] = arr
+        blocks.append([r0, m, c0, nn, kind, rank, off])
+
+    def rec(s, m):
+        if m <= leaf:
+            A = rng.standard_normal((m, m)) + 1j * rng.standard_normal((m, m))
+            Q, R = np.linalg.qr(A + 4 * np.eye(m))
+            add(s, m, s, m, 2 if lower else 3, Q if lower else R)
+            return
+        m1 = m // 2
+        m2 = m - m1
+        rec(s, m1)
+        rec(s + m1, m2)
+        if lower:
+            r0, mm, c0, nn = s + m1, m2, s, m1
+        else:
+            r0, mm, c0, nn = s, m1, s + m1, m2
+        if rng.random() < 0.5:
+            add(r0, mm, c0, nn, 0, 0.1 * (rng.standard_normal((mm, nn)) + 1j * rng.standard_normal((mm, nn))))
+        else:
+            kk = 3
+            add(r0, mm, c0, nn, 1, (0.1 * rng.standard_normal((mm, kk)) + 0j,
+                                    rng.standard_normal((kk, nn)) + 0j))
+
+    rec(0, n)
+    return np.array(blocks, np.int64), np.concatenate(data), D
+
+
+def test_block_triangular_solves(orc):
+    rng = np.random.default_rng(3)
+    n = 150
+    Lb, Ld, LD = _random_block_triangular(n, 20, rng, True)
+    Ub, Ud, UD = _random_block_triangular(n, 20, rng, False)
+    b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    # L is block lower triangular with unitary diagonal blocks Q: the leaf
+    # solve applies Q^H (harithm.cpp:1324-1327)
+    diagQ = np.zeros((n, n), complex)
+    for r0, m, c0, nn, kind, rank, off in Lb:
+        if kind == 2:
+            diagQ[r0:r0 + m, c0:c0 + nn] = LD[r0:r0 + m, c0:c0 + nn]
+    y = orc.lower_solve(n, Lb, Ld, b)
+    assert rel(LD @ y, b) < 1e-12
+    x = orc.upper_solve(n, Ub, Ud, y)
+    assert rel(UD @ x, y) < 1e-12
