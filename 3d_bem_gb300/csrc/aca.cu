@@ -148,6 +148,10 @@ __device__ void argmax_abs(const double2* v, int len, int exclude, Red& red, dou
     }
   }
   block_argmax(bv, bi, red, best, bidx);
+  if (bidx < 0 || bidx >= len) {  // all entries NaN: report a zero pivot at 0
+    bidx = 0;
+    best = 0.0;
+  }
 }
 
 // normEstimate increment (hmatrix.cpp:570-574):
