@@ -36,7 +36,7 @@ EXPORTS = [
     "bem_get_permutation", "bem_get_partition", "bem_set_bc", "bem_operators",
     "bem_assemble", "bem_hmatvec", "bem_hmatvec_device", "bem_get_block", "bem_get_ranks",
     "bem_gmres", "bem_solve", "bem_solve_device", "bem_sweep", "bem_points_assemble",
-    "bem_launch_count",
+    "bem_launch_count", "bem_stream",
 ]
 
 
@@ -114,6 +114,8 @@ def lib():
     L.bem_points_assemble.argtypes = [vp, vp, i64, vp, i64, dbl, vp, vp]
     L.bem_launch_count.argtypes = [vp]
     L.bem_launch_count.restype = i64
+    L.bem_stream.argtypes = [vp]
+    L.bem_stream.restype = vp
     for name in EXPORTS:
         f = getattr(L, name)
         if f.restype is ct.c_int:  # default restype: status codes are int32
@@ -279,7 +281,8 @@ class Solver:
         return x, info.as_dict()
 
     def solve(self, freq: float, g, want=("phi", "dphi", "p")):
-        g = np.asfortranarray(np.asarray(g, np.complex128).reshape(self.n, -1))
+        g = np.asarray(g, np.complex128)
+        g = np.asfortranarray(g.reshape(self.n or g.shape[0], -1))
         R = g.shape[1]
         outs = {k: (np.zeros((self.n, R), np.complex128, order="F") if k in want else None)
                 for k in ("phi", "dphi", "p")}

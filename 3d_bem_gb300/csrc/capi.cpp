@@ -902,4 +902,6 @@ bem_status bem_points_assemble(bem_handle* h, const double* rowpts, int64_t nr,
 
 int64_t bem_launch_count(const bem_handle* h) { return h ? h->launches : 0; }
 
+void* bem_stream(const bem_handle* h) { return h ? (void*)h->stream : nullptr; }
+
 }  // extern "C"

@@ -159,6 +159,10 @@ bem_status bem_points_assemble(bem_handle* h, const double* rowpts, int64_t nr,
  * created (instrumentation for benchmarks). */
 int64_t bem_launch_count(const bem_handle* h);
 
+/* The CUDA stream (cudaStream_t) every kernel of this handle runs on, so a
+ * caller can order its own work or record timing events on it. */
+void* bem_stream(const bem_handle* h);
+
 #ifdef __cplusplus
 }
 #endif
