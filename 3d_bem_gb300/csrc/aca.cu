@@ -9,6 +9,11 @@
 // stopping test; the random start column / seed member picks are replaced by
 // a seeded hash so runs are reproducible.
 //
+// Two precisions share the code: T = double2 (complex FP64 storage and
+// arithmetic, the plain method) and T = float2 (mixed: FP32 regular
+// quadrature with an FP64-formed centroid difference, FP64 singular and
+// near-singular rules, complex FP32 storage and residual updates).
+//
 // Layout: U column l of a block at U + uoff + l*m (unscaled residual columns),
 // V row l at V + voff + l*n (residual rows), s_l = 1/pivot at S + soff + l.
 // The working residual column/row of the next step live in slot `rank` of the
@@ -29,6 +34,19 @@ constexpr double TINY = 10.0 * 2.220446049250313080847263336181640625e-16;  // g
 constexpr int NT = 128;
 constexpr int NW = NT / 32;
 
+// complex arithmetic on the storage type
+__device__ __forceinline__ double2 cx_mul(double2 a, double2 b) { return cmul(a, b); }
+__device__ __forceinline__ float2 cx_mul(float2 a, float2 b) { return fmul(a, b); }
+__device__ __forceinline__ double2 cx_sub(double2 a, double2 b) { return csub(a, b); }
+__device__ __forceinline__ float2 cx_sub(float2 a, float2 b) { return fsub(a, b); }
+__device__ __forceinline__ double2 to_d(double2 a) { return a; }
+__device__ __forceinline__ double2 to_d(float2 a) { return make_double2(a.x, a.y); }
+template <typename T> __device__ __forceinline__ T from_d(double2 a);
+template <> __device__ __forceinline__ double2 from_d<double2>(double2 a) { return a; }
+template <> __device__ __forceinline__ float2 from_d<float2>(double2 a) {
+  return make_float2((float)a.x, (float)a.y);
+}
+
 struct Red {
   double v[NW];
   int i[NW];
@@ -36,6 +54,11 @@ struct Red {
 };
 
 __device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_sumf(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
@@ -83,13 +106,23 @@ __device__ __forceinline__ void block_argmax(double v, int idx, Red& red, double
     }
 }
 
-template <int MODE>
-__device__ __forceinline__ double2 aca_entry(const AcaArgs& a, int64_t row, int64_t col) {
+template <int MODE, typename T>
+__device__ __forceinline__ T aca_entry(const AcaArgs& a, int64_t row, int64_t col) {
   if (MODE == 0) {
+    if (sizeof(T) == sizeof(float2)) {
+      // mixed precision: FP32 regular rule, FP64 singular / near-singular
+      if (row != col && !near_pair(a.E[row], a.E[col], a.near_r)) {
+        OpsF o = ops_regular32(a.E, a.EF, row, col, (float)a.k, c_rules);
+        float2 p, d;
+        substitute32(o, a.bc[col], make_float2((float)a.alpha.x, (float)a.alpha.y), p, d);
+        double2 r = to_d(a.which ? d : p);
+        return from_d<T>(r);
+      }
+    }
     Ops o = ops_eval(a.E, row, col, a.k, a.near_r, c_rules);
     double2 p, d;
     substitute(o, row == col, a.bc[col], a.alpha, p, d);
-    return a.which ? d : p;
+    return from_d<T>(a.which ? d : p);
   } else {
     // point-cloud Helmholtz kernel of the reference's tests
     // (Tests/tests.h:30-42): exp(ikr)/(4 pi r), 1 at r = 0
@@ -97,51 +130,49 @@ __device__ __forceinline__ double2 aca_entry(const AcaArgs& a, int64_t row, int6
     const double* y = a.colpts + 3 * col;
     double dx = x[0] - y[0], dy = x[1] - y[1], dz = x[2] - y[2];
     double r = sqrt(dx * dx + dy * dy + dz * dz);
-    if (r == 0.0) return make_double2(1.0, 0.0);
+    if (r == 0.0) return from_d<T>(make_double2(1.0, 0.0));
     double s, c;
     sincos(a.k * r, &s, &c);
     double g = 1.0 / (4.0 * 3.14159265358979323846 * r);
-    return make_double2(c * g, s * g);
+    return from_d<T>(make_double2(c * g, s * g));
   }
 }
 
 // dst[i] = A(r0+i, c0+ci) - sum_l U[:,l] (s_l V[l,ci])
-template <int MODE>
-__device__ void residual_col(const AcaArgs& a, const FarBlock& fb, const double2* U,
-                             const double2* V, const double2* S, int k, int ci, double2* dst,
-                             double2* coef) {
-  for (int l = threadIdx.x; l < k; l += NT) coef[l] = cmul(S[l], V[(int64_t)l * fb.n + ci]);
+template <int MODE, typename T>
+__device__ void residual_col(const AcaArgs& a, const FarBlock& fb, const T* U, const T* V,
+                             const T* S, int k, int ci, T* dst, T* coef) {
+  for (int l = threadIdx.x; l < k; l += NT) coef[l] = cx_mul(S[l], V[(int64_t)l * fb.n + ci]);
   __syncthreads();
   for (int i = threadIdx.x; i < fb.m; i += NT) {
-    double2 v = aca_entry<MODE>(a, fb.r0 + i, fb.c0 + ci);
-    for (int l = 0; l < k; l++) v = csub(v, cmul(U[(int64_t)l * fb.m + i], coef[l]));
+    T v = aca_entry<MODE, T>(a, fb.r0 + i, fb.c0 + ci);
+    for (int l = 0; l < k; l++) v = cx_sub(v, cx_mul(U[(int64_t)l * fb.m + i], coef[l]));
     dst[i] = v;
   }
   __syncthreads();
 }
 
 // dst[j] = A(r0+ri, c0+j) - sum_l (U[ri,l] s_l) V[l,:]
-template <int MODE>
-__device__ void residual_row(const AcaArgs& a, const FarBlock& fb, const double2* U,
-                             const double2* V, const double2* S, int k, int ri, double2* dst,
-                             double2* coef) {
-  for (int l = threadIdx.x; l < k; l += NT) coef[l] = cmul(U[(int64_t)l * fb.m + ri], S[l]);
+template <int MODE, typename T>
+__device__ void residual_row(const AcaArgs& a, const FarBlock& fb, const T* U, const T* V,
+                             const T* S, int k, int ri, T* dst, T* coef) {
+  for (int l = threadIdx.x; l < k; l += NT) coef[l] = cx_mul(U[(int64_t)l * fb.m + ri], S[l]);
   __syncthreads();
   for (int j = threadIdx.x; j < fb.n; j += NT) {
-    double2 v = aca_entry<MODE>(a, fb.r0 + ri, fb.c0 + j);
-    for (int l = 0; l < k; l++) v = csub(v, cmul(coef[l], V[(int64_t)l * fb.n + j]));
+    T v = aca_entry<MODE, T>(a, fb.r0 + ri, fb.c0 + j);
+    for (int l = 0; l < k; l++) v = cx_sub(v, cx_mul(coef[l], V[(int64_t)l * fb.n + j]));
     dst[j] = v;
   }
   __syncthreads();
 }
 
-// argmax_i |col[i]| over i != exclude
-__device__ void argmax_abs(const double2* v, int len, int exclude, Red& red, double& best,
-                           int& bidx) {
+// argmax_i |v[i]| over i != exclude
+template <typename T>
+__device__ void argmax_abs(const T* v, int len, int exclude, Red& red, double& best, int& bidx) {
   double bv = -1.0;
   int bi = 0x7fffffff;
   for (int i = threadIdx.x; i < len; i += NT) {
-    double x = (i == exclude) ? 0.0 : sqrt(cabs2(v[i]));
+    double x = (i == exclude) ? 0.0 : sqrt(cabs2(to_d(v[i])));
     if (x > bv) {
       bv = x;
       bi = i;
@@ -156,36 +187,57 @@ __device__ void argmax_abs(const double2* v, int len, int exclude, Red& red, dou
 
 // normEstimate increment (hmatrix.cpp:570-574):
 // |alpha|^2 |row|^2 |col|^2 + sum_{l<k} 2 conj(alpha) s_l (col^H U_l)(V_l row^H)
-__device__ void norm_increment(const FarBlock& fb, const double2* U, const double2* V,
-                               const double2* S, int k, const double2* col, const double2* row,
-                               double2 alpha, Red& red, double& gain, double2& incr) {
+template <typename T>
+__device__ void norm_increment(const FarBlock& fb, const T* U, const T* V, const T* S, int k,
+                               const T* col, const T* row, double2 alpha, Red& red,
+                               double& gain, double2& incr) {
   double cn = 0, rn = 0;
-  for (int i = threadIdx.x; i < fb.m; i += NT) cn += cabs2(col[i]);
-  for (int j = threadIdx.x; j < fb.n; j += NT) rn += cabs2(row[j]);
+  for (int i = threadIdx.x; i < fb.m; i += NT) cn += cabs2(to_d(col[i]));
+  for (int j = threadIdx.x; j < fb.n; j += NT) rn += cabs2(to_d(row[j]));
   cn = block_sum(cn, red);
   rn = block_sum(rn, red);
   gain = cabs2(alpha) * rn * cn;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double2 acc = make_double2(0, 0);
   for (int l = w; l < k; l += NW) {
-    double cux = 0, cuy = 0, vrx = 0, vry = 0;
-    const double2* Ul = U + (int64_t)l * fb.m;
-    const double2* Vl = V + (int64_t)l * fb.n;
-    for (int i = lane; i < fb.m; i += 32) {
-      double2 c = col[i], u = Ul[i];  // conj(c) * u
-      cux += c.x * u.x + c.y * u.y;
-      cuy += c.x * u.y - c.y * u.x;
+    double cux, cuy, vrx, vry;
+    const T* Ul = U + (int64_t)l * fb.m;
+    const T* Vl = V + (int64_t)l * fb.n;
+    if (sizeof(T) == sizeof(float2)) {
+      // FP32 partial sums (stopping heuristic only), combined in FP64
+      float ax = 0, ay = 0, bx = 0, by = 0;
+      for (int i = lane; i < fb.m; i += 32) {
+        double2 c = to_d(col[i]), u = to_d(Ul[i]);
+        ax += (float)(c.x * u.x + c.y * u.y);
+        ay += (float)(c.x * u.y - c.y * u.x);
+      }
+      for (int j = lane; j < fb.n; j += 32) {
+        double2 v = to_d(Vl[j]), r = to_d(row[j]);
+        bx += (float)(v.x * r.x + v.y * r.y);
+        by += (float)(v.y * r.x - v.x * r.y);
+      }
+      cux = warp_sumf(ax);
+      cuy = warp_sumf(ay);
+      vrx = warp_sumf(bx);
+      vry = warp_sumf(by);
+    } else {
+      cux = cuy = vrx = vry = 0;
+      for (int i = lane; i < fb.m; i += 32) {
+        double2 c = to_d(col[i]), u = to_d(Ul[i]);  // conj(c) * u
+        cux += c.x * u.x + c.y * u.y;
+        cuy += c.x * u.y - c.y * u.x;
+      }
+      for (int j = lane; j < fb.n; j += 32) {
+        double2 v = to_d(Vl[j]), r = to_d(row[j]);  // v * conj(r)
+        vrx += v.x * r.x + v.y * r.y;
+        vry += v.y * r.x - v.x * r.y;
+      }
+      cux = warp_sum(cux);
+      cuy = warp_sum(cuy);
+      vrx = warp_sum(vrx);
+      vry = warp_sum(vry);
     }
-    for (int j = lane; j < fb.n; j += 32) {
-      double2 v = Vl[j], r = row[j];  // v * conj(r)
-      vrx += v.x * r.x + v.y * r.y;
-      vry += v.y * r.x - v.x * r.y;
-    }
-    cux = warp_sum(cux);
-    cuy = warp_sum(cuy);
-    vrx = warp_sum(vrx);
-    vry = warp_sum(vry);
-    double2 t = cmul(cmul(cconj(alpha), S[l]), cmul(make_double2(cux, cuy), make_double2(vrx, vry)));
+    double2 t = cmul(cmul(cconj(alpha), to_d(S[l])), cmul(make_double2(cux, cuy), make_double2(vrx, vry)));
     acc = cadd(acc, cscale(2.0, t));
   }
   __syncthreads();
@@ -197,9 +249,9 @@ __device__ void norm_increment(const FarBlock& fb, const double2* U, const doubl
   __syncthreads();
 }
 
-template <int MODE>
+template <int MODE, typename T>
 __global__ void __launch_bounds__(NT) aca_kernel(AcaArgs a) {
-  __shared__ double2 coef[ACA_MAX_KCAP];
+  __shared__ T coef[ACA_MAX_KCAP];
   __shared__ Red red;
   const int bi = a.order[blockIdx.x];
   const FarBlock fb = a.far[bi];
@@ -207,9 +259,9 @@ __global__ void __launch_bounds__(NT) aca_kernel(AcaArgs a) {
   int natural = min(m, n);
   if (a.max_rank > 0) natural = min(natural, a.max_rank);
   const int kmax = min(natural, fb.kcap);
-  double2* U = a.U + fb.uoff;
-  double2* V = a.V + fb.voff;
-  double2* S = a.S + fb.soff;
+  T* U = (T*)a.U + fb.uoff;
+  T* V = (T*)a.V + fb.voff;
+  T* S = (T*)a.S + fb.soff;
   const double tol = a.tol;
   int k = 0;
   double2 est = make_double2(0, 0);
@@ -218,22 +270,22 @@ __global__ void __launch_bounds__(NT) aca_kernel(AcaArgs a) {
   if (!a.extra) {
     // --- partialPivotACA ---
     int ci = (int)(pivot_hash(a.seed, (uint64_t)fb.id, 0) % (uint64_t)n);
-    residual_col<MODE>(a, fb, U, V, S, 0, ci, U, coef);  // start column into slot 0
+    residual_col<MODE, T>(a, fb, U, V, S, 0, ci, U, coef);  // start column into slot 0
     int ri = -1;
     while (k < kmax) {
-      const double2* colv = U + (int64_t)(k > 0 ? k - 1 : 0) * m;
+      const T* colv = U + (int64_t)(k > 0 ? k - 1 : 0) * m;
       double cmax;
       argmax_abs(colv, m, k >= 1 ? ri : -1, red, cmax, ri);
       if (cmax <= TINY && k >= 1) break;
-      double2* rowv = V + (int64_t)k * n;
-      residual_row<MODE>(a, fb, U, V, S, k, ri, rowv, coef);
+      T* rowv = V + (int64_t)k * n;
+      residual_row<MODE, T>(a, fb, U, V, S, k, ri, rowv, coef);
       double rmax;
       argmax_abs(rowv, n, -1, red, rmax, ci);
       if (rmax <= TINY && k >= 1) break;
-      double2* newcol = U + (int64_t)k * m;
-      residual_col<MODE>(a, fb, U, V, S, k, ci, newcol, coef);
-      double2 alpha = cdiv(make_double2(1.0, 0.0), rowv[ci]);
-      if (threadIdx.x == 0) S[k] = alpha;
+      T* newcol = U + (int64_t)k * m;
+      residual_col<MODE, T>(a, fb, U, V, S, k, ci, newcol, coef);
+      double2 alpha = cdiv(make_double2(1.0, 0.0), to_d(rowv[ci]));
+      if (threadIdx.x == 0) S[k] = from_d<T>(alpha);
       __syncthreads();
       double gain;
       double2 incr;
@@ -252,31 +304,32 @@ __global__ void __launch_bounds__(NT) aca_kernel(AcaArgs a) {
     const int npiv = a.piv_cnt[bi];
     for (int p = 0; p < npiv && k < kmax; p++) {
       int ri = piv[2 * p], ci = piv[2 * p + 1];
-      double2 pivv = aca_entry<MODE>(a, fb.r0 + ri, fb.c0 + ci);
+      double2 pivv = to_d(aca_entry<MODE, T>(a, fb.r0 + ri, fb.c0 + ci));
       double pabs = sqrt(cabs2(pivv));
       if (pabs < TINY) continue;
       // approximation already good at the seed?
       double2 approx = make_double2(0, 0);
       for (int l = 0; l < k; l++)
-        approx = cadd(approx, cmul(cmul(U[(int64_t)l * m + ri], S[l]), V[(int64_t)l * n + ci]));
+        approx = cadd(approx, cmul(cmul(to_d(U[(int64_t)l * m + ri]), to_d(S[l])),
+                                   to_d(V[(int64_t)l * n + ci])));
       if (sqrt(cabs2(cdiv(csub(pivv, approx), pivv))) < tol) continue;
-      residual_col<MODE>(a, fb, U, V, S, k, ci, U + (int64_t)k * m, coef);
+      residual_col<MODE, T>(a, fb, U, V, S, k, ci, U + (int64_t)k * m, coef);
       bool first = true;
       while (k < kmax) {
-        const double2* colv = first ? U + (int64_t)k * m : U + (int64_t)(k - 1) * m;
+        const T* colv = first ? U + (int64_t)k * m : U + (int64_t)(k - 1) * m;
         double cmax;
         argmax_abs(colv, m, first ? -1 : ri, red, cmax, ri);
         first = false;
         if (cmax <= TINY && k >= 1) break;
-        double2* rowv = V + (int64_t)k * n;
-        residual_row<MODE>(a, fb, U, V, S, k, ri, rowv, coef);
+        T* rowv = V + (int64_t)k * n;
+        residual_row<MODE, T>(a, fb, U, V, S, k, ri, rowv, coef);
         double rmax;
         argmax_abs(rowv, n, -1, red, rmax, ci);
         if (rmax <= TINY && k >= 1) break;
-        double2* newcol = U + (int64_t)k * m;
-        residual_col<MODE>(a, fb, U, V, S, k, ci, newcol, coef);
-        double2 alpha = cdiv(make_double2(1.0, 0.0), rowv[ci]);
-        if (threadIdx.x == 0) S[k] = alpha;
+        T* newcol = U + (int64_t)k * m;
+        residual_col<MODE, T>(a, fb, U, V, S, k, ci, newcol, coef);
+        double2 alpha = cdiv(make_double2(1.0, 0.0), to_d(rowv[ci]));
+        if (threadIdx.x == 0) S[k] = from_d<T>(alpha);
         __syncthreads();
         double gain;
         double2 incr;
@@ -306,10 +359,14 @@ __global__ void __launch_bounds__(NT) aca_kernel(AcaArgs a) {
 
 void launch_aca(const AcaArgs& a, cudaStream_t s) {
   if (a.nfar <= 0) return;
-  if (a.mode == 0)
-    aca_kernel<0><<<(unsigned)a.nfar, NT, 0, s>>>(a);
-  else
-    aca_kernel<1><<<(unsigned)a.nfar, NT, 0, s>>>(a);
+  const unsigned g = (unsigned)a.nfar;
+  if (a.precision == 0) {
+    if (a.mode == 0) aca_kernel<0, double2><<<g, NT, 0, s>>>(a);
+    else aca_kernel<1, double2><<<g, NT, 0, s>>>(a);
+  } else {
+    if (a.mode == 0) aca_kernel<0, float2><<<g, NT, 0, s>>>(a);
+    else aca_kernel<1, float2><<<g, NT, 0, s>>>(a);
+  }
 }
 
 }  // namespace bemgpu

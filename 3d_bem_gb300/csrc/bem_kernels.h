@@ -34,7 +34,9 @@ struct LeafRows {
 };
 
 struct NearfieldArgs {
+  int precision;  // 0: complex FP64 output, 1: complex FP32 output (FP32 regular rule)
   const Elem* E;
+  const ElemF* EF;
   const BcCoef* bc;
   const NearBlock* blocks;
   const NearTile* tiles;
@@ -46,13 +48,15 @@ struct NearfieldArgs {
   int64_t nspecial;
   double k;
   double2 alpha;
-  double2* phi;
-  double2* dphi;
+  void* phi;   // double2 or float2 per precision
+  void* dphi;
 };
 
 struct AcaArgs {
-  int mode;  // 0 = BEM entries, 1 = point-cloud Helmholtz kernel (tests)
+  int mode;       // 0 = BEM entries, 1 = point-cloud Helmholtz kernel (tests)
+  int precision;  // 0: complex FP64, 1: complex FP32 storage + FP32 regular rule
   const Elem* E;
+  const ElemF* EF;
   const BcCoef* bc;
   double k;
   double near_r;
@@ -63,9 +67,9 @@ struct AcaArgs {
   const FarBlock* far;
   const int32_t* order;
   int64_t nfar;
-  double2* U;
-  double2* V;
-  double2* S;
+  void* U;
+  void* V;
+  void* S;
   int32_t* rank;
   int32_t* flags;
   double tol;
@@ -79,6 +83,7 @@ struct AcaArgs {
 
 struct HmvArgs {
   int precision;  // 0: double2 storage, 1: float2 storage
+  int fp32_math;  // float2 storage only: FP32 products within a block, FP64 across blocks
   int nrhs;
   const FarBlock* far;
   const int32_t* rank;

@@ -18,6 +18,17 @@ struct __align__(16) Elem {
   double area;
 };
 
+// FP32 companion of Elem for the mixed-precision rules: vertices relative to
+// the element's own centroid (small numbers, so FP32 keeps ~7 digits of the
+// local geometry), unit normal and area. The centroid itself stays FP64 in
+// Elem; pair differences c_i - c_j are formed in FP64 and then rounded.
+struct __align__(16) ElemF {
+  float v[9];    // node1 - c, node2 - c, node3 - c
+  float nrm[3];
+  float area;
+  float pad[3];
+};
+
 // Rule tables: 16-point triangle rule (order 8), 5-point Gauss-Legendre
 // (near-singular rule), positive half of the 32-point Gauss-Legendre rule
 // (singular rule). Values: trianglequadraturerules.cpp:91-110,
@@ -26,6 +37,7 @@ struct QuadRules {
   double reg_x1[16], reg_x2[16], reg_w[16];
   double line_x[5], line_w[5];
   double gl_x[16], gl_w[16];
+  float freg_x1[16], freg_x2[16], freg_w[16];
 };
 
 // Per-column Robin data after the substitution rule |a| < |b|
@@ -36,6 +48,8 @@ struct BcCoef {
   double2 ratio;
   int subst;
   int pad;
+  float2 finv_main;  // FP32 copies for the mixed-precision kernels
+  float2 fratio;
 };
 
 // Dense near-field block (column-major m x n at data offset `off`, complex).

@@ -70,20 +70,24 @@ struct DBuf {
   }
 };
 
+// One H-matrix: near-field entries F, low-rank factors U, V and s, stored as
+// complex FP64 (16 bytes) or complex FP32 (8 bytes) per the precision mode.
 struct DevHM {
-  DBuf<double2> F, U, V, S;
+  DBuf<unsigned char> F, U, V, S;
   DBuf<int32_t> rank, flags;
   std::vector<int32_t> h_rank, h_flags;
+  int prec = 0;
   bool assembled = false;
 };
 
 struct GmresWS {
   int64_t N = 0;
   int R = 0, m = 0;
-  DBuf<double2> Vb, w, H, g, cs, sn, h, y, cpart, bcopy;
+  DBuf<double2> Vb, w, H, g, cs, sn, h, y, cpart, bcopy, r, d;
   DBuf<double> npart, hnorm;
   DBuf<GmresState> st;
   std::vector<GmresState> hst;
+  std::vector<double> hpart;
 };
 
 }  // namespace
@@ -101,6 +105,7 @@ struct bem_handle {
   double avgdim = 0, near_r = 0;
   Layout L;
   DBuf<Elem> dE;
+  DBuf<ElemF> dEF;
   DBuf<NearBlock> dNear;
   DBuf<FarBlock> dFar;
   DBuf<int32_t> dOrder, dSpRow, dSpCol, dListOff, dList, dPivCnt, dPivRc;
@@ -180,14 +185,36 @@ void upload_layout(bem_handle* h) {
   for (auto& m : h->hm) m.assembled = false;
 }
 
+// storage precision of the matrices: point clouds (test kernel) stay FP64
+int storage_prec(const bem_handle* h) { return h->points_mode ? 0 : h->cfg.precision; }
+
 void alloc_hm(bem_handle* h, DevHM& m) {
   const Layout& L = h->L;
-  m.F.ensure(L.near_entries);
-  m.U.ensure(L.u_size);
-  m.V.ensure(L.v_size);
-  m.S.ensure(L.s_size);
+  m.prec = storage_prec(h);
+  const size_t es = m.prec ? sizeof(float2) : sizeof(double2);
+  m.F.ensure(L.near_entries * es);
+  m.U.ensure(L.u_size * es);
+  m.V.ensure(L.v_size * es);
+  m.S.ensure(L.s_size * es);
   m.rank.ensure(L.far.size());
   m.flags.ensure(L.far.size());
+}
+
+std::vector<ElemF> make_elemf(const std::vector<Elem>& E) {
+  std::vector<ElemF> F(E.size());
+  for (size_t i = 0; i < E.size(); i++) {
+    const Elem& e = E[i];
+    ElemF f{};
+    for (int d = 0; d < 3; d++) {
+      f.v[d] = (float)(e.n1[d] - e.c[d]);
+      f.v[3 + d] = (float)(e.n2[d] - e.c[d]);
+      f.v[6 + d] = (float)(e.n3[d] - e.c[d]);
+      f.nrm[d] = (float)e.nrm[d];
+    }
+    f.area = (float)e.area;
+    F[i] = f;
+  }
+  return F;
 }
 
 void set_frequency(bem_handle* h, double k) {
@@ -203,6 +230,8 @@ void set_frequency(bem_handle* h, double k) {
     cplx ratio = c.subst ? a / b : b / a;
     c.inv_main = make_double2(inv.real(), inv.imag());
     c.ratio = make_double2(ratio.real(), ratio.imag());
+    c.finv_main = make_float2((float)inv.real(), (float)inv.imag());
+    c.fratio = make_float2((float)ratio.real(), (float)ratio.imag());
     bc[i] = c;
     av[i] = make_double2(a.real(), a.imag());
     bv[i] = make_double2(b.real(), b.imag());
@@ -230,7 +259,9 @@ void fetch_ranks(bem_handle* h, DevHM& m) {
 AcaArgs aca_args(bem_handle* h, DevHM& m, int which, int extra) {
   AcaArgs a{};
   a.mode = h->points_mode ? 1 : 0;
+  a.precision = m.prec;
   a.E = h->dE.p;
+  a.EF = h->dEF.p;
   a.bc = h->dBc.p;
   a.k = h->k;
   a.near_r = h->near_r;
@@ -267,7 +298,9 @@ void assemble(bem_handle* h, double freq, double* t_near, double* t_aca) {
   cudaStream_t s = h->stream;
   cplx al = coupling_parameter(h->cfg.coupling, k);
   NearfieldArgs na{};
+  na.precision = h->hm[0].prec;
   na.E = h->dE.p;
+  na.EF = h->dEF.p;
   na.bc = h->dBc.p;
   na.blocks = h->dNear.p;
   na.tiles = h->dTiles.p;
@@ -296,7 +329,10 @@ void assemble(bem_handle* h, double freq, double* t_near, double* t_aca) {
   if (t_aca) *t_aca = elapsed(h->ev[1], h->ev[2]);
 }
 
-void hmatvec_dev(bem_handle* h, int which, const double2* x, double2* y, int64_t R, int acc) {
+// y = (acc ? y : 0) + H x. f32: FP32 products within blocks (complex-FP32
+// storage only); otherwise FP64 arithmetic on the stored entries.
+void hmatvec_dev(bem_handle* h, int which, const double2* x, double2* y, int64_t R, int acc,
+                 bool f32 = false) {
   require(which == 0 || which == 1, BEM_EINVAL, "which must be 0 (phi) or 1 (dPhi)");
   DevHM& m = h->hm[which];
   require(m.assembled, BEM_EINVAL, "matrix not assembled");
@@ -305,7 +341,8 @@ void hmatvec_dev(bem_handle* h, int which, const double2* x, double2* y, int64_t
   h->dT.ensure(std::max<int64_t>(h->L.s_size, 1) * 8);
   for (int64_t r0 = 0; r0 < R; r0 += 8) {
     HmvArgs a{};
-    a.precision = 0;
+    a.precision = m.prec;
+    a.fp32_math = (f32 && m.prec == 1) ? 1 : 0;
     a.nrhs = (int)std::min<int64_t>(8, R - r0);
     a.far = h->dFar.p;
     a.rank = m.rank.p;
@@ -388,28 +425,35 @@ bool read_states(bem_handle* h) {
   return true;
 }
 
-// Restarted GMRES for R right-hand sides on the dPhi matrix (device b, x).
-void gmres_dev(bem_handle* h, const double2* b, double2* x, int R, bem_solve_info* info) {
-  require(h->hm[1].assembled, BEM_EINVAL, "system matrix not assembled");
+struct GmresResult {
+  int64_t iters = 0;
+  double resid = 0;
+  bool converged = false;
+};
+
+// Restarted GMRES for R right-hand sides on the dPhi matrix (device b, x;
+// x holds the initial guess). f32 selects the FP32-arithmetic operator.
+GmresResult gmres_core(bem_handle* h, const double2* b, double2* x, int R, double tol,
+                       int64_t maxit, bool f32) {
   ensure_gmres(h, R);
   GmresWS& g = h->gw;
   const int64_t N = h->N;
   cudaStream_t s = h->stream;
   KrylovArgs a = krylov_args(h, x);
+  a.tol = tol;
   CK(cudaMemcpyAsync(g.bcopy.p, b, (size_t)R * N * sizeof(double2), cudaMemcpyDeviceToDevice, s));
   CK(cudaMemcpyAsync(g.w.p, b, (size_t)R * N * sizeof(double2), cudaMemcpyDeviceToDevice, s));
   krylov_restart(a, 1, s);  // measures ||b||
   h->launches += 2;
   int64_t total = 0;
-  const int64_t maxit = h->cfg.gmres_maxit;
   while (true) {
-    hmatvec_dev(h, 1, x, g.w.p, R, 0);
+    hmatvec_dev(h, 1, x, g.w.p, R, 0, f32);
     krylov_residual(g.bcopy.p, g.w.p, (int64_t)R * N, s);
     krylov_restart(a, 0, s);
     h->launches += 3;
     if (read_states(h) || total >= maxit) break;
     for (int j = 0; j < g.m; j++) {
-      hmatvec_dev(h, 1, g.Vb.p + (int64_t)j * R * N, g.w.p, R, 0);
+      hmatvec_dev(h, 1, g.Vb.p + (int64_t)j * R * N, g.w.p, R, 0, f32);
       krylov_orthogonalize(a, j, s);
       h->launches += 9;
       total++;
@@ -423,19 +467,88 @@ void gmres_dev(bem_handle* h, const double2* b, double2* x, int R, bem_solve_inf
     h->launches += 2;
   }
   CK(cudaGetLastError());
-  if (info) {
-    int64_t it = 0;
-    double res = 0;
-    bool all = true;
-    for (const auto& st : g.hst) {
-      it = std::max<int64_t>(it, st.iters);
-      res = std::max(res, st.resid);
-      all = all && st.done;
+  GmresResult res;
+  res.converged = true;
+  for (const auto& st : g.hst) {
+    res.iters = std::max<int64_t>(res.iters, st.iters);
+    res.resid = std::max(res.resid, st.resid);
+    res.converged = res.converged && st.done;
+  }
+  return res;
+}
+
+// per-RHS 2-norms of R device vectors of length N
+std::vector<double> norms(bem_handle* h, const double2* v, int R) {
+  GmresWS& g = h->gw;
+  const int nct = krylov_num_ctas(h->N);
+  g.npart.ensure((size_t)nct * R);
+  krylov_norm_partials(v, h->N, R, g.npart.p, h->stream);
+  h->launches++;
+  g.hpart.resize((size_t)nct * R);
+  CK(cudaMemcpyAsync(g.hpart.data(), g.npart.p, g.hpart.size() * sizeof(double),
+                     cudaMemcpyDeviceToHost, h->stream));
+  sync(h);
+  std::vector<double> out(R, 0.0);
+  for (int c = 0; c < nct; c++)
+    for (int r = 0; r < R; r++) out[r] += g.hpart[(size_t)c * R + r];
+  for (auto& v2 : out) v2 = std::sqrt(v2);
+  return out;
+}
+
+// Solve dPhi x = b for R right-hand sides (device b, x; x = initial guess).
+// precision 0: GMRES with the complex-FP64 operator (GMRES::gmresSolve,
+// gmres.h:170-180). precision 1: FP64 iterative refinement -- the residual
+// b - A x uses FP64 arithmetic on the stored complex-FP32 operator, each
+// correction comes from GMRES on the FP32-arithmetic operator.
+void gmres_dev(bem_handle* h, const double2* b, double2* x, int R, bem_solve_info* info) {
+  require(h->hm[1].assembled, BEM_EINVAL, "system matrix not assembled");
+  const double tol = h->cfg.gmres_tol;
+  const int64_t maxit = h->cfg.gmres_maxit;
+  bem_solve_info loc{};
+  if (h->hm[1].prec == 0) {
+    GmresResult r = gmres_core(h, b, x, R, tol, maxit, false);
+    loc.iterations = r.iters;
+    loc.rel_residual = loc.true_residual = r.resid;
+    loc.status = r.converged ? BEM_OK : BEM_EMAXIT;
+  } else {
+    GmresWS& g = h->gw;
+    const int64_t N = h->N;
+    cudaStream_t s = h->stream;
+    ensure_gmres(h, R);
+    g.r.ensure((size_t)R * N);
+    g.d.ensure((size_t)R * N);
+    const std::vector<double> bn = norms(h, b, R);
+    int64_t total = 0;
+    double rel = 0, inner_res = 0;
+    for (int outer = 0; outer < 30; outer++) {
+      // r = b - A x with FP64 arithmetic on the stored operator
+      hmatvec_dev(h, 1, x, g.r.p, R, 0, false);
+      krylov_residual(b, g.r.p, (int64_t)R * N, s);
+      h->launches++;
+      const std::vector<double> rn = norms(h, g.r.p, R);
+      rel = 0;
+      for (int q = 0; q < R; q++) rel = std::max(rel, bn[q] > 0 ? rn[q] / bn[q] : 0.0);
+      if (rel < tol || total >= maxit) break;
+      // the correction only has to gain the missing digits, but FP32
+      // products cap what one inner solve can deliver at about 1e-6
+      const double inner_tol = std::max(1e-6, 0.3 * tol / rel);
+      CK(cudaMemsetAsync(g.d.p, 0, (size_t)R * N * sizeof(double2), s));
+      GmresResult ir = gmres_core(h, g.r.p, g.d.p, R, inner_tol, maxit - total, true);
+      total += ir.iters;
+      inner_res = ir.resid;
+      krylov_axpy(x, g.d.p, (int64_t)R * N, s);
+      h->launches++;
     }
-    info->iterations = it;
-    info->rel_residual = res;
-    info->true_residual = res;  // the loop exits right after a true-residual restart
-    info->status = all ? BEM_OK : BEM_EMAXIT;
+    loc.iterations = total;
+    loc.rel_residual = inner_res;
+    loc.true_residual = rel;
+    loc.status = rel < tol ? BEM_OK : BEM_EMAXIT;
+  }
+  if (info) {
+    info->iterations = loc.iterations;
+    info->rel_residual = loc.rel_residual;
+    info->true_residual = loc.true_residual;
+    info->status = loc.status;
   }
 }
 
@@ -543,7 +656,8 @@ bem_status bem_create(const bem_config* cfg, bem_handle** out) {
     require(h->cfg.gmres_restart >= 1 && h->cfg.gmres_maxit >= 1, BEM_EINVAL,
             "gmres_restart and gmres_maxit must be >= 1");
     require(h->cfg.coupling >= 0 && h->cfg.coupling <= 2, BEM_EINVAL, "coupling must be 0, 1 or 2");
-    require(h->cfg.precision == 0, BEM_EINVAL, "precision must be 0 (complex FP64)");
+    require(h->cfg.precision == 0 || h->cfg.precision == 1, BEM_EINVAL,
+            "precision must be 0 (complex FP64) or 1 (mixed)");
     require(h->cfg.wave_speed > 0, BEM_EINVAL, "wave_speed must be positive");
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     for (auto& e : h->ev) CK(cudaEventCreate(&e));
@@ -594,6 +708,7 @@ bem_status bem_set_mesh(bem_handle* h, const double* tri, int64_t n) {
                  h->cfg.aca_max_rank, true, h->cfg.seed, h->L);
     h->points_mode = false;
     h->dE.upload(h->E, h->stream);
+    h->dEF.upload(make_elemf(h->E), h->stream);
     h->dPerm.upload(h->rows.perm, h->stream);
     upload_layout(h);
     h->have_mesh = true;
@@ -748,26 +863,37 @@ bem_status bem_get_block(bem_handle* h, int32_t which, int64_t block, int64_t* r
     int64_t nearI = 0, farI = 0;
     for (int64_t i = 0; i < block; i++) (h->L.blocks[i].adm ? farI : nearI)++;
     const HBlockDesc& b = h->L.blocks[block];
+    const size_t es = m.prec ? sizeof(float2) : sizeof(double2);
+    // copy `cnt` stored complex numbers starting at element `off` into dst
+    // (complex FP64), widening complex-FP32 storage
+    auto fetch = [&](double* dst, const DBuf<unsigned char>& src, int64_t off, int64_t cnt) {
+      std::vector<unsigned char> tmp(cnt * es);
+      if (cnt > 0)
+        CK(cudaMemcpyAsync(tmp.data(), src.p + off * es, cnt * es, cudaMemcpyDeviceToHost, h->stream));
+      sync(h);
+      for (int64_t i = 0; i < cnt; i++) {
+        if (m.prec) {
+          const float* f = reinterpret_cast<const float*>(tmp.data()) + 2 * i;
+          dst[2 * i] = f[0];
+          dst[2 * i + 1] = f[1];
+        } else {
+          const double* d = reinterpret_cast<const double*>(tmp.data()) + 2 * i;
+          dst[2 * i] = d[0];
+          dst[2 * i + 1] = d[1];
+        }
+      }
+    };
     if (b.adm) {
       const FarBlock& fb = h->L.far[farI];
       const int k = m.h_rank[farI];
       if (rank) *rank = k;
-      for (int l = 0; l < k; l++) {
-        if (U)
-          CK(cudaMemcpyAsync(U + 2 * (int64_t)l * b.m, m.U.p + fb.uoff + (int64_t)l * b.m,
-                             b.m * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
-        if (V)
-          CK(cudaMemcpyAsync(V + 2 * (int64_t)l * b.n, m.V.p + fb.voff + (int64_t)l * b.n,
-                             b.n * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
-      }
-      if (s && k > 0)
-        CK(cudaMemcpyAsync(s, m.S.p + fb.soff, k * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+      if (U) fetch(U, m.U, fb.uoff, (int64_t)k * b.m);
+      if (V) fetch(V, m.V, fb.voff, (int64_t)k * b.n);
+      if (s) fetch(s, m.S, fb.soff, k);
     } else {
       const NearBlock& nb = h->L.near[nearI];
       if (rank) *rank = -1;
-      if (F)
-        CK(cudaMemcpyAsync(F, m.F.p + nb.off, (size_t)b.m * b.n * sizeof(double2),
-                           cudaMemcpyDeviceToHost, h->stream));
+      if (F) fetch(F, m.F, nb.off, (int64_t)b.m * b.n);
     }
     sync(h);
   });
@@ -886,8 +1012,8 @@ bem_status bem_points_assemble(bem_handle* h, const double* rowpts, int64_t nr,
     DevHM& m = h->hm[0];
     alloc_hm(h, m);
     launch_points_nearfield(h->dNear.p, (int64_t)h->L.near.size(), h->dTiles.p,
-                            (int64_t)h->L.tiles.size(), h->dRowPts.p, h->dColPts.p, k, m.F.p,
-                            h->stream);
+                            (int64_t)h->L.tiles.size(), h->dRowPts.p, h->dColPts.p, k,
+                            (double2*)m.F.p, h->stream);
     AcaArgs a = aca_args(h, m, 0, 0);
     a.mode = 1;
     launch_aca(a, h->stream);

@@ -8,6 +8,13 @@
 //   pass U: one CTA per leaf row cluster sums, for its rows, every block whose
 //           row range contains them (U_b rows . t_b and dense F_b rows . x_C).
 // Every stored matrix entry is read once per call for all R vectors.
+//
+// Arithmetic variants (GB300's FP64 rate is far below what HBM can feed):
+//   double2 storage, FP64 math  -- the plain complex-FP64 method;
+//   float2 storage,  FP64 math  -- exact products of the stored operator, used
+//                                  for the iterative-refinement residual;
+//   float2 storage,  FP32 math  -- FP32 products inside a block, FP64 sums
+//                                  across blocks; the inner GMRES operator.
 #include "bem_kernels.h"
 #include "quadrature.cuh"
 
@@ -17,8 +24,29 @@ namespace {
 constexpr int VT = 128;  // threads of a pass-V CTA
 constexpr int UT = 128;  // threads of a pass-U CTA
 
+template <typename T, bool F32> struct Acc;
+// FP64 accumulation
+template <typename T> struct Acc<T, false> {
+  double x = 0, y = 0;
+  __device__ __forceinline__ void fma(double2 a, double2 b) {
+    x += a.x * b.x - a.y * b.y;
+    y += a.x * b.y + a.y * b.x;
+  }
+};
+// FP32 accumulation
+template <typename T> struct Acc<T, true> {
+  float x = 0, y = 0;
+  __device__ __forceinline__ void fma(float2 a, float2 b) {
+    x += a.x * b.x - a.y * b.y;
+    y += a.x * b.y + a.y * b.x;
+  }
+};
+
+__device__ __forceinline__ float2 ld32(const float2* p) { return __ldg(p); }
+__device__ __forceinline__ float2 tof(double2 v) { return make_float2((float)v.x, (float)v.y); }
+
 // t[r][soff + l] = s_l * sum_j V[l, j] x[c0 + j, r]
-template <typename T, int R>
+template <typename T, bool F32, int R>
 __global__ void __launch_bounds__(VT) hmv_vpass(const FarBlock* __restrict__ far,
                                                 const int32_t* __restrict__ rank,
                                                 const T* __restrict__ Vp,
@@ -33,13 +61,35 @@ __global__ void __launch_bounds__(VT) hmv_vpass(const FarBlock* __restrict__ far
     double ax[R], ay[R];
 #pragma unroll
     for (int r = 0; r < R; r++) ax[r] = ay[r] = 0.0;
-    for (int j = lane; j < fb.n; j += 32) {
-      double2 v = load_c(Vl + j);
+    if constexpr (F32) {
+      float fx[R], fy[R];
+#pragma unroll
+      for (int r = 0; r < R; r++) fx[r] = fy[r] = 0.0f;
+#pragma unroll 4
+      for (int j = lane; j < fb.n; j += 32) {
+        const float2 v = ld32((const float2*)(Vl + j));
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+          const float2 xv = tof(x[r * ldx + fb.c0 + j]);
+          fx[r] += v.x * xv.x - v.y * xv.y;
+          fy[r] += v.x * xv.y + v.y * xv.x;
+        }
+      }
 #pragma unroll
       for (int r = 0; r < R; r++) {
-        double2 xv = x[r * ldx + fb.c0 + j];
-        ax[r] += v.x * xv.x - v.y * xv.y;
-        ay[r] += v.x * xv.y + v.y * xv.x;
+        ax[r] = fx[r];
+        ay[r] = fy[r];
+      }
+    } else {
+#pragma unroll 4
+      for (int j = lane; j < fb.n; j += 32) {
+        const double2 v = load_c(Vl + j);
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+          const double2 xv = x[r * ldx + fb.c0 + j];
+          ax[r] += v.x * xv.x - v.y * xv.y;
+          ay[r] += v.x * xv.y + v.y * xv.x;
+        }
       }
     }
 #pragma unroll
@@ -51,7 +101,7 @@ __global__ void __launch_bounds__(VT) hmv_vpass(const FarBlock* __restrict__ far
       }
     }
     if (lane == 0) {
-      double2 s = load_c(Sp + fb.soff + l);
+      const double2 s = load_c(Sp + fb.soff + l);
 #pragma unroll
       for (int r = 0; r < R; r++) t[r * ldt + fb.soff + l] = cmul(s, make_double2(ax[r], ay[r]));
     }
@@ -60,7 +110,7 @@ __global__ void __launch_bounds__(VT) hmv_vpass(const FarBlock* __restrict__ far
 
 // One CTA per leaf row cluster; warps split the leaf's block list, lanes own
 // rows (32 rows per pass).
-template <typename T, int R>
+template <typename T, bool F32, int R>
 __global__ void __launch_bounds__(UT) hmv_upass(
     const LeafRows* __restrict__ leaves, const int32_t* __restrict__ list_off,
     const int32_t* __restrict__ list, const FarBlock* __restrict__ far,
@@ -81,37 +131,51 @@ __global__ void __launch_bounds__(UT) hmv_upass(
     for (int r = 0; r < R; r++) ax[r] = ay[r] = 0.0;
     for (int e = beg + w; e < end; e += UT / 32) {
       const int32_t code = list[e];
-      if (code >= 0) {  // admissible block
+      Acc<T, F32> acc[R];
+      if (code >= 0) {  // admissible block: U rows . t
         const FarBlock fb = far[code];
         const int k = rank[code];
-        const int64_t li = grow - fb.r0;
-        const T* U = Up + fb.uoff + li;
+        const T* U = Up + fb.uoff + (grow - fb.r0);
         if (active) {
+#pragma unroll 4
           for (int l = 0; l < k; l++) {
-            double2 u = load_c(U + (int64_t)l * fb.m);
+            if constexpr (F32) {
+              const float2 u = ld32((const float2*)(U + (int64_t)l * fb.m));
 #pragma unroll
-            for (int r = 0; r < R; r++) {
-              double2 tv = t[r * ldt + fb.soff + l];
-              ax[r] += u.x * tv.x - u.y * tv.y;
-              ay[r] += u.x * tv.y + u.y * tv.x;
+              for (int r = 0; r < R; r++)
+                acc[r].fma(u, tof(t[r * ldt + fb.soff + l]));
+            } else {
+              const double2 u = load_c(U + (int64_t)l * fb.m);
+#pragma unroll
+              for (int r = 0; r < R; r++)
+                acc[r].fma(u, t[r * ldt + fb.soff + l]);
             }
           }
         }
-      } else {  // dense near-field block
+      } else {  // dense near-field block: F rows . x
         const NearBlock nb = nearb[-code - 1];
-        const int64_t li = grow - nb.r0;
-        const T* Fb = F + nb.off + li;
+        const T* Fb = F + nb.off + (grow - nb.r0);
         if (active) {
+#pragma unroll 4
           for (int j = 0; j < nb.n; j++) {
-            double2 f = load_c(Fb + (int64_t)j * nb.m);
+            if constexpr (F32) {
+              const float2 f = ld32((const float2*)(Fb + (int64_t)j * nb.m));
 #pragma unroll
-            for (int r = 0; r < R; r++) {
-              double2 xv = x[r * ldx + nb.c0 + j];
-              ax[r] += f.x * xv.x - f.y * xv.y;
-              ay[r] += f.x * xv.y + f.y * xv.x;
+              for (int r = 0; r < R; r++)
+                acc[r].fma(f, tof(x[r * ldx + nb.c0 + j]));
+            } else {
+              const double2 f = load_c(Fb + (int64_t)j * nb.m);
+#pragma unroll
+              for (int r = 0; r < R; r++)
+                acc[r].fma(f, x[r * ldx + nb.c0 + j]);
             }
           }
         }
+      }
+#pragma unroll
+      for (int r = 0; r < R; r++) {  // block partial into the FP64 row sum
+        ax[r] += (double)acc[r].x;
+        ay[r] += (double)acc[r].y;
       }
     }
 #pragma unroll
@@ -131,35 +195,36 @@ __global__ void __launch_bounds__(UT) hmv_upass(
   }
 }
 
-template <typename T, int R>
+template <typename T, bool F32, int R>
 void launch_r(const HmvArgs& a, cudaStream_t s) {
   if (a.nfar > 0)
-    hmv_vpass<T, R><<<(unsigned)a.nfar, VT, 0, s>>>(a.far, a.rank, (const T*)a.V, (const T*)a.S,
-                                                    a.x, a.ldx, a.t, a.ldt);
+    hmv_vpass<T, F32, R><<<(unsigned)a.nfar, VT, 0, s>>>(a.far, a.rank, (const T*)a.V,
+                                                         (const T*)a.S, a.x, a.ldx, a.t, a.ldt);
   if (a.nleaves > 0)
-    hmv_upass<T, R><<<(unsigned)a.nleaves, UT, 0, s>>>(
+    hmv_upass<T, F32, R><<<(unsigned)a.nleaves, UT, 0, s>>>(
         a.leaves, a.list_off, a.list, a.far, a.rank, a.nearb, (const T*)a.U, (const T*)a.F, a.x,
         a.ldx, a.t, a.ldt, a.y, a.ldy, a.accumulate);
 }
 
-template <typename T>
+template <typename T, bool F32>
 void launch_t(const HmvArgs& a, cudaStream_t s) {
   switch (a.nrhs) {
-    case 1: launch_r<T, 1>(a, s); break;
-    case 2: launch_r<T, 2>(a, s); break;
-    case 3: launch_r<T, 3>(a, s); break;
-    case 4: launch_r<T, 4>(a, s); break;
-    case 5: launch_r<T, 5>(a, s); break;
-    case 6: launch_r<T, 6>(a, s); break;
-    case 7: launch_r<T, 7>(a, s); break;
-    default: launch_r<T, 8>(a, s); break;  // the runtime splits R > 8 into chunks of 8
+    case 1: launch_r<T, F32, 1>(a, s); break;
+    case 2: launch_r<T, F32, 2>(a, s); break;
+    case 3: launch_r<T, F32, 3>(a, s); break;
+    case 4: launch_r<T, F32, 4>(a, s); break;
+    case 5: launch_r<T, F32, 5>(a, s); break;
+    case 6: launch_r<T, F32, 6>(a, s); break;
+    case 7: launch_r<T, F32, 7>(a, s); break;
+    default: launch_r<T, F32, 8>(a, s); break;  // the runtime splits R > 8 into chunks of 8
   }
 }
 }  // namespace
 
 void launch_hmatvec(const HmvArgs& a, cudaStream_t s) {
-  if (a.precision == 0) launch_t<double2>(a, s);
-  else launch_t<float2>(a, s);
+  if (a.precision == 0) launch_t<double2, false>(a, s);
+  else if (a.fp32_math) launch_t<float2, true>(a, s);
+  else launch_t<float2, false>(a, s);
 }
 
 }  // namespace bemgpu

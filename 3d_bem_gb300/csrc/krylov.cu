@@ -205,6 +205,13 @@ __global__ void __launch_bounds__(DT) update_x_kernel(const double2* __restrict_
   x[(int64_t)r * N + i] = acc;
 }
 
+__global__ void __launch_bounds__(DT) add_kernel(double2* __restrict__ x,
+                                                 const double2* __restrict__ d, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * DT + threadIdx.x;
+  if (i >= n) return;
+  x[i] = cadd(x[i], d[i]);
+}
+
 // r = b - w (stored into w), per RHS
 __global__ void __launch_bounds__(DT) residual_kernel(const double2* __restrict__ b,
                                                       double2* __restrict__ w, int64_t n) {
@@ -287,6 +294,16 @@ void krylov_restart(const KrylovArgs& a, int init, cudaStream_t s) {
     dim3 g((unsigned)((a.N + DT - 1) / DT), (unsigned)a.R);
     copy_scale_kernel<<<g, DT, 0, s>>>(a.w, a.Vb, a.N, a.hnorm);
   }
+}
+
+void krylov_axpy(double2* x, const double2* d, int64_t n, cudaStream_t s) {
+  add_kernel<<<(unsigned)((n + DT - 1) / DT), DT, 0, s>>>(x, d, n);
+}
+
+void krylov_norm_partials(const double2* v, int64_t N, int R, double* partial, cudaStream_t s) {
+  const int nct = krylov_num_ctas(N);
+  const int64_t chunk = (N + nct - 1) / nct;
+  nrm_partial_kernel<<<nct, DT, 0, s>>>(v, N, R, chunk, partial);
 }
 
 void krylov_residual(const double2* b, double2* w, int64_t n, cudaStream_t s) {

@@ -39,6 +39,10 @@ int krylov_num_ctas(int64_t N);
 void krylov_orthogonalize(const KrylovArgs& a, int j, cudaStream_t s);
 void krylov_restart(const KrylovArgs& a, int init, cudaStream_t s);
 void krylov_residual(const double2* b, double2* w, int64_t n, cudaStream_t s);
+// partial[cta][r] = squared norm of v[r] over the CTA's chunk (krylov_num_ctas CTAs)
+void krylov_norm_partials(const double2* v, int64_t N, int R, double* partial, cudaStream_t s);
+// x[i] += d[i]
+void krylov_axpy(double2* x, const double2* d, int64_t n, cudaStream_t s);
 void krylov_update(const KrylovArgs& a, cudaStream_t s);
 
 }  // namespace bemgpu

@@ -21,6 +21,11 @@ void nearfield_upload_rules(const QuadRules& r, cudaStream_t s) {
   cudaMemcpyToSymbolAsync(c_rules, &r, sizeof(QuadRules), 0, cudaMemcpyHostToDevice, s);
 }
 
+__device__ __forceinline__ void store(double2* p, int64_t g, double2 v) { p[g] = v; }
+__device__ __forceinline__ void store(float2* p, int64_t g, double2 v) {
+  p[g] = make_float2((float)v.x, (float)v.y);
+}
+
 // Regular entries of all near-field blocks; entries the host classified as
 // special (flag bit set) are left to nearfield_special.
 __global__ void __launch_bounds__(256) nearfield_regular_kernel(
@@ -43,13 +48,36 @@ __global__ void __launch_bounds__(256) nearfield_regular_kernel(
   dphi[g] = d;
 }
 
+// Mixed precision: the same entries with the FP32 regular rule, stored as
+// complex FP32.
+__global__ void __launch_bounds__(256) nearfield_regular32_kernel(
+    const Elem* __restrict__ E, const ElemF* __restrict__ EF, const BcCoef* __restrict__ bc,
+    const NearBlock* __restrict__ blocks, const NearTile* __restrict__ tiles,
+    const uint32_t* __restrict__ special_bits, float k, float2 alpha, float2* __restrict__ phi,
+    float2* __restrict__ dphi) {
+  const NearTile t = tiles[blockIdx.x];
+  if ((int)threadIdx.x >= t.count) return;
+  const NearBlock b = blocks[t.block];
+  const int e = t.first + threadIdx.x;
+  const int64_t g = b.off + e;
+  if (special_bits[g >> 5] & (1u << (g & 31))) return;
+  const int r = e % b.m, c = e / b.m;
+  const int64_t row = b.r0 + r, col = b.c0 + c;
+  OpsF o = ops_regular32(E, EF, row, col, k, c_rules);
+  float2 p, d;
+  substitute32(o, bc[col], alpha, p, d);
+  phi[g] = p;
+  dphi[g] = d;
+}
+
 // Special entries: (global entry index, row, col) triples sorted so that the
-// singular (row == col) ones come first.
+// singular (row == col) ones come first. Always FP64 arithmetic.
+template <typename T>
 __global__ void __launch_bounds__(128) nearfield_special_kernel(
     const Elem* __restrict__ E, const BcCoef* __restrict__ bc,
     const int64_t* __restrict__ sp_entry, const int32_t* __restrict__ sp_row,
     const int32_t* __restrict__ sp_col, int64_t count, double k, double2 alpha,
-    double2* __restrict__ phi, double2* __restrict__ dphi) {
+    T* __restrict__ phi, T* __restrict__ dphi) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
   const int64_t row = sp_row[i], col = sp_col[i];
@@ -58,8 +86,8 @@ __global__ void __launch_bounds__(128) nearfield_special_kernel(
   double2 p, d;
   substitute(o, row == col, bc[col], alpha, p, d);
   const int64_t g = sp_entry[i];
-  phi[g] = p;
-  dphi[g] = d;
+  store(phi, g, p);
+  store(dphi, g, d);
 }
 
 // Raw operators L, M, Mt, N for arbitrary pairs (reference BemOperatorsConst,
@@ -113,13 +141,25 @@ void launch_points_nearfield(const NearBlock* blocks, int64_t nblocks, const Nea
 }
 
 void launch_nearfield(const NearfieldArgs& a, cudaStream_t s) {
-  if (a.ntiles > 0)
-    nearfield_regular_kernel<<<(unsigned)a.ntiles, 256, 0, s>>>(
-        a.E, a.bc, a.blocks, a.tiles, a.special_bits, a.k, a.alpha, a.phi, a.dphi);
-  if (a.nspecial > 0) {
-    unsigned g = (unsigned)((a.nspecial + 127) / 128);
-    nearfield_special_kernel<<<g, 128, 0, s>>>(a.E, a.bc, a.sp_entry, a.sp_row, a.sp_col,
-                                               a.nspecial, a.k, a.alpha, a.phi, a.dphi);
+  const unsigned g = (unsigned)((a.nspecial + 127) / 128);
+  if (a.precision == 0) {
+    if (a.ntiles > 0)
+      nearfield_regular_kernel<<<(unsigned)a.ntiles, 256, 0, s>>>(
+          a.E, a.bc, a.blocks, a.tiles, a.special_bits, a.k, a.alpha, (double2*)a.phi,
+          (double2*)a.dphi);
+    if (a.nspecial > 0)
+      nearfield_special_kernel<double2><<<g, 128, 0, s>>>(a.E, a.bc, a.sp_entry, a.sp_row,
+                                                          a.sp_col, a.nspecial, a.k, a.alpha,
+                                                          (double2*)a.phi, (double2*)a.dphi);
+  } else {
+    if (a.ntiles > 0)
+      nearfield_regular32_kernel<<<(unsigned)a.ntiles, 256, 0, s>>>(
+          a.E, a.EF, a.bc, a.blocks, a.tiles, a.special_bits, (float)a.k,
+          make_float2((float)a.alpha.x, (float)a.alpha.y), (float2*)a.phi, (float2*)a.dphi);
+    if (a.nspecial > 0)
+      nearfield_special_kernel<float2><<<g, 128, 0, s>>>(a.E, a.bc, a.sp_entry, a.sp_row,
+                                                         a.sp_col, a.nspecial, a.k, a.alpha,
+                                                         (float2*)a.phi, (float2*)a.dphi);
   }
 }
 

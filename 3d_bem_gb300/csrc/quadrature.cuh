@@ -348,6 +348,91 @@ __device__ __forceinline__ Ops ops_eval(const Elem* __restrict__ E, int64_t row,
   return ops_regular(P, Q, k, R);
 }
 
+// ----- FP32 regular rule (mixed precision) -----
+__host__ __device__ __forceinline__ float2 fmk(float r, float i) { return make_float2(r, i); }
+__host__ __device__ __forceinline__ float2 fadd(float2 a, float2 b) { return fmk(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ float2 fsub(float2 a, float2 b) { return fmk(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ float2 fmul(float2 a, float2 b) {
+  return fmk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+struct OpsF {
+  float2 L, M, Mt, N;
+};
+
+// Same integrand and 16-point rule as ops_regular, evaluated in FP32. The
+// centroid difference c_p - c_q is formed in FP64 and rounded once; source
+// points are offsets from c_q, so r = |p - q| keeps ~7 significant digits
+// even for neighbouring panels.
+__device__ __forceinline__ OpsF ops_regular32(const Elem* __restrict__ E,
+                                              const ElemF* __restrict__ EF, int64_t row,
+                                              int64_t col, float k, const QuadRules& R) {
+  const float dx = (float)(E[row].c[0] - E[col].c[0]);
+  const float dy = (float)(E[row].c[1] - E[col].c[1]);
+  const float dz = (float)(E[row].c[2] - E[col].c[2]);
+  const ElemF& Q = EF[col];
+  const float npx = EF[row].nrm[0], npy = EF[row].nrm[1], npz = EF[row].nrm[2];
+  const float nqx = Q.nrm[0], nqy = Q.nrm[1], nqz = Q.nrm[2];
+  const float upNq = npx * nqx + npy * nqy + npz * nqz;
+  const float inv4pi = 0.0795774715459476679f;
+  float Lx = 0, Ly = 0, Mx = 0, My = 0, Tx = 0, Ty = 0, Nx = 0, Ny = 0;
+#pragma unroll
+  for (int i = 0; i < 16; i++) {
+    const float a1 = R.freg_x1[i], a2 = R.freg_x2[i], a3 = 1.0f - a2 - a1, w = R.freg_w[i];
+    const float rx = dx - (a1 * Q.v[0] + a2 * Q.v[3] + a3 * Q.v[6]);
+    const float ry = dy - (a1 * Q.v[1] + a2 * Q.v[4] + a3 * Q.v[7]);
+    const float rz = dz - (a1 * Q.v[2] + a2 * Q.v[5] + a3 * Q.v[8]);
+    const float rr = rx * rx + ry * ry + rz * rz;
+    const float ir = rsqrtf(rr);
+    const float r = rr * ir;
+    const float rnq = -(rx * nqx + ry * nqy + rz * nqz) * ir;
+    const float rnp = (rx * npx + ry * npy + rz * npz) * ir;
+    const float kr = k * r;
+    float s, c;
+    sincosf(kr, &s, &c);
+    const float g0 = ir * inv4pi;
+    const float Gx = c * g0, Gy = s * g0;
+    const float Grx = Gx * ir, Gry = Gy * ir;
+    const float dGx = -Grx - kr * Gry, dGy = -Gry + kr * Grx;
+    const float Grrx = Grx * ir, Grry = Gry * ir;
+    const float a2c = 2.0f - kr * kr, b2c = -2.0f * kr;
+    const float d2Gx = Grrx * a2c - Grry * b2c, d2Gy = Grrx * b2c + Grry * a2c;
+    Lx += w * Gx;
+    Ly += w * Gy;
+    const float wm = w * rnq, wt = w * rnp;
+    Mx += wm * dGx;
+    My += wm * dGy;
+    Tx += wt * dGx;
+    Ty += wt * dGy;
+    const float f1 = -(upNq + rnp * rnq) * ir, f2 = rnp * rnq;
+    Nx += w * (f1 * dGx + f2 * d2Gx);
+    Ny += w * (f1 * dGy + f2 * d2Gy);
+  }
+  const float A = Q.area;
+  OpsF o;
+  o.L = fmk(A * Lx, A * Ly);
+  o.M = fmk(A * Mx, A * My);
+  o.Mt = fmk(A * Tx, A * Ty);
+  o.N = fmk(A * Nx, A * Ny);
+  return o;
+}
+
+// FP32 BC substitution for off-diagonal regular entries (no jump terms).
+__device__ __forceinline__ void substitute32(const OpsF& o, const BcCoef& bc, float2 alpha,
+                                             float2& phi, float2& dphi) {
+  const float2 X = fadd(o.L, fmul(alpha, o.Mt));
+  const float2 Y = fadd(o.M, fmul(alpha, o.N));
+  if (bc.subst) {
+    const float2 t = fmul(X, bc.finv_main);
+    phi = fmk(-t.x, -t.y);
+    const float2 u = fmul(bc.fratio, X);
+    dphi = fmk(-u.x - Y.x, -u.y - Y.y);
+  } else {
+    phi = fmul(Y, bc.finv_main);
+    dphi = fadd(X, fmul(bc.fratio, Y));
+  }
+}
+
 // BC substitution of implicitPhiMatrix2 / implicitDPhiMatrix2 (:2004-2040).
 // bc[col] holds a, b, b/a or a/b and the substitution flag.
 __device__ __forceinline__ void substitute(const Ops& o, bool diag, const BcCoef& bc,

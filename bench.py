@@ -4,13 +4,21 @@
 Workload (the configuration the headline metric is quoted on): pulsating
 sphere, radius 1 m, icosphere with 20,480 flat triangles, uniform normal
 velocity (a = 0, b = 1, g = 1), c = 343 m/s, rho = 1.2, f = 1.5 kHz, leaf 32,
-eta = 2, ACA tol 1e-5, GMRES tol 1e-10, Kirkup coupling, complex FP64.
+eta = 2, ACA tol 1e-5, GMRES tol 1e-10, Kirkup coupling.
 
 A step is one complete frequency solve: near-field quadrature, ACA assembly of
 both H-matrices, right-hand side, GMRES, BC back-substitution and pressure.
-Consecutive steps use distinct frequencies 1500 * (1 + 0.002 i) Hz so nothing
-is reused between steps; every step's working set (GBs of H-matrix data) is
-far larger than the 129 MB L2, so no explicit flush is needed.
+Consecutive steps use distinct frequencies 1500 (1 + 1e-4 i) Hz so nothing is
+reused between steps; every step's working set (the H-matrices, GBs) is far
+larger than the 129 MB L2, so no explicit flush is needed.
+
+Two arms of the same method run on the GPU:
+  mixed (headline) -- FP32 regular quadrature with FP64-formed centroid
+      differences, FP64 singular/near-singular rules, complex-FP32 storage,
+      FP32-arithmetic inner GMRES inside FP64 iterative refinement;
+  plain            -- complex FP64 throughout.
+The line reports the mixed arm; the plain arm's rate and the relative surface-
+pressure difference between the two ride along.
 
   value : freq-solves/s with g resident in GPU memory (bem_solve_device)
   e2e   : freq-solves/s through bem_solve with host buffers (g copied in, p
@@ -39,16 +47,20 @@ sys.path.insert(0, ROOT)
 FREQ = 1500.0
 C0, RHO = 343.0, 1.2
 ACA_TOL, GMRES_TOL = 1e-5, 1e-10
-SUBDIV = 5  # 20 * 4**5 = 20,480 triangles
+WORKLOADS = {
+    # name: (icosphere subdivisions, description)
+    "sphere20k": (5, "pulsating sphere r=1 m, icosphere 20,480 triangles, f=1.5 kHz"),
+    "sphere5k": (4, "pulsating sphere r=1 m, icosphere 5,120 triangles, f=1.5 kHz (profiling case)"),
+}
 METRIC = "freq-solves/sec (H-matrix Helmholtz BEM solve, <=1e-5 rel. surface-pressure error)"
 UNIT = "freq-solves/s"
 
 
-def workload_config(extra=None):
-    cfg = {"workload": "pulsating sphere r=1 m, icosphere 20,480 triangles, f=1.5 kHz",
-           "n_elements": 20480, "freq_hz": FREQ, "aca_tol": ACA_TOL, "gmres_tol": GMRES_TOL,
-           "leaf_size": 32, "eta": 2.0, "coupling": "Kirkup", "bc": "Neumann v=1",
-           "nrhs": 1, "precision": "complex fp64",
+def workload_config(name, extra=None):
+    sub, desc = WORKLOADS[name]
+    cfg = {"workload": desc, "n_elements": 20 * 4 ** sub, "freq_hz": FREQ, "aca_tol": ACA_TOL,
+           "gmres_tol": GMRES_TOL, "leaf_size": 32, "eta": 2.0, "coupling": "Kirkup",
+           "bc": "Neumann v=1", "nrhs": 1,
            "l2": "working set (H-matrix, GBs) >> 129 MB L2; no flush needed"}
     if extra:
         cfg.update(extra)
@@ -56,7 +68,8 @@ def workload_config(extra=None):
 
 
 def freqs(count, offset=0):
-    return [FREQ * (1.0 + 0.002 * (offset + i)) for i in range(count)]
+    """Distinct frequencies near 1.5 kHz (index i -> 1500 (1 + 1e-4 i))."""
+    return [FREQ * (1.0 + 1e-4 * (offset + i)) for i in range(count)]
 
 
 class Clocks:
@@ -117,17 +130,74 @@ def dist_env():
     return ws, rank, local
 
 
-def matvec_bytes(info, ranks, n, R=1, elem=16):
-    """Algorithmic bytes of one H-matvec: stored entries once, plus each
-    block's x segment and the y read-modify-write per block row."""
+def matvec_bytes(info, ranks, n, elem, R=1):
+    """Algorithmic bytes of one H-matvec: stored entries once (near-field
+    m*n, low-rank (m+n)*k + k), plus each block's x segment and y once."""
     near = info[:, 4] == 0
     far = ~near
     m, nn = info[:, 1], info[:, 3]
     k = np.where(far, ranks, 0)
     mat = (m[near] * nn[near]).sum() * elem + ((m[far] + nn[far]) * k[far]).sum() * elem \
         + k[far].sum() * elem
-    vec = R * (nn.sum() * elem + 2 * n * elem)
+    vec = R * (nn.sum() * 16 + 2 * n * 16)
     return int(mat + vec)
+
+
+def make_solver(pkg, meshes, sub, precision):
+    tri = meshes.icosphere(sub, 1.0)
+    n = tri.shape[0]
+    s = pkg.Solver(aca_tol=ACA_TOL, gmres_tol=GMRES_TOL, wave_speed=C0, density=RHO,
+                   precision=precision)
+    s.set_mesh(tri)
+    s.set_bc(np.zeros(n), np.ones(n))
+    return s, n
+
+
+def timed_arm(torch, pkg, s, n, args, ws):
+    """W warm-up solves, then K timed solves bracketed by barrier + sync;
+    returns (ms, infos, p of the last solve, launches)."""
+    stream = torch.cuda.ExternalStream(pkg.lib().bem_stream(s._h))
+    g = torch.ones(n, dtype=torch.complex128, device="cuda")
+    p = torch.zeros(n, dtype=torch.complex128, device="cuda")
+    for f in freqs(args.warmup, -args.warmup - 1):
+        s.solve_device(f, g.data_ptr(), 1, 0, 0, p.data_ptr())
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    l0 = s.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    infos = []
+    e0.record(stream)
+    for f in freqs(args.steps, 0):
+        infos.append(s.solve_device(f, g.data_ptr(), 1, 0, 0, p.data_ptr()))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    ms = e0.elapsed_time(e1)
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, infos, p.cpu().numpy(), s.launch_count() - l0
+
+
+def time_matvec(torch, pkg, s, n, reps=50):
+    """Average duration of one system-matrix H-matvec (V pass + U pass) with
+    CUDA events on the library's stream."""
+    stream = torch.cuda.ExternalStream(pkg.lib().bem_stream(s._h))
+    x = torch.randn(n, dtype=torch.complex128, device="cuda")
+    y = torch.zeros(n, dtype=torch.complex128, device="cuda")
+    for _ in range(3):
+        pkg.lib().bem_hmatvec_device(s._h, 1, x.data_ptr(), y.data_ptr(), 1, 0)
+    h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    h0.record(stream)
+    for _ in range(reps):
+        pkg.lib().bem_hmatvec_device(s._h, 1, x.data_ptr(), y.data_ptr(), 1, 0)
+    h1.record(stream)
+    torch.cuda.synchronize()
+    return h0.elapsed_time(h1) / reps
 
 
 def run_ours(args):
@@ -140,76 +210,48 @@ def run_ours(args):
     pkg = importlib.import_module("3d_bem_gb300")
     meshes = importlib.import_module("3d_bem_gb300.meshes")
     pkg.build()
-    tri = meshes.icosphere(SUBDIV, 1.0)
-    n = tri.shape[0]
-    s = pkg.Solver(aca_tol=ACA_TOL, gmres_tol=GMRES_TOL, wave_speed=C0, density=RHO)
-    s.set_mesh(tri)
-    s.set_bc(np.zeros(n), np.ones(n))
-    stream = torch.cuda.ExternalStream(pkg.lib().bem_stream(s._h))
-    g = torch.ones(n, dtype=torch.complex128, device="cuda")
-    p = torch.zeros(n, dtype=torch.complex128, device="cuda")
-    for f in freqs(args.warmup, 1000 + rank * 100):
-        s.solve_device(f, g.data_ptr(), 1, 0, 0, p.data_ptr())
-    torch.cuda.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
+    sub = WORKLOADS[args.workload][0]
+
+    # plain complex-FP64 arm (comparison), then the mixed arm (headline)
+    plain = None
+    if not args.no_plain:
+        s64, n = make_solver(pkg, meshes, sub, 0)
+        ms64, infos64, p64, _ = timed_arm(torch, pkg, s64, n, args, ws)
+        plain = {"value": round(ws * args.steps / (ms64 / 1e3), 4),
+                 "ms_per_step": round(ms64 / args.steps, 3),
+                 "phases_s": {k: round(float(np.mean([i[k] for i in infos64])), 5)
+                              for k in ("t_nearfield", "t_aca", "t_rhs", "t_gmres")}}
+        s64.close()
+    s, n = make_solver(pkg, meshes, sub, 1)
     clk = Clocks(local)
     clk.start()
-    l0 = s.launch_count()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    infos = []
-    e0.record(stream)
-    for f in freqs(args.steps, rank * 100):
-        infos.append(s.solve_device(f, g.data_ptr(), 1, 0, 0, p.data_ptr()))
-    e1.record(stream)
-    torch.cuda.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
+    ms, infos, pm, launches = timed_arm(torch, pkg, s, n, args, ws)
     clocks = clk.stop()
-    launches = s.launch_count() - l0
-    ms = e0.elapsed_time(e1)
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
     value = ws * args.steps / (ms / 1e3)
 
-    # accuracy of the last solve against the analytic monopole (the fixed
-    # discretisation error of this mesh) and the converged GMRES residual
-    k = 2 * np.pi * freqs(args.steps, rank * 100)[-1] / C0
+    k = 2 * np.pi * freqs(args.steps, 0)[-1] / C0
     pa = RHO * C0 * (1j * k) / (1j * k - 1)
-    ph = p.cpu().numpy()
-    analytic_err = float(np.abs(ph - pa).max() / abs(pa))
+    analytic_err = float(np.abs(pm - pa).max() / abs(pa))
+    mixed_vs_fp64 = None
+    if plain is not None:
+        mixed_vs_fp64 = float(np.linalg.norm(pm - p64) / np.linalg.norm(p64))
 
     # end-to-end through the host-buffer API (pinned host memory)
     gh = torch.ones(n, dtype=torch.complex128).pin_memory()
-    ph_host = torch.zeros(n, dtype=torch.complex128).pin_memory()
     K2 = max(1, args.steps // 2)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for f in freqs(K2, 500 + rank * 100):
-        _, _, pp, _ = s.solve(f, gh.numpy(), want=("p",))
+    for f in freqs(K2, 200):
+        s.solve(f, gh.numpy(), want=("p",))
     torch.cuda.synchronize()
     e2e = K2 / (time.perf_counter() - t0)
 
-    # roofline of the H-matvec kernels (the GMRES inner operator), timed with
-    # events on the library's stream over repeated applications
+    # roofline of the H-matvec (complex-FP32 storage, FP64 accumulation: the
+    # refinement-residual operator; the bytes are those of the stored matrix)
     info_part = s.partition()
     ranks = s.ranks(1)
-    B = matvec_bytes(info_part, ranks, n)
-    x = torch.randn(n, dtype=torch.complex128, device="cuda")
-    y = torch.zeros(n, dtype=torch.complex128, device="cuda")
-    reps = 50
-    for _ in range(3):
-        pkg.lib().bem_hmatvec_device(s._h, 1, x.data_ptr(), y.data_ptr(), 1, 0)
-    h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    h0.record(stream)
-    for _ in range(reps):
-        pkg.lib().bem_hmatvec_device(s._h, 1, x.data_ptr(), y.data_ptr(), 1, 0)
-    h1.record(stream)
-    torch.cuda.synchronize()
-    mv_ms = h0.elapsed_time(h1) / reps
+    B = matvec_bytes(info_part, ranks, n, elem=8)
+    mv_ms = time_matvec(torch, pkg, s, n)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -224,12 +266,14 @@ def run_ours(args):
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "c128 (fp64)",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64 storage + fp32 quadrature, fp64 refinement/Arnoldi/singular rules",
         "data": "synthetic (seeded icosphere; analytic monopole as accuracy check)",
-        "config": workload_config({"parallelism": f"replicas{ws}" if ws > 1 else "single-gpu"}),
+        "config": workload_config(args.workload, {
+            "precision": "mixed", "parallelism": f"replicas{ws}" if ws > 1 else "single-gpu"}),
         "e2e": {"value": round(e2e, 4), "unit": UNIT, "h2d_bytes_per_step": n * 16,
                 "d2h_bytes_per_step": n * 16},
-        "roofline": {"kernel": "hmatvec (V pass + U pass)", "bound": "hbm",
+        "roofline": {"kernel": "hmatvec (V pass + U pass), c64 storage", "bound": "hbm",
                      "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "traffic": None,
                      "bytes_per_launch": B, "ms_per_launch": round(mv_ms, 4),
@@ -239,7 +283,9 @@ def run_ours(args):
         "gmres_iterations": int(max(i["iterations"] for i in infos)),
         "true_residual": float(max(i["true_residual"] for i in infos)),
         "max_rank": int(max(i["max_rank"] for i in infos)),
+        "rel_err_vs_plain_fp64": mixed_vs_fp64,
         "analytic_rel_err": round(analytic_err, 5),
+        "plain_fp64": plain,
         "clocks": clocks,
     }
     if not args.no_cpu_baseline and rank == 0 and ws == 1:
@@ -266,7 +312,7 @@ def cpu_baseline_sample(args):
     """The oracle (FP64 C++/OpenMP restatement of the reference path) on all
     host cores, one full frequency solve of the same workload."""
     meshes = importlib.import_module("3d_bem_gb300.meshes")
-    tri = meshes.icosphere(SUBDIV, 1.0)
+    tri = meshes.icosphere(WORKLOADS[args.workload][0], 1.0)
     cores = os.cpu_count() or 1
     dt, st = cpu_solve_once(tri, FREQ, cores)
     return {"value": round(1.0 / dt, 5), "unit": UNIT, "cores": cores, "kind": "port",
@@ -279,7 +325,7 @@ def run_reference(args):
     if rank != 0:
         return
     meshes = importlib.import_module("3d_bem_gb300.meshes")
-    tri = meshes.icosphere(SUBDIV, 1.0)
+    tri = meshes.icosphere(WORKLOADS[args.workload][0], 1.0)
     cores = os.cpu_count() or 1
     # each step is one full frequency solve; bounded to a few minutes total
     budget = float(os.environ.get("BEM_REF_BUDGET_S", "240"))
@@ -296,7 +342,8 @@ def run_reference(args):
         "steps": len(times), "warmup": 0, "ms_per_step": round(1e3 * sum(times) / len(times), 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "c128 (fp64)", "data": "synthetic (seeded icosphere)",
-        "config": workload_config({"parallelism": "cpu-openmp"}),
+        "config": workload_config(args.workload, {"precision": "fp64",
+                                                  "parallelism": "cpu-openmp"}),
         "impl": "reference",
         "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{len(times)} full frequency solve(s) of the workload; "
@@ -311,10 +358,12 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="sphere20k", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the complex-FP64 arm")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

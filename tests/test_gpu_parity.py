@@ -222,3 +222,54 @@ def test_large_sphere_properties(bem, meshes, orc):
     go = s.operators(k, rows, cols)
     oo = P.operators(k, rows, cols)
     assert (np.abs(go - oo) / np.abs(oo).max(axis=0)).max() < TIGHT
+
+
+def test_mixed_precision_entries_and_solution(bem, meshes, orc):
+    """Mixed mode: FP32 regular quadrature (FP64-formed centroid difference),
+    complex-FP32 storage, FP64 refinement. Near-field entries within 2e-6 of
+    the FP64 oracle; the surface pressure within 1e-5 of the FP64 GPU solve."""
+    tri = meshes.icosphere(3, 1.0)
+    n = tri.shape[0]
+    P = orc.Problem(tri, 32, 2.0)
+    k = 2 * np.pi * 200 / 343
+    sm = bem.Solver(aca_tol=1e-5, gmres_tol=1e-10, precision=1)
+    sm.set_mesh(tri)
+    sm.set_bc(np.zeros(n), np.ones(n))
+    sm.assemble(200.0)
+    info = sm.partition()
+    errs = []
+    for i, row in enumerate(info):
+        r0, m, c0, nn, adm = row
+        if adm:
+            continue
+        F = sm.block(1, i, row)
+        rr, cc = np.meshgrid(np.arange(r0, r0 + m), np.arange(c0, c0 + nn), indexing="ij")
+        _, dphi = P.entries(k, 2, np.zeros(n), np.ones(n), rr.ravel(), cc.ravel())
+        ref = dphi.reshape(m, nn)
+        errs.append(np.abs(F - ref).max() / np.abs(ref).max())
+    assert max(errs) < 2e-6
+    s64 = bem.Solver(aca_tol=1e-5, gmres_tol=1e-10, precision=0)
+    s64.set_mesh(tri)
+    s64.set_bc(np.zeros(n), np.ones(n))
+    for f in (200.0, 900.0):
+        _, _, pm, im = sm.solve(f, np.ones(n))
+        _, _, p64, i64 = s64.solve(f, np.ones(n))
+        assert im["status"] == 0 and im["true_residual"] < 1e-10
+        assert rel(pm[:, 0], p64[:, 0]) < 1e-5
+
+
+def test_mixed_precision_robin_box(bem, meshes, orc):
+    tri = meshes.box(n_target=1200, seed=11)
+    n = tri.shape[0]
+    rng = np.random.default_rng(5)
+    a = np.where(rng.random(n) < 0.3, 2.0 + 1j * rng.random(n), 0.3j * rng.random(n))
+    b = np.ones(n, complex)
+    g = rng.uniform(-1, 1, (n, 2)) + 0j
+    out = {}
+    for prec in (0, 1):
+        s = bem.Solver(aca_tol=1e-5, gmres_tol=1e-10, precision=prec)
+        s.set_mesh(tri)
+        s.set_bc(a, b)
+        out[prec] = s.solve(1200.0, g)
+    assert rel(out[1][0], out[0][0]) < 1e-5
+    assert rel(out[1][1], out[0][1]) < 1e-5
