@@ -414,6 +414,9 @@ QuadRules make_rules() {
     R.reg_x1[i] = t8[i][0];
     R.reg_x2[i] = t8[i][1];
     R.reg_w[i] = t8[i][2];
+    R.freg_x1[i] = (float)t8[i][0];
+    R.freg_x2[i] = (float)t8[i][1];
+    R.freg_w[i] = (float)t8[i][2];
   }
   gauss_legendre(5, R.line_x, R.line_w);
   double x32[32], w32[32];
