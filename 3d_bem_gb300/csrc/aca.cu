@@ -106,12 +106,24 @@ __device__ __forceinline__ void block_argmax(double v, int idx, Red& red, double
     }
 }
 
+// FP32 near-singular test on the FP64-formed centroid difference; used only
+// to pick the rule inside ACA rows/columns (the near-field blocks use the
+// host's exact classification).
+__device__ __forceinline__ bool near_pair32(const Elem* __restrict__ E, int64_t row, int64_t col,
+                                            float near_r2) {
+  const float dx = (float)(E[row].c[0] - E[col].c[0]);
+  const float dy = (float)(E[row].c[1] - E[col].c[1]);
+  const float dz = (float)(E[row].c[2] - E[col].c[2]);
+  return dx * dx + dy * dy + dz * dz < near_r2;
+}
+
 template <int MODE, typename T>
 __device__ __forceinline__ T aca_entry(const AcaArgs& a, int64_t row, int64_t col) {
   if (MODE == 0) {
     if (sizeof(T) == sizeof(float2)) {
       // mixed precision: FP32 regular rule, FP64 singular / near-singular
-      if (row != col && !near_pair(a.E[row], a.E[col], a.near_r)) {
+      const float nr = (float)a.near_r;
+      if (row != col && !near_pair32(a.E, row, col, nr * nr)) {
         OpsF o = ops_regular32(a.E, a.EF, row, col, (float)a.k, c_rules);
         float2 p, d;
         substitute32(o, a.bc[col], make_float2((float)a.alpha.x, (float)a.alpha.y), p, d);
@@ -166,23 +178,30 @@ __device__ void residual_row(const AcaArgs& a, const FarBlock& fb, const T* U, c
   __syncthreads();
 }
 
-// argmax_i |v[i]| over i != exclude
+// squared modulus in the storage precision (the argmax compares |v|^2, which
+// orders like |v|; the FP32 path stays off the FP64 pipe)
+__device__ __forceinline__ double mag2(double2 v) { return v.x * v.x + v.y * v.y; }
+__device__ __forceinline__ float mag2(float2 v) { return v.x * v.x + v.y * v.y; }
+
+// argmax_i |v[i]| over i != exclude; best = |v[bidx]|
 template <typename T>
 __device__ void argmax_abs(const T* v, int len, int exclude, Red& red, double& best, int& bidx) {
-  double bv = -1.0;
+  using R = decltype(mag2(v[0]));
+  R bv = (R)-1;
   int bi = 0x7fffffff;
   for (int i = threadIdx.x; i < len; i += NT) {
-    double x = (i == exclude) ? 0.0 : sqrt(cabs2(to_d(v[i])));
+    const R x = (i == exclude) ? (R)0 : mag2(v[i]);
     if (x > bv) {
       bv = x;
       bi = i;
     }
   }
-  block_argmax(bv, bi, red, best, bidx);
+  block_argmax((double)bv, bi, red, best, bidx);
   if (bidx < 0 || bidx >= len) {  // all entries NaN: report a zero pivot at 0
     bidx = 0;
     best = 0.0;
   }
+  best = sqrt(best);
 }
 
 // normEstimate increment (hmatrix.cpp:570-574):
@@ -191,11 +210,16 @@ template <typename T>
 __device__ void norm_increment(const FarBlock& fb, const T* U, const T* V, const T* S, int k,
                                const T* col, const T* row, double2 alpha, Red& red,
                                double& gain, double2& incr) {
-  double cn = 0, rn = 0;
-  for (int i = threadIdx.x; i < fb.m; i += NT) cn += cabs2(to_d(col[i]));
-  for (int j = threadIdx.x; j < fb.n; j += NT) rn += cabs2(to_d(row[j]));
-  cn = block_sum(cn, red);
-  rn = block_sum(rn, red);
+  // per-thread partial sums in the storage precision, combined in FP64
+  double cn, rn;
+  {
+    using R = decltype(mag2(col[0]));
+    R c0 = 0, r0 = 0;
+    for (int i = threadIdx.x; i < fb.m; i += NT) c0 += mag2(col[i]);
+    for (int j = threadIdx.x; j < fb.n; j += NT) r0 += mag2(row[j]);
+    cn = block_sum((double)c0, red);
+    rn = block_sum((double)r0, red);
+  }
   gain = cabs2(alpha) * rn * cn;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double2 acc = make_double2(0, 0);
@@ -203,18 +227,18 @@ __device__ void norm_increment(const FarBlock& fb, const T* U, const T* V, const
     double cux, cuy, vrx, vry;
     const T* Ul = U + (int64_t)l * fb.m;
     const T* Vl = V + (int64_t)l * fb.n;
-    if (sizeof(T) == sizeof(float2)) {
+    if constexpr (sizeof(T) == sizeof(float2)) {
       // FP32 partial sums (stopping heuristic only), combined in FP64
       float ax = 0, ay = 0, bx = 0, by = 0;
       for (int i = lane; i < fb.m; i += 32) {
-        double2 c = to_d(col[i]), u = to_d(Ul[i]);
-        ax += (float)(c.x * u.x + c.y * u.y);
-        ay += (float)(c.x * u.y - c.y * u.x);
+        const float2 c = col[i], u = Ul[i];  // conj(c) * u
+        ax += c.x * u.x + c.y * u.y;
+        ay += c.x * u.y - c.y * u.x;
       }
       for (int j = lane; j < fb.n; j += 32) {
-        double2 v = to_d(Vl[j]), r = to_d(row[j]);
-        bx += (float)(v.x * r.x + v.y * r.y);
-        by += (float)(v.y * r.x - v.x * r.y);
+        const float2 v = Vl[j], r = row[j];  // v * conj(r)
+        bx += v.x * r.x + v.y * r.y;
+        by += v.y * r.x - v.x * r.y;
       }
       cux = warp_sumf(ax);
       cuy = warp_sumf(ay);

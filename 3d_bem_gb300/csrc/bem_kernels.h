@@ -104,6 +104,8 @@ struct HmvArgs {
   double2* y;
   int64_t ldy;
   int accumulate;
+  float2* xf;  // FP32 scratch copies of x (ldx x nrhs) and t (ldt x nrhs)
+  float2* tf;  // for the FP32-arithmetic variant
 };
 
 void nearfield_upload_rules(const QuadRules& r, cudaStream_t s);
@@ -115,6 +117,6 @@ void launch_points_nearfield(const NearBlock* blocks, int64_t nblocks, const Nea
                              int64_t ntiles, const double* rp, const double* cp, double k,
                              double2* F, cudaStream_t s);
 void launch_aca(const AcaArgs& a, cudaStream_t s);
-void launch_hmatvec(const HmvArgs& a, cudaStream_t s);
+int launch_hmatvec(const HmvArgs& a, cudaStream_t s);  // returns kernels launched
 
 }  // namespace bemgpu

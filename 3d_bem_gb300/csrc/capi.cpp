@@ -122,6 +122,7 @@ struct bem_handle {
   double k = 0;
   DevHM hm[2];
   DBuf<double2> dT;
+  DBuf<float2> dTf, dXf;
   GmresWS gw;
   DBuf<double2> dG, dX, dRhs, dIn, dOut1, dOut2, dOut3;
   DBuf<int> dBad;
@@ -339,6 +340,10 @@ void hmatvec_dev(bem_handle* h, int which, const double2* x, double2* y, int64_t
   const int64_t nrows = h->points_mode ? (int64_t)h->rows.perm.size() : h->N;
   const int64_t ncols = h->points_mode ? (int64_t)h->cols.perm.size() : h->N;
   h->dT.ensure(std::max<int64_t>(h->L.s_size, 1) * 8);
+  if (f32 && m.prec == 1) {
+    h->dTf.ensure(std::max<int64_t>(h->L.s_size, 1) * 8);
+    h->dXf.ensure((size_t)ncols * 8);
+  }
   for (int64_t r0 = 0; r0 < R; r0 += 8) {
     HmvArgs a{};
     a.precision = m.prec;
@@ -363,8 +368,9 @@ void hmatvec_dev(bem_handle* h, int which, const double2* x, double2* y, int64_t
     a.y = y + r0 * nrows;
     a.ldy = nrows;
     a.accumulate = acc;
-    launch_hmatvec(a, h->stream);
-    h->launches += (a.nfar > 0) + (a.nleaves > 0);
+    a.xf = h->dXf.p;
+    a.tf = h->dTf.p;
+    h->launches += launch_hmatvec(a, h->stream);
   }
 }
 

@@ -195,6 +195,175 @@ __global__ void __launch_bounds__(UT) hmv_upass(
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP32-arithmetic variant (complex-FP32 storage): x and t travel as FP32, the
+// block partials are added across blocks with a compensated (two-sum) FP32
+// accumulator, so no instruction of the inner loops touches the FP64 pipe.
+// ---------------------------------------------------------------------------
+struct TwoSum {
+  float hi = 0, lo = 0;
+  __device__ __forceinline__ void add(float v) {
+    const float s = hi + v;
+    const float bp = s - hi;
+    lo += (hi - (s - bp)) + (v - bp);
+    hi = s;
+  }
+};
+
+template <int R>
+__global__ void __launch_bounds__(VT) hmv32_vpass(const FarBlock* __restrict__ far,
+                                                  const int32_t* __restrict__ rank,
+                                                  const float2* __restrict__ Vp,
+                                                  const float2* __restrict__ Sp,
+                                                  const float2* __restrict__ x, int64_t ldx,
+                                                  float2* __restrict__ t, int64_t ldt) {
+  const FarBlock fb = far[blockIdx.x];
+  const int k = rank[blockIdx.x];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int l = w; l < k; l += VT / 32) {
+    const float2* Vl = Vp + fb.voff + (int64_t)l * fb.n;
+    float fx[R], fy[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) fx[r] = fy[r] = 0.0f;
+#pragma unroll 4
+    for (int j = lane; j < fb.n; j += 32) {
+      const float2 v = __ldg(Vl + j);
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        const float2 xv = __ldg(x + r * ldx + fb.c0 + j);
+        fx[r] += v.x * xv.x - v.y * xv.y;
+        fy[r] += v.x * xv.y + v.y * xv.x;
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        fx[r] += __shfl_xor_sync(0xffffffffu, fx[r], o);
+        fy[r] += __shfl_xor_sync(0xffffffffu, fy[r], o);
+      }
+    }
+    if (lane == 0) {
+      const float2 s = __ldg(Sp + fb.soff + l);
+#pragma unroll
+      for (int r = 0; r < R; r++) t[r * ldt + fb.soff + l] = fmul(s, make_float2(fx[r], fy[r]));
+    }
+  }
+}
+
+template <int R>
+__global__ void __launch_bounds__(UT) hmv32_upass(
+    const LeafRows* __restrict__ leaves, const int32_t* __restrict__ list_off,
+    const int32_t* __restrict__ list, const FarBlock* __restrict__ far,
+    const int32_t* __restrict__ rank, const NearBlock* __restrict__ nearb,
+    const float2* __restrict__ Up, const float2* __restrict__ F, const float2* __restrict__ x,
+    int64_t ldx, const float2* __restrict__ t, int64_t ldt, double2* __restrict__ y,
+    int64_t ldy, int accumulate) {
+  __shared__ float4 part[UT / 32][32][R];
+  const LeafRows lf = leaves[blockIdx.x];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int beg = list_off[blockIdx.x], end = list_off[blockIdx.x + 1];
+  for (int base = 0; base < lf.size; base += 32) {
+    const int ri = base + lane;
+    const bool active = ri < lf.size;
+    const int64_t grow = lf.start + ri;
+    TwoSum sx[R], sy[R];
+    for (int e = beg + w; e < end; e += UT / 32) {
+      const int32_t code = list[e];
+      float ax[R], ay[R];
+#pragma unroll
+      for (int r = 0; r < R; r++) ax[r] = ay[r] = 0.0f;
+      if (code >= 0) {
+        const FarBlock fb = far[code];
+        const int k = rank[code];
+        const float2* U = Up + fb.uoff + (grow - fb.r0);
+        if (active) {
+#pragma unroll 4
+          for (int l = 0; l < k; l++) {
+            const float2 u = __ldg(U + (int64_t)l * fb.m);
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+              const float2 tv = __ldg(t + r * ldt + fb.soff + l);
+              ax[r] += u.x * tv.x - u.y * tv.y;
+              ay[r] += u.x * tv.y + u.y * tv.x;
+            }
+          }
+        }
+      } else {
+        const NearBlock nb = nearb[-code - 1];
+        const float2* Fb = F + nb.off + (grow - nb.r0);
+        if (active) {
+#pragma unroll 4
+          for (int j = 0; j < nb.n; j++) {
+            const float2 f = __ldg(Fb + (int64_t)j * nb.m);
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+              const float2 xv = __ldg(x + r * ldx + nb.c0 + j);
+              ax[r] += f.x * xv.x - f.y * xv.y;
+              ay[r] += f.x * xv.y + f.y * xv.x;
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        sx[r].add(ax[r]);
+        sy[r].add(ay[r]);
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++) part[w][lane][r] = make_float4(sx[r].hi, sx[r].lo, sy[r].hi, sy[r].lo);
+    __syncthreads();
+    if (w == 0 && active) {
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        double vx = 0, vy = 0;  // one FP64 sum per row: off the inner loops
+#pragma unroll
+        for (int q = 0; q < UT / 32; q++) {
+          const float4 p = part[q][lane][r];
+          vx += (double)p.x + (double)p.y;
+          vy += (double)p.z + (double)p.w;
+        }
+        double2* yp = y + r * ldy + grow;
+        *yp = accumulate ? cadd(*yp, make_double2(vx, vy)) : make_double2(vx, vy);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void to_float_kernel(const double2* __restrict__ x, float2* __restrict__ xf,
+                                int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x;
+  if (i < n) xf[i] = make_float2((float)x[i].x, (float)x[i].y);
+}
+
+template <int R>
+void launch32_r(const HmvArgs& a, cudaStream_t s) {
+  to_float_kernel<<<(unsigned)((a.ldx * R + 255) / 256), 256, 0, s>>>(a.x, a.xf, a.ldx * R);
+  if (a.nfar > 0)
+    hmv32_vpass<R><<<(unsigned)a.nfar, VT, 0, s>>>(a.far, a.rank, (const float2*)a.V,
+                                                   (const float2*)a.S, a.xf, a.ldx, a.tf,
+                                                   a.ldt);
+  if (a.nleaves > 0)
+    hmv32_upass<R><<<(unsigned)a.nleaves, UT, 0, s>>>(
+        a.leaves, a.list_off, a.list, a.far, a.rank, a.nearb, (const float2*)a.U,
+        (const float2*)a.F, a.xf, a.ldx, a.tf, a.ldt, a.y, a.ldy, a.accumulate);
+}
+
+void launch32(const HmvArgs& a, cudaStream_t s) {
+  switch (a.nrhs) {
+    case 1: launch32_r<1>(a, s); break;
+    case 2: launch32_r<2>(a, s); break;
+    case 3: launch32_r<3>(a, s); break;
+    case 4: launch32_r<4>(a, s); break;
+    case 5: launch32_r<5>(a, s); break;
+    case 6: launch32_r<6>(a, s); break;
+    case 7: launch32_r<7>(a, s); break;
+    default: launch32_r<8>(a, s); break;
+  }
+}
+
 template <typename T, bool F32, int R>
 void launch_r(const HmvArgs& a, cudaStream_t s) {
   if (a.nfar > 0)
@@ -221,10 +390,13 @@ void launch_t(const HmvArgs& a, cudaStream_t s) {
 }
 }  // namespace
 
-void launch_hmatvec(const HmvArgs& a, cudaStream_t s) {
+int launch_hmatvec(const HmvArgs& a, cudaStream_t s) {
   if (a.precision == 0) launch_t<double2, false>(a, s);
-  else if (a.fp32_math) launch_t<float2, true>(a, s);
-  else launch_t<float2, false>(a, s);
+  else if (a.fp32_math) {
+    launch32(a, s);
+    return 1 + (a.nfar > 0) + (a.nleaves > 0);
+  } else launch_t<float2, false>(a, s);
+  return (a.nfar > 0) + (a.nleaves > 0);
 }
 
 }  // namespace bemgpu
