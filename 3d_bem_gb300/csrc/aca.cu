@@ -150,6 +150,38 @@ __device__ __forceinline__ T aca_entry(const AcaArgs& a, int64_t row, int64_t co
   }
 }
 
+// sum_l p[l * stride] * c[l] with 8 independent loads in flight (the chain
+// of dependent loads was the ACA's latency bottleneck)
+template <typename T>
+__device__ __forceinline__ T dot_strided(const T* p, int64_t stride, const T* c, int k) {
+  T acc[8];
+#pragma unroll
+  for (int q = 0; q < 8; q++) acc[q] = T{0, 0};
+  int l = 0;
+  for (; l + 8 <= k; l += 8) {
+    T v[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) v[q] = p[(int64_t)(l + q) * stride];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const T cq = c[l + q];
+      acc[q].x += v[q].x * cq.x - v[q].y * cq.y;
+      acc[q].y += v[q].x * cq.y + v[q].y * cq.x;
+    }
+  }
+  for (; l < k; l++) {
+    const T v = p[(int64_t)l * stride], cq = c[l];
+    acc[0].x += v.x * cq.x - v.y * cq.y;
+    acc[0].y += v.x * cq.y + v.y * cq.x;
+  }
+#pragma unroll
+  for (int q = 1; q < 8; q++) {
+    acc[0].x += acc[q].x;
+    acc[0].y += acc[q].y;
+  }
+  return acc[0];
+}
+
 // dst[i] = A(r0+i, c0+ci) - sum_l U[:,l] (s_l V[l,ci])
 template <int MODE, typename T>
 __device__ void residual_col(const AcaArgs& a, const FarBlock& fb, const T* U, const T* V,
@@ -158,8 +190,7 @@ __device__ void residual_col(const AcaArgs& a, const FarBlock& fb, const T* U, c
   __syncthreads();
   for (int i = threadIdx.x; i < fb.m; i += NT) {
     T v = aca_entry<MODE, T>(a, fb.r0 + i, fb.c0 + ci);
-    for (int l = 0; l < k; l++) v = cx_sub(v, cx_mul(U[(int64_t)l * fb.m + i], coef[l]));
-    dst[i] = v;
+    dst[i] = cx_sub(v, dot_strided(U + i, (int64_t)fb.m, coef, k));
   }
   __syncthreads();
 }
@@ -172,8 +203,7 @@ __device__ void residual_row(const AcaArgs& a, const FarBlock& fb, const T* U, c
   __syncthreads();
   for (int j = threadIdx.x; j < fb.n; j += NT) {
     T v = aca_entry<MODE, T>(a, fb.r0 + ri, fb.c0 + j);
-    for (int l = 0; l < k; l++) v = cx_sub(v, cx_mul(coef[l], V[(int64_t)l * fb.n + j]));
-    dst[j] = v;
+    dst[j] = cx_sub(v, dot_strided(V + j, (int64_t)fb.n, coef, k));
   }
   __syncthreads();
 }

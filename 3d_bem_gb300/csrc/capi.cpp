@@ -440,7 +440,7 @@ struct GmresResult {
 // Restarted GMRES for R right-hand sides on the dPhi matrix (device b, x;
 // x holds the initial guess). f32 selects the FP32-arithmetic operator.
 GmresResult gmres_core(bem_handle* h, const double2* b, double2* x, int R, double tol,
-                       int64_t maxit, bool f32) {
+                       int64_t maxit, bool f32, bool x_zero = false) {
   ensure_gmres(h, R);
   GmresWS& g = h->gw;
   const int64_t N = h->N;
@@ -452,11 +452,18 @@ GmresResult gmres_core(bem_handle* h, const double2* b, double2* x, int R, doubl
   krylov_restart(a, 1, s);  // measures ||b||
   h->launches += 2;
   int64_t total = 0;
+  bool first = true;
   while (true) {
-    hmatvec_dev(h, 1, x, g.w.p, R, 0, f32);
-    krylov_residual(g.bcopy.p, g.w.p, (int64_t)R * N, s);
+    if (first && x_zero) {  // r = b: skip the product with the zero guess
+      CK(cudaMemcpyAsync(g.w.p, b, (size_t)R * N * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    } else {
+      hmatvec_dev(h, 1, x, g.w.p, R, 0, f32);
+      krylov_residual(g.bcopy.p, g.w.p, (int64_t)R * N, s);
+      h->launches++;
+    }
+    first = false;
     krylov_restart(a, 0, s);
-    h->launches += 3;
+    h->launches += 2;
     if (read_states(h) || total >= maxit) break;
     for (int j = 0; j < g.m; j++) {
       hmatvec_dev(h, 1, g.Vb.p + (int64_t)j * R * N, g.w.p, R, 0, f32);
@@ -506,13 +513,14 @@ std::vector<double> norms(bem_handle* h, const double2* v, int R) {
 // gmres.h:170-180). precision 1: FP64 iterative refinement -- the residual
 // b - A x uses FP64 arithmetic on the stored complex-FP32 operator, each
 // correction comes from GMRES on the FP32-arithmetic operator.
-void gmres_dev(bem_handle* h, const double2* b, double2* x, int R, bem_solve_info* info) {
+void gmres_dev(bem_handle* h, const double2* b, double2* x, int R, bem_solve_info* info,
+               bool x_zero = false) {
   require(h->hm[1].assembled, BEM_EINVAL, "system matrix not assembled");
   const double tol = h->cfg.gmres_tol;
   const int64_t maxit = h->cfg.gmres_maxit;
   bem_solve_info loc{};
   if (h->hm[1].prec == 0) {
-    GmresResult r = gmres_core(h, b, x, R, tol, maxit, false);
+    GmresResult r = gmres_core(h, b, x, R, tol, maxit, false, x_zero);
     loc.iterations = r.iters;
     loc.rel_residual = loc.true_residual = r.resid;
     loc.status = r.converged ? BEM_OK : BEM_EMAXIT;
@@ -528,9 +536,13 @@ void gmres_dev(bem_handle* h, const double2* b, double2* x, int R, bem_solve_inf
     double rel = 0, inner_res = 0;
     for (int outer = 0; outer < 30; outer++) {
       // r = b - A x with FP64 arithmetic on the stored operator
-      hmatvec_dev(h, 1, x, g.r.p, R, 0, false);
-      krylov_residual(b, g.r.p, (int64_t)R * N, s);
-      h->launches++;
+      if (outer == 0 && x_zero) {
+        CK(cudaMemcpyAsync(g.r.p, b, (size_t)R * N * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+      } else {
+        hmatvec_dev(h, 1, x, g.r.p, R, 0, false);
+        krylov_residual(b, g.r.p, (int64_t)R * N, s);
+        h->launches++;
+      }
       const std::vector<double> rn = norms(h, g.r.p, R);
       rel = 0;
       for (int q = 0; q < R; q++) rel = std::max(rel, bn[q] > 0 ? rn[q] / bn[q] : 0.0);
@@ -539,7 +551,7 @@ void gmres_dev(bem_handle* h, const double2* b, double2* x, int R, bem_solve_inf
       // products cap what one inner solve can deliver at about 1e-6
       const double inner_tol = std::max(1e-6, 0.3 * tol / rel);
       CK(cudaMemsetAsync(g.d.p, 0, (size_t)R * N * sizeof(double2), s));
-      GmresResult ir = gmres_core(h, g.r.p, g.d.p, R, inner_tol, maxit - total, true);
+      GmresResult ir = gmres_core(h, g.r.p, g.d.p, R, inner_tol, maxit - total, true, true);
       total += ir.iters;
       inner_res = ir.resid;
       krylov_axpy(x, g.d.p, (int64_t)R * N, s);
@@ -592,7 +604,7 @@ void solve_dev(bem_handle* h, double freq, const double2* g_caller, int64_t R, d
   hmatvec_dev(h, 0, h->dG.p, h->dRhs.p, R, 0);
   CK(cudaEventRecord(h->ev[4], s));
   CK(cudaMemsetAsync(h->dX.p, 0, (size_t)R * N * sizeof(double2), s));
-  gmres_dev(h, h->dRhs.p, h->dX.p, (int)R, &loc);
+  gmres_dev(h, h->dRhs.p, h->dX.p, (int)R, &loc, true);
   CK(cudaEventRecord(h->ev[5], s));
   const double omega = 2.0 * M_PI * freq;
   double2 pfac = make_double2(0.0, h->cfg.density * omega);
