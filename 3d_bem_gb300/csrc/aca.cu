@@ -31,8 +31,7 @@ void aca_upload_rules(const QuadRules& r, cudaStream_t s) {
 
 namespace {
 constexpr double TINY = 10.0 * 2.220446049250313080847263336181640625e-16;  // global.h:53
-constexpr int NT = 128;
-constexpr int NW = NT / 32;
+constexpr int NW_MAX = 16;  // up to 512 threads per CTA
 
 // complex arithmetic on the storage type
 __device__ __forceinline__ double2 cx_mul(double2 a, double2 b) { return cmul(a, b); }
@@ -48,9 +47,9 @@ template <> __device__ __forceinline__ float2 from_d<float2>(double2 a) {
 }
 
 struct Red {
-  double v[NW];
-  int i[NW];
-  double2 c[NW];
+  double v[NW_MAX];
+  int i[NW_MAX];
+  double2 c[NW_MAX];
 };
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -65,7 +64,9 @@ __device__ __forceinline__ float warp_sumf(float v) {
 }
 
 // block-wide sum, result returned to every thread (deterministic order)
+template <int NT>
 __device__ __forceinline__ double block_sum(double v, Red& red) {
+  constexpr int NW = NT / 32;
   v = warp_sum(v);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   __syncthreads();
@@ -78,8 +79,10 @@ __device__ __forceinline__ double block_sum(double v, Red& red) {
 }
 
 // block-wide argmax of |.|, first index among equal maxima (Eigen maxCoeff)
+template <int NT>
 __device__ __forceinline__ void block_argmax(double v, int idx, Red& red, double& best,
                                              int& bidx) {
+  constexpr int NW = NT / 32;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     double v2 = __shfl_xor_sync(0xffffffffu, v, o);
@@ -183,7 +186,7 @@ __device__ __forceinline__ T dot_strided(const T* p, int64_t stride, const T* c,
 }
 
 // dst[i] = A(r0+i, c0+ci) - sum_l U[:,l] (s_l V[l,ci])
-template <int MODE, typename T>
+template <int MODE, typename T, int NT>
 __device__ void residual_col(const AcaArgs& a, const FarBlock& fb, const T* U, const T* V,
                              const T* S, int k, int ci, T* dst, T* coef) {
   for (int l = threadIdx.x; l < k; l += NT) coef[l] = cx_mul(S[l], V[(int64_t)l * fb.n + ci]);
@@ -196,7 +199,7 @@ __device__ void residual_col(const AcaArgs& a, const FarBlock& fb, const T* U, c
 }
 
 // dst[j] = A(r0+ri, c0+j) - sum_l (U[ri,l] s_l) V[l,:]
-template <int MODE, typename T>
+template <int MODE, typename T, int NT>
 __device__ void residual_row(const AcaArgs& a, const FarBlock& fb, const T* U, const T* V,
                              const T* S, int k, int ri, T* dst, T* coef) {
   for (int l = threadIdx.x; l < k; l += NT) coef[l] = cx_mul(U[(int64_t)l * fb.m + ri], S[l]);
@@ -214,7 +217,7 @@ __device__ __forceinline__ double mag2(double2 v) { return v.x * v.x + v.y * v.y
 __device__ __forceinline__ float mag2(float2 v) { return v.x * v.x + v.y * v.y; }
 
 // argmax_i |v[i]| over i != exclude; best = |v[bidx]|
-template <typename T>
+template <typename T, int NT>
 __device__ void argmax_abs(const T* v, int len, int exclude, Red& red, double& best, int& bidx) {
   using R = decltype(mag2(v[0]));
   R bv = (R)-1;
@@ -226,7 +229,7 @@ __device__ void argmax_abs(const T* v, int len, int exclude, Red& red, double& b
       bi = i;
     }
   }
-  block_argmax((double)bv, bi, red, best, bidx);
+  block_argmax<NT>((double)bv, bi, red, best, bidx);
   if (bidx < 0 || bidx >= len) {  // all entries NaN: report a zero pivot at 0
     bidx = 0;
     best = 0.0;
@@ -236,7 +239,7 @@ __device__ void argmax_abs(const T* v, int len, int exclude, Red& red, double& b
 
 // normEstimate increment (hmatrix.cpp:570-574):
 // |alpha|^2 |row|^2 |col|^2 + sum_{l<k} 2 conj(alpha) s_l (col^H U_l)(V_l row^H)
-template <typename T>
+template <typename T, int NT>
 __device__ void norm_increment(const FarBlock& fb, const T* U, const T* V, const T* S, int k,
                                const T* col, const T* row, double2 alpha, Red& red,
                                double& gain, double2& incr) {
@@ -247,10 +250,11 @@ __device__ void norm_increment(const FarBlock& fb, const T* U, const T* V, const
     R c0 = 0, r0 = 0;
     for (int i = threadIdx.x; i < fb.m; i += NT) c0 += mag2(col[i]);
     for (int j = threadIdx.x; j < fb.n; j += NT) r0 += mag2(row[j]);
-    cn = block_sum((double)c0, red);
-    rn = block_sum((double)r0, red);
+    cn = block_sum<NT>((double)c0, red);
+    rn = block_sum<NT>((double)r0, red);
   }
   gain = cabs2(alpha) * rn * cn;
+  constexpr int NW = NT / 32;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double2 acc = make_double2(0, 0);
   for (int l = w; l < k; l += NW) {
@@ -303,7 +307,7 @@ __device__ void norm_increment(const FarBlock& fb, const T* U, const T* V, const
   __syncthreads();
 }
 
-template <int MODE, typename T>
+template <int MODE, typename T, int NT>
 __global__ void __launch_bounds__(NT) aca_kernel(AcaArgs a) {
   __shared__ T coef[ACA_MAX_KCAP];
   __shared__ Red red;
@@ -324,26 +328,26 @@ __global__ void __launch_bounds__(NT) aca_kernel(AcaArgs a) {
   if (!a.extra) {
     // --- partialPivotACA ---
     int ci = (int)(pivot_hash(a.seed, (uint64_t)fb.id, 0) % (uint64_t)n);
-    residual_col<MODE, T>(a, fb, U, V, S, 0, ci, U, coef);  // start column into slot 0
+    residual_col<MODE, T, NT>(a, fb, U, V, S, 0, ci, U, coef);  // start column into slot 0
     int ri = -1;
     while (k < kmax) {
       const T* colv = U + (int64_t)(k > 0 ? k - 1 : 0) * m;
       double cmax;
-      argmax_abs(colv, m, k >= 1 ? ri : -1, red, cmax, ri);
+      argmax_abs<T, NT>(colv, m, k >= 1 ? ri : -1, red, cmax, ri);
       if (cmax <= TINY && k >= 1) break;
       T* rowv = V + (int64_t)k * n;
-      residual_row<MODE, T>(a, fb, U, V, S, k, ri, rowv, coef);
+      residual_row<MODE, T, NT>(a, fb, U, V, S, k, ri, rowv, coef);
       double rmax;
-      argmax_abs(rowv, n, -1, red, rmax, ci);
+      argmax_abs<T, NT>(rowv, n, -1, red, rmax, ci);
       if (rmax <= TINY && k >= 1) break;
       T* newcol = U + (int64_t)k * m;
-      residual_col<MODE, T>(a, fb, U, V, S, k, ci, newcol, coef);
+      residual_col<MODE, T, NT>(a, fb, U, V, S, k, ci, newcol, coef);
       double2 alpha = cdiv(make_double2(1.0, 0.0), to_d(rowv[ci]));
       if (threadIdx.x == 0) S[k] = from_d<T>(alpha);
       __syncthreads();
       double gain;
       double2 incr;
-      norm_increment(fb, U, V, S, k, newcol, rowv, alpha, red, gain, incr);
+      norm_increment<T, NT>(fb, U, V, S, k, newcol, rowv, alpha, red, gain, incr);
       k++;
       est = cadd(est, incr);
       double target = tol * tol * est.x;
@@ -367,27 +371,27 @@ __global__ void __launch_bounds__(NT) aca_kernel(AcaArgs a) {
         approx = cadd(approx, cmul(cmul(to_d(U[(int64_t)l * m + ri]), to_d(S[l])),
                                    to_d(V[(int64_t)l * n + ci])));
       if (sqrt(cabs2(cdiv(csub(pivv, approx), pivv))) < tol) continue;
-      residual_col<MODE, T>(a, fb, U, V, S, k, ci, U + (int64_t)k * m, coef);
+      residual_col<MODE, T, NT>(a, fb, U, V, S, k, ci, U + (int64_t)k * m, coef);
       bool first = true;
       while (k < kmax) {
         const T* colv = first ? U + (int64_t)k * m : U + (int64_t)(k - 1) * m;
         double cmax;
-        argmax_abs(colv, m, first ? -1 : ri, red, cmax, ri);
+        argmax_abs<T, NT>(colv, m, first ? -1 : ri, red, cmax, ri);
         first = false;
         if (cmax <= TINY && k >= 1) break;
         T* rowv = V + (int64_t)k * n;
-        residual_row<MODE, T>(a, fb, U, V, S, k, ri, rowv, coef);
+        residual_row<MODE, T, NT>(a, fb, U, V, S, k, ri, rowv, coef);
         double rmax;
-        argmax_abs(rowv, n, -1, red, rmax, ci);
+        argmax_abs<T, NT>(rowv, n, -1, red, rmax, ci);
         if (rmax <= TINY && k >= 1) break;
         T* newcol = U + (int64_t)k * m;
-        residual_col<MODE, T>(a, fb, U, V, S, k, ci, newcol, coef);
+        residual_col<MODE, T, NT>(a, fb, U, V, S, k, ci, newcol, coef);
         double2 alpha = cdiv(make_double2(1.0, 0.0), to_d(rowv[ci]));
         if (threadIdx.x == 0) S[k] = from_d<T>(alpha);
         __syncthreads();
         double gain;
         double2 incr;
-        norm_increment(fb, U, V, S, k, newcol, rowv, alpha, red, gain, incr);
+        norm_increment<T, NT>(fb, U, V, S, k, newcol, rowv, alpha, red, gain, incr);
         double2 old = est;
         k++;
         est = cadd(est, incr);
@@ -411,16 +415,26 @@ __global__ void __launch_bounds__(NT) aca_kernel(AcaArgs a) {
 }
 }  // namespace
 
-void launch_aca(const AcaArgs& a, cudaStream_t s) {
-  if (a.nfar <= 0) return;
+template <int NT>
+void launch_nt(const AcaArgs& a, cudaStream_t s) {
   const unsigned g = (unsigned)a.nfar;
   if (a.precision == 0) {
-    if (a.mode == 0) aca_kernel<0, double2><<<g, NT, 0, s>>>(a);
-    else aca_kernel<1, double2><<<g, NT, 0, s>>>(a);
+    if (a.mode == 0) aca_kernel<0, double2, NT><<<g, NT, 0, s>>>(a);
+    else aca_kernel<1, double2, NT><<<g, NT, 0, s>>>(a);
   } else {
-    if (a.mode == 0) aca_kernel<0, float2><<<g, NT, 0, s>>>(a);
-    else aca_kernel<1, float2><<<g, NT, 0, s>>>(a);
+    if (a.mode == 0) aca_kernel<0, float2, NT><<<g, NT, 0, s>>>(a);
+    else aca_kernel<1, float2, NT><<<g, NT, 0, s>>>(a);
   }
+}
+
+// a.order / a.nfar select the blocks of this launch; threads is 128 or 512
+// (large blocks get 16 warps so their O(k (m+n)) residual and norm updates
+// stream with enough loads in flight).
+int launch_aca(const AcaArgs& a, int threads, cudaStream_t s) {
+  if (a.nfar <= 0) return 0;
+  if (threads >= 512) launch_nt<512>(a, s);
+  else launch_nt<128>(a, s);
+  return 1;
 }
 
 }  // namespace bemgpu

@@ -116,7 +116,8 @@ void launch_operators(const Elem* E, const int64_t* rows, const int64_t* cols, i
 void launch_points_nearfield(const NearBlock* blocks, int64_t nblocks, const NearTile* tiles,
                              int64_t ntiles, const double* rp, const double* cp, double k,
                              double2* F, cudaStream_t s);
-void launch_aca(const AcaArgs& a, cudaStream_t s);
+int launch_aca(const AcaArgs& a, int threads, cudaStream_t s);
+constexpr int ACA_BIG_MN = 512;  // blocks with m + n >= this get 512-thread CTAs
 int launch_hmatvec(const HmvArgs& a, cudaStream_t s);  // returns kernels launched
 
 }  // namespace bemgpu

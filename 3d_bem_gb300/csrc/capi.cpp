@@ -96,6 +96,8 @@ struct bem_handle {
   bem_config cfg{};
   std::string err;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;  // second stream for concurrent ACA launches
+  cudaEvent_t fork = nullptr, join = nullptr;
   int64_t launches = 0;
   // mesh
   int64_t N = 0;
@@ -289,6 +291,26 @@ AcaArgs aca_args(bem_handle* h, DevHM& m, int which, int extra) {
   return a;
 }
 
+// ACA launches of one or more matrices: blocks with m + n >= ACA_BIG_MN run
+// with 512-thread CTAs on the side stream while the rest run with 128-thread
+// CTAs on the main stream; the main stream waits for both.
+void launch_aca_split(bem_handle* h, std::initializer_list<AcaArgs> mats) {
+  cudaStream_t s = h->stream, s2 = h->side;
+  const int64_t nbig = h->L.nbig, nfar = (int64_t)h->L.far.size();
+  CK(cudaEventRecord(h->fork, s));
+  CK(cudaStreamWaitEvent(s2, h->fork, 0));
+  for (AcaArgs a : mats) {
+    AcaArgs big = a, small = a;
+    big.nfar = nbig;
+    small.order = a.order + nbig;
+    small.nfar = nfar - nbig;
+    h->launches += launch_aca(big, 512, s2);
+    h->launches += launch_aca(small, 128, s);
+  }
+  CK(cudaEventRecord(h->join, s2));
+  CK(cudaStreamWaitEvent(s, h->join, 0));
+}
+
 // both H-matrices at wavenumber k; optional timing events
 void assemble(bem_handle* h, double freq, double* t_near, double* t_aca) {
   require(h->have_mesh && !h->points_mode, BEM_EINVAL, "mesh not set (bem_set_mesh)");
@@ -319,9 +341,7 @@ void assemble(bem_handle* h, double freq, double* t_near, double* t_aca) {
   launch_nearfield(na, s);
   h->launches += (na.ntiles > 0) + (na.nspecial > 0);
   CK(cudaEventRecord(h->ev[1], s));
-  launch_aca(aca_args(h, h->hm[0], 0, 0), s);
-  launch_aca(aca_args(h, h->hm[1], 1, 1), s);
-  h->launches += 2;
+  launch_aca_split(h, {aca_args(h, h->hm[0], 0, 0), aca_args(h, h->hm[1], 1, 1)});
   CK(cudaEventRecord(h->ev[2], s));
   CK(cudaGetLastError());
   fetch_ranks(h, h->hm[0]);
@@ -678,6 +698,9 @@ bem_status bem_create(const bem_config* cfg, bem_handle** out) {
             "precision must be 0 (complex FP64) or 1 (mixed)");
     require(h->cfg.wave_speed > 0, BEM_EINVAL, "wave_speed must be positive");
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&h->join, cudaEventDisableTiming));
     for (auto& e : h->ev) CK(cudaEventCreate(&e));
     h->rules = make_rules();
     nearfield_upload_rules(h->rules, h->stream);
@@ -696,11 +719,15 @@ bem_status bem_create(const bem_config* cfg, bem_handle** out) {
 void bem_destroy(bem_handle* h) {
   if (!h) return;
   if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->side) cudaStreamSynchronize(h->side);
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
-  cudaStream_t s = h->stream;
+  if (h->fork) cudaEventDestroy(h->fork);
+  if (h->join) cudaEventDestroy(h->join);
+  cudaStream_t s = h->stream, s2 = h->side;
   delete h;  // device buffers are released by their destructors
   if (s) cudaStreamDestroy(s);
+  if (s2) cudaStreamDestroy(s2);
 }
 
 const char* bem_last_error(const bem_handle* h) { return h ? h->err.c_str() : "null handle"; }
@@ -1034,8 +1061,8 @@ bem_status bem_points_assemble(bem_handle* h, const double* rowpts, int64_t nr,
                             (double2*)m.F.p, h->stream);
     AcaArgs a = aca_args(h, m, 0, 0);
     a.mode = 1;
-    launch_aca(a, h->stream);
-    h->launches += 2;
+    h->launches++;
+    launch_aca_split(h, {a});
     CK(cudaGetLastError());
     fetch_ranks(h, m);
     h->hm[1].assembled = false;

@@ -294,6 +294,10 @@ void build_layout(const HTree& rows, const HTree& cols, const std::vector<Elem>*
   std::stable_sort(L.far_order.begin(), L.far_order.end(), [&](int32_t a, int32_t b) {
     return (int64_t)L.far[a].m + L.far[a].n > (int64_t)L.far[b].m + L.far[b].n;
   });
+  L.nbig = 0;
+  while (L.nbig < (int64_t)L.far_order.size() &&
+         (int64_t)L.far[L.far_order[L.nbig]].m + L.far[L.far_order[L.nbig]].n >= ACA_BIG_MN)
+    L.nbig++;
   // near-field tiles of <= 256 entries
   for (size_t bi = 0; bi < L.near.size(); bi++) {
     const int64_t cnt = (int64_t)L.near[bi].m * L.near[bi].n;
