@@ -109,35 +109,46 @@ __device__ __forceinline__ void block_argmax(double v, int idx, Red& red, double
     }
 }
 
-// FP32 near-singular test on the FP64-formed centroid difference; used only
-// to pick the rule inside ACA rows/columns (the near-field blocks use the
-// host's exact classification).
-__device__ __forceinline__ bool near_pair32(const Elem* __restrict__ E, int64_t row, int64_t col,
-                                            float near_r2) {
-  const float dx = (float)(E[row].c[0] - E[col].c[0]);
-  const float dy = (float)(E[row].c[1] - E[col].c[1]);
-  const float dz = (float)(E[row].c[2] - E[col].c[2]);
+// FP32 near-singular test on the two-float centroid difference; used only to
+// pick the rule inside ACA rows/columns (the near-field blocks use the host's
+// exact classification).
+__device__ __forceinline__ bool near_pair32(const ElemF* __restrict__ EF, int64_t row,
+                                            int64_t col, float near_r2) {
+  float dx, dy, dz;
+  centroid_diff(EF[row], EF[col], dx, dy, dz);
   return dx * dx + dy * dy + dz * dz < near_r2;
+}
+
+// the complex-FP64 entry (singular / near-singular pairs of the mixed path,
+// every pair of the plain path); kept out of line so the FP32 fast path does
+// not carry its registers
+__device__ __noinline__ double2 entry64(const AcaArgs& a, int64_t row, int64_t col) {
+  Ops o = ops_eval(a.E, row, col, a.k, a.near_r, c_rules);
+  double2 p, d;
+  substitute(o, row == col, a.bc[col], a.alpha, p, d);
+  return a.which ? d : p;
+}
+
+__device__ __noinline__ float2 entry64f(const AcaArgs& a, int64_t row, int64_t col) {
+  const double2 v = entry64(a, row, col);
+  return make_float2((float)v.x, (float)v.y);
 }
 
 template <int MODE, typename T>
 __device__ __forceinline__ T aca_entry(const AcaArgs& a, int64_t row, int64_t col) {
-  if (MODE == 0) {
-    if (sizeof(T) == sizeof(float2)) {
+  if constexpr (MODE == 0) {
+    if constexpr (sizeof(T) == sizeof(float2)) {
       // mixed precision: FP32 regular rule, FP64 singular / near-singular
-      const float nr = (float)a.near_r;
-      if (row != col && !near_pair32(a.E, row, col, nr * nr)) {
-        OpsF o = ops_regular32(a.E, a.EF, row, col, (float)a.k, c_rules);
+      if (row != col && !near_pair32(a.EF, row, col, a.near_r2f)) {
+        OpsF o = ops_regular32(a.EF, row, col, a.kf, c_rules);
         float2 p, d;
-        substitute32(o, a.bc[col], make_float2((float)a.alpha.x, (float)a.alpha.y), p, d);
-        double2 r = to_d(a.which ? d : p);
-        return from_d<T>(r);
+        substitute32(o, a.bc[col], a.alphaf, p, d);
+        return a.which ? d : p;
       }
+      return entry64f(a, row, col);
+    } else {
+      return entry64(a, row, col);
     }
-    Ops o = ops_eval(a.E, row, col, a.k, a.near_r, c_rules);
-    double2 p, d;
-    substitute(o, row == col, a.bc[col], a.alpha, p, d);
-    return from_d<T>(a.which ? d : p);
   } else {
     // point-cloud Helmholtz kernel of the reference's tests
     // (Tests/tests.h:30-42): exp(ikr)/(4 pi r), 1 at r = 0
@@ -153,20 +164,20 @@ __device__ __forceinline__ T aca_entry(const AcaArgs& a, int64_t row, int64_t co
   }
 }
 
-// sum_l p[l * stride] * c[l] with 8 independent loads in flight (the chain
+// sum_l p[l * stride] * c[l] with 4 independent loads in flight (the chain
 // of dependent loads was the ACA's latency bottleneck)
 template <typename T>
 __device__ __forceinline__ T dot_strided(const T* p, int64_t stride, const T* c, int k) {
-  T acc[8];
+  T acc[4];
 #pragma unroll
-  for (int q = 0; q < 8; q++) acc[q] = T{0, 0};
+  for (int q = 0; q < 4; q++) acc[q] = T{0, 0};
   int l = 0;
-  for (; l + 8 <= k; l += 8) {
-    T v[8];
+  for (; l + 4 <= k; l += 4) {
+    T v[4];
 #pragma unroll
-    for (int q = 0; q < 8; q++) v[q] = p[(int64_t)(l + q) * stride];
+    for (int q = 0; q < 4; q++) v[q] = p[(int64_t)(l + q) * stride];
 #pragma unroll
-    for (int q = 0; q < 8; q++) {
+    for (int q = 0; q < 4; q++) {
       const T cq = c[l + q];
       acc[q].x += v[q].x * cq.x - v[q].y * cq.y;
       acc[q].y += v[q].x * cq.y + v[q].y * cq.x;
@@ -178,7 +189,7 @@ __device__ __forceinline__ T dot_strided(const T* p, int64_t stride, const T* c,
     acc[0].y += v.x * cq.y + v.y * cq.x;
   }
 #pragma unroll
-  for (int q = 1; q < 8; q++) {
+  for (int q = 1; q < 4; q++) {
     acc[0].x += acc[q].x;
     acc[0].y += acc[q].y;
   }

@@ -61,6 +61,9 @@ struct AcaArgs {
   double k;
   double near_r;
   double2 alpha;
+  float kf;        // FP32 copies for the mixed path
+  float near_r2f;
+  float2 alphaf;
   int which;  // 0 phi, 1 dphi
   const double* rowpts;
   const double* colpts;

@@ -20,13 +20,17 @@ struct __align__(16) Elem {
 
 // FP32 companion of Elem for the mixed-precision rules: vertices relative to
 // the element's own centroid (small numbers, so FP32 keeps ~7 digits of the
-// local geometry), unit normal and area. The centroid itself stays FP64 in
-// Elem; pair differences c_i - c_j are formed in FP64 and then rounded.
+// local geometry), unit normal, area, and the centroid as an unevaluated sum
+// c = c_hi + c_lo of two floats. The pair difference
+// (c_hi,i - c_hi,j) + (c_lo,i - c_lo,j) is then accurate to ~1e-7 relative
+// without any FP64 instruction (GB300's FP64 rate is 1/64 of FP32).
 struct __align__(16) ElemF {
   float v[9];    // node1 - c, node2 - c, node3 - c
   float nrm[3];
   float area;
-  float pad[3];
+  float c_hi[3];
+  float c_lo[3];
+  float pad[1];
 };
 
 // Rule tables: 16-point triangle rule (order 8), 5-point Gauss-Legendre

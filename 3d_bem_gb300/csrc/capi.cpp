@@ -213,6 +213,8 @@ std::vector<ElemF> make_elemf(const std::vector<Elem>& E) {
       f.v[3 + d] = (float)(e.n2[d] - e.c[d]);
       f.v[6 + d] = (float)(e.n3[d] - e.c[d]);
       f.nrm[d] = (float)e.nrm[d];
+      f.c_hi[d] = (float)e.c[d];
+      f.c_lo[d] = (float)(e.c[d] - (double)f.c_hi[d]);
     }
     f.area = (float)e.area;
     F[i] = f;
@@ -270,6 +272,9 @@ AcaArgs aca_args(bem_handle* h, DevHM& m, int which, int extra) {
   a.near_r = h->near_r;
   cplx al = coupling_parameter(h->cfg.coupling, h->k);
   a.alpha = make_double2(al.real(), al.imag());
+  a.kf = (float)h->k;
+  a.near_r2f = (float)(h->near_r * h->near_r);
+  a.alphaf = make_float2((float)al.real(), (float)al.imag());
   a.which = which;
   a.rowpts = h->dRowPts.p;
   a.colpts = h->dColPts.p;

@@ -22,7 +22,7 @@ namespace bemgpu {
 namespace {
 
 constexpr int VT = 128;  // threads of a pass-V CTA
-constexpr int UT = 128;  // threads of a pass-U CTA
+constexpr int UT = 512;  // threads of a pass-U CTA (16 warps split a leaf's block list)
 
 template <typename T, bool F32> struct Acc;
 // FP64 accumulation
@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(UT) hmv_upass(
     const T* __restrict__ Up, const T* __restrict__ F, const double2* __restrict__ x,
     int64_t ldx, const double2* __restrict__ t, int64_t ldt, double2* __restrict__ y,
     int64_t ldy, int accumulate) {
-  __shared__ double2 part[UT / 32][32][R];
+  __shared__ double2 part[UT / 32][32];
   const LeafRows lf = leaves[blockIdx.x];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int beg = list_off[blockIdx.x], end = list_off[blockIdx.x + 1];
@@ -179,19 +179,18 @@ __global__ void __launch_bounds__(UT) hmv_upass(
       }
     }
 #pragma unroll
-    for (int r = 0; r < R; r++) part[w][lane][r] = make_double2(ax[r], ay[r]);
-    __syncthreads();
-    if (w == 0 && active) {
+    for (int r = 0; r < R; r++) {
+      part[w][lane] = make_double2(ax[r], ay[r]);
+      __syncthreads();
+      if (w == 0 && active) {
+        double2 s = part[0][lane];
 #pragma unroll
-      for (int r = 0; r < R; r++) {
-        double2 s = part[0][lane][r];
-#pragma unroll
-        for (int q = 1; q < UT / 32; q++) s = cadd(s, part[q][lane][r]);
+        for (int q = 1; q < UT / 32; q++) s = cadd(s, part[q][lane]);
         double2* yp = y + r * ldy + grow;
         *yp = accumulate ? cadd(*yp, s) : s;
       }
+      __syncthreads();
     }
-    __syncthreads();
   }
 }
 
@@ -259,7 +258,7 @@ __global__ void __launch_bounds__(UT) hmv32_upass(
     const float2* __restrict__ Up, const float2* __restrict__ F, const float2* __restrict__ x,
     int64_t ldx, const float2* __restrict__ t, int64_t ldt, double2* __restrict__ y,
     int64_t ldy, int accumulate) {
-  __shared__ float4 part[UT / 32][32][R];
+  __shared__ float4 part[UT / 32][32];
   const LeafRows lf = leaves[blockIdx.x];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int beg = list_off[blockIdx.x], end = list_off[blockIdx.x + 1];
@@ -312,23 +311,25 @@ __global__ void __launch_bounds__(UT) hmv32_upass(
       }
     }
 #pragma unroll
-    for (int r = 0; r < R; r++) part[w][lane][r] = make_float4(sx[r].hi, sx[r].lo, sy[r].hi, sy[r].lo);
-    __syncthreads();
-    if (w == 0 && active) {
-#pragma unroll
-      for (int r = 0; r < R; r++) {
-        double vx = 0, vy = 0;  // one FP64 sum per row: off the inner loops
+    for (int r = 0; r < R; r++) {
+      part[w][lane] = make_float4(sx[r].hi, sx[r].lo, sy[r].hi, sy[r].lo);
+      __syncthreads();
+      if (w == 0 && active) {
+        TwoSum ux, uy;  // combine the warps' partials in FP32, then one FP64 add
 #pragma unroll
         for (int q = 0; q < UT / 32; q++) {
-          const float4 p = part[q][lane][r];
-          vx += (double)p.x + (double)p.y;
-          vy += (double)p.z + (double)p.w;
+          const float4 p = part[q][lane];
+          ux.add(p.x);
+          ux.add(p.y);
+          uy.add(p.z);
+          uy.add(p.w);
         }
+        const double2 v = make_double2((double)ux.hi + (double)ux.lo, (double)uy.hi + (double)uy.lo);
         double2* yp = y + r * ldy + grow;
-        *yp = accumulate ? cadd(*yp, make_double2(vx, vy)) : make_double2(vx, vy);
+        *yp = accumulate ? cadd(*yp, v) : v;
       }
+      __syncthreads();
     }
-    __syncthreads();
   }
 }
 

@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(256) nearfield_regular32_kernel(
   if (special_bits[g >> 5] & (1u << (g & 31))) return;
   const int r = e % b.m, c = e / b.m;
   const int64_t row = b.r0 + r, col = b.c0 + c;
-  OpsF o = ops_regular32(E, EF, row, col, k, c_rules);
+  OpsF o = ops_regular32(EF, row, col, k, c_rules);
   float2 p, d;
   substitute32(o, bc[col], alpha, p, d);
   phi[g] = p;

@@ -360,23 +360,29 @@ struct OpsF {
   float2 L, M, Mt, N;
 };
 
+// c_p - c_q from the two-float centroids (see ElemF), all FP32
+__device__ __forceinline__ void centroid_diff(const ElemF& P, const ElemF& Q, float& dx,
+                                              float& dy, float& dz) {
+  dx = (P.c_hi[0] - Q.c_hi[0]) + (P.c_lo[0] - Q.c_lo[0]);
+  dy = (P.c_hi[1] - Q.c_hi[1]) + (P.c_lo[1] - Q.c_lo[1]);
+  dz = (P.c_hi[2] - Q.c_hi[2]) + (P.c_lo[2] - Q.c_lo[2]);
+}
+
 // Same integrand and 16-point rule as ops_regular, evaluated in FP32. The
-// centroid difference c_p - c_q is formed in FP64 and rounded once; source
-// points are offsets from c_q, so r = |p - q| keeps ~7 significant digits
-// even for neighbouring panels.
-__device__ __forceinline__ OpsF ops_regular32(const Elem* __restrict__ E,
-                                              const ElemF* __restrict__ EF, int64_t row,
+// centroid difference c_p - c_q keeps ~7 significant digits (two-float
+// centroids); source points are offsets from c_q, so r = |p - q| keeps ~7
+// significant digits even for neighbouring panels.
+__device__ __forceinline__ OpsF ops_regular32(const ElemF* __restrict__ EF, int64_t row,
                                               int64_t col, float k, const QuadRules& R) {
-  const float dx = (float)(E[row].c[0] - E[col].c[0]);
-  const float dy = (float)(E[row].c[1] - E[col].c[1]);
-  const float dz = (float)(E[row].c[2] - E[col].c[2]);
+  float dx, dy, dz;
+  centroid_diff(EF[row], EF[col], dx, dy, dz);
   const ElemF& Q = EF[col];
   const float npx = EF[row].nrm[0], npy = EF[row].nrm[1], npz = EF[row].nrm[2];
   const float nqx = Q.nrm[0], nqy = Q.nrm[1], nqz = Q.nrm[2];
   const float upNq = npx * nqx + npy * nqy + npz * nqz;
   const float inv4pi = 0.0795774715459476679f;
   float Lx = 0, Ly = 0, Mx = 0, My = 0, Tx = 0, Ty = 0, Nx = 0, Ny = 0;
-#pragma unroll
+#pragma unroll 2
   for (int i = 0; i < 16; i++) {
     const float a1 = R.freg_x1[i], a2 = R.freg_x2[i], a3 = 1.0f - a2 - a1, w = R.freg_w[i];
     const float rx = dx - (a1 * Q.v[0] + a2 * Q.v[3] + a3 * Q.v[6]);
