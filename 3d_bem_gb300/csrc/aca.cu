@@ -46,47 +46,66 @@ template <> __device__ __forceinline__ float2 from_d<float2>(double2 a) {
   return make_float2((float)a.x, (float)a.y);
 }
 
-struct Red {
-  double v[NW_MAX];
-  int i[NW_MAX];
-  double2 c[NW_MAX];
+// real type and complex helpers of the storage precision
+template <typename T> struct Cx;
+template <> struct Cx<double2> {
+  using R = double;
+  static __device__ __forceinline__ double2 make(double x, double y) { return make_double2(x, y); }
+};
+template <> struct Cx<float2> {
+  using R = float;
+  static __device__ __forceinline__ float2 make(float x, float y) { return make_float2(x, y); }
 };
 
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
+// complex reciprocal (Smith) in the storage precision
+template <typename T>
+__device__ __forceinline__ T cx_recip(T b) {
+  using R = typename Cx<T>::R;
+  if (fabs(b.x) >= fabs(b.y)) {
+    const R r = b.y / b.x, d = b.x + b.y * r;
+    return Cx<T>::make((R)1 / d, -r / d);
+  }
+  const R r = b.x / b.y, d = b.y + b.x * r;
+  return Cx<T>::make(r / d, (R)-1 / d);
 }
-__device__ __forceinline__ float warp_sumf(float v) {
+
+template <typename R>
+struct Red {
+  R v[NW_MAX];
+  int i[NW_MAX];
+  R cx[NW_MAX], cy[NW_MAX];
+};
+
+template <typename R>
+__device__ __forceinline__ R warp_sum(R v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
 
 // block-wide sum, result returned to every thread (deterministic order)
-template <int NT>
-__device__ __forceinline__ double block_sum(double v, Red& red) {
+template <int NT, typename R>
+__device__ __forceinline__ R block_sum(R v, Red<R>& red) {
   constexpr int NW = NT / 32;
   v = warp_sum(v);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   __syncthreads();
   if (l == 0) red.v[w] = v;
   __syncthreads();
-  double s = 0;
+  R s = 0;
 #pragma unroll
   for (int q = 0; q < NW; q++) s += red.v[q];
   return s;
 }
 
-// block-wide argmax of |.|, first index among equal maxima (Eigen maxCoeff)
-template <int NT>
-__device__ __forceinline__ void block_argmax(double v, int idx, Red& red, double& best,
-                                             int& bidx) {
+// block-wide argmax, first index among equal maxima (Eigen maxCoeff)
+template <int NT, typename R>
+__device__ __forceinline__ void block_argmax(R v, int idx, Red<R>& red, R& best, int& bidx) {
   constexpr int NW = NT / 32;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    double v2 = __shfl_xor_sync(0xffffffffu, v, o);
-    int i2 = __shfl_xor_sync(0xffffffffu, idx, o);
+    const R v2 = __shfl_xor_sync(0xffffffffu, v, o);
+    const int i2 = __shfl_xor_sync(0xffffffffu, idx, o);
     if (v2 > v || (v2 == v && i2 < idx)) {
       v = v2;
       idx = i2;
@@ -227,10 +246,12 @@ __device__ void residual_row(const AcaArgs& a, const FarBlock& fb, const T* U, c
 __device__ __forceinline__ double mag2(double2 v) { return v.x * v.x + v.y * v.y; }
 __device__ __forceinline__ float mag2(float2 v) { return v.x * v.x + v.y * v.y; }
 
-// argmax_i |v[i]| over i != exclude; best = |v[bidx]|
+// argmax_i |v[i]| over i != exclude; best = |v[bidx]| (compares |v|^2,
+// which orders like |v|)
 template <typename T, int NT>
-__device__ void argmax_abs(const T* v, int len, int exclude, Red& red, double& best, int& bidx) {
-  using R = decltype(mag2(v[0]));
+__device__ void argmax_abs(const T* v, int len, int exclude, Red<typename Cx<T>::R>& red,
+                           typename Cx<T>::R& best, int& bidx) {
+  using R = typename Cx<T>::R;
   R bv = (R)-1;
   int bi = 0x7fffffff;
   for (int i = threadIdx.x; i < len; i += NT) {
@@ -240,88 +261,74 @@ __device__ void argmax_abs(const T* v, int len, int exclude, Red& red, double& b
       bi = i;
     }
   }
-  block_argmax<NT>((double)bv, bi, red, best, bidx);
+  block_argmax<NT, R>(bv, bi, red, best, bidx);
   if (bidx < 0 || bidx >= len) {  // all entries NaN: report a zero pivot at 0
     bidx = 0;
-    best = 0.0;
+    best = 0;
   }
   best = sqrt(best);
 }
 
 // normEstimate increment (hmatrix.cpp:570-574):
-// |alpha|^2 |row|^2 |col|^2 + sum_{l<k} 2 conj(alpha) s_l (col^H U_l)(V_l row^H)
+// |alpha|^2 |row|^2 |col|^2 + sum_{l<k} 2 conj(alpha) s_l (col^H U_l)(V_l row^H),
+// all in the storage precision (the estimate only steers the stopping test)
 template <typename T, int NT>
 __device__ void norm_increment(const FarBlock& fb, const T* U, const T* V, const T* S, int k,
-                               const T* col, const T* row, double2 alpha, Red& red,
-                               double& gain, double2& incr) {
-  // per-thread partial sums in the storage precision, combined in FP64
-  double cn, rn;
-  {
-    using R = decltype(mag2(col[0]));
-    R c0 = 0, r0 = 0;
-    for (int i = threadIdx.x; i < fb.m; i += NT) c0 += mag2(col[i]);
-    for (int j = threadIdx.x; j < fb.n; j += NT) r0 += mag2(row[j]);
-    cn = block_sum<NT>((double)c0, red);
-    rn = block_sum<NT>((double)r0, red);
-  }
-  gain = cabs2(alpha) * rn * cn;
+                               const T* col, const T* row, T alpha, Red<typename Cx<T>::R>& red,
+                               typename Cx<T>::R& gain, T& incr) {
+  using R = typename Cx<T>::R;
+  R c0 = 0, r0 = 0;
+  for (int i = threadIdx.x; i < fb.m; i += NT) c0 += mag2(col[i]);
+  for (int j = threadIdx.x; j < fb.n; j += NT) r0 += mag2(row[j]);
+  const R cn = block_sum<NT, R>(c0, red);
+  const R rn = block_sum<NT, R>(r0, red);
+  gain = mag2(alpha) * rn * cn;
   constexpr int NW = NT / 32;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  double2 acc = make_double2(0, 0);
+  R accx = 0, accy = 0;
+  const T ca = Cx<T>::make(alpha.x, -alpha.y);
   for (int l = w; l < k; l += NW) {
-    double cux, cuy, vrx, vry;
     const T* Ul = U + (int64_t)l * fb.m;
     const T* Vl = V + (int64_t)l * fb.n;
-    if constexpr (sizeof(T) == sizeof(float2)) {
-      // FP32 partial sums (stopping heuristic only), combined in FP64
-      float ax = 0, ay = 0, bx = 0, by = 0;
-      for (int i = lane; i < fb.m; i += 32) {
-        const float2 c = col[i], u = Ul[i];  // conj(c) * u
-        ax += c.x * u.x + c.y * u.y;
-        ay += c.x * u.y - c.y * u.x;
-      }
-      for (int j = lane; j < fb.n; j += 32) {
-        const float2 v = Vl[j], r = row[j];  // v * conj(r)
-        bx += v.x * r.x + v.y * r.y;
-        by += v.y * r.x - v.x * r.y;
-      }
-      cux = warp_sumf(ax);
-      cuy = warp_sumf(ay);
-      vrx = warp_sumf(bx);
-      vry = warp_sumf(by);
-    } else {
-      cux = cuy = vrx = vry = 0;
-      for (int i = lane; i < fb.m; i += 32) {
-        double2 c = to_d(col[i]), u = to_d(Ul[i]);  // conj(c) * u
-        cux += c.x * u.x + c.y * u.y;
-        cuy += c.x * u.y - c.y * u.x;
-      }
-      for (int j = lane; j < fb.n; j += 32) {
-        double2 v = to_d(Vl[j]), r = to_d(row[j]);  // v * conj(r)
-        vrx += v.x * r.x + v.y * r.y;
-        vry += v.y * r.x - v.x * r.y;
-      }
-      cux = warp_sum(cux);
-      cuy = warp_sum(cuy);
-      vrx = warp_sum(vrx);
-      vry = warp_sum(vry);
+    R ax = 0, ay = 0, bx = 0, by = 0;
+    for (int i = lane; i < fb.m; i += 32) {
+      const T c = col[i], u = Ul[i];  // conj(c) * u
+      ax += c.x * u.x + c.y * u.y;
+      ay += c.x * u.y - c.y * u.x;
     }
-    double2 t = cmul(cmul(cconj(alpha), to_d(S[l])), cmul(make_double2(cux, cuy), make_double2(vrx, vry)));
-    acc = cadd(acc, cscale(2.0, t));
+    for (int j = lane; j < fb.n; j += 32) {
+      const T vv = Vl[j], r = row[j];  // v * conj(r)
+      bx += vv.x * r.x + vv.y * r.y;
+      by += vv.y * r.x - vv.x * r.y;
+    }
+    ax = warp_sum(ax);
+    ay = warp_sum(ay);
+    bx = warp_sum(bx);
+    by = warp_sum(by);
+    const T t = cx_mul(cx_mul(ca, S[l]), cx_mul(Cx<T>::make(ax, ay), Cx<T>::make(bx, by)));
+    accx += 2 * t.x;
+    accy += 2 * t.y;
   }
   __syncthreads();
-  if (lane == 0) red.c[w] = acc;
+  if (lane == 0) {
+    red.cx[w] = accx;
+    red.cy[w] = accy;
+  }
   __syncthreads();
-  incr = make_double2(gain, 0.0);
+  incr = Cx<T>::make(gain, 0);
 #pragma unroll
-  for (int q = 0; q < NW; q++) incr = cadd(incr, red.c[q]);
+  for (int q = 0; q < NW; q++) {
+    incr.x += red.cx[q];
+    incr.y += red.cy[q];
+  }
   __syncthreads();
 }
 
 template <int MODE, typename T, int NT>
 __global__ void __launch_bounds__(NT) aca_kernel(AcaArgs a) {
   __shared__ T coef[ACA_MAX_KCAP];
-  __shared__ Red red;
+  using R = typename Cx<T>::R;
+  __shared__ Red<R> red;
   const int bi = a.order[blockIdx.x];
   const FarBlock fb = a.far[bi];
   const int m = fb.m, n = fb.n;
@@ -331,9 +338,10 @@ __global__ void __launch_bounds__(NT) aca_kernel(AcaArgs a) {
   T* U = (T*)a.U + fb.uoff;
   T* V = (T*)a.V + fb.voff;
   T* S = (T*)a.S + fb.soff;
-  const double tol = a.tol;
+  const R tol = (R)a.tol;
+  const R tiny = (R)TINY;
   int k = 0;
-  double2 est = make_double2(0, 0);
+  T est = Cx<T>::make(0, 0);
   bool converged = false;
 
   if (!a.extra) {
@@ -343,25 +351,26 @@ __global__ void __launch_bounds__(NT) aca_kernel(AcaArgs a) {
     int ri = -1;
     while (k < kmax) {
       const T* colv = U + (int64_t)(k > 0 ? k - 1 : 0) * m;
-      double cmax;
+      R cmax;
       argmax_abs<T, NT>(colv, m, k >= 1 ? ri : -1, red, cmax, ri);
-      if (cmax <= TINY && k >= 1) break;
+      if (cmax <= tiny && k >= 1) break;
       T* rowv = V + (int64_t)k * n;
       residual_row<MODE, T, NT>(a, fb, U, V, S, k, ri, rowv, coef);
-      double rmax;
+      R rmax;
       argmax_abs<T, NT>(rowv, n, -1, red, rmax, ci);
-      if (rmax <= TINY && k >= 1) break;
+      if (rmax <= tiny && k >= 1) break;
       T* newcol = U + (int64_t)k * m;
       residual_col<MODE, T, NT>(a, fb, U, V, S, k, ci, newcol, coef);
-      double2 alpha = cdiv(make_double2(1.0, 0.0), to_d(rowv[ci]));
-      if (threadIdx.x == 0) S[k] = from_d<T>(alpha);
+      const T alpha = cx_recip(rowv[ci]);
+      if (threadIdx.x == 0) S[k] = alpha;
       __syncthreads();
-      double gain;
-      double2 incr;
+      R gain;
+      T incr;
       norm_increment<T, NT>(fb, U, V, S, k, newcol, rowv, alpha, red, gain, incr);
       k++;
-      est = cadd(est, incr);
-      double target = tol * tol * est.x;
+      est.x += incr.x;
+      est.y += incr.y;
+      const R target = tol * tol * est.x;
       if (tol > 0 && gain < target) {
         converged = true;
         break;
@@ -373,40 +382,43 @@ __global__ void __launch_bounds__(NT) aca_kernel(AcaArgs a) {
     const int npiv = a.piv_cnt[bi];
     for (int p = 0; p < npiv && k < kmax; p++) {
       int ri = piv[2 * p], ci = piv[2 * p + 1];
-      double2 pivv = to_d(aca_entry<MODE, T>(a, fb.r0 + ri, fb.c0 + ci));
-      double pabs = sqrt(cabs2(pivv));
-      if (pabs < TINY) continue;
+      const T pivv = aca_entry<MODE, T>(a, fb.r0 + ri, fb.c0 + ci);
+      const R pabs2 = mag2(pivv);
+      if (sqrt(pabs2) < tiny) continue;
       // approximation already good at the seed?
-      double2 approx = make_double2(0, 0);
-      for (int l = 0; l < k; l++)
-        approx = cadd(approx, cmul(cmul(to_d(U[(int64_t)l * m + ri]), to_d(S[l])),
-                                   to_d(V[(int64_t)l * n + ci])));
-      if (sqrt(cabs2(cdiv(csub(pivv, approx), pivv))) < tol) continue;
+      T approx = Cx<T>::make(0, 0);
+      for (int l = 0; l < k; l++) {
+        const T t = cx_mul(cx_mul(U[(int64_t)l * m + ri], S[l]), V[(int64_t)l * n + ci]);
+        approx.x += t.x;
+        approx.y += t.y;
+      }
+      if (sqrt(mag2(cx_sub(pivv, approx)) / pabs2) < tol) continue;
       residual_col<MODE, T, NT>(a, fb, U, V, S, k, ci, U + (int64_t)k * m, coef);
       bool first = true;
       while (k < kmax) {
         const T* colv = first ? U + (int64_t)k * m : U + (int64_t)(k - 1) * m;
-        double cmax;
+        R cmax;
         argmax_abs<T, NT>(colv, m, first ? -1 : ri, red, cmax, ri);
         first = false;
-        if (cmax <= TINY && k >= 1) break;
+        if (cmax <= tiny && k >= 1) break;
         T* rowv = V + (int64_t)k * n;
         residual_row<MODE, T, NT>(a, fb, U, V, S, k, ri, rowv, coef);
-        double rmax;
+        R rmax;
         argmax_abs<T, NT>(rowv, n, -1, red, rmax, ci);
-        if (rmax <= TINY && k >= 1) break;
+        if (rmax <= tiny && k >= 1) break;
         T* newcol = U + (int64_t)k * m;
         residual_col<MODE, T, NT>(a, fb, U, V, S, k, ci, newcol, coef);
-        double2 alpha = cdiv(make_double2(1.0, 0.0), to_d(rowv[ci]));
-        if (threadIdx.x == 0) S[k] = from_d<T>(alpha);
+        const T alpha = cx_recip(rowv[ci]);
+        if (threadIdx.x == 0) S[k] = alpha;
         __syncthreads();
-        double gain;
-        double2 incr;
+        R gain;
+        T incr;
         norm_increment<T, NT>(fb, U, V, S, k, newcol, rowv, alpha, red, gain, incr);
-        double2 old = est;
+        const T old = est;
         k++;
-        est = cadd(est, incr);
-        double target = tol * tol * est.x;
+        est.x += incr.x;
+        est.y += incr.y;
+        const R target = tol * tol * est.x;
         if (tol > 0 && gain < target) {
           if (gain < 0.1 * target) {  // roll back the last rank (hmatrix.cpp:724-728)
             k--;
