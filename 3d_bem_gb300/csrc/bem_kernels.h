@@ -123,4 +123,10 @@ int launch_aca(const AcaArgs& a, int threads, cudaStream_t s);
 constexpr int ACA_BIG_MN = 512;  // blocks with m + n >= this get 512-thread CTAs
 int launch_hmatvec(const HmvArgs& a, cudaStream_t s);  // returns kernels launched
 
+// Fixed device scratch of the allocation-free H-matvec (complex FP64 entries,
+// 32 MiB): holds ldt x nrhs projections of one pass.
+constexpr int64_t HMV_NOALLOC_SCRATCH = int64_t(1) << 21;
+int64_t hmatvec_noalloc_capacity();
+cudaError_t hmatvec_noalloc_scratch(double2** out);
+
 }  // namespace bemgpu

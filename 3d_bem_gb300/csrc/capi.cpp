@@ -901,6 +901,60 @@ bem_status bem_hmatvec_device(bem_handle* h, int32_t which, const void* x, void*
   });
 }
 
+// Allocation-free H-matvec: same kernels and arithmetic as bem_hmatvec_device
+// with fp64 products, but the projections t live in the library's fixed
+// device array (hmatvec.cu) instead of the handle's allocated buffer, and
+// nothing on this path allocates GPU memory.
+bem_status bem_hmatvec_noalloc(bem_handle* h, int32_t which, const void* x, void* y,
+                               int64_t nrhs, int32_t accumulate) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] {
+    require(which == 0 || which == 1, BEM_EINVAL, "which must be 0 (phi) or 1 (dPhi)");
+    require(x && y && nrhs >= 1, BEM_EINVAL, "bad arguments");
+    DevHM& m = h->hm[which];
+    require(m.assembled, BEM_EINVAL, "matrix not assembled");
+    const int64_t nrows = h->points_mode ? (int64_t)h->rows.perm.size() : h->N;
+    const int64_t ncols = h->points_mode ? (int64_t)h->cols.perm.size() : h->N;
+    const int64_t ldt = std::max<int64_t>(h->L.s_size, 1);
+    const int64_t cap = hmatvec_noalloc_capacity();
+    require(ldt <= cap, BEM_EINVAL,
+            "bem_hmatvec_noalloc: the matrix's rank reservation exceeds the fixed scratch "
+            "(2^21 complex values); use bem_hmatvec_device");
+    double2* t = nullptr;
+    CK(hmatvec_noalloc_scratch(&t));
+    const int64_t chunk = std::min<int64_t>(8, cap / ldt);
+    const double2* xd = (const double2*)x;
+    double2* yd = (double2*)y;
+    for (int64_t r0 = 0; r0 < nrhs; r0 += chunk) {
+      HmvArgs a{};
+      a.precision = m.prec;
+      a.fp32_math = 0;
+      a.nrhs = (int)std::min<int64_t>(chunk, nrhs - r0);
+      a.far = h->dFar.p;
+      a.rank = m.rank.p;
+      a.nfar = (int64_t)h->L.far.size();
+      a.nearb = h->dNear.p;
+      a.leaves = h->dLeaves.p;
+      a.nleaves = (int64_t)h->L.leaves.size();
+      a.list_off = h->dListOff.p;
+      a.list = h->dList.p;
+      a.U = m.U.p;
+      a.V = m.V.p;
+      a.S = m.S.p;
+      a.F = m.F.p;
+      a.x = xd + r0 * ncols;
+      a.ldx = ncols;
+      a.t = t;
+      a.ldt = ldt;
+      a.y = yd + r0 * nrows;
+      a.ldy = nrows;
+      a.accumulate = accumulate;
+      h->launches += launch_hmatvec(a, h->stream);
+    }
+    CK(cudaGetLastError());
+  });
+}
+
 bem_status bem_get_block(bem_handle* h, int32_t which, int64_t block, int64_t* rank, double* U,
                          double* s, double* V, double* F) {
   if (!h) return BEM_EINVAL;

@@ -15,6 +15,8 @@
 //                                  for the iterative-refinement residual;
 //   float2 storage,  FP32 math  -- FP32 products inside a block, FP64 sums
 //                                  across blocks; the inner GMRES operator.
+#include <mutex>
+
 #include "bem_kernels.h"
 #include "quadrature.cuh"
 
@@ -390,6 +392,39 @@ void launch_t(const HmvArgs& a, cudaStream_t s) {
   }
 }
 }  // namespace
+
+// ---------------------------------------------------------------------------
+// Fixed scratch for bem_hmatvec_noalloc: the per-block projections t = s o (V x)
+// of one pass (ldt x nrhs complex FP64 values) live in this file-scope device
+// array instead of a cudaMalloc'd buffer. Every GPU that loads the library
+// holds it (32 MiB) until the process exits; all calls share it, so calls that
+// overlap on the GPU race. Nothing in it needs clearing: pass V writes every
+// entry pass U reads.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) double2 g_noalloc_t[HMV_NOALLOC_SCRATCH];
+
+int64_t hmatvec_noalloc_capacity() { return HMV_NOALLOC_SCRATCH; }
+
+// Device address of the scratch array on the current device. The first call
+// on each device looks it up (cudaGetSymbolAddress, with that device current);
+// later calls reuse the cached address.
+cudaError_t hmatvec_noalloc_scratch(double2** out) {
+  static std::mutex mu;
+  static void* addr[256] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_t);
+    if (e != cudaSuccess) return e;
+    addr[dev] = p;
+  }
+  *out = static_cast<double2*>(addr[dev]);
+  return cudaSuccess;
+}
 
 int launch_hmatvec(const HmvArgs& a, cudaStream_t s) {
   if (a.precision == 0) launch_t<double2, false>(a, s);

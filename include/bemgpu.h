@@ -119,6 +119,22 @@ bem_status bem_hmatvec(bem_handle* h, int32_t which, const double* x, double* y,
 bem_status bem_hmatvec_device(bem_handle* h, int32_t which, const void* x, void* y,
                               int64_t nrhs, int32_t accumulate);
 
+/* Allocation-free variant of bem_hmatvec_device (no counterpart in the
+ * reference). For callers that must not allocate GPU memory during the call:
+ * code running while a CUDA stream is being captured into a graph, real-time
+ * loops that forbid allocator calls, and hosts whose GPU memory is handed out
+ * by an outside pool. x and y are device pointers the caller owns; the
+ * per-block projections go to a fixed 32 MiB device array inside the library
+ * (2^21 complex-FP64 values: the matrix's total rank reservation times the
+ * vectors per pass must fit, or the call returns BEM_EINVAL). The call never
+ * calls cudaMalloc / cudaFree. Every call shares that array, so calls that
+ * overlap on the GPU (other streams, other handles) race; the first call on
+ * each device looks the array up (cudaGetSymbolAddress) and should come before
+ * any stream capture. FP64 arithmetic on the stored entries, identical to
+ * bem_hmatvec_device. */
+bem_status bem_hmatvec_noalloc(bem_handle* h, int32_t which, const void* x, void* y,
+                               int64_t nrhs, int32_t accumulate);
+
 /* Block data of the assembled matrix `which`, block index in partition
  * order. Admissible: rank returned, U (m x k col-major), s (k), V (k x n
  * row-major) written when non-NULL. Full: *rank = -1, F (m x n col-major). */
