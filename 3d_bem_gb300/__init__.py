@@ -36,8 +36,9 @@ EXPORTS = [
     "bem_get_permutation", "bem_get_partition", "bem_set_bc", "bem_operators",
     "bem_assemble", "bem_hmatvec", "bem_hmatvec_device", "bem_get_block", "bem_get_ranks",
     "bem_gmres", "bem_solve", "bem_solve_device", "bem_sweep", "bem_points_assemble",
-    "bem_launch_count", "bem_stream", "bem_hmatvec_noalloc",
+    "bem_launch_count", "bem_stream", "bem_hmatvec_noalloc", "bem_hmatvec_device_ex",
 ]
+BEM_ARITH_FP64, BEM_ARITH_FP32, BEM_ARITH_TWOFLOAT = 0, 1, 2
 
 
 class BemError(RuntimeError):
@@ -106,6 +107,7 @@ def lib():
     L.bem_hmatvec.argtypes = [vp, i32, vp, vp, i64, i32]
     L.bem_hmatvec_device.argtypes = [vp, i32, vp, vp, i64, i32]
     L.bem_hmatvec_noalloc.argtypes = [vp, i32, vp, vp, i64, i32]
+    L.bem_hmatvec_device_ex.argtypes = [vp, i32, vp, vp, i64, i32, i32]
     L.bem_get_block.argtypes = [vp, i32, i64, P(i64), vp, vp, vp, vp]
     L.bem_get_ranks.argtypes = [vp, i32, vp]
     L.bem_gmres.argtypes = [vp, vp, vp, i64, P(SolveInfo)]

@@ -86,7 +86,8 @@ struct AcaArgs {
 
 struct HmvArgs {
   int precision;  // 0: double2 storage, 1: float2 storage
-  int fp32_math;  // float2 storage only: FP32 products within a block, FP64 across blocks
+  int fp32_math;  // float2 storage only: 0 FP64 arithmetic, 1 FP32 products with
+                  // compensated FP32 sums, 2 two-float (FP64-accurate) on FP32 units
   int nrhs;
   const FarBlock* far;
   const int32_t* rank;

@@ -355,25 +355,33 @@ void assemble(bem_handle* h, double freq, double* t_near, double* t_aca) {
   if (t_aca) *t_aca = elapsed(h->ev[1], h->ev[2]);
 }
 
-// y = (acc ? y : 0) + H x. f32: FP32 products within blocks (complex-FP32
-// storage only); otherwise FP64 arithmetic on the stored entries.
+// Arithmetic of an H-matvec on complex-FP32 storage.
+enum Arith { ARITH_FP64 = 0, ARITH_FP32 = 1, ARITH_TWOFLOAT = 2 };
+
+// y = (acc ? y : 0) + H x. arith applies to complex-FP32 storage: FP64
+// products, FP32 products with compensated sums (inner GMRES operator), or
+// two-float products on the FP32 units (FP64-accurate refinement residual).
+// Complex-FP64 storage always uses FP64 arithmetic.
 void hmatvec_dev(bem_handle* h, int which, const double2* x, double2* y, int64_t R, int acc,
-                 bool f32 = false) {
+                 int arith = ARITH_FP64) {
   require(which == 0 || which == 1, BEM_EINVAL, "which must be 0 (phi) or 1 (dPhi)");
   DevHM& m = h->hm[which];
   require(m.assembled, BEM_EINVAL, "matrix not assembled");
   const int64_t nrows = h->points_mode ? (int64_t)h->rows.perm.size() : h->N;
   const int64_t ncols = h->points_mode ? (int64_t)h->cols.perm.size() : h->N;
+  if (m.prec == 0) arith = ARITH_FP64;
+  const int64_t per = arith == ARITH_TWOFLOAT ? 4 : 8;  // vectors per pass
+  const size_t words = arith == ARITH_TWOFLOAT ? 2 : 1;  // float2 words per value
   h->dT.ensure(std::max<int64_t>(h->L.s_size, 1) * 8);
-  if (f32 && m.prec == 1) {
-    h->dTf.ensure(std::max<int64_t>(h->L.s_size, 1) * 8);
-    h->dXf.ensure((size_t)ncols * 8);
+  if (arith != ARITH_FP64) {
+    h->dTf.ensure(std::max<int64_t>(h->L.s_size, 1) * 8 * words);
+    h->dXf.ensure((size_t)ncols * 8 * words);
   }
-  for (int64_t r0 = 0; r0 < R; r0 += 8) {
+  for (int64_t r0 = 0; r0 < R; r0 += per) {
     HmvArgs a{};
     a.precision = m.prec;
-    a.fp32_math = (f32 && m.prec == 1) ? 1 : 0;
-    a.nrhs = (int)std::min<int64_t>(8, R - r0);
+    a.fp32_math = arith;
+    a.nrhs = (int)std::min<int64_t>(per, R - r0);
     a.far = h->dFar.p;
     a.rank = m.rank.p;
     a.nfar = (int64_t)h->L.far.size();
@@ -564,7 +572,7 @@ void gmres_dev(bem_handle* h, const double2* b, double2* x, int R, bem_solve_inf
       if (outer == 0 && x_zero) {
         CK(cudaMemcpyAsync(g.r.p, b, (size_t)R * N * sizeof(double2), cudaMemcpyDeviceToDevice, s));
       } else {
-        hmatvec_dev(h, 1, x, g.r.p, R, 0, false);
+        hmatvec_dev(h, 1, x, g.r.p, R, 0, ARITH_TWOFLOAT);
         krylov_residual(b, g.r.p, (int64_t)R * N, s);
         h->launches++;
       }
@@ -897,6 +905,17 @@ bem_status bem_hmatvec_device(bem_handle* h, int32_t which, const void* x, void*
   return guarded(h, [&] {
     require(x && y && nrhs >= 1, BEM_EINVAL, "bad arguments");
     hmatvec_dev(h, which, (const double2*)x, (double2*)y, nrhs, accumulate);
+    CK(cudaGetLastError());
+  });
+}
+
+bem_status bem_hmatvec_device_ex(bem_handle* h, int32_t which, const void* x, void* y,
+                                 int64_t nrhs, int32_t accumulate, int32_t arith) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] {
+    require(x && y && nrhs >= 1, BEM_EINVAL, "bad arguments");
+    require(arith >= 0 && arith <= 2, BEM_EINVAL, "arith must be 0, 1 or 2");
+    hmatvec_dev(h, which, (const double2*)x, (double2*)y, nrhs, accumulate, arith);
     CK(cudaGetLastError());
   });
 }

@@ -394,6 +394,186 @@ void launch_t(const HmvArgs& a, cudaStream_t s) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
+// Double-float variant (complex-FP32 storage): FP64-accurate products of the
+// stored operator computed on the FP32 units. x and t are unevaluated sums
+// hi + lo of two floats; each stored entry a (exact in FP32) times hi is
+// split exactly with an FMA (p + e = a * hi), and sums run in two-float
+// precision (~2^-48). Used for the iterative-refinement residual b - A x,
+// which needs ~1e-14 relative accuracy but would be FP64-pipe-bound in
+// native FP64 on GB300.
+// ---------------------------------------------------------------------------
+struct DF {
+  float hi = 0, lo = 0;
+  // this += a * (yh + yl), a exact
+  __device__ __forceinline__ void fma(float a, float yh, float yl) {
+    const float p = a * yh;
+    const float ep = fmaf(a, yh, -p);
+    const float s = hi + p;
+    const float bb = s - hi;
+    const float e = (hi - (s - bb)) + (p - bb);
+    lo += e + ep + a * yl;
+    hi = s;
+  }
+  __device__ __forceinline__ void add(float h2, float l2) {
+    const float s = hi + h2;
+    const float bb = s - hi;
+    const float e = (hi - (s - bb)) + (h2 - bb);
+    lo += e + l2;
+    hi = s;
+  }
+  __device__ __forceinline__ void shfl_reduce() {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+      const float l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+      add(h2, l2);
+    }
+  }
+};
+
+// complex df accumulator: re + i im
+struct CDF {
+  DF re, im;
+  // += a * y, a = (ax, ay) exact floats, y = (yrh + yrl) + i (yih + yil)
+  __device__ __forceinline__ void fma(float2 a, float4 y) {
+    re.fma(a.x, y.x, y.y);
+    re.fma(-a.y, y.z, y.w);
+    im.fma(a.x, y.z, y.w);
+    im.fma(a.y, y.x, y.y);
+  }
+};
+
+__global__ void to_df_kernel(const double2* __restrict__ x, float4* __restrict__ xd, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x;
+  if (i >= n) return;
+  const double2 v = x[i];
+  const float rh = (float)v.x, ih = (float)v.y;
+  xd[i] = make_float4(rh, (float)(v.x - (double)rh), ih, (float)(v.y - (double)ih));
+}
+
+// t[r][soff + l] = s_l * sum_j V[l, j] x[c0 + j, r], all in two-float
+template <int R>
+__global__ void __launch_bounds__(VT) hmvdf_vpass(const FarBlock* __restrict__ far,
+                                                  const int32_t* __restrict__ rank,
+                                                  const float2* __restrict__ Vp,
+                                                  const float2* __restrict__ Sp,
+                                                  const float4* __restrict__ x, int64_t ldx,
+                                                  float4* __restrict__ t, int64_t ldt) {
+  const FarBlock fb = far[blockIdx.x];
+  const int k = rank[blockIdx.x];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int l = w; l < k; l += VT / 32) {
+    const float2* Vl = Vp + fb.voff + (int64_t)l * fb.n;
+    CDF acc[R];
+#pragma unroll 2
+    for (int j = lane; j < fb.n; j += 32) {
+      const float2 v = __ldg(Vl + j);
+#pragma unroll
+      for (int r = 0; r < R; r++) acc[r].fma(v, __ldg(x + r * ldx + fb.c0 + j));
+    }
+    const float2 s = __ldg(Sp + fb.soff + l);
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      acc[r].re.shfl_reduce();
+      acc[r].im.shfl_reduce();
+      if (lane == 0) {
+        // (s) * (re + i im): s exact floats
+        CDF o;
+        o.fma(s, make_float4(acc[r].re.hi, acc[r].re.lo, acc[r].im.hi, acc[r].im.lo));
+        t[r * ldt + fb.soff + l] = make_float4(o.re.hi, o.re.lo, o.im.hi, o.im.lo);
+      }
+    }
+  }
+}
+
+template <int R>
+__global__ void __launch_bounds__(UT) hmvdf_upass(
+    const LeafRows* __restrict__ leaves, const int32_t* __restrict__ list_off,
+    const int32_t* __restrict__ list, const FarBlock* __restrict__ far,
+    const int32_t* __restrict__ rank, const NearBlock* __restrict__ nearb,
+    const float2* __restrict__ Up, const float2* __restrict__ F, const float4* __restrict__ x,
+    int64_t ldx, const float4* __restrict__ t, int64_t ldt, double2* __restrict__ y,
+    int64_t ldy, int accumulate) {
+  __shared__ float4 part[UT / 32][32];
+  const LeafRows lf = leaves[blockIdx.x];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int beg = list_off[blockIdx.x], end = list_off[blockIdx.x + 1];
+  for (int base = 0; base < lf.size; base += 32) {
+    const int ri = base + lane;
+    const bool active = ri < lf.size;
+    const int64_t grow = lf.start + ri;
+    CDF acc[R];
+    for (int e = beg + w; e < end; e += UT / 32) {
+      const int32_t code = list[e];
+      if (!active) continue;
+      if (code >= 0) {
+        const FarBlock fb = far[code];
+        const int k = rank[code];
+        const float2* U = Up + fb.uoff + (grow - fb.r0);
+#pragma unroll 2
+        for (int l = 0; l < k; l++) {
+          const float2 u = __ldg(U + (int64_t)l * fb.m);
+#pragma unroll
+          for (int r = 0; r < R; r++) acc[r].fma(u, __ldg(t + r * ldt + fb.soff + l));
+        }
+      } else {
+        const NearBlock nb = nearb[-code - 1];
+        const float2* Fb = F + nb.off + (grow - nb.r0);
+#pragma unroll 2
+        for (int j = 0; j < nb.n; j++) {
+          const float2 f = __ldg(Fb + (int64_t)j * nb.m);
+#pragma unroll
+          for (int r = 0; r < R; r++) acc[r].fma(f, __ldg(x + r * ldx + nb.c0 + j));
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      part[w][lane] = make_float4(acc[r].re.hi, acc[r].re.lo, acc[r].im.hi, acc[r].im.lo);
+      __syncthreads();
+      if (w == 0 && active) {
+        CDF sum;
+#pragma unroll
+        for (int q = 0; q < UT / 32; q++) {
+          const float4 p = part[q][lane];
+          sum.re.add(p.x, p.y);
+          sum.im.add(p.z, p.w);
+        }
+        const double2 v = make_double2((double)sum.re.hi + (double)sum.re.lo,
+                                       (double)sum.im.hi + (double)sum.im.lo);
+        double2* yp = y + r * ldy + grow;
+        *yp = accumulate ? cadd(*yp, v) : v;
+      }
+      __syncthreads();
+    }
+  }
+}
+
+template <int R>
+void launchdf_r(const HmvArgs& a, cudaStream_t s) {
+  float4* xd = (float4*)a.xf;
+  float4* td = (float4*)a.tf;
+  to_df_kernel<<<(unsigned)((a.ldx * R + 255) / 256), 256, 0, s>>>(a.x, xd, a.ldx * R);
+  if (a.nfar > 0)
+    hmvdf_vpass<R><<<(unsigned)a.nfar, VT, 0, s>>>(a.far, a.rank, (const float2*)a.V,
+                                                   (const float2*)a.S, xd, a.ldx, td, a.ldt);
+  if (a.nleaves > 0)
+    hmvdf_upass<R><<<(unsigned)a.nleaves, UT, 0, s>>>(
+        a.leaves, a.list_off, a.list, a.far, a.rank, a.nearb, (const float2*)a.U,
+        (const float2*)a.F, xd, a.ldx, td, a.ldt, a.y, a.ldy, a.accumulate);
+}
+
+void launchdf(const HmvArgs& a, cudaStream_t s) {
+  switch (a.nrhs) {
+    case 1: launchdf_r<1>(a, s); break;
+    case 2: launchdf_r<2>(a, s); break;
+    case 3: launchdf_r<3>(a, s); break;
+    case 4: launchdf_r<4>(a, s); break;
+    default: launchdf_r<4>(a, s); break;  // the runtime passes at most 4 per pass
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Fixed scratch for bem_hmatvec_noalloc: the per-block projections t = s o (V x)
 // of one pass (ldt x nrhs complex FP64 values) live in this file-scope device
 // array instead of a cudaMalloc'd buffer. Every GPU that loads the library
@@ -428,8 +608,11 @@ cudaError_t hmatvec_noalloc_scratch(double2** out) {
 
 int launch_hmatvec(const HmvArgs& a, cudaStream_t s) {
   if (a.precision == 0) launch_t<double2, false>(a, s);
-  else if (a.fp32_math) {
+  else if (a.fp32_math == 1) {
     launch32(a, s);
+    return 1 + (a.nfar > 0) + (a.nleaves > 0);
+  } else if (a.fp32_math == 2) {
+    launchdf(a, s);
     return 1 + (a.nfar > 0) + (a.nleaves > 0);
   } else launch_t<float2, false>(a, s);
   return (a.nfar > 0) + (a.nleaves > 0);

@@ -119,6 +119,17 @@ bem_status bem_hmatvec(bem_handle* h, int32_t which, const double* x, double* y,
 bem_status bem_hmatvec_device(bem_handle* h, int32_t which, const void* x, void* y,
                               int64_t nrhs, int32_t accumulate);
 
+/* bem_hmatvec_device with an explicit arithmetic for complex-FP32 storage
+ * (precision 1): 0 = FP64 products (as bem_hmatvec_device), 1 = FP32 products
+ * with compensated FP32 sums (the inner GMRES operator), 2 = two-float
+ * products on the FP32 units, FP64-accurate (the refinement residual).
+ * Complex-FP64 storage always uses FP64 arithmetic. */
+#define BEM_ARITH_FP64 0
+#define BEM_ARITH_FP32 1
+#define BEM_ARITH_TWOFLOAT 2
+bem_status bem_hmatvec_device_ex(bem_handle* h, int32_t which, const void* x, void* y,
+                                 int64_t nrhs, int32_t accumulate, int32_t arith);
+
 /* Allocation-free variant of bem_hmatvec_device (no counterpart in the
  * reference). For callers that must not allocate GPU memory during the call:
  * code running while a CUDA stream is being captured into a graph, real-time
