@@ -634,7 +634,7 @@ void solve_dev(bem_handle* h, double freq, const double2* g_caller, int64_t R, d
   h->launches++;
   CK(cudaEventRecord(h->ev[3], s));
   // rhs = source term (none) + phi * g  (boundaryelementsolver.cpp:578-579)
-  hmatvec_dev(h, 0, h->dG.p, h->dRhs.p, R, 0);
+  hmatvec_dev(h, 0, h->dG.p, h->dRhs.p, R, 0, ARITH_TWOFLOAT);  // FP64-accurate, FP32 units
   CK(cudaEventRecord(h->ev[4], s));
   CK(cudaMemsetAsync(h->dX.p, 0, (size_t)R * N * sizeof(double2), s));
   gmres_dev(h, h->dRhs.p, h->dX.p, (int)R, &loc, true);

@@ -221,33 +221,50 @@ __global__ void __launch_bounds__(VT) hmv32_vpass(const FarBlock* __restrict__ f
   const FarBlock fb = far[blockIdx.x];
   const int k = rank[blockIdx.x];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int l = w; l < k; l += VT / 32) {
-    const float2* Vl = Vp + fb.voff + (int64_t)l * fb.n;
-    float fx[R], fy[R];
+  // each warp streams G rows of V at once (G independent loads in flight per
+  // lane; short rows would otherwise leave one load per reduction chain)
+  constexpr int G = 4;
+  for (int l0 = w * G; l0 < k; l0 += (VT / 32) * G) {
+    const int ng = min(G, k - l0);
+    const float2* V0 = Vp + fb.voff + (int64_t)l0 * fb.n;
+    float fx[G][R], fy[G][R];
 #pragma unroll
-    for (int r = 0; r < R; r++) fx[r] = fy[r] = 0.0f;
-#pragma unroll 4
+    for (int g = 0; g < G; g++)
+#pragma unroll
+      for (int r = 0; r < R; r++) fx[g][r] = fy[g][r] = 0.0f;
     for (int j = lane; j < fb.n; j += 32) {
-      const float2 v = __ldg(Vl + j);
+      float2 v[G];
+#pragma unroll
+      for (int g = 0; g < G; g++) v[g] = g < ng ? __ldg(V0 + (int64_t)g * fb.n + j) : make_float2(0, 0);
 #pragma unroll
       for (int r = 0; r < R; r++) {
         const float2 xv = __ldg(x + r * ldx + fb.c0 + j);
-        fx[r] += v.x * xv.x - v.y * xv.y;
-        fy[r] += v.x * xv.y + v.y * xv.x;
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+          fx[g][r] += v[g].x * xv.x - v[g].y * xv.y;
+          fy[g][r] += v[g].x * xv.y + v[g].y * xv.x;
+        }
       }
     }
 #pragma unroll
-    for (int r = 0; r < R; r++) {
+    for (int g = 0; g < G; g++)
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        fx[r] += __shfl_xor_sync(0xffffffffu, fx[r], o);
-        fy[r] += __shfl_xor_sync(0xffffffffu, fy[r], o);
+      for (int r = 0; r < R; r++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          fx[g][r] += __shfl_xor_sync(0xffffffffu, fx[g][r], o);
+          fy[g][r] += __shfl_xor_sync(0xffffffffu, fy[g][r], o);
+        }
       }
-    }
-    if (lane == 0) {
-      const float2 s = __ldg(Sp + fb.soff + l);
+    if (lane < ng) {
 #pragma unroll
-      for (int r = 0; r < R; r++) t[r * ldt + fb.soff + l] = fmul(s, make_float2(fx[r], fy[r]));
+      for (int g = 0; g < G; g++) {
+        if (g != lane) continue;  // lane g writes row l0 + g
+        const float2 s = __ldg(Sp + fb.soff + l0 + g);
+#pragma unroll
+        for (int r = 0; r < R; r++)
+          t[r * ldt + fb.soff + l0 + g] = fmul(s, make_float2(fx[g][r], fy[g][r]));
+      }
     }
   }
 }
