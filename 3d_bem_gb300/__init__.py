@@ -37,6 +37,7 @@ EXPORTS = [
     "bem_assemble", "bem_hmatvec", "bem_hmatvec_device", "bem_get_block", "bem_get_ranks",
     "bem_gmres", "bem_solve", "bem_solve_device", "bem_sweep", "bem_points_assemble",
     "bem_launch_count", "bem_stream", "bem_hmatvec_noalloc", "bem_hmatvec_device_ex",
+    "bem_hlu_build", "bem_hlu_solve", "bem_hlu_export",
 ]
 BEM_ARITH_FP64, BEM_ARITH_FP32, BEM_ARITH_TWOFLOAT = 0, 1, 2
 
@@ -53,7 +54,9 @@ class Config(ct.Structure):
                 ("gmres_tol", ct.c_double), ("gmres_restart", ct.c_int64),
                 ("gmres_maxit", ct.c_int64), ("coupling", ct.c_int32),
                 ("precision", ct.c_int32), ("wave_speed", ct.c_double),
-                ("density", ct.c_double), ("seed", ct.c_uint64)]
+                ("density", ct.c_double), ("seed", ct.c_uint64),
+                ("use_preconditioner", ct.c_int32), ("pad0", ct.c_int32),
+                ("precond_rank", ct.c_int64), ("precond_tol", ct.c_double)]
 
 
 class SolveInfo(ct.Structure):
@@ -61,7 +64,8 @@ class SolveInfo(ct.Structure):
                 ("true_residual", ct.c_double), ("max_rank", ct.c_int64),
                 ("capped_blocks", ct.c_int64), ("t_nearfield", ct.c_double),
                 ("t_aca", ct.c_double), ("t_rhs", ct.c_double), ("t_gmres", ct.c_double),
-                ("t_total", ct.c_double), ("status", ct.c_int32), ("pad", ct.c_int32)]
+                ("t_total", ct.c_double), ("status", ct.c_int32), ("pad", ct.c_int32),
+                ("t_precond", ct.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
@@ -115,6 +119,9 @@ def lib():
     L.bem_solve_device.argtypes = [vp, dbl, vp, i64, vp, vp, vp, P(SolveInfo)]
     L.bem_sweep.argtypes = [vp, vp, i64, vp, i64, vp, vp]
     L.bem_points_assemble.argtypes = [vp, vp, i64, vp, i64, dbl, vp, vp]
+    L.bem_hlu_build.argtypes = [vp]
+    L.bem_hlu_solve.argtypes = [vp, vp, vp, i64]
+    L.bem_hlu_export.argtypes = [vp, i32, P(i64), vp, P(i64), vp, P(i64), vp]
     L.bem_launch_count.argtypes = [vp]
     L.bem_launch_count.restype = i64
     L.bem_stream.argtypes = [vp]
@@ -234,6 +241,30 @@ class Solver:
                     "bem_hmatvec")
         return out
 
+    def hlu_build(self):
+        """H-LU factors of the assembled system matrix (HArithm::LUDecomposition)."""
+        self._check(lib().bem_hlu_build(self._h), "bem_hlu_build")
+
+    def hlu_solve(self, b) -> np.ndarray:
+        """x = U^-1 L^-1 b on the GPU, cluster order (HArithm::LUSubstitutionSolve)."""
+        b = _c128(b)
+        R = 1 if b.ndim == 1 else b.shape[1]
+        x = np.zeros_like(b)
+        self._check(lib().bem_hlu_solve(self._h, _ptr(b), _ptr(x), R), "bem_hlu_solve")
+        return x
+
+    def hlu_export(self, which: int):
+        """Flat factor ``which`` (0 L, 1 U): (leaves n x 7, data, schedule)."""
+        nl, nd, ns = ct.c_int64(), ct.c_int64(), ct.c_int64()
+        self._check(lib().bem_hlu_export(self._h, which, ct.byref(nl), None, ct.byref(nd), None,
+                                         ct.byref(ns), None), "bem_hlu_export")
+        leaves = np.zeros((nl.value, 7), np.int64)
+        data = np.zeros(nd.value, np.complex128)
+        sched = np.zeros(ns.value, np.int32)
+        self._check(lib().bem_hlu_export(self._h, which, ct.byref(nl), _ptr(leaves), ct.byref(nd),
+                                         _ptr(data), ct.byref(ns), _ptr(sched)), "bem_hlu_export")
+        return leaves, data, sched
+
     def ranks(self, which: int) -> np.ndarray:
         r = np.zeros(self.partition().shape[0], np.int64)
         self._check(lib().bem_get_ranks(self._h, which, _ptr(r)), "bem_get_ranks")
@@ -340,6 +371,9 @@ class BemSolverParameters:
     hMatSolving: bool = True
     acaRelativeError: float = 0.01
     acaMaxRank: int = 0
+    usePreconditioner: bool = False
+    preconditionerRank: int = 2
+    preconditionerRelError: float = 0.0
     coupling: int = 2  # KirkupCoupling
     leafSize: int = 32
     eta: float = 2.0
@@ -380,7 +414,9 @@ class BoundaryElementSolver:
         s = Solver(leaf_size=p.leafSize, eta=p.eta, aca_tol=p.acaRelativeError,
                    aca_max_rank=p.acaMaxRank, gmres_tol=tol, gmres_restart=p.gmresRestart,
                    gmres_maxit=p.gmresMaxIterations, coupling=p.coupling,
-                   wave_speed=self.waveSpeed, density=self.airDensity)
+                   wave_speed=self.waveSpeed, density=self.airDensity,
+                   use_preconditioner=int(p.usePreconditioner),
+                   precond_rank=p.preconditionerRank, precond_tol=p.preconditionerRelError)
         s.set_mesh(self.boundaryElements.triangles)
         s.set_bc(self.boundaryElements.a, self.boundaryElements.b)
         return s

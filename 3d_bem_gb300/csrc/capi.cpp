@@ -18,6 +18,8 @@
 
 #include "../../include/bemgpu.h"
 #include "bem_kernels.h"
+#include "hlu.h"
+#include "hlu_solve.h"
 #include "host_tree.h"
 #include "krylov.h"
 #include "post.h"
@@ -127,6 +129,12 @@ struct bem_handle {
   DBuf<float2> dTf, dXf;
   GmresWS gw;
   DBuf<double2> dG, dX, dRhs, dIn, dOut1, dOut2, dOut3;
+  // H-LU preconditioner: host factors and their device copies
+  bool have_hlu = false;
+  FlatFactor hL, hU;
+  DBuf<int32_t> dLs, dUs;
+  DBuf<int64_t> dLl, dUl;
+  DBuf<double2> dLd, dUd, dP1, dP2;
   DBuf<int> dBad;
   QuadRules rules{};
   cudaEvent_t ev[10]{};
@@ -186,6 +194,7 @@ void upload_layout(bem_handle* h) {
   h->dPivCnt.upload(L.piv_cnt, s);
   h->dPivRc.upload(L.piv_rc, s);
   for (auto& m : h->hm) m.assembled = false;
+  h->have_hlu = false;
 }
 
 // storage precision of the matrices: point clouds (test kernel) stay FP64
@@ -259,6 +268,7 @@ void fetch_ranks(bem_handle* h, DevHM& m) {
   }
   sync(h);
   m.assembled = true;
+  if (&m == &h->hm[1]) h->have_hlu = false;  // factors of the previous matrix
 }
 
 AcaArgs aca_args(bem_handle* h, DevHM& m, int which, int extra) {
@@ -464,6 +474,122 @@ bool read_states(bem_handle* h) {
   return true;
 }
 
+// ---- H-LU preconditioner ----
+
+// copy of the stored pool [off, off + cnt) as complex FP64
+void pool_to_host(const DevHM& m, const DBuf<unsigned char>& src, size_t total,
+                  std::vector<cplx>& out, cudaStream_t s) {
+  out.resize(total);
+  if (!total) return;
+  if (m.prec == 0) {
+    CK(cudaMemcpyAsync(out.data(), src.p, total * sizeof(double2), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return;
+  }
+  std::vector<float2> tmp(total);
+  CK(cudaMemcpyAsync(tmp.data(), src.p, total * sizeof(float2), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  for (size_t i = 0; i < total; i++) out[i] = cplx(tmp[i].x, tmp[i].y);
+}
+
+// Truncated copy of the assembled dPhi matrix (HMatrix(const HMatrix&, rank,
+// err), hmatrix.cpp:770-776) factorized on the host; factors uploaded.
+// Returns false, keeping no factors, when they hold NaN or Inf: the solve
+// then runs unpreconditioned (LUPair.first.hasNan() ...,
+// boundaryelementsolver.cpp:661-668).
+bool build_hlu(bem_handle* h) {
+  h->have_hlu = false;
+  require(h->hm[1].assembled && !h->points_mode, BEM_EINVAL, "system matrix not assembled");
+  require(h->cfg.leaf_size <= HLU_MAX_LEAF + 1, BEM_EINVAL,
+          "the preconditioner needs leaf_size <= 513");
+  DevHM& m = h->hm[1];
+  const Layout& L = h->L;
+  cudaStream_t s = h->stream;
+  std::vector<cplx> F, U, V, S;
+  pool_to_host(m, m.F, L.near_entries, F, s);
+  pool_to_host(m, m.U, L.u_size, U, s);
+  pool_to_host(m, m.V, L.v_size, V, s);
+  pool_to_host(m, m.S, L.s_size, S, s);
+  const size_t nb = L.blocks.size();
+  std::vector<InBlock> in(nb);
+  size_t ni = 0, fi = 0;
+  std::vector<int64_t> far_of(nb, -1), near_of(nb, -1);
+  for (size_t i = 0; i < nb; i++) (L.blocks[i].adm ? far_of[i] = fi++ : near_of[i] = ni++);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t i = 0; i < (int64_t)nb; i++) {
+    const HBlockDesc& b = L.blocks[i];
+    InBlock& ib = in[i];
+    if (!b.adm) {
+      const NearBlock& nbk = L.near[near_of[i]];
+      ib.F.assign(F.begin() + nbk.off, F.begin() + nbk.off + b.m * b.n);
+      continue;
+    }
+    const FarBlock& fb = L.far[far_of[i]];
+    const int64_t k = m.h_rank[far_of[i]];
+    ib.lowrank = true;
+    ib.k = k;
+    ib.A.resize(b.m * k);
+    ib.B.resize(b.n * k);
+    for (int64_t l = 0; l < k; l++) {
+      const cplx sl = S[fb.soff + l];
+      for (int64_t r = 0; r < b.m; r++) ib.A[l * b.m + r] = U[fb.uoff + l * b.m + r] * sl;
+      for (int64_t c = 0; c < b.n; c++) ib.B[l * b.n + c] = V[fb.voff + l * b.n + c];
+    }
+    rk_truncate(b.m, b.n, ib.k, ib.A, ib.B, h->cfg.precond_rank, h->cfg.precond_tol);
+  }
+  hlu_factor(h->rows, L.blocks, in, h->cfg.precond_rank, h->cfg.precond_tol, h->hL, h->hU);
+  for (const FlatFactor* f : {&h->hL, &h->hU})
+    for (const cplx& v : f->data)
+      if (!std::isfinite(v.real()) || !std::isfinite(v.imag())) return false;
+  // every leaf the sweep kernel reads stays inside the vectors, the data pool
+  // and its shared-memory staging
+  for (const FlatFactor* f : {&h->hL, &h->hU}) {
+    const int64_t nd = (int64_t)f->data.size();
+    for (int64_t i = 0; i < f->nleaves(); i++) {
+      const int64_t* lv = &f->leaves[7 * i];
+      const int64_t r0 = lv[0], mm = lv[1], c0 = lv[2], nn = lv[3], kind = lv[4], k = lv[5];
+      require(kind != 1 || k <= HLU_MAX_RANK, BEM_EINVAL,
+              "preconditioner rank exceeds 512 (set precond_rank)");
+      require(kind < 2 || mm <= HLU_MAX_LEAF, BEM_EINVAL, "diagonal leaf exceeds 512 rows");
+      const int64_t size = kind == 1 ? (mm + nn) * k : mm * nn;
+      require(r0 >= 0 && c0 >= 0 && mm >= 0 && nn >= 0 && r0 + mm <= h->N && c0 + nn <= h->N &&
+                  lv[6] >= 0 && lv[6] + size <= nd,
+              BEM_EINVAL, "H-LU leaf out of range");
+    }
+    for (int32_t op : f->schedule)
+      require((op >= 0 ? op : -(int64_t)op - 1) < f->nleaves(), BEM_EINVAL,
+              "H-LU schedule out of range");
+  }
+  auto up = [&](const FlatFactor& f, DBuf<int32_t>& ds, DBuf<int64_t>& dl, DBuf<double2>& dd) {
+    ds.upload(f.schedule, s);
+    dl.upload(f.leaves, s);
+    dd.ensure(f.data.size());
+    if (!f.data.empty())
+      CK(cudaMemcpyAsync(dd.p, f.data.data(), f.data.size() * sizeof(double2), cudaMemcpyHostToDevice, s));
+  };
+  up(h->hL, h->dLs, h->dLl, h->dLd);
+  up(h->hU, h->dUs, h->dUl, h->dUd);
+  CK(cudaStreamSynchronize(s));
+  h->have_hlu = true;
+  return true;
+}
+
+// w := U^{-1} L^{-1} w for R device vectors (LUPrecondidionedHMatrixWrapper's
+// two substitutions, gmres.h:134-147)
+void apply_precond(bem_handle* h, double2* w, int R) {
+  const int64_t N = h->N;
+  cudaStream_t s = h->stream;
+  h->dP1.ensure((size_t)R * N);
+  h->dP2.ensure((size_t)R * N);
+  CK(cudaMemcpyAsync(h->dP1.p, w, (size_t)R * N * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+  h->launches += launch_hlu_sweep(h->dLs.p, (int)h->hL.schedule.size(), h->dLl.p, h->dLd.p,
+                                  h->dP1.p, h->dP2.p, N, R, 0, s);
+  h->launches += launch_hlu_sweep(h->dUs.p, (int)h->hU.schedule.size(), h->dUl.p, h->dUd.p,
+                                  h->dP2.p, w, N, R, 1, s);
+}
+
+bool use_precond(const bem_handle* h) { return h->cfg.use_preconditioner && h->have_hlu; }
+
 struct GmresResult {
   int64_t iters = 0;
   double resid = 0;
@@ -480,17 +606,23 @@ GmresResult gmres_core(bem_handle* h, const double2* b, double2* x, int R, doubl
   cudaStream_t s = h->stream;
   KrylovArgs a = krylov_args(h, x);
   a.tol = tol;
+  // with the H-LU preconditioner the iteration runs on (LU)^{-1} A x =
+  // (LU)^{-1} b and the tolerance applies to that residual, as in
+  // GMRES::gmresLUPreconditionedSolve (gmres.h:191-207)
+  const bool pc = use_precond(h);
   CK(cudaMemcpyAsync(g.bcopy.p, b, (size_t)R * N * sizeof(double2), cudaMemcpyDeviceToDevice, s));
-  CK(cudaMemcpyAsync(g.w.p, b, (size_t)R * N * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+  if (pc) apply_precond(h, g.bcopy.p, R);
+  CK(cudaMemcpyAsync(g.w.p, g.bcopy.p, (size_t)R * N * sizeof(double2), cudaMemcpyDeviceToDevice, s));
   krylov_restart(a, 1, s);  // measures ||b||
   h->launches += 2;
   int64_t total = 0;
   bool first = true;
   while (true) {
     if (first && x_zero) {  // r = b: skip the product with the zero guess
-      CK(cudaMemcpyAsync(g.w.p, b, (size_t)R * N * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+      CK(cudaMemcpyAsync(g.w.p, g.bcopy.p, (size_t)R * N * sizeof(double2), cudaMemcpyDeviceToDevice, s));
     } else {
       hmatvec_dev(h, 1, x, g.w.p, R, 0, f32);
+      if (pc) apply_precond(h, g.w.p, R);
       krylov_residual(g.bcopy.p, g.w.p, (int64_t)R * N, s);
       h->launches++;
     }
@@ -500,6 +632,7 @@ GmresResult gmres_core(bem_handle* h, const double2* b, double2* x, int R, doubl
     if (read_states(h) || total >= maxit) break;
     for (int j = 0; j < g.m; j++) {
       hmatvec_dev(h, 1, g.Vb.p + (int64_t)j * R * N, g.w.p, R, 0, f32);
+      if (pc) apply_precond(h, g.w.p, R);
       krylov_orthogonalize(a, j, s);
       h->launches += 9;
       total++;
@@ -557,6 +690,17 @@ void gmres_dev(bem_handle* h, const double2* b, double2* x, int R, bem_solve_inf
     loc.iterations = r.iters;
     loc.rel_residual = loc.true_residual = r.resid;
     loc.status = r.converged ? BEM_OK : BEM_EMAXIT;
+    if (use_precond(h)) {  // r.resid is the preconditioned residual
+      GmresWS& g = h->gw;
+      g.r.ensure((size_t)R * h->N);
+      hmatvec_dev(h, 1, x, g.r.p, R, 0);
+      krylov_residual(b, g.r.p, (int64_t)R * h->N, h->stream);
+      h->launches++;
+      const std::vector<double> bn = norms(h, b, R), rn = norms(h, g.r.p, R);
+      loc.true_residual = 0;
+      for (int q = 0; q < R; q++)
+        loc.true_residual = std::max(loc.true_residual, bn[q] > 0 ? rn[q] / bn[q] : 0.0);
+    }
   } else {
     GmresWS& g = h->gw;
     const int64_t N = h->N;
@@ -627,6 +771,11 @@ void solve_dev(bem_handle* h, double freq, const double2* g_caller, int64_t R, d
   auto t0 = std::chrono::steady_clock::now();
   bem_solve_info loc{};
   assemble(h, freq, &loc.t_nearfield, &loc.t_aca);
+  if (h->cfg.use_preconditioner) {
+    const auto tp = std::chrono::steady_clock::now();
+    build_hlu(h);  // non-finite factors: continue without the preconditioner
+    loc.t_precond = std::chrono::duration<double>(std::chrono::steady_clock::now() - tp).count();
+  }
   h->dG.ensure((size_t)R * N);
   h->dRhs.ensure((size_t)R * N);
   h->dX.ensure((size_t)R * N);
@@ -636,8 +785,14 @@ void solve_dev(bem_handle* h, double freq, const double2* g_caller, int64_t R, d
   // rhs = source term (none) + phi * g  (boundaryelementsolver.cpp:578-579)
   hmatvec_dev(h, 0, h->dG.p, h->dRhs.p, R, 0, ARITH_TWOFLOAT);  // FP64-accurate, FP32 units
   CK(cudaEventRecord(h->ev[4], s));
-  CK(cudaMemsetAsync(h->dX.p, 0, (size_t)R * N * sizeof(double2), s));
-  gmres_dev(h, h->dRhs.p, h->dX.p, (int)R, &loc, true);
+  if (use_precond(h)) {  // initial guess (LU)^{-1} rhs (boundaryelementsolver.cpp:688)
+    CK(cudaMemcpyAsync(h->dX.p, h->dRhs.p, (size_t)R * N * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    apply_precond(h, h->dX.p, (int)R);
+    gmres_dev(h, h->dRhs.p, h->dX.p, (int)R, &loc, false);
+  } else {
+    CK(cudaMemsetAsync(h->dX.p, 0, (size_t)R * N * sizeof(double2), s));
+    gmres_dev(h, h->dRhs.p, h->dX.p, (int)R, &loc, true);
+  }
   CK(cudaEventRecord(h->ev[5], s));
   const double omega = 2.0 * M_PI * freq;
   double2 pfac = make_double2(0.0, h->cfg.density * omega);
@@ -689,6 +844,9 @@ void bem_config_default(bem_config* c) {
   c->wave_speed = 343.0;
   c->density = 1.2;
   c->seed = 1234;
+  c->use_preconditioner = 0;
+  c->precond_rank = 2;
+  c->precond_tol = 0.0;
 }
 
 bem_status bem_create(const bem_config* cfg, bem_handle** out) {
@@ -896,6 +1054,43 @@ bem_status bem_hmatvec(bem_handle* h, int32_t which, const double* x, double* y,
     CK(cudaGetLastError());
     copy_out(h, y, h->dOut1.p, (size_t)nr * nrhs);
     sync(h);
+  });
+}
+
+bem_status bem_hlu_build(bem_handle* h) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] {
+    require(build_hlu(h), BEM_ENONFINITE, "non-finite values in the H-LU factors");
+  });
+}
+
+bem_status bem_hlu_solve(bem_handle* h, const double* b, double* x, int64_t nrhs) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] {
+    require(b && x && nrhs >= 1, BEM_EINVAL, "bad arguments");
+    require(h->have_hlu, BEM_EINVAL, "preconditioner not built (bem_hlu_build)");
+    copy_in(h, h->dIn, b, (size_t)h->N * nrhs);
+    apply_precond(h, h->dIn.p, (int)nrhs);
+    CK(cudaGetLastError());
+    copy_out(h, x, h->dIn.p, (size_t)h->N * nrhs);
+    sync(h);
+  });
+}
+
+bem_status bem_hlu_export(const bem_handle* hc, int32_t which, int64_t* nleaves, int64_t* leaves,
+                          int64_t* ndata, double* data, int64_t* nsched, int32_t* sched) {
+  if (!hc) return BEM_EINVAL;
+  bem_handle* h = const_cast<bem_handle*>(hc);
+  return guarded(h, [&] {
+    require(which == 0 || which == 1, BEM_EINVAL, "which must be 0 (L) or 1 (U)");
+    require(h->have_hlu, BEM_EINVAL, "preconditioner not built (bem_hlu_build)");
+    const FlatFactor& f = which ? h->hU : h->hL;
+    if (nleaves) *nleaves = f.nleaves();
+    if (ndata) *ndata = (int64_t)f.data.size();
+    if (nsched) *nsched = (int64_t)f.schedule.size();
+    if (leaves) std::memcpy(leaves, f.leaves.data(), f.leaves.size() * sizeof(int64_t));
+    if (data) std::memcpy(data, f.data.data(), f.data.size() * sizeof(double2));
+    if (sched) std::memcpy(sched, f.schedule.data(), f.schedule.size() * sizeof(int32_t));
   });
 }
 

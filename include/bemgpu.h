@@ -55,6 +55,10 @@ typedef struct bem_config {
   double wave_speed;       /* c */
   double density;          /* rho (p = i rho omega phi) */
   uint64_t seed;           /* seeds the ACA start columns / pivot members */
+  int32_t use_preconditioner; /* usePreconditioner: H-LU left preconditioning */
+  int32_t pad0;
+  int64_t precond_rank;    /* preconditionerRank (ref default 2) */
+  double precond_tol;      /* preconditionerRelError (ref default 0) */
 } bem_config;
 
 typedef struct bem_solve_info {
@@ -70,6 +74,7 @@ typedef struct bem_solve_info {
   double t_total;
   int32_t status;
   int32_t pad;
+  double t_precond;        /* H-LU build (host) including transfers */
 } bem_solve_info;
 
 void bem_config_default(bem_config* cfg);
@@ -158,6 +163,22 @@ bem_status bem_get_ranks(bem_handle* h, int32_t which, int64_t* ranks);
  * (GMRES::gmresSolve, gmres.h:170-180; x0 = the content of x). */
 bem_status bem_gmres(bem_handle* h, const double* b, double* x, int64_t nrhs,
                      bem_solve_info* info);
+
+/* H-LU preconditioner of the assembled dPhi matrix: a truncated copy
+ * (precond_rank, precond_tol: HMatrix(const HMatrix&, rank, err),
+ * hmatrix.cpp:770-776) is factorized on the host like
+ * HArithm::LUDecomposition (harithm.cpp:1192-1296) and the factors go to
+ * the GPU. bem_solve does this itself when cfg.use_preconditioner is set. */
+bem_status bem_hlu_build(bem_handle* h);
+/* x = U^{-1} L^{-1} b on the GPU for nrhs vectors (cluster order, host
+ * buffers): HArithm::LUSubstitutionSolve (harithm.cpp:1168-1190). */
+bem_status bem_hlu_solve(bem_handle* h, const double* b, double* x, int64_t nrhs);
+/* Export a factor (which = 0 L, 1 U) as a flat leaf list: per leaf r0, m,
+ * c0, n, kind (0 full, 1 low rank, 2 diagonal Q, 3 diagonal R), rank, data
+ * offset; data in complex doubles; sched = the order of leaf applications
+ * (>= 0 diagonal leaf, < 0 -(leaf) - 1). Call with NULL arrays to get sizes. */
+bem_status bem_hlu_export(const bem_handle* h, int32_t which, int64_t* nleaves, int64_t* leaves,
+                          int64_t* ndata, double* data, int64_t* nsched, int32_t* sched);
 
 /* Whole frequency solve (calculateBoundarySolution -> hMatrixSolve ->
  * phiSolutionToSoundPressure): g is n x nrhs (caller order); phi, dphi and p

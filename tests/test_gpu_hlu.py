@@ -1,0 +1,138 @@
+"""H-LU preconditioner: the host factorization (HArithm::LUDecomposition,
+HMatrix/harithm.cpp:1192-1296) checked against the dense system matrix, the
+GPU forward/backward block-triangular solves (harithm.cpp:1314-1340,
+:1386-1412) against the oracle's leaf-by-leaf restatement, and the
+preconditioned GMRES (GMRES::gmresLUPreconditionedSolve, HMatrix/gmres.h:191-207)
+against the unpreconditioned solve."""
+import numpy as np
+import pytest
+
+from conftest import rel
+
+pytestmark = pytest.mark.gpu
+FREQ = 200.0
+
+
+def setup(bem, meshes, sub=3, precision=0, **cfg):
+    tri = meshes.icosphere(sub, 1.0)
+    s = bem.Solver(**{"aca_tol": 1e-6, "gmres_tol": 1e-9, "precision": precision, **cfg})
+    s.set_mesh(tri)
+    n = tri.shape[0]
+    s.set_bc(np.zeros(n), np.ones(n))
+    return tri, s
+
+
+def dense_factor(n, leaves, data):
+    D = np.zeros((n, n), complex)
+    for r0, m, c0, nn, kind, k, off in leaves:
+        if kind == 1:
+            U = data[off:off + m * k].reshape(k, m).T
+            V = data[off + m * k:off + m * k + k * nn].reshape(k, nn)
+            D[r0:r0 + m, c0:c0 + nn] = U @ V
+        else:
+            D[r0:r0 + m, c0:c0 + nn] = data[off:off + m * nn].reshape(nn, m).T
+    return D
+
+
+def check_structure(n, leaves, data, sched, lower):
+    # every leaf scheduled once; the diagonal leaves tile the diagonal
+    ops = [int(o) if o >= 0 else -int(o) - 1 for o in sched]
+    assert sorted(ops) == list(range(len(leaves)))
+    diag = leaves[leaves[:, 4] >= 2]
+    assert (diag[:, 0] == diag[:, 2]).all() and (diag[:, 1] == diag[:, 3]).all()
+    assert diag[:, 1].sum() == n
+    assert (diag[:, 4] == (2 if lower else 3)).all()
+    off = leaves[leaves[:, 4] < 2]
+    if lower:
+        assert (off[:, 2] + off[:, 3] <= off[:, 0]).all()
+    else:
+        assert (off[:, 0] + off[:, 1] <= off[:, 2]).all()
+    for r0, m, c0, nn, kind, k, o in diag:
+        B = data[o:o + m * m].reshape(m, m).T
+        if lower:
+            assert np.abs(B.conj().T @ B - np.eye(m)).max() < 1e-12
+        else:
+            assert np.abs(np.tril(B, -1)).max() == 0
+
+
+def test_hlu_factors_reproduce_matrix(bem, meshes):
+    """Untruncated (rank 0, tolerance 1e-12) factors: L U = A to the truncation."""
+    tri, s = setup(bem, meshes, 3, precond_rank=0, precond_tol=1e-12)
+    n = tri.shape[0]
+    s.assemble(FREQ)
+    s.hlu_build()
+    Ll, Ld, Ls = s.hlu_export(0)
+    Ul, Ud, Us = s.hlu_export(1)
+    check_structure(n, Ll, Ld, Ls, True)
+    check_structure(n, Ul, Ud, Us, False)
+    A = s.dense(1)
+    LU = dense_factor(n, Ll, Ld) @ dense_factor(n, Ul, Ud)
+    assert np.linalg.norm(LU - A) / np.linalg.norm(A) < 1e-9
+    # and the GPU solve inverts it
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    z = s.hlu_solve(s.hmatvec(1, x))
+    assert rel(z, x) < 1e-7
+
+
+@pytest.mark.parametrize("rank", [2, 8])
+def test_hlu_solve_vs_oracle(bem, meshes, orc, rank):
+    tri, s = setup(bem, meshes, 3, precond_rank=rank)
+    n = tri.shape[0]
+    s.assemble(FREQ)
+    s.hlu_build()
+    Ll, Ld, _ = s.hlu_export(0)
+    Ul, Ud, _ = s.hlu_export(1)
+    assert Ll[Ll[:, 4] == 1, 5].max() <= rank and Ul[Ul[:, 4] == 1, 5].max() <= rank
+    rng = np.random.default_rng(rank)
+    B = rng.standard_normal((n, 3)) + 1j * rng.standard_normal((n, 3))
+    X = s.hlu_solve(B)
+    for q in range(3):
+        y = orc.lower_solve(n, Ll, Ld, B[:, q])
+        x = orc.upper_solve(n, Ul, Ud, y)
+        assert rel(X[:, q], x) < 1e-12, q
+
+
+def test_hlu_solve_edge_cases(bem, meshes):
+    tri, s = setup(bem, meshes, 2, precond_rank=2)
+    with pytest.raises(bem.BemError):
+        s.hlu_solve(np.ones(tri.shape[0]))  # not built
+    s.assemble(FREQ)
+    with pytest.raises(bem.BemError):
+        s.hlu_export(0)
+    s.hlu_build()
+    n = tri.shape[0]
+    assert np.array_equal(s.hlu_solve(np.zeros(n)), np.zeros(n))
+    s.assemble(FREQ * 1.5)  # reassembly drops the factors of the old matrix
+    with pytest.raises(bem.BemError):
+        s.hlu_solve(np.ones(n))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_preconditioned_solve(bem, meshes, precision):
+    tri, s0 = setup(bem, meshes, 3, precision=precision)
+    _, s1 = setup(bem, meshes, 3, precision=precision, use_preconditioner=1, precond_rank=2)
+    n = tri.shape[0]
+    c = tri.reshape(-1, 3, 3).mean(axis=1)
+    g = np.stack([np.ones(n), c[:, 2]], axis=1).astype(complex)
+    phi0, _, _, i0 = s0.solve(FREQ, g)
+    phi1, _, _, i1 = s1.solve(FREQ, g)
+    assert i1["status"] == 0 and i0["status"] == 0
+    assert i1["t_precond"] > 0
+    assert i1["true_residual"] < 1e-8
+    assert i1["iterations"] < i0["iterations"], (i0["iterations"], i1["iterations"])
+    assert rel(phi1, phi0) < 1e-7
+
+
+def test_facade_preconditioner(bem, meshes):
+    tri = meshes.icosphere(3, 1.0)
+    n = tri.shape[0]
+    out = []
+    for pc in (False, True):
+        be = bem.BoundaryElements(tri, np.zeros(n, complex), np.ones(n, complex),
+                                  np.ones(n, complex))
+        par = bem.BemSolverParameters(acaRelativeError=1e-5, usePreconditioner=pc)
+        sol = bem.BoundaryElementSolver(be, FREQ, bemSolverParameters=par)
+        sol.calculateBoundarySolution()
+        out.append(be.phiSolution)
+    assert rel(out[1], out[0]) < 1e-6
