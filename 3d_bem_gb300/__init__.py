@@ -37,7 +37,7 @@ EXPORTS = [
     "bem_assemble", "bem_hmatvec", "bem_hmatvec_device", "bem_get_block", "bem_get_ranks",
     "bem_gmres", "bem_solve", "bem_solve_device", "bem_sweep", "bem_points_assemble",
     "bem_launch_count", "bem_stream", "bem_hmatvec_noalloc", "bem_hmatvec_device_ex",
-    "bem_hlu_build", "bem_hlu_solve", "bem_hlu_export",
+    "bem_hlu_build", "bem_hlu_solve", "bem_hlu_export", "bem_recompress",
 ]
 BEM_ARITH_FP64, BEM_ARITH_FP32, BEM_ARITH_TWOFLOAT = 0, 1, 2
 
@@ -56,7 +56,8 @@ class Config(ct.Structure):
                 ("precision", ct.c_int32), ("wave_speed", ct.c_double),
                 ("density", ct.c_double), ("seed", ct.c_uint64),
                 ("use_preconditioner", ct.c_int32), ("pad0", ct.c_int32),
-                ("precond_rank", ct.c_int64), ("precond_tol", ct.c_double)]
+                ("precond_rank", ct.c_int64), ("precond_tol", ct.c_double),
+                ("recompress_tol", ct.c_double)]
 
 
 class SolveInfo(ct.Structure):
@@ -119,6 +120,7 @@ def lib():
     L.bem_solve_device.argtypes = [vp, dbl, vp, i64, vp, vp, vp, P(SolveInfo)]
     L.bem_sweep.argtypes = [vp, vp, i64, vp, i64, vp, vp]
     L.bem_points_assemble.argtypes = [vp, vp, i64, vp, i64, dbl, vp, vp]
+    L.bem_recompress.argtypes = [vp, i32, i64, dbl]
     L.bem_hlu_build.argtypes = [vp]
     L.bem_hlu_solve.argtypes = [vp, vp, vp, i64]
     L.bem_hlu_export.argtypes = [vp, i32, P(i64), vp, P(i64), vp, P(i64), vp]
@@ -240,6 +242,10 @@ class Solver:
         self._check(lib().bem_hmatvec(self._h, which, _ptr(x), _ptr(out), R, int(accumulate)),
                     "bem_hmatvec")
         return out
+
+    def recompress(self, which: int, rank: int = 0, tol: float = 0.0):
+        """Truncating SVD recompression of every admissible block on the GPU."""
+        self._check(lib().bem_recompress(self._h, which, rank, tol), "bem_recompress")
 
     def hlu_build(self):
         """H-LU factors of the assembled system matrix (HArithm::LUDecomposition)."""

@@ -20,6 +20,7 @@
 #include "bem_kernels.h"
 #include "hlu.h"
 #include "hlu_solve.h"
+#include "recompress.h"
 #include "host_tree.h"
 #include "krylov.h"
 #include "post.h"
@@ -130,6 +131,9 @@ struct bem_handle {
   GmresWS gw;
   DBuf<double2> dG, dX, dRhs, dIn, dOut1, dOut2, dOut3;
   // H-LU preconditioner: host factors and their device copies
+  // truncating recompression scratch (QR copies of U / V^T, cores)
+  DBuf<unsigned char> rcA, rcB, rcC;
+  DBuf<int64_t> dCoff;
   bool have_hlu = false;
   FlatFactor hL, hU;
   DBuf<int32_t> dLs, dUs;
@@ -326,6 +330,47 @@ void launch_aca_split(bem_handle* h, std::initializer_list<AcaArgs> mats) {
   CK(cudaStreamWaitEvent(s, h->join, 0));
 }
 
+// Truncating recompression of every admissible block of m on the GPU
+// (compressAdmissibleBlock, hmatrix.cpp:101-140, as applied by
+// HMatrix(const HMatrix&, rank, relError), hmatrix.cpp:770-776).
+void recompress(bem_handle* h, DevHM& m, int64_t rank, double tol) {
+  require(m.assembled, BEM_EINVAL, "matrix not assembled");
+  require(rank >= 0 && tol >= 0 && std::isfinite(tol), BEM_EINVAL, "bad rank / tolerance");
+  const Layout& L = h->L;
+  const size_t nf = L.far.size();
+  if (!nf) return;
+  std::vector<int64_t> coff(nf);
+  int64_t tot = 0;
+  for (size_t i = 0; i < nf; i++) {
+    coff[i] = tot;
+    tot += 2 * (int64_t)m.h_rank[i] * m.h_rank[i];
+  }
+  const size_t es = m.prec ? sizeof(float2) : sizeof(double2);
+  cudaStream_t s = h->stream;
+  h->rcA.ensure(L.u_size * es);
+  h->rcB.ensure(L.v_size * es);
+  h->rcC.ensure(std::max<int64_t>(tot, 1) * es);
+  h->dCoff.upload(coff, s);
+  RecompressArgs a{};
+  a.precision = m.prec;
+  a.far = h->dFar.p;
+  a.order = h->dOrder.p;
+  a.nfar = (int64_t)nf;
+  a.U = m.U.p;
+  a.V = m.V.p;
+  a.S = m.S.p;
+  a.rank = m.rank.p;
+  a.wa = h->rcA.p;
+  a.wb = h->rcB.p;
+  a.wc = h->rcC.p;
+  a.coff = h->dCoff.p;
+  a.max_rank = rank;
+  a.tol = tol;
+  h->launches += launch_recompress(a, s);
+  CK(cudaGetLastError());
+  fetch_ranks(h, m);
+}
+
 // both H-matrices at wavenumber k; optional timing events
 void assemble(bem_handle* h, double freq, double* t_near, double* t_aca) {
   require(h->have_mesh && !h->points_mode, BEM_EINVAL, "mesh not set (bem_set_mesh)");
@@ -363,6 +408,13 @@ void assemble(bem_handle* h, double freq, double* t_near, double* t_aca) {
   fetch_ranks(h, h->hm[1]);
   if (t_near) *t_near = elapsed(h->ev[0], h->ev[1]);
   if (t_aca) *t_aca = elapsed(h->ev[1], h->ev[2]);
+  if (h->cfg.recompress_tol > 0) {
+    CK(cudaEventRecord(h->ev[1], s));
+    for (auto& m : h->hm) recompress(h, m, 0, h->cfg.recompress_tol);
+    CK(cudaEventRecord(h->ev[2], s));
+    sync(h);
+    if (t_aca) *t_aca += elapsed(h->ev[1], h->ev[2]);
+  }
 }
 
 // Arithmetic of an H-matvec on complex-FP32 storage.
@@ -1054,6 +1106,14 @@ bem_status bem_hmatvec(bem_handle* h, int32_t which, const double* x, double* y,
     CK(cudaGetLastError());
     copy_out(h, y, h->dOut1.p, (size_t)nr * nrhs);
     sync(h);
+  });
+}
+
+bem_status bem_recompress(bem_handle* h, int32_t which, int64_t rank, double tol) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] {
+    require(which == 0 || which == 1, BEM_EINVAL, "which must be 0 (phi) or 1 (dPhi)");
+    recompress(h, h->hm[which], rank, tol);
   });
 }
 

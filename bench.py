@@ -143,11 +143,11 @@ def matvec_bytes(info, ranks, n, elem, R=1):
     return int(mat + vec)
 
 
-def make_solver(pkg, meshes, sub, precision):
+def make_solver(pkg, meshes, sub, precision, **extra):
     tri = meshes.icosphere(sub, 1.0)
     n = tri.shape[0]
     s = pkg.Solver(aca_tol=ACA_TOL, gmres_tol=GMRES_TOL, wave_speed=C0, density=RHO,
-                   precision=precision)
+                   precision=precision, **extra)
     s.set_mesh(tri)
     s.set_bc(np.zeros(n), np.ones(n))
     return s, n
@@ -222,7 +222,12 @@ def run_ours(args):
                  "phases_s": {k: round(float(np.mean([i[k] for i in infos64])), 5)
                               for k in ("t_nearfield", "t_aca", "t_rhs", "t_gmres")}}
         s64.close()
-    s, n = make_solver(pkg, meshes, sub, 1)
+    extra = {}
+    if args.recompress > 0:
+        extra["recompress_tol"] = args.recompress
+    if args.precond:
+        extra.update(use_preconditioner=1, precond_rank=2)
+    s, n = make_solver(pkg, meshes, sub, 1, **extra)
     clk = Clocks(local)
     clk.start()
     ms, infos, pm, launches = timed_arm(torch, pkg, s, n, args, ws)
@@ -261,7 +266,7 @@ def run_ours(args):
     achieved = B / (mv_ms * 1e-3) / 1e9
 
     phase = {key: float(np.mean([i[key] for i in infos]))
-             for key in ("t_nearfield", "t_aca", "t_rhs", "t_gmres", "t_total")}
+             for key in ("t_nearfield", "t_aca", "t_rhs", "t_gmres", "t_precond", "t_total")}
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup,
@@ -270,7 +275,8 @@ def run_ours(args):
         "dtype": "c64 storage + fp32 quadrature, fp64 refinement/Arnoldi/singular rules",
         "data": "synthetic (seeded icosphere; analytic monopole as accuracy check)",
         "config": workload_config(args.workload, {
-            "precision": "mixed", "parallelism": f"replicas{ws}" if ws > 1 else "single-gpu"}),
+            "precision": "mixed", "parallelism": f"replicas{ws}" if ws > 1 else "single-gpu",
+            "recompress_tol": args.recompress, "hlu_preconditioner": bool(args.precond)}),
         "e2e": {"value": round(e2e, 4), "unit": UNIT, "h2d_bytes_per_step": n * 16,
                 "d2h_bytes_per_step": n * 16},
         "roofline": {"kernel": "hmatvec (V pass + U pass), c64 storage", "bound": "hbm",
@@ -364,6 +370,10 @@ def main():
     ap.add_argument("--workload", default="sphere20k", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the complex-FP64 arm")
+    ap.add_argument("--recompress", type=float, default=0.0,
+                    help="mixed arm: truncating SVD recompression tolerance after ACA (0: off)")
+    ap.add_argument("--precond", action="store_true",
+                    help="mixed arm: H-LU preconditioned GMRES (rank 2)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -59,6 +59,8 @@ typedef struct bem_config {
   int32_t pad0;
   int64_t precond_rank;    /* preconditionerRank (ref default 2) */
   double precond_tol;      /* preconditionerRelError (ref default 0) */
+  double recompress_tol;   /* > 0: truncating SVD recompression of every ACA
+                              block to this relative error after assembly */
 } bem_config;
 
 typedef struct bem_solve_info {
@@ -173,6 +175,13 @@ bem_status bem_hlu_build(bem_handle* h);
 /* x = U^{-1} L^{-1} b on the GPU for nrhs vectors (cluster order, host
  * buffers): HArithm::LUSubstitutionSolve (harithm.cpp:1168-1190). */
 bem_status bem_hlu_solve(bem_handle* h, const double* b, double* x, int64_t nrhs);
+/* Truncating SVD recompression of every admissible block of matrix `which`
+ * on the GPU: QR of U and V^T, SVD of the core, smallest rank with relative
+ * Frobenius tail < tol, capped at rank (0: no cap). Replaces
+ * BlockCluster::compressAdmissibleBlock (HMatrix/hmatrix.cpp:101-140) as
+ * applied to every block by HMatrix(const HMatrix&, rank, relError)
+ * (hmatrix.cpp:770-776). */
+bem_status bem_recompress(bem_handle* h, int32_t which, int64_t rank, double tol);
 /* Export a factor (which = 0 L, 1 U) as a flat leaf list: per leaf r0, m,
  * c0, n, kind (0 full, 1 low rank, 2 diagonal Q, 3 diagonal R), rank, data
  * offset; data in complex doubles; sched = the order of leaf applications
