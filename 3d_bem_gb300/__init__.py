@@ -38,6 +38,8 @@ EXPORTS = [
     "bem_gmres", "bem_solve", "bem_solve_device", "bem_sweep", "bem_points_assemble",
     "bem_launch_count", "bem_stream", "bem_hmatvec_noalloc", "bem_hmatvec_device_ex",
     "bem_hlu_build", "bem_hlu_solve", "bem_hlu_export", "bem_recompress",
+    "bem_sel_nparam", "bem_sel_label", "bem_mlp_grad", "bem_mlp_adam", "bem_mlp_forward",
+    "bem_sel_infer", "bem_set_selector", "bem_sel_stats", "bem_sel_classes",
 ]
 BEM_ARITH_FP64, BEM_ARITH_FP32, BEM_ARITH_TWOFLOAT = 0, 1, 2
 
@@ -55,9 +57,9 @@ class Config(ct.Structure):
                 ("gmres_maxit", ct.c_int64), ("coupling", ct.c_int32),
                 ("precision", ct.c_int32), ("wave_speed", ct.c_double),
                 ("density", ct.c_double), ("seed", ct.c_uint64),
-                ("use_preconditioner", ct.c_int32), ("pad0", ct.c_int32),
+                ("use_preconditioner", ct.c_int32), ("selector", ct.c_int32),
                 ("precond_rank", ct.c_int64), ("precond_tol", ct.c_double),
-                ("recompress_tol", ct.c_double)]
+                ("recompress_tol", ct.c_double), ("selector_guard", ct.c_double)]
 
 
 class SolveInfo(ct.Structure):
@@ -121,6 +123,17 @@ def lib():
     L.bem_sweep.argtypes = [vp, vp, i64, vp, i64, vp, vp]
     L.bem_points_assemble.argtypes = [vp, vp, i64, vp, i64, dbl, vp, vp]
     L.bem_recompress.argtypes = [vp, i32, i64, dbl]
+    L.bem_sel_nparam.argtypes = []
+    L.bem_sel_nparam.restype = i64
+    L.bem_sel_label.argtypes = [vp, vp, vp, i64, dbl, dbl, vp, vp, vp]
+    L.bem_mlp_grad.argtypes = [vp, vp, vp, i64, vp, vp, vp, vp]
+    L.bem_mlp_adam.argtypes = [vp, vp, vp, vp, i64, ct.c_float, ct.c_float, ct.c_float,
+                               ct.c_float, vp]
+    L.bem_mlp_forward.argtypes = [vp, vp, i64, vp, vp]
+    L.bem_sel_infer.argtypes = [vp, vp, vp, vp, i64, vp, vp, vp]
+    L.bem_set_selector.argtypes = [vp, vp, vp, vp]
+    L.bem_sel_stats.argtypes = [vp, vp]
+    L.bem_sel_classes.argtypes = [vp, vp]
     L.bem_hlu_build.argtypes = [vp]
     L.bem_hlu_solve.argtypes = [vp, vp, vp, i64]
     L.bem_hlu_export.argtypes = [vp, i32, P(i64), vp, P(i64), vp, P(i64), vp]
@@ -170,6 +183,39 @@ def _c128(a, n=None):
     return np.asfortranarray(a) if a.ndim == 2 else np.ascontiguousarray(a)
 
 
+SELECTOR_WEIGHTS = os.path.join(_HERE, "selector_weights.npz")
+SEL_NFEAT, SEL_NCLASS = 24, 5
+SEL_RULE_POINTS = (1, 3, 7, 13, 25)
+
+
+def load_selector_weights(path: str = SELECTOR_WEIGHTS) -> dict:
+    if not os.path.exists(path):
+        raise BemError(BEM_EINVAL, f"no trained selector weights at {path} "
+                       "(train them with 3d_bem_gb300/selector_train.py)")
+    z = np.load(path)
+    return {k: z[k] for k in z.files}
+
+
+def _status(st, what):
+    if st != BEM_OK:
+        raise BemError(st, what)
+
+
+def sel_label(ptri, qtri, k, tol=1e-7, near_ratio=1.0, want_err=False):
+    """Features (n x 24), labels (n) and optionally the per-rule errors (n x 6)
+    of n pairs, computed on the GPU (bem_sel_label)."""
+    ptri = np.ascontiguousarray(ptri, np.float64).reshape(-1, 9)
+    qtri = np.ascontiguousarray(qtri, np.float64).reshape(-1, 9)
+    k = np.ascontiguousarray(k, np.float64).ravel()
+    n = k.size
+    feat = np.zeros((n, SEL_NFEAT), np.float32)
+    lab = np.zeros(n, np.uint8)
+    err = np.zeros((n, 6), np.float32) if want_err else None
+    _status(lib().bem_sel_label(_ptr(ptri), _ptr(qtri), _ptr(k), n, tol, near_ratio,
+                                _ptr(feat), _ptr(lab), _ptr(err)), "bem_sel_label")
+    return (feat, lab, err) if want_err else (feat, lab)
+
+
 class Solver:
     """One GPU solver handle (mesh, BCs, assembled H-matrices, GMRES state)."""
 
@@ -182,6 +228,8 @@ class Solver:
             raise BemError(st, "bem_create failed (is a CUDA device visible?)")
         self._h = h
         self.n = 0
+        if self.config.selector:
+            self.set_selector()
 
     def close(self):
         if getattr(self, "_h", None):
@@ -242,6 +290,29 @@ class Solver:
         self._check(lib().bem_hmatvec(self._h, which, _ptr(x), _ptr(out), R, int(accumulate)),
                     "bem_hmatvec")
         return out
+
+    def set_selector(self, weights=None):
+        """Install trained selector weights (a dict / npz with params, mu,
+        sigma; default: the package's ``selector_weights.npz``)."""
+        w = load_selector_weights() if weights is None else weights
+        prm = np.ascontiguousarray(w["params"], np.float32)
+        mu = np.ascontiguousarray(w["mu"], np.float32)
+        sg = np.ascontiguousarray(w["sigma"], np.float32)
+        self._check(lib().bem_set_selector(self._h, _ptr(prm), _ptr(mu), _ptr(sg)),
+                    "bem_set_selector")
+
+    def sel_stats(self) -> dict:
+        st = np.zeros(4, np.int64)
+        self._check(lib().bem_sel_stats(self._h, _ptr(st)), "bem_sel_stats")
+        return {"points": int(st[0]), "checked": int(st[1]), "fallback": int(st[2]),
+                "regular_entries": int(st[3])}
+
+    def sel_classes(self) -> np.ndarray:
+        info = self.partition()
+        near = info[info[:, 4] == 0]
+        cls = np.zeros(int((near[:, 1] * near[:, 3]).sum()), np.uint8)
+        self._check(lib().bem_sel_classes(self._h, _ptr(cls)), "bem_sel_classes")
+        return cls
 
     def recompress(self, which: int, rank: int = 0, tol: float = 0.0):
         """Truncating SVD recompression of every admissible block on the GPU."""

@@ -24,7 +24,8 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(
     os.path.join(CUDA_HOME, "bin", "nvcc")) else shutil.which("nvcc") or "nvcc"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["nearfield.cu", "aca.cu", "hmatvec.cu", "krylov.cu", "post.cu", "hlu_solve.cu", "recompress.cu"]
+CU_SOURCES = ["nearfield.cu", "aca.cu", "hmatvec.cu", "krylov.cu", "post.cu", "hlu_solve.cu", "recompress.cu",
+              "selector.cu"]
 CPP_SOURCES = ["host_tree.cpp", "hlu.cpp", "capi.cpp"]
 
 

@@ -21,6 +21,7 @@
 #include "hlu.h"
 #include "hlu_solve.h"
 #include "recompress.h"
+#include "selector.h"
 #include "host_tree.h"
 #include "krylov.h"
 #include "post.h"
@@ -131,6 +132,12 @@ struct bem_handle {
   GmresWS gw;
   DBuf<double2> dG, dX, dRhs, dIn, dOut1, dOut2, dOut3;
   // H-LU preconditioner: host factors and their device copies
+  // learned quadrature-order selector (device blob, per-entry classes, counters)
+  DBuf<SelBlob> dSel;
+  bool have_selector = false;
+  DBuf<uint8_t> dCls;
+  DBuf<unsigned long long> dSelCnt;
+  unsigned long long sel_stats[3] = {0, 0, 0};
   // truncating recompression scratch (QR copies of U / V^T, cores)
   DBuf<unsigned char> rcA, rcB, rcC;
   DBuf<int64_t> dCoff;
@@ -398,9 +405,48 @@ void assemble(bem_handle* h, double freq, double* t_near, double* t_aca) {
   na.phi = h->hm[0].F.p;
   na.dphi = h->hm[1].F.p;
   CK(cudaEventRecord(h->ev[0], s));
+  const bool learned = h->cfg.selector && na.precision == 1;
+  if (learned) {
+    require(h->have_selector, BEM_EINVAL, "selector weights not set (bem_set_selector)");
+    h->dCls.ensure(h->L.near_entries);
+    h->dSelCnt.ensure(3);
+    CK(cudaMemsetAsync(h->dSelCnt.p, 0, 3 * sizeof(unsigned long long), s));
+    SelNearArgs ca{};
+    ca.blob = h->dSel.p;
+    ca.E = h->dE.p;
+    ca.blocks = na.blocks;
+    ca.tiles = na.tiles;
+    ca.ntiles = na.ntiles;
+    ca.special_bits = na.special_bits;
+    ca.k = k;
+    ca.guard_prob = (float)h->cfg.selector_guard;
+    ca.cls = h->dCls.p;
+    launch_sel_near_classes(ca, s);
+    SelNearfieldArgs fa{};
+    fa.EF = h->dEF.p;
+    fa.bc = h->dBc.p;
+    fa.blocks = na.blocks;
+    fa.tiles = na.tiles;
+    fa.ntiles = na.ntiles;
+    fa.special_bits = na.special_bits;
+    fa.cls = h->dCls.p;
+    fa.k = (float)k;
+    fa.alpha = make_float2((float)al.real(), (float)al.imag());
+    fa.phi = (float2*)h->hm[0].F.p;
+    fa.dphi = (float2*)h->hm[1].F.p;
+    fa.check_every = 16;
+    fa.check_tol = 1e-6f;
+    fa.counters = h->dSelCnt.p;
+    launch_sel_nearfield32(fa, s);
+    h->launches += 2 * (na.ntiles > 0);
+    na.ntiles = 0;  // the special entries only
+  }
   launch_nearfield(na, s);
   h->launches += (na.ntiles > 0) + (na.nspecial > 0);
   CK(cudaEventRecord(h->ev[1], s));
+  if (learned)
+    CK(cudaMemcpyAsync(h->sel_stats, h->dSelCnt.p, 3 * sizeof(unsigned long long),
+                       cudaMemcpyDeviceToHost, s));
   launch_aca_split(h, {aca_args(h, h->hm[0], 0, 0), aca_args(h, h->hm[1], 1, 1)});
   CK(cudaEventRecord(h->ev[2], s));
   CK(cudaGetLastError());
@@ -899,6 +945,8 @@ void bem_config_default(bem_config* c) {
   c->use_preconditioner = 0;
   c->precond_rank = 2;
   c->precond_tol = 0.0;
+  c->selector = 0;
+  c->selector_guard = 0.9;
 }
 
 bem_status bem_create(const bem_config* cfg, bem_handle** out) {
@@ -1105,6 +1153,127 @@ bem_status bem_hmatvec(bem_handle* h, int32_t which, const double* x, double* y,
     hmatvec_dev(h, which, h->dIn.p, h->dOut1.p, nrhs, accumulate);
     CK(cudaGetLastError());
     copy_out(h, y, h->dOut1.p, (size_t)nr * nrhs);
+    sync(h);
+  });
+}
+
+// ---- selector data generation and training (no handle; stream NULL = default) ----
+
+int64_t bem_sel_nparam(void) { return SEL_NPARAM; }
+
+bem_status bem_sel_label(const double* ptri, const double* qtri, const double* k, int64_t n,
+                         double tol, double near_ratio, float* feat, uint8_t* label,
+                         float* err) {
+  return guarded(nullptr, [&] {
+    require(n >= 0 && (n == 0 || (ptri && qtri && k && feat && label)), BEM_EINVAL,
+            "bad arguments");
+    require(tol > 0 && near_ratio >= 0, BEM_EINVAL, "bad tolerance / near ratio");
+    const int64_t chunk = 1 << 18;
+    DBuf<Elem> dP, dQ;
+    DBuf<double> dk;
+    DBuf<float> df, de;
+    DBuf<uint8_t> dl;
+    std::vector<Elem> EP, EQ;
+    for (int64_t o = 0; o < n; o += chunk) {
+      const int64_t m = std::min(chunk, n - o);
+      std::vector<int64_t> id(m);
+      for (int64_t i = 0; i < m; i++) id[i] = i;
+      double avg;
+      prepare_elements(ptri + 9 * o, id, EP, avg);
+      prepare_elements(qtri + 9 * o, id, EQ, avg);
+      for (int64_t i = 0; i < m; i++)
+        require(std::isfinite(k[o + i]) && k[o + i] > 0 && EQ[i].area > 0 && EP[i].area > 0,
+                BEM_EINVAL, "degenerate pair or wavenumber");
+      dP.upload(EP, 0);
+      dQ.upload(EQ, 0);
+      dk.ensure(m);
+      CK(cudaMemcpy(dk.p, k + o, m * sizeof(double), cudaMemcpyHostToDevice));
+      df.ensure(m * SEL_NF);
+      dl.ensure(m);
+      if (err) de.ensure(m * 6);
+      launch_sel_label(dP.p, dQ.p, dk.p, m, tol, near_ratio, df.p, dl.p, err ? de.p : nullptr, 0);
+      CK(cudaGetLastError());
+      CK(cudaMemcpy(feat + o * SEL_NF, df.p, m * SEL_NF * sizeof(float), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(label + o, dl.p, m, cudaMemcpyDeviceToHost));
+      if (err) CK(cudaMemcpy(err + o * 6, de.p, m * 6 * sizeof(float), cudaMemcpyDeviceToHost));
+    }
+  });
+}
+
+bem_status bem_mlp_grad(const float* params, const float* X, const uint8_t* y, int64_t B,
+                        float* grad, float* loss, float* work, void* stream) {
+  return guarded(nullptr, [&] {
+    require(params && X && y && grad && loss && work && B >= 1, BEM_EINVAL, "bad arguments");
+    launch_mlp_grad(params, X, y, B, grad, loss, work, (cudaStream_t)stream);
+    CK(cudaGetLastError());
+  });
+}
+
+bem_status bem_mlp_adam(float* params, const float* grad, float* m, float* v, int64_t step,
+                        float lr, float beta1, float beta2, float eps, void* stream) {
+  return guarded(nullptr, [&] {
+    require(params && grad && m && v && step >= 1, BEM_EINVAL, "bad arguments");
+    launch_mlp_adam(params, grad, m, v, step, lr, beta1, beta2, eps, (cudaStream_t)stream);
+    CK(cudaGetLastError());
+  });
+}
+
+bem_status bem_mlp_forward(const float* params, const float* X, int64_t B, float* logits,
+                           void* stream) {
+  return guarded(nullptr, [&] {
+    require(params && X && logits && B >= 0, BEM_EINVAL, "bad arguments");
+    launch_mlp_forward(params, X, B, logits, (cudaStream_t)stream);
+    CK(cudaGetLastError());
+  });
+}
+
+bem_status bem_sel_infer(const float* params, const float* mu, const float* sigma,
+                         const float* feat, int64_t B, float* logits, uint8_t* cls,
+                         void* stream) {
+  return guarded(nullptr, [&] {
+    require(params && mu && sigma && feat && cls && B >= 0, BEM_EINVAL, "bad arguments");
+    SelBlob b;
+    sel_make_blob(params, mu, sigma, b);
+    DBuf<SelBlob> db;
+    db.ensure(1);
+    cudaStream_t s = (cudaStream_t)stream;
+    CK(cudaMemcpyAsync(db.p, &b, sizeof(SelBlob), cudaMemcpyHostToDevice, s));
+    launch_sel_infer_rows(db.p, feat, B, logits, cls, s);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s));
+  });
+}
+
+bem_status bem_set_selector(bem_handle* h, const float* params, const float* mu,
+                            const float* sigma) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] {
+    require(params && mu && sigma, BEM_EINVAL, "bad arguments");
+    for (int i = 0; i < SEL_NPARAM; i++)
+      require(std::isfinite(params[i]), BEM_ENONFINITE, "non-finite selector weights");
+    SelBlob b;
+    sel_make_blob(params, mu, sigma, b);
+    h->dSel.ensure(1);
+    CK(cudaMemcpyAsync(h->dSel.p, &b, sizeof(SelBlob), cudaMemcpyHostToDevice, h->stream));
+    sync(h);
+    h->have_selector = true;
+  });
+}
+
+bem_status bem_sel_stats(const bem_handle* h, int64_t* stats) {
+  if (!h || !stats) return BEM_EINVAL;
+  for (int i = 0; i < 3; i++) stats[i] = (int64_t)h->sel_stats[i];
+  stats[3] = h->L.near_entries - (int64_t)h->L.sp_entry.size();  // selector-governed entries
+  return BEM_OK;
+}
+
+bem_status bem_sel_classes(bem_handle* h, uint8_t* cls) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] {
+    require(cls, BEM_EINVAL, "bad arguments");
+    require(h->dCls.n >= (size_t)h->L.near_entries && h->L.near_entries > 0, BEM_EINVAL,
+            "no selector classes (assemble with cfg.selector = 1 first)");
+    CK(cudaMemcpyAsync(cls, h->dCls.p, h->L.near_entries, cudaMemcpyDeviceToHost, h->stream));
     sync(h);
   });
 }

@@ -365,9 +365,9 @@ void build_layout(const HTree& rows, const HTree& cols, const std::vector<Elem>*
   }
 }
 
-// 16-point Dunavant rule (order 8) in the point order of
-// trianglequadraturerules.cpp:91-110; Gauss-Legendre nodes by Newton iteration.
-static void gauss_legendre(int n, double* x, double* w) {
+// Gauss-Legendre nodes (ascending) and weights on [-1, 1] by Newton iteration
+// on the Legendre recurrence.
+void gauss_legendre(int n, double* x, double* w) {
   const double PI = 3.14159265358979323846;
   for (int i = 0; i < n; i++) {
     double z = std::cos(PI * (i + 0.75) / (n + 0.5));
@@ -395,6 +395,8 @@ static void gauss_legendre(int n, double* x, double* w) {
   }
 }
 
+// 16-point Dunavant rule (order 8) in the point order of
+// trianglequadraturerules.cpp:91-110.
 QuadRules make_rules() {
   QuadRules R{};
   static const double t8[16][3] = {

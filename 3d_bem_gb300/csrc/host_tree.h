@@ -81,4 +81,7 @@ void build_layout(const HTree& rows, const HTree& cols, const std::vector<Elem>*
 // Quadrature rule tables of the kernels.
 QuadRules make_rules();
 
+// Gauss-Legendre nodes (ascending) and weights on [-1, 1], n <= 64.
+void gauss_legendre(int n, double* x, double* w);
+
 }  // namespace bemgpu

@@ -227,6 +227,8 @@ def run_ours(args):
         extra["recompress_tol"] = args.recompress
     if args.precond:
         extra.update(use_preconditioner=1, precond_rank=2)
+    if args.selector:
+        extra["selector"] = 1
     s, n = make_solver(pkg, meshes, sub, 1, **extra)
     clk = Clocks(local)
     clk.start()
@@ -276,7 +278,8 @@ def run_ours(args):
         "data": "synthetic (seeded icosphere; analytic monopole as accuracy check)",
         "config": workload_config(args.workload, {
             "precision": "mixed", "parallelism": f"replicas{ws}" if ws > 1 else "single-gpu",
-            "recompress_tol": args.recompress, "hlu_preconditioner": bool(args.precond)}),
+            "recompress_tol": args.recompress, "hlu_preconditioner": bool(args.precond),
+            "learned_selector": bool(args.selector)}),
         "e2e": {"value": round(e2e, 4), "unit": UNIT, "h2d_bytes_per_step": n * 16,
                 "d2h_bytes_per_step": n * 16},
         "roofline": {"kernel": "hmatvec (V pass + U pass), c64 storage", "bound": "hbm",
@@ -294,6 +297,8 @@ def run_ours(args):
         "plain_fp64": plain,
         "clocks": clocks,
     }
+    if args.selector:
+        line["selector_stats"] = s.sel_stats()
     if not args.no_cpu_baseline and rank == 0 and ws == 1:
         line["cpu_baseline"] = cpu_baseline_sample(args)
     if rank == 0:
@@ -374,6 +379,8 @@ def main():
                     help="mixed arm: truncating SVD recompression tolerance after ACA (0: off)")
     ap.add_argument("--precond", action="store_true",
                     help="mixed arm: H-LU preconditioned GMRES (rank 2)")
+    ap.add_argument("--selector", action="store_true",
+                    help="mixed arm: learned quadrature order per near-field pair")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -56,11 +56,14 @@ typedef struct bem_config {
   double density;          /* rho (p = i rho omega phi) */
   uint64_t seed;           /* seeds the ACA start columns / pivot members */
   int32_t use_preconditioner; /* usePreconditioner: H-LU left preconditioning */
-  int32_t pad0;
+  int32_t selector;         /* 1: learned quadrature order per near-field pair
+                              (mixed precision; weights via bem_set_selector) */
   int64_t precond_rank;    /* preconditionerRank (ref default 2) */
   double precond_tol;      /* preconditionerRelError (ref default 0) */
   double recompress_tol;   /* > 0: truncating SVD recompression of every ACA
                               block to this relative error after assembly */
+  double selector_guard;   /* pairs whose top class probability is below this
+                              get the highest order (guard band) */
 } bem_config;
 
 typedef struct bem_solve_info {
@@ -175,6 +178,48 @@ bem_status bem_hlu_build(bem_handle* h);
 /* x = U^{-1} L^{-1} b on the GPU for nrhs vectors (cluster order, host
  * buffers): HArithm::LUSubstitutionSolve (harithm.cpp:1168-1190). */
 bem_status bem_hlu_solve(bem_handle* h, const double* b, double* x, int64_t nrhs);
+/* ---- Learned quadrature-order selector (no counterpart in the reference,
+ * which integrates every regular pair with one 16-point rule,
+ * boundaryelementsolver.cpp:857-893). A 24-64-64-5 ReLU network picks per
+ * near-field pair one of the 1, 3, 7, 13, 25-point rules of the same family
+ * (trianglequadraturerules.cpp orders 1, 2, 5, 7, 10). ---- */
+#define BEM_SEL_NFEAT 24
+#define BEM_SEL_NCLASS 5
+int64_t bem_sel_nparam(void); /* 6085: W1 24x64, b1, W2 64x64, b2, W3 64x5, b3 */
+/* Training data: n pairs (collocation triangle P, source triangle Q, 9
+ * doubles each; wavenumber k) -> features (n x 24), label = cheapest class
+ * whose L, M, Mt, N are within tol (relative) of the reference (the 64-point
+ * product rule on a subdivision of Q; the split-polar near-singular rule when
+ * the centroid distance is below near_ratio * sqrt(area Q)), 5 if none;
+ * err (n x 6, may be NULL): relative errors of the 5 classes and of the
+ * plain 16-point rule. Host buffers; runs on the current device. */
+bem_status bem_sel_label(const double* ptri, const double* qtri, const double* k, int64_t n,
+                         double tol, double near_ratio, float* feat, uint8_t* label, float* err);
+/* FP32 training on device buffers: gradient of the mean softmax cross-entropy
+ * (bitwise reproducible) with work = B * 265 floats; an Adam step; FP32
+ * logits (B x 5). stream: cudaStream_t or NULL. */
+bem_status bem_mlp_grad(const float* params, const float* X, const uint8_t* y, int64_t B,
+                        float* grad, float* loss, float* work, void* stream);
+bem_status bem_mlp_adam(float* params, const float* grad, float* m, float* v, int64_t step,
+                        float lr, float beta1, float beta2, float eps, void* stream);
+bem_status bem_mlp_forward(const float* params, const float* X, int64_t B, float* logits,
+                           void* stream);
+/* BF16 tensor-core inference (host weights, device features): logits
+ * (B x 8, padded; may be NULL) and classes. Raw features; mu / sigma
+ * normalise them. */
+bem_status bem_sel_infer(const float* params, const float* mu, const float* sigma,
+                         const float* feat, int64_t B, float* logits, uint8_t* cls,
+                         void* stream);
+/* Install trained weights in a handle (used when cfg.selector = 1). */
+bem_status bem_set_selector(bem_handle* h, const float* params, const float* mu,
+                            const float* sigma);
+/* After an assembly with the selector: stats[0] quadrature points used,
+ * [1] entries re-integrated by the check, [2] entries that fell back to the
+ * highest order, [3] regular near-field entries. */
+bem_status bem_sel_stats(const bem_handle* h, int64_t* stats);
+/* The per-entry classes of the last assembly (near-field entry order). */
+bem_status bem_sel_classes(bem_handle* h, uint8_t* cls);
+
 /* Truncating SVD recompression of every admissible block of matrix `which`
  * on the GPU: QR of U and V^T, SVD of the core, smallest rank with relative
  * Frobenius tail < tol, capped at rank (0: no cap). Replaces

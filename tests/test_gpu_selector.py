@@ -1,0 +1,214 @@
+"""Learned quadrature-order selector on the GPU: labels and per-rule errors
+against the CPU oracle, the FP32 training gradient against the oracle's
+backpropagation, BF16 tensor-core inference against a BF16 emulation of the
+network, training, the trained network's gain over the plain 16-point rule on
+held-out pairs, and the selector inside the mixed-precision solve."""
+import ctypes as ct
+import importlib
+
+import numpy as np
+import pytest
+
+from conftest import rel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def sd():
+    return importlib.import_module("3d_bem_gb300.selector_data")
+
+
+@pytest.fixture(scope="module")
+def st():
+    return importlib.import_module("3d_bem_gb300.selector_train")
+
+
+def test_labels_and_errors_vs_oracle(bem, orc, sd):
+    from oracle import selector_ref as sr
+    P, Q, k, dh = sd.pairs(1500, seed=11)
+    feat, lab, err = bem.sel_label(P, Q, k, tol=1e-7, want_err=True)
+    m = dh >= 1.0  # regular regime: reference = subdivided 64-point rule
+    rules = {o: orc.triangle_rule(o) for o in sr.CLASS_ORDERS + (sr.PLAIN_ORDER,)}
+    e_np, l_np = sr.errors_and_labels(P[m], Q[m], k[m], rules, 1e-7)
+    eg = err[m].astype(np.float64)
+    assert np.all(np.abs(eg - e_np) <= 1e-11 + 1e-5 * e_np)
+    border = (np.abs(e_np[:, :5] / 1e-7 - 1) < 0.01).any(1)
+    assert np.array_equal(lab[m][~border], l_np[~border])
+    # features: distance ratios and wavenumbers
+    _, cp, npv, _ = sr.geometry(P)
+    _, cq, nq, aq = sr.geometry(Q)
+    h = np.sqrt(aq)
+    d = np.linalg.norm(cp - cq, axis=1)
+    assert np.allclose(feat[:, 0], d / h, rtol=1e-6)
+    assert np.allclose(feat[:, 8], k * h, rtol=1e-6)
+    assert np.allclose(feat[:, 9], k * d, rtol=1e-6)
+    assert np.allclose(feat[:, 6], (npv * nq).sum(1), atol=1e-6)
+    assert np.isfinite(feat).all()
+
+
+def test_near_pairs_labelled_against_split_polar_rule(bem, orc, sd):
+    """Below one source size the reference is the near-singular rule; the
+    oracle's own near-singular evaluation reproduces the GPU's errors."""
+    from oracle import selector_ref as sr
+    P, Q, k, dh = sd.pairs(3000, seed=12)
+    sel = np.flatnonzero((dh < 0.9) & (dh > 0.4))[:40]
+    _, lab, err = bem.sel_label(P[sel], Q[sel], k[sel], tol=1e-7, want_err=True)
+    rules = {o: orc.triangle_rule(o) for o in sr.CLASS_ORDERS + (sr.PLAIN_ORDER,)}
+    checked = 0
+    for t, i in enumerate(sel):
+        # the oracle dispatches this pair to its near-singular rule only when
+        # the centroids are closer than 2 mean(sqrt(area)); compare those
+        _, cp, _, ap = sr.geometry(P[i:i + 1])
+        _, cq, _, aq = sr.geometry(Q[i:i + 1])
+        if np.linalg.norm(cp - cq) >= np.sqrt(ap[0]) + np.sqrt(aq[0]):
+            continue
+        tri = np.stack([P[i], Q[i]])
+        prob = orc.Problem(tri, 32, 2.0)
+        inv = np.argsort(prob.perm)
+        ref = prob.operators(float(k[i]), [inv[0]], [inv[1]])
+        e_np, _ = sr.errors_and_labels(P[i:i + 1], Q[i:i + 1], k[i:i + 1], rules, 1e-7, ref=ref)
+        assert np.allclose(err[t], e_np[0], rtol=1e-5, atol=1e-11)
+        checked += 1
+    assert checked >= 10
+
+
+def _dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def test_mlp_gradient_vs_oracle(bem, torch):
+    from oracle import mlp
+    rng = np.random.default_rng(4)
+    B = 777
+    p = mlp.init(2).astype(np.float32)
+    X = rng.standard_normal((B, 24)).astype(np.float32)
+    y = rng.integers(0, 5, B).astype(np.uint8)
+    L = bem.lib()
+    pd, Xd, yd = _dev(torch, p), _dev(torch, X), _dev(torch, y)
+    g = torch.zeros(6085, dtype=torch.float32, device="cuda")
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    work = torch.zeros(B * (4 * 64 + 9), dtype=torch.float32, device="cuda")
+    args = [ct.c_void_p(pd.data_ptr()), ct.c_void_p(Xd.data_ptr()), ct.c_void_p(yd.data_ptr()),
+            B, ct.c_void_p(g.data_ptr()), ct.c_void_p(loss.data_ptr()),
+            ct.c_void_p(work.data_ptr()), None]
+    assert L.bem_mlp_grad(*args) == 0
+    torch.cuda.synchronize()
+    g1 = g.cpu().numpy().copy()
+    assert L.bem_mlp_grad(*args) == 0
+    torch.cuda.synchronize()
+    assert np.array_equal(g1, g.cpu().numpy())  # bitwise reproducible
+    go = mlp.grad(p.astype(np.float64), X.astype(np.float64), y.astype(int))
+    assert np.linalg.norm(g1 - go) / np.linalg.norm(go) < 1e-5
+    assert np.abs(g1 - go).max() < 1e-5 * np.abs(go).max() + 1e-7
+    assert abs(float(loss.item()) - mlp.loss(p.astype(np.float64), X, y.astype(int))) < 1e-5
+    # one Adam step against the textbook update
+    m = torch.zeros_like(g)
+    v = torch.zeros_like(g)
+    assert L.bem_mlp_adam(ct.c_void_p(pd.data_ptr()), ct.c_void_p(g.data_ptr()),
+                          ct.c_void_p(m.data_ptr()), ct.c_void_p(v.data_ptr()), 1, 1e-3, 0.9,
+                          0.999, 1e-8, None) == 0
+    torch.cuda.synchronize()
+    mh = 0.1 * g1 / (1 - 0.9)
+    vh = 0.001 * g1 * g1 / (1 - 0.999)
+    expect = p - 1e-3 * mh / (np.sqrt(vh) + 1e-8)
+    assert np.allclose(pd.cpu().numpy(), expect, rtol=1e-5, atol=1e-7)
+
+
+def _bf16_forward(mlp, p, mu, sigma, F):
+    """The inference kernel's arithmetic: BF16 inputs / weights / hidden
+    activations, FP32 accumulation and biases."""
+    w = mlp.unpack(p.astype(np.float64))
+    x = mlp.bf16((F - mu) / sigma).astype(np.float64)
+    h1 = mlp.bf16(np.maximum(x @ mlp.bf16(w["W1"]).astype(np.float64) + w["b1"], 0))
+    h2 = mlp.bf16(np.maximum(h1.astype(np.float64) @ mlp.bf16(w["W2"]).astype(np.float64)
+                             + w["b2"], 0))
+    return h2.astype(np.float64) @ mlp.bf16(w["W3"]).astype(np.float64) + w["b3"]
+
+
+def test_bf16_inference_vs_emulation(bem, torch):
+    from oracle import mlp
+    rng = np.random.default_rng(5)
+    B = 1000
+    p = (mlp.init(3) * 1.5).astype(np.float32)
+    p[mlp.NPARAM - 5:] = rng.standard_normal(5)
+    F = rng.standard_normal((B, 24)).astype(np.float32) * 3 + 1
+    mu = rng.standard_normal(24).astype(np.float32)
+    sigma = (rng.random(24) * 2 + 0.5).astype(np.float32)
+    Fd = _dev(torch, F)
+    logits = torch.zeros((B, 8), dtype=torch.float32, device="cuda")
+    cls = torch.zeros(B, dtype=torch.uint8, device="cuda")
+    assert bem.lib().bem_sel_infer(p.ctypes.data_as(ct.c_void_p), mu.ctypes.data_as(ct.c_void_p),
+                                   sigma.ctypes.data_as(ct.c_void_p),
+                                   ct.c_void_p(Fd.data_ptr()), B,
+                                   ct.c_void_p(logits.data_ptr()),
+                                   ct.c_void_p(cls.data_ptr()), None) == 0
+    z = logits.cpu().numpy()[:, :5]
+    ze = _bf16_forward(mlp, p, mu, sigma, F)
+    scale = np.abs(ze).max()
+    assert np.abs(z - ze).max() < 2e-2 * scale
+    c = cls.cpu().numpy()
+    assert np.array_equal(c, z.argmax(1))
+    assert np.mean(c == ze.argmax(1)) > 0.97
+    # the full-precision network agrees on almost every pair
+    zf, _ = mlp.forward(p.astype(np.float64), (F - mu) / sigma)
+    assert np.mean(c == zf.argmax(1)) > 0.95
+
+
+def test_training_reduces_loss(bem, sd, st, torch):
+    P, Q, k, dh = sd.pairs(40000, seed=13)
+    feat, lab = bem.sel_label(P, Q, k, tol=1e-7)
+    mu, sigma = feat.mean(0), np.maximum(feat.std(0), 1e-6)
+    X = ((feat - mu) / sigma).astype(np.float32)
+    y = np.minimum(lab, 4)
+    params, hist = st.train(bem, X, y, epochs=4, batch=2048, lr=3e-3, seed=1, log=lambda s: None)
+    assert hist[-1] < 0.6 * hist[0]
+    from oracle import mlp
+    z, _ = mlp.forward(params.astype(np.float64), X)
+    acc = np.mean(z.argmax(1) == y)
+    major = np.bincount(y).max() / len(y)
+    assert acc > major + 0.5 * (1 - major)  # removes most errors of the majority guess
+
+
+def test_trained_selector_gain(bem, sd, st):
+    """The committed network on pairs it never saw: wherever one of the
+    candidate rules can reach the 1e-7 label tolerance, the selected rule
+    (with the guard band) reaches it on >99 % of pairs, far more often than
+    the plain 16-point rule, and it under-integrates almost none."""
+    w = bem.load_selector_weights()
+    P, Q, k, dh = sd.pairs(60000, seed=99)
+    feat, lab, err = bem.sel_label(P, Q, k, tol=1e-7, want_err=True)
+    reg = dh >= 2.0  # the pairs the product integrates with Gauss rules
+    ev = st.evaluate(bem, w["params"], w["mu"], w["sigma"], feat[reg], lab[reg], err[reg],
+                     1e-7, 0.9)
+    assert ev["achievable_within_tol_learned"] > 0.99
+    assert ev["achievable_within_tol_learned"] > ev["achievable_within_tol_plain16"] + 0.05
+    assert ev["within_tol_learned"] > ev["within_tol_plain16"]
+    assert ev["under_integrated"] < 0.01
+
+
+def test_solve_with_selector(bem, meshes):
+    tri = meshes.icosphere(3, 1.0)
+    n = tri.shape[0]
+    out = {}
+    for sel in (0, 1):
+        s = bem.Solver(aca_tol=1e-5, gmres_tol=1e-10, precision=1, selector=sel)
+        s.set_mesh(tri)
+        s.set_bc(np.zeros(n), np.ones(n))
+        # 500 Hz: kh = 0.9 on this mesh, inside the trained range (0.01-1.5)
+        phi, dphi, p, info = s.solve(500.0, np.ones(n))
+        assert info["status"] == 0
+        out[sel] = p[:, 0]
+        if sel:
+            stats = s.sel_stats()
+            cls = s.sel_classes()
+            assert stats["regular_entries"] > 0 and stats["checked"] > 0
+            assert stats["fallback"] <= 0.05 * stats["checked"]
+            assert cls.max() <= 4
+    # the learned rules change entries by ~1e-6 relative at most
+    assert rel(out[1], out[0]) < 1e-5
