@@ -413,7 +413,7 @@ void assemble(bem_handle* h, double freq, double* t_near, double* t_aca) {
     CK(cudaMemsetAsync(h->dSelCnt.p, 0, 3 * sizeof(unsigned long long), s));
     SelNearArgs ca{};
     ca.blob = h->dSel.p;
-    ca.E = h->dE.p;
+    ca.EF = h->dEF.p;
     ca.blocks = na.blocks;
     ca.tiles = na.tiles;
     ca.ntiles = na.ntiles;

@@ -220,6 +220,75 @@ __device__ void sel_features(const double* p, const double* np, const Elem& Q, d
   f[23] = (float)((lmin >= 0 ? fabs(hn) : dv) / h);
 }
 
+// The same features from the FP32 element copies (mixed-precision path): the
+// centroid offset comes from the two-float centroids, vertices are stored
+// relative to their centroid, so every quantity keeps ~7 digits -- far below
+// the BF16 rounding of the network input.
+__device__ void sel_features32(const ElemF& P, const ElemF& Q, float k, float* f) {
+  const float h = sqrtf(Q.area);
+  float rx, ry, rz;
+  centroid_diff(P, Q, rx, ry, rz);
+  const float d = fmaxf(sqrtf(rx * rx + ry * ry + rz * rz), 1e-12f * h);
+  const float hn = rx * Q.nrm[0] + ry * Q.nrm[1] + rz * Q.nrm[2];
+  const float* V[3] = {Q.v, Q.v + 3, Q.v + 6};
+  float e[3];
+  for (int i = 0; i < 3; i++) {
+    const float* A = V[i];
+    const float* B = V[(i + 1) % 3];
+    e[i] = sqrtf((B[0] - A[0]) * (B[0] - A[0]) + (B[1] - A[1]) * (B[1] - A[1]) +
+                 (B[2] - A[2]) * (B[2] - A[2]));
+  }
+  float ang[3];
+  for (int i = 0; i < 3; i++) {
+    const float a = e[i], b = e[(i + 1) % 3], c = e[(i + 2) % 3];
+    ang[i] = acosf(fminf(1.0f, fmaxf(-1.0f, (b * b + c * c - a * a) / (2.0f * b * c))));
+  }
+  const float emin = fminf(e[0], fminf(e[1], e[2])), emax = fmaxf(e[0], fmaxf(e[1], e[2]));
+  const float emid = e[0] + e[1] + e[2] - emin - emax;
+  float dv = 3e38f;
+  for (int i = 0; i < 3; i++) {
+    const float x = rx - V[i][0], y = ry - V[i][1], z = rz - V[i][2];
+    dv = fminf(dv, sqrtf(x * x + y * y + z * z));
+  }
+  const float px = rx - hn * Q.nrm[0], py = ry - hn * Q.nrm[1], pz = rz - hn * Q.nrm[2];
+  float lam[3];
+  for (int i = 0; i < 3; i++) {
+    const float* A = V[(i + 1) % 3];
+    const float* B = V[(i + 2) % 3];
+    const float ax = A[0] - px, ay = A[1] - py, az = A[2] - pz;
+    const float bx = B[0] - px, by = B[1] - py, bz = B[2] - pz;
+    const float cx = ay * bz - az * by, cy = az * bx - ax * bz, cz = ax * by - ay * bx;
+    lam[i] = fminf(10.0f, fmaxf(-10.0f, 0.5f * (cx * Q.nrm[0] + cy * Q.nrm[1] + cz * Q.nrm[2]) / Q.area));
+  }
+  const float lmin = fminf(lam[0], fminf(lam[1], lam[2]));
+  const float kh = fmaxf(k * h, 1e-6f);
+  const float* np = P.nrm;
+  f[0] = d / h;
+  f[1] = h / d;
+  f[2] = logf(d / h);
+  f[3] = (h / d) * (h / d);
+  f[4] = hn / d;
+  f[5] = fabsf(hn) / h;
+  f[6] = np[0] * Q.nrm[0] + np[1] * Q.nrm[1] + np[2] * Q.nrm[2];
+  f[7] = (rx * np[0] + ry * np[1] + rz * np[2]) / d;
+  f[8] = kh;
+  f[9] = k * d;
+  f[10] = logf(kh);
+  f[11] = emin / h;
+  f[12] = emid / h;
+  f[13] = emax / h;
+  f[14] = emax * emax / (2.0f * Q.area);
+  f[15] = fminf(ang[0], fminf(ang[1], ang[2]));
+  f[16] = fmaxf(ang[0], fmaxf(ang[1], ang[2]));
+  f[17] = dv / h;
+  f[18] = lam[0];
+  f[19] = lam[1];
+  f[20] = lam[2];
+  f[21] = lmin;
+  f[22] = emax / d;
+  f[23] = (lmin >= 0 ? fabsf(hn) : dv) / h;
+}
+
 // ---------------- FP64 operators with a table rule ----------------
 // The rule on each of the n^2 congruent sub-triangles of a uniform n-fold
 // edge subdivision of Q (n = 1: the rule itself, points as tabulated).
@@ -627,8 +696,7 @@ __global__ void __launch_bounds__(32 * IW) sel_near_classes_kernel(SelNearArgs a
       if (e < tile.count && !is_special(a.special_bits, b.off + tile.first + e)) {
         const int idx = tile.first + e;
         const int r = idx % b.m, c = idx / b.m;
-        const Elem& P = a.E[b.r0 + r];
-        sel_features(P.c, P.nrm, a.E[b.c0 + c], a.k, f);
+        sel_features32(a.EF[b.r0 + r], a.EF[b.c0 + c], a.k, f);
       } else {
         for (int j = 0; j < SEL_NF; j++) f[j] = sb.mu[j];
       }
@@ -653,8 +721,13 @@ __global__ void __launch_bounds__(32 * IW) sel_near_classes_kernel(SelNearArgs a
 }
 
 // ---------------- near-field entries with the selected rules ----------------
+constexpr int SEL_CLASS_PTS = 1 + 3 + 7 + 13 + 25;  // classes 0-4, stored first
+
+// rule points from a shared-memory copy of the class rules (divergent
+// classes within a warp then cost no constant-cache serialisation)
 __device__ __forceinline__ OpsF ops_rule32(const ElemF* __restrict__ EF, int64_t row, int64_t col,
-                                           float k, int rule) {
+                                           float k, int b, int e, const float* rx1,
+                                           const float* rx2, const float* rw) {
   float dx, dy, dz;
   centroid_diff(EF[row], EF[col], dx, dy, dz);
   const ElemF& Q = EF[col];
@@ -663,9 +736,8 @@ __device__ __forceinline__ OpsF ops_rule32(const ElemF* __restrict__ EF, int64_t
   const float upNq = npx * nqx + npy * nqy + npz * nqz;
   const float inv4pi = 0.0795774715459476679f;
   float Lx = 0, Ly = 0, Mx = 0, My = 0, Tx = 0, Ty = 0, Nx = 0, Ny = 0;
-  const int b = c_sel.off[rule], e = b + c_sel.cnt[rule];
   for (int i = b; i < e; i++) {
-    const float a1 = c_sel.fx1[i], a2 = c_sel.fx2[i], a3 = 1.0f - a2 - a1, w = c_sel.fw[i];
+    const float a1 = rx1[i], a2 = rx2[i], a3 = 1.0f - a2 - a1, w = rw[i];
     const float rx = dx - (a1 * Q.v[0] + a2 * Q.v[3] + a3 * Q.v[6]);
     const float ry = dy - (a1 * Q.v[1] + a2 * Q.v[4] + a3 * Q.v[7]);
     const float rz = dz - (a1 * Q.v[2] + a2 * Q.v[5] + a3 * Q.v[8]);
@@ -706,38 +778,67 @@ __device__ __forceinline__ OpsF ops_rule32(const ElemF* __restrict__ EF, int64_t
 
 __device__ __forceinline__ float fabs2(float2 a) { return sqrtf(a.x * a.x + a.y * a.y); }
 
+// One CTA per near-field tile. The tile's regular entries are first grouped
+// by class in shared memory, so that a warp integrates one rule (its cost is
+// the rule's points, not the largest rule among its lanes).
 __global__ void __launch_bounds__(256) sel_nearfield32_kernel(SelNearfieldArgs a) {
+  __shared__ float rx1[SEL_CLASS_PTS], rx2[SEL_CLASS_PTS], rw[SEL_CLASS_PTS];
+  __shared__ int roff[SEL_C + 1];
+  __shared__ int cnt[SEL_C], base[SEL_C + 1];
+  __shared__ int16_t order[256];
+  for (int i = threadIdx.x; i < SEL_CLASS_PTS; i += blockDim.x) {
+    rx1[i] = c_sel.fx1[i];
+    rx2[i] = c_sel.fx2[i];
+    rw[i] = c_sel.fw[i];
+  }
+  if (threadIdx.x <= SEL_C) roff[threadIdx.x] = threadIdx.x < SEL_C ? c_sel.off[threadIdx.x] : SEL_CLASS_PTS;
+  if (threadIdx.x < SEL_C) cnt[threadIdx.x] = 0;
+  __syncthreads();
   const NearTile t = a.tiles[blockIdx.x];
-  const bool live = (int)threadIdx.x < t.count;
+  const NearBlock b = a.blocks[t.block];
+  // group this tile's regular entries by class
+  int my_cls = -1, slot = 0;
+  if ((int)threadIdx.x < t.count && !is_special(a.special_bits, b.off + t.first + threadIdx.x)) {
+    my_cls = min((int)a.cls[b.off + t.first + threadIdx.x], SEL_C - 1);
+    slot = atomicAdd(&cnt[my_cls], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    base[0] = 0;
+    for (int c = 0; c < SEL_C; c++) base[c + 1] = base[c] + cnt[c];
+  }
+  __syncthreads();
+  if (my_cls >= 0) order[base[my_cls] + slot] = (int16_t)threadIdx.x;
+  __syncthreads();
   unsigned long long pts = 0, chk = 0, fb = 0;
-  if (live) {
-    const NearBlock b = a.blocks[t.block];
-    const int e = t.first + threadIdx.x;
+  if ((int)threadIdx.x < base[SEL_C]) {
+    const int le = order[threadIdx.x];
+    const int e = t.first + le;
     const int64_t g = b.off + e;
-    if (!is_special(a.special_bits, g)) {
-      const int r = e % b.m, c = e / b.m;
-      const int64_t row = b.r0 + r, col = b.c0 + c;
-      const int cls = min((int)a.cls[g], SEL_C - 1);
-      float2 p, d;
-      substitute32(ops_rule32(a.EF, row, col, a.k, cls), a.bc[col], a.alpha, p, d);
-      pts = c_sel.cnt[cls];
-      const uint32_t hsh = (uint32_t)((uint64_t)g * 2654435761ull >> 7);
-      if (cls < SEL_C - 1 && a.check_every > 0 && hsh % (uint32_t)a.check_every == 0) {
-        float2 p4, d4;
-        substitute32(ops_rule32(a.EF, row, col, a.k, SEL_C - 1), a.bc[col], a.alpha, p4, d4);
-        pts += c_sel.cnt[SEL_C - 1];
-        chk = 1;
-        const float scale = fmaxf(fmaxf(fabs2(p4), fabs2(d4)), 1e-30f);
-        const float diff = fmaxf(fabs2(fsub(p, p4)), fabs2(fsub(d, d4)));
-        if (diff > a.check_tol * scale) {
-          p = p4;
-          d = d4;
-          fb = 1;
-        }
+    const int r = e % b.m, c = e / b.m;
+    const int64_t row = b.r0 + r, col = b.c0 + c;
+    const int cls = min((int)a.cls[g], SEL_C - 1);
+    float2 p, d;
+    substitute32(ops_rule32(a.EF, row, col, a.k, roff[cls], roff[cls + 1], rx1, rx2, rw),
+                 a.bc[col], a.alpha, p, d);
+    pts = roff[cls + 1] - roff[cls];
+    const uint32_t hsh = (uint32_t)((uint64_t)g * 2654435761ull >> 7);
+    if (cls < SEL_C - 1 && a.check_every > 0 && hsh % (uint32_t)a.check_every == 0) {
+      float2 p4, d4;
+      substitute32(ops_rule32(a.EF, row, col, a.k, roff[SEL_C - 1], roff[SEL_C], rx1, rx2, rw),
+                   a.bc[col], a.alpha, p4, d4);
+      pts += roff[SEL_C] - roff[SEL_C - 1];
+      chk = 1;
+      const float scale = fmaxf(fmaxf(fabs2(p4), fabs2(d4)), 1e-30f);
+      const float diff = fmaxf(fabs2(fsub(p, p4)), fabs2(fsub(d, d4)));
+      if (diff > a.check_tol * scale) {
+        p = p4;
+        d = d4;
+        fb = 1;
       }
-      a.phi[g] = p;
-      a.dphi[g] = d;
     }
+    a.phi[g] = p;
+    a.dphi[g] = d;
   }
   // per-warp sums of the counters
 #pragma unroll

@@ -79,7 +79,7 @@ void launch_sel_infer_rows(const SelBlob* blob, const float* feat, int64_t B, fl
 // the highest order). Special entries are left untouched.
 struct SelNearArgs {
   const SelBlob* blob;
-  const Elem* E;
+  const ElemF* EF;  // features in FP32 from the mixed-precision element copies
   const NearBlock* blocks;
   const NearTile* tiles;
   int64_t ntiles;

@@ -212,3 +212,44 @@ def test_solve_with_selector(bem, meshes):
             assert cls.max() <= 4
     # the learned rules change entries by ~1e-6 relative at most
     assert rel(out[1], out[0]) < 1e-5
+
+
+def test_mesh_classes_match_rows_inference(bem, meshes, torch):
+    """The solver's per-entry classes (FP32 features from the element copies,
+    fused with the BF16 network) agree with FP64 features of the same pairs
+    fed to the row-wise inference entry point."""
+    tri = meshes.icosphere(3, 1.0)
+    n = tri.shape[0]
+    s = bem.Solver(aca_tol=1e-5, gmres_tol=1e-10, precision=1, selector=1, selector_guard=0.0)
+    s.set_mesh(tri)
+    s.set_bc(np.zeros(n), np.ones(n))
+    freq = 500.0
+    s.assemble(freq)
+    cls = s.sel_classes()
+    perm = s.permutation
+    info = s.partition()
+    rows, cols = [], []
+    for r0, m, c0, nn, adm in info:
+        if adm:
+            continue
+        rr, cc = np.meshgrid(np.arange(r0, r0 + m), np.arange(c0, c0 + nn), indexing="ij")
+        rows.append(rr.ravel(order="F"))
+        cols.append(cc.ravel(order="F"))
+    rows, cols = perm[np.concatenate(rows)], perm[np.concatenate(cols)]
+    t = tri.reshape(-1, 9)
+    c = tri.reshape(-1, 3, 3).mean(1)
+    area = 0.5 * np.linalg.norm(np.cross(t[:, 3:6] - t[:, :3], t[:, 6:] - t[:, :3]), axis=1)
+    near_r = 2 * np.sqrt(area).mean()
+    reg = np.linalg.norm(c[rows] - c[cols], axis=1) >= 1.05 * near_r
+    k = np.full(reg.sum(), 2 * np.pi * freq / 343.0)
+    feat, _ = bem.sel_label(t[rows[reg]], t[cols[reg]], k)
+    w = bem.load_selector_weights()
+    Fd = _dev(torch, feat)
+    cr = torch.zeros(len(k), dtype=torch.uint8, device="cuda")
+    prm = np.ascontiguousarray(w["params"], np.float32)
+    mu = np.ascontiguousarray(w["mu"], np.float32)
+    sg = np.ascontiguousarray(w["sigma"], np.float32)
+    assert bem.lib().bem_sel_infer(prm.ctypes.data_as(ct.c_void_p), mu.ctypes.data_as(ct.c_void_p),
+                                   sg.ctypes.data_as(ct.c_void_p), ct.c_void_p(Fd.data_ptr()),
+                                   len(k), None, ct.c_void_p(cr.data_ptr()), None) == 0
+    assert np.mean(cls[reg] == cr.cpu().numpy()) > 0.99
