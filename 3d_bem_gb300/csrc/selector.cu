@@ -13,8 +13,9 @@
 //    parameter with the samples summed in order, so the result is bitwise
 //    reproducible; Adam).
 //  * sel_infer / sel_near_classes: BF16 inference on the tensor cores, one warp
-//    per 16 pairs, mma.sync m16n8k16 with FP32 accumulation; low-confidence
-//    pairs get the highest order (the guard band).
+//    per 32 pairs (two m16 row tiles sharing the weight fragments), mma.sync
+//    m16n8k16 with FP32 accumulation; low-confidence pairs get the highest
+//    order (the guard band).
 //  * sel_nearfield32: the mixed-precision near-field kernel with the selected
 //    rule per entry; a hashed sample of entries is re-integrated with the
 //    highest order and keeps that value when the two disagree.
@@ -531,67 +532,85 @@ __device__ __forceinline__ void mma16816(float* d, uint32_t a0, uint32_t a1, uin
       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
-// One dense layer for the warp's 16 rows: A (16 x K, ld lda) times W^T stored
-// output-major (N x K, ld ldw). The fragment rows / columns follow the
-// m16n8k16 layout: lane = 4 g + t holds A(g, 2t..2t+1), A(g+8, ..), A(g, 2t+8..),
-// A(g+8, 2t+8..); B(2t..2t+1, g), B(2t+8.., g); D(g, 2t..2t+1), D(g+8, ..).
+// One dense layer for the warp's 32 rows (two m16 row tiles sharing every B
+// fragment): A (32 x K, ld lda) times W^T stored output-major (N x K, ld
+// ldw). Fragments follow the m16n8k16 layout: lane = 4 g + t holds
+// A(g, 2t..2t+1), A(g+8, ..), A(g, 2t+8..), A(g+8, 2t+8..); B(2t..2t+1, g),
+// B(2t+8.., g); D(g, 2t..2t+1), D(g+8, ..).
 template <int K, int NT>
 __device__ __forceinline__ void warp_layer(const uint16_t* A, int lda, const uint16_t* Wt, int ldw,
-                                           float (*acc)[4]) {
+                                           float (*acc)[NT][4]) {
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
 #pragma unroll
-  for (int nt = 0; nt < NT; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+  for (int m = 0; m < 2; m++)
+#pragma unroll
+    for (int nt = 0; nt < NT; nt++) acc[m][nt][0] = acc[m][nt][1] = acc[m][nt][2] = acc[m][nt][3] = 0.0f;
 #pragma unroll
   for (int k0 = 0; k0 < K; k0 += 16) {
-    const uint32_t a0 = ld32(A + g * lda + k0 + 2 * t);
-    const uint32_t a1 = ld32(A + (g + 8) * lda + k0 + 2 * t);
-    const uint32_t a2 = ld32(A + g * lda + k0 + 8 + 2 * t);
-    const uint32_t a3 = ld32(A + (g + 8) * lda + k0 + 8 + 2 * t);
+    uint32_t a[2][4];
+#pragma unroll
+    for (int m = 0; m < 2; m++) {
+      const uint16_t* r0 = A + (16 * m + g) * lda + k0 + 2 * t;
+      const uint16_t* r1 = r0 + 8 * lda;
+      a[m][0] = ld32(r0);
+      a[m][1] = ld32(r1);
+      a[m][2] = ld32(r0 + 8);
+      a[m][3] = ld32(r1 + 8);
+    }
 #pragma unroll
     for (int nt = 0; nt < NT; nt++) {
       const uint16_t* w = Wt + (nt * 8 + g) * ldw + k0 + 2 * t;
-      mma16816(acc[nt], a0, a1, a2, a3, ld32(w), ld32(w + 8));
+      const uint32_t b0 = ld32(w), b1 = ld32(w + 8);
+      mma16816(acc[0][nt], a[0][0], a[0][1], a[0][2], a[0][3], b0, b1);
+      mma16816(acc[1][nt], a[1][0], a[1][1], a[1][2], a[1][3], b0, b1);
     }
   }
 }
 
-// bias + ReLU, back to BF16 rows of H (16 x 64)
-__device__ __forceinline__ void store_hidden(float (*acc)[4], const float* bias, uint16_t* H) {
+// bias + ReLU, back to BF16 rows of H (32 x 64)
+__device__ __forceinline__ void store_hidden(float (*acc)[8][4], const float* bias, uint16_t* H) {
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
 #pragma unroll
-  for (int nt = 0; nt < 8; nt++) {
-    const int c = nt * 8 + 2 * t;
-    H[g * 64 + c] = f2bf(fmaxf(acc[nt][0] + bias[c], 0.0f));
-    H[g * 64 + c + 1] = f2bf(fmaxf(acc[nt][1] + bias[c + 1], 0.0f));
-    H[(g + 8) * 64 + c] = f2bf(fmaxf(acc[nt][2] + bias[c], 0.0f));
-    H[(g + 8) * 64 + c + 1] = f2bf(fmaxf(acc[nt][3] + bias[c + 1], 0.0f));
-  }
+  for (int m = 0; m < 2; m++)
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++) {
+      const int c = nt * 8 + 2 * t;
+      uint16_t* r0 = H + (16 * m + g) * 64 + c;
+      uint16_t* r1 = r0 + 8 * 64;
+      r0[0] = f2bf(fmaxf(acc[m][nt][0] + bias[c], 0.0f));
+      r0[1] = f2bf(fmaxf(acc[m][nt][1] + bias[c + 1], 0.0f));
+      r1[0] = f2bf(fmaxf(acc[m][nt][2] + bias[c], 0.0f));
+      r1[1] = f2bf(fmaxf(acc[m][nt][3] + bias[c + 1], 0.0f));
+    }
 }
 
+// two 32 x 64 BF16 tiles per warp: the input (columns 0..31) and then the
+// second hidden layer in `a`, the first hidden layer in `b`
 struct WarpBufs {
-  uint16_t x[16 * 32];
-  uint16_t h1[16 * 64];
-  uint16_t h2[16 * 64];
+  uint16_t a[32 * 64];
+  uint16_t b[32 * 64];
 };
 
-// the network on the warp's 16 rows (x already staged); returns, for rows
-// g and g + 8 of this lane's group, the logits in lg[0..1] / lg[2..3]
-// (columns 2t, 2t+1)
-__device__ __forceinline__ void warp_mlp(const SelBlob& B, WarpBufs& wb, float* lg) {
-  float acc[8][4];
-  warp_layer<32, 8>(wb.x, 32, B.w1t, 32, acc);
-  store_hidden(acc, B.b1, wb.h1);
+// the network on the warp's 32 rows (inputs staged in wb.a); lg[m] holds,
+// for rows 16 m + g and 16 m + g + 8, the logits of columns 2t, 2t+1
+__device__ __forceinline__ void warp_mlp(const SelBlob& B, WarpBufs& wb, float (*lg)[4]) {
+  float acc[2][8][4];
+  warp_layer<32, 8>(wb.a, 64, B.w1t, 32, acc);
+  store_hidden(acc, B.b1, wb.b);
   __syncwarp();
-  warp_layer<64, 8>(wb.h1, 64, B.w2t, 64, acc);
-  store_hidden(acc, B.b2, wb.h2);
+  warp_layer<64, 8>(wb.b, 64, B.w2t, 64, acc);
+  store_hidden(acc, B.b2, wb.a);
   __syncwarp();
-  float o[1][4];
-  warp_layer<64, 1>(wb.h2, 64, B.w3t, 64, o);
+  float o[2][1][4];
+  warp_layer<64, 1>(wb.a, 64, B.w3t, 64, o);
   const int t = (threadIdx.x & 31) & 3;
-  lg[0] = o[0][0] + B.b3[2 * t];
-  lg[1] = o[0][1] + B.b3[2 * t + 1];
-  lg[2] = o[0][2] + B.b3[2 * t];
-  lg[3] = o[0][3] + B.b3[2 * t + 1];
+#pragma unroll
+  for (int m = 0; m < 2; m++) {
+    lg[m][0] = o[m][0][0] + B.b3[2 * t];
+    lg[m][1] = o[m][0][1] + B.b3[2 * t + 1];
+    lg[m][2] = o[m][0][2] + B.b3[2 * t];
+    lg[m][3] = o[m][0][3] + B.b3[2 * t + 1];
+  }
 }
 
 // argmax over the 8 logits of a row spread over the 4 lanes of a group, and
@@ -622,7 +641,7 @@ __device__ __forceinline__ void stage_blob(const SelBlob* src, SelBlob& dst) {
   __syncthreads();
 }
 
-// normalised features of one row into the warp's BF16 input tile
+// normalised features of one row into the warp's BF16 input tile (ld 64)
 __device__ __forceinline__ void stage_row(const SelBlob& B, const float* f, uint16_t* xrow) {
 #pragma unroll
   for (int j = 0; j < SEL_NF; j++) xrow[j] = f2bf((f[j] - B.mu[j]) * B.inv_sigma[j]);
@@ -641,36 +660,39 @@ __global__ void __launch_bounds__(32 * IW) sel_infer_rows_kernel(const SelBlob* 
   __shared__ __align__(16) WarpBufs wb[IW];
   stage_blob(blob, sb);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  const int64_t nchunk = (B + 15) / 16;
+  const int64_t nchunk = (B + 31) / 32;
   for (int64_t ch = (int64_t)blockIdx.x * IW + warp; ch < nchunk; ch += (int64_t)gridDim.x * IW) {
-    const int64_t r0 = ch * 16;
-    if (lane < 16) {
+    const int64_t r0 = ch * 32;
+    {
       float f[SEL_NF];
       const int64_t r = r0 + lane;
       for (int j = 0; j < SEL_NF; j++) f[j] = r < B ? feat[r * SEL_NF + j] : 0.0f;
-      stage_row(sb, f, wb[warp].x + lane * 32);
+      stage_row(sb, f, wb[warp].a + lane * 64);
     }
     __syncwarp();
-    float lg[4];
+    float lg[2][4];
     warp_mlp(sb, wb[warp], lg);
-    int c0, c1;
-    float p0, p1;
-    group_argmax(lg[0], lg[1], t, c0, p0);
-    group_argmax(lg[2], lg[3], t, c1, p1);
-    const int64_t ra = r0 + g, rb = r0 + g + 8;
-    if (logits) {
-      if (ra < B) {
-        logits[ra * 8 + 2 * t] = lg[0];
-        logits[ra * 8 + 2 * t + 1] = lg[1];
+#pragma unroll
+    for (int m = 0; m < 2; m++) {
+      int c0, c1;
+      float p0, p1;
+      group_argmax(lg[m][0], lg[m][1], t, c0, p0);
+      group_argmax(lg[m][2], lg[m][3], t, c1, p1);
+      const int64_t ra = r0 + 16 * m + g, rb = ra + 8;
+      if (logits) {
+        if (ra < B) {
+          logits[ra * 8 + 2 * t] = lg[m][0];
+          logits[ra * 8 + 2 * t + 1] = lg[m][1];
+        }
+        if (rb < B) {
+          logits[rb * 8 + 2 * t] = lg[m][2];
+          logits[rb * 8 + 2 * t + 1] = lg[m][3];
+        }
       }
-      if (rb < B) {
-        logits[rb * 8 + 2 * t] = lg[2];
-        logits[rb * 8 + 2 * t + 1] = lg[3];
+      if (t == 0) {
+        if (ra < B) cls[ra] = (uint8_t)c0;
+        if (rb < B) cls[rb] = (uint8_t)c1;
       }
-    }
-    if (t == 0) {
-      if (ra < B) cls[ra] = (uint8_t)c0;
-      if (rb < B) cls[rb] = (uint8_t)c1;
     }
     __syncwarp();
   }
@@ -680,43 +702,49 @@ __device__ __forceinline__ bool is_special(const uint32_t* bits, int64_t g) {
   return (bits[g >> 5] >> (g & 31)) & 1u;
 }
 
-// classes of the regular near-field entries of a mesh, one CTA per tile
+// classes of the regular near-field entries of a mesh: a persistent grid,
+// each CTA stages the network once and walks tiles, each warp 32 entries
 __global__ void __launch_bounds__(32 * IW) sel_near_classes_kernel(SelNearArgs a) {
   __shared__ __align__(16) SelBlob sb;
   __shared__ __align__(16) WarpBufs wb[IW];
   stage_blob(a.blob, sb);
-  const NearTile tile = a.tiles[blockIdx.x];
-  const NearBlock b = a.blocks[tile.block];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  const int nchunk = (tile.count + 15) / 16;
-  for (int ch = warp; ch < nchunk; ch += IW) {
-    if (lane < 16) {
-      const int e = ch * 16 + lane;
-      float f[SEL_NF];
-      if (e < tile.count && !is_special(a.special_bits, b.off + tile.first + e)) {
-        const int idx = tile.first + e;
-        const int r = idx % b.m, c = idx / b.m;
-        sel_features32(a.EF[b.r0 + r], a.EF[b.c0 + c], a.k, f);
-      } else {
-        for (int j = 0; j < SEL_NF; j++) f[j] = sb.mu[j];
+  for (int64_t ti = blockIdx.x; ti < a.ntiles; ti += gridDim.x) {
+    const NearTile tile = a.tiles[ti];
+    const NearBlock b = a.blocks[tile.block];
+    const int nchunk = (tile.count + 31) / 32;
+    for (int ch = warp; ch < nchunk; ch += IW) {
+      {
+        const int e = ch * 32 + lane;
+        float f[SEL_NF];
+        if (e < tile.count && !is_special(a.special_bits, b.off + tile.first + e)) {
+          const int idx = tile.first + e;
+          const int r = idx % b.m, c = idx / b.m;
+          sel_features32(a.EF[b.r0 + r], a.EF[b.c0 + c], a.k, f);
+        } else {
+          for (int j = 0; j < SEL_NF; j++) f[j] = sb.mu[j];
+        }
+        stage_row(sb, f, wb[warp].a + lane * 64);
       }
-      stage_row(sb, f, wb[warp].x + lane * 32);
+      __syncwarp();
+      float lg[2][4];
+      warp_mlp(sb, wb[warp], lg);
+#pragma unroll
+      for (int m = 0; m < 2; m++) {
+        int c0, c1;
+        float p0, p1;
+        group_argmax(lg[m][0], lg[m][1], t, c0, p0);
+        group_argmax(lg[m][2], lg[m][3], t, c1, p1);
+        if (t == 0) {
+          const int ea = ch * 32 + 16 * m + g, eb = ea + 8;
+          if (ea < tile.count)
+            a.cls[b.off + tile.first + ea] = (uint8_t)(p0 < a.guard_prob ? SEL_C - 1 : c0);
+          if (eb < tile.count)
+            a.cls[b.off + tile.first + eb] = (uint8_t)(p1 < a.guard_prob ? SEL_C - 1 : c1);
+        }
+      }
+      __syncwarp();
     }
-    __syncwarp();
-    float lg[4];
-    warp_mlp(sb, wb[warp], lg);
-    int c0, c1;
-    float p0, p1;
-    group_argmax(lg[0], lg[1], t, c0, p0);
-    group_argmax(lg[2], lg[3], t, c1, p1);
-    if (t == 0) {
-      const int ea = ch * 16 + g, eb = ch * 16 + g + 8;
-      if (ea < tile.count)
-        a.cls[b.off + tile.first + ea] = (uint8_t)(p0 < a.guard_prob ? SEL_C - 1 : c0);
-      if (eb < tile.count)
-        a.cls[b.off + tile.first + eb] = (uint8_t)(p1 < a.guard_prob ? SEL_C - 1 : c1);
-    }
-    __syncwarp();
   }
 }
 
@@ -904,14 +932,15 @@ void launch_mlp_forward(const float* params, const float* X, int64_t B, float* l
 void launch_sel_infer_rows(const SelBlob* blob, const float* feat, int64_t B, float* logits,
                            uint8_t* cls, cudaStream_t s) {
   if (B <= 0) return;
-  const int64_t nchunk = (B + 15) / 16;
+  const int64_t nchunk = (B + 31) / 32;
   const unsigned grid = (unsigned)std::min<int64_t>((nchunk + IW - 1) / IW, 152 * 8);
   sel_infer_rows_kernel<<<grid, 32 * IW, 0, s>>>(blob, feat, B, logits, cls);
 }
 
 void launch_sel_near_classes(const SelNearArgs& a, cudaStream_t s) {
   if (a.ntiles <= 0) return;
-  sel_near_classes_kernel<<<(unsigned)a.ntiles, 32 * IW, 0, s>>>(a);
+  const unsigned grid = (unsigned)std::min<int64_t>(a.ntiles, 152 * 8);
+  sel_near_classes_kernel<<<grid, 32 * IW, 0, s>>>(a);
 }
 
 void launch_sel_nearfield32(const SelNearfieldArgs& a, cudaStream_t s) {
