@@ -39,7 +39,7 @@ EXPORTS = [
     "bem_launch_count", "bem_stream", "bem_hmatvec_noalloc", "bem_hmatvec_device_ex",
     "bem_hlu_build", "bem_hlu_solve", "bem_hlu_export", "bem_recompress",
     "bem_sel_nparam", "bem_sel_label", "bem_mlp_grad", "bem_mlp_adam", "bem_mlp_forward",
-    "bem_sel_infer", "bem_set_selector", "bem_sel_stats", "bem_sel_classes",
+    "bem_sel_infer", "bem_set_selector", "bem_sel_stats", "bem_sel_classes", "bem_autotune",
 ]
 BEM_ARITH_FP64, BEM_ARITH_FP32, BEM_ARITH_TWOFLOAT = 0, 1, 2
 
@@ -59,7 +59,8 @@ class Config(ct.Structure):
                 ("density", ct.c_double), ("seed", ct.c_uint64),
                 ("use_preconditioner", ct.c_int32), ("selector", ct.c_int32),
                 ("precond_rank", ct.c_int64), ("precond_tol", ct.c_double),
-                ("recompress_tol", ct.c_double), ("selector_guard", ct.c_double)]
+                ("recompress_tol", ct.c_double), ("selector_guard", ct.c_double),
+                ("sweep_workers", ct.c_int64), ("aca_big_mn", ct.c_int64)]
 
 
 class SolveInfo(ct.Structure):
@@ -134,6 +135,7 @@ def lib():
     L.bem_set_selector.argtypes = [vp, vp, vp, vp]
     L.bem_sel_stats.argtypes = [vp, vp]
     L.bem_sel_classes.argtypes = [vp, vp]
+    L.bem_autotune.argtypes = [vp, dbl, i64, vp]
     L.bem_hlu_build.argtypes = [vp]
     L.bem_hlu_solve.argtypes = [vp, vp, vp, i64]
     L.bem_hlu_export.argtypes = [vp, i32, P(i64), vp, P(i64), vp, P(i64), vp]
@@ -313,6 +315,12 @@ class Solver:
         cls = np.zeros(int((near[:, 1] * near[:, 3]).sum()), np.uint8)
         self._check(lib().bem_sel_classes(self._h, _ptr(cls)), "bem_sel_classes")
         return cls
+
+    def autotune(self, freq: float, nrhs: int = 1) -> dict:
+        """Tune the batched sweep (workers, ACA size bin) at a probe frequency."""
+        out = np.zeros(2, np.int64)
+        self._check(lib().bem_autotune(self._h, freq, nrhs, _ptr(out)), "bem_autotune")
+        return {"workers": int(out[0]), "aca_big_mn": int(out[1])}
 
     def recompress(self, which: int, rank: int = 0, tol: float = 0.0):
         """Truncating SVD recompression of every admissible block on the GPU."""

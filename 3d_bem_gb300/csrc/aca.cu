@@ -18,6 +18,9 @@
 // V row l at V + voff + l*n (residual rows), s_l = 1/pivot at S + soff + l.
 // The working residual column/row of the next step live in slot `rank` of the
 // same storage, so the kernel needs no scratch memory.
+#include <mutex>
+#include <set>
+
 #include "bem_kernels.h"
 #include "quadrature.cuh"
 
@@ -25,8 +28,17 @@ namespace bemgpu {
 
 static __constant__ QuadRules c_rules;
 
+// The tables (always the same) go to each device's constant memory once,
+// synchronously, so no later handle rewrites them under running kernels.
 void aca_upload_rules(const QuadRules& r, cudaStream_t s) {
-  cudaMemcpyToSymbolAsync(c_rules, &r, sizeof(QuadRules), 0, cudaMemcpyHostToDevice, s);
+  (void)s;
+  static std::mutex mu;
+  static std::set<int> done;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  if (done.count(dev)) return;
+  if (cudaMemcpyToSymbol(c_rules, &r, sizeof(QuadRules)) == cudaSuccess) done.insert(dev);
 }
 
 namespace {

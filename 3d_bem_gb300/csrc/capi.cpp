@@ -13,7 +13,9 @@
 #include <complex>
 #include <cstring>
 #include <new>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/bemgpu.h"
@@ -99,6 +101,12 @@ struct GmresWS {
 struct bem_handle {
   bem_config cfg{};
   std::string err;
+  int device = 0;
+  // batched sweep: worker handles (own streams and buffers) cloned from this
+  // one's mesh / BC / selector state, and what the autotuner chose
+  std::vector<bem_handle*> workers;
+  uint64_t state_gen = 0, workers_gen = ~0ull;
+  int64_t tuned_workers = 0;
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;  // second stream for concurrent ACA launches
   cudaEvent_t fork = nullptr, join = nullptr;
@@ -185,6 +193,17 @@ cplx coupling_parameter(int kind, double k) {
   if (kind == 0) return 0.0;
   if (kind == 1) return std::fabs(k) < tiny ? I : I / k;
   return I / (k + 1.0);
+}
+
+// ACA size bin: the far blocks (sorted by m + n, largest first) with
+// m + n >= thr get the 512-thread ACA kernel (0: the default threshold)
+void set_big_mn(bem_handle* h, int64_t thr) {
+  Layout& L = h->L;
+  if (thr <= 0) thr = ACA_BIG_MN;
+  L.nbig = 0;
+  while (L.nbig < (int64_t)L.far_order.size() &&
+         (int64_t)L.far[L.far_order[L.nbig]].m + L.far[L.far_order[L.nbig]].n >= thr)
+    L.nbig++;
 }
 
 void upload_layout(bem_handle* h) {
@@ -922,6 +941,163 @@ void copy_out(bem_handle* h, double* dst, const double2* src, size_t cnt) {
   CK(cudaMemcpyAsync(dst, src, cnt * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
 }
 
+// ---- batched frequency sweep ----
+
+// A worker gets the parent's mesh, layout, BCs and selector weights (host
+// copies plus its own device uploads), so it can solve any frequency alone.
+void clone_state(bem_handle* c, bem_handle* p) {
+  c->rows = p->rows;
+  c->cols = p->cols;
+  c->N = p->N;
+  c->E = p->E;
+  c->avgdim = p->avgdim;
+  c->near_r = p->near_r;
+  c->L = p->L;
+  c->points_mode = false;
+  c->dE.upload(c->E, c->stream);
+  c->dEF.upload(make_elemf(c->E), c->stream);
+  c->dPerm.upload(c->rows.perm, c->stream);
+  upload_layout(c);
+  c->have_mesh = true;
+  c->a = p->a;
+  c->b = p->b;
+  c->have_bc = p->have_bc;
+  c->have_selector = false;
+  if (p->have_selector) {
+    c->dSel.ensure(1);
+    CK(cudaMemcpyAsync(c->dSel.p, p->dSel.p, sizeof(SelBlob), cudaMemcpyDeviceToDevice, c->stream));
+    c->have_selector = true;
+  }
+  sync(c);
+}
+
+// nw worker handles beside h, cloned from h's current state
+void ensure_workers(bem_handle* h, int nw) {
+  CK(cudaSetDevice(h->device));
+  if (h->workers_gen != h->state_gen) {
+    for (bem_handle* w : h->workers) bem_destroy(w);
+    h->workers.clear();
+    h->workers_gen = h->state_gen;
+  }
+  while ((int)h->workers.size() < nw) {
+    bem_config c = h->cfg;
+    c.sweep_workers = 1;
+    bem_handle* w = nullptr;
+    const bem_status st = bem_create(&c, &w);
+    require(st == BEM_OK && w, st == BEM_OK ? BEM_ECUDA : st, "could not create a sweep worker");
+    h->workers.push_back(w);
+    try {
+      clone_state(w, h);
+    } catch (...) {
+      bem_destroy(w);
+      h->workers.pop_back();
+      throw;
+    }
+  }
+}
+
+// Frequencies idx[0..n) of a sweep on W handles (h and W - 1 workers), one
+// host thread per handle, each on its own stream; frequency i goes to handle
+// i mod W. p (caller order, n_freq slices) gets each frequency's pressure.
+void run_sweep(bem_handle* h, int W, const double* freqs, const int64_t* idx, int64_t n,
+               const double* g, int64_t nrhs, double* p, bem_solve_info* info,
+               bem_status& worst) {
+  require(h->have_mesh && h->have_bc && !h->points_mode, BEM_EINVAL,
+          "mesh and boundary conditions must be set");
+  W = (int)std::max<int64_t>(1, std::min<int64_t>(W, n));
+  ensure_workers(h, W - 1);
+  std::vector<bem_handle*> hs{h};
+  for (int w = 0; w + 1 < W; w++) hs.push_back(h->workers[w]);
+  const size_t cnt = (size_t)h->N * nrhs;
+  std::vector<bem_status> st(W, BEM_OK), wst(W, BEM_OK);
+  auto body = [&](int w) {
+    bem_handle* x = hs[w];
+    st[w] = guarded(x, [&] {
+      CK(cudaSetDevice(h->device));
+      copy_in(x, x->dIn, g, cnt);
+      x->dOut3.ensure(cnt);
+      for (int64_t i = w; i < n; i += W) {
+        const int64_t f = idx[i];
+        bem_solve_info loc{};
+        solve_dev(x, freqs[f], x->dIn.p, nrhs, nullptr, nullptr, x->dOut3.p, &loc);
+        copy_out(x, p + 2 * cnt * f, x->dOut3.p, cnt);
+        sync(x);
+        if (info) info[f] = loc;
+        if (loc.status != BEM_OK) wst[w] = loc.status;
+      }
+    });
+  };
+  if (W == 1) {
+    body(0);
+  } else {
+    std::vector<std::thread> th;
+    for (int w = 1; w < W; w++) th.emplace_back(body, w);
+    body(0);
+    for (auto& t : th) t.join();
+  }
+  for (int w = 0; w < W; w++) {
+    if (st[w] != BEM_OK) throw BemError{st[w], "sweep worker: " + hs[w]->err};
+    if (wst[w] != BEM_OK) worst = wst[w];
+  }
+}
+
+// Wall-clock rate (frequencies per second) of W workers on nrep * W copies of
+// a probe frequency (distinct by 1e-6 relative, so nothing is reused).
+double probe_rate(bem_handle* h, int W, double freq, int64_t nrhs, int nrep) {
+  const int64_t n = (int64_t)W * nrep;
+  std::vector<double> fr(n);
+  std::vector<int64_t> idx(n);
+  for (int64_t i = 0; i < n; i++) {
+    fr[i] = freq * (1.0 + 1e-6 * (double)(i + 1));
+    idx[i] = i;
+  }
+  std::vector<double> g(2 * (size_t)h->N * nrhs, 0.0), p(2 * (size_t)h->N * nrhs * n);
+  for (size_t i = 0; i < (size_t)h->N * nrhs; i++) g[2 * i] = 1.0;
+  bem_status worst = BEM_OK;
+  const auto t0 = std::chrono::steady_clock::now();
+  run_sweep(h, W, fr.data(), idx.data(), n, g.data(), nrhs, p.data(), nullptr, worst);
+  const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return (double)n / dt;
+}
+
+void autotune(bem_handle* h, double freq, int64_t nrhs) {
+  require(h->have_mesh && h->have_bc && !h->points_mode, BEM_EINVAL,
+          "mesh and boundary conditions must be set");
+  require(freq > 0 && std::isfinite(freq) && nrhs >= 1, BEM_EINVAL, "bad probe");
+  // ACA size bin: the threshold with the shortest ACA phase (best of two)
+  int64_t best_thr = h->cfg.aca_big_mn > 0 ? h->cfg.aca_big_mn : ACA_BIG_MN;
+  double best_t = 1e300;
+  for (int64_t thr : {256, 512, 1024}) {
+    set_big_mn(h, thr);
+    double t = 1e300;
+    for (int rep = 0; rep < 2; rep++) {
+      double tn = 0, ta = 0;
+      assemble(h, freq * (1.0 + 1e-6 * (rep + 1)), &tn, &ta);
+      t = std::min(t, ta);
+    }
+    if (t < best_t) {
+      best_t = t;
+      best_thr = thr;
+    }
+  }
+  set_big_mn(h, best_thr);
+  h->cfg.aca_big_mn = best_thr;
+  h->state_gen++;  // workers must take the tuned layout
+  // workers: warm every candidate handle once, then time 1..4 of them
+  const int maxw = 4;
+  probe_rate(h, maxw, freq, nrhs, 1);
+  int best_w = 1;
+  double best_r = 0;
+  for (int W = 1; W <= maxw; W++) {
+    const double r = probe_rate(h, W, freq, nrhs, 2);
+    if (r > best_r * 1.03) {  // a worker must earn its memory
+      best_r = r;
+      best_w = W;
+    }
+  }
+  h->tuned_workers = best_w;
+}
+
 }  // namespace
 
 extern "C" {
@@ -947,6 +1123,8 @@ void bem_config_default(bem_config* c) {
   c->precond_tol = 0.0;
   c->selector = 0;
   c->selector_guard = 0.9;
+  c->sweep_workers = 0;
+  c->aca_big_mn = 0;
 }
 
 bem_status bem_create(const bem_config* cfg, bem_handle** out) {
@@ -968,6 +1146,10 @@ bem_status bem_create(const bem_config* cfg, bem_handle** out) {
     require(h->cfg.precision == 0 || h->cfg.precision == 1, BEM_EINVAL,
             "precision must be 0 (complex FP64) or 1 (mixed)");
     require(h->cfg.wave_speed > 0, BEM_EINVAL, "wave_speed must be positive");
+    require(h->cfg.sweep_workers >= 0 && h->cfg.sweep_workers <= 16, BEM_EINVAL,
+            "sweep_workers must be 0 (auto) .. 16");
+    require(h->cfg.aca_big_mn >= 0, BEM_EINVAL, "aca_big_mn must be >= 0");
+    CK(cudaGetDevice(&h->device));
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     CK(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming));
@@ -989,6 +1171,8 @@ bem_status bem_create(const bem_config* cfg, bem_handle** out) {
 
 void bem_destroy(bem_handle* h) {
   if (!h) return;
+  for (bem_handle* w : h->workers) bem_destroy(w);
+  h->workers.clear();
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->side) cudaStreamSynchronize(h->side);
   for (auto& e : h->ev)
@@ -1026,9 +1210,11 @@ bem_status bem_set_mesh(bem_handle* h, const double* tri, int64_t n) {
     h->dE.upload(h->E, h->stream);
     h->dEF.upload(make_elemf(h->E), h->stream);
     h->dPerm.upload(h->rows.perm, h->stream);
+    set_big_mn(h, h->cfg.aca_big_mn);
     upload_layout(h);
     h->have_mesh = true;
     h->have_bc = false;
+    h->state_gen++;
     sync(h);
   });
 }
@@ -1106,6 +1292,7 @@ bem_status bem_set_bc(bem_handle* h, const double* a, const double* b) {
       h->b[i] = bv;
     }
     h->have_bc = true;
+    h->state_gen++;
   });
 }
 
@@ -1257,6 +1444,7 @@ bem_status bem_set_selector(bem_handle* h, const float* params, const float* mu,
     CK(cudaMemcpyAsync(h->dSel.p, &b, sizeof(SelBlob), cudaMemcpyHostToDevice, h->stream));
     sync(h);
     h->have_selector = true;
+    h->state_gen++;
   });
 }
 
@@ -1511,24 +1699,38 @@ bem_status bem_solve(bem_handle* h, double freq, const double* g, int64_t nrhs, 
   return st != BEM_OK ? st : loc.status;
 }
 
+bem_status bem_autotune(bem_handle* h, double freq, int64_t nrhs, int64_t* tuned) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] {
+    autotune(h, freq, nrhs);
+    if (tuned) {
+      tuned[0] = h->tuned_workers;
+      tuned[1] = h->cfg.aca_big_mn;
+    }
+  });
+}
+
 bem_status bem_sweep(bem_handle* h, const double* freqs, int64_t nf, const double* g, int64_t nrhs,
                      double* p, bem_solve_info* info) {
   if (!h) return BEM_EINVAL;
   bem_status worst = BEM_OK;
   bem_status st = guarded(h, [&] {
     require(freqs && g && p && nf >= 1 && nrhs >= 1, BEM_EINVAL, "bad arguments");
-    const int64_t N = h->N;
-    const size_t cnt = (size_t)N * nrhs;
-    copy_in(h, h->dIn, g, cnt);
-    h->dOut3.ensure(cnt);
-    for (int64_t f = 0; f < nf; f++) {
-      bem_solve_info loc{};
-      solve_dev(h, freqs[f], h->dIn.p, nrhs, nullptr, nullptr, h->dOut3.p, &loc);
-      copy_out(h, p + 2 * cnt * f, h->dOut3.p, cnt);
-      if (info) info[f] = loc;
-      if (loc.status != BEM_OK) worst = loc.status;
+    for (int64_t f = 0; f < nf; f++)
+      require(freqs[f] > 0 && std::isfinite(freqs[f]), BEM_EINVAL, "frequencies must be positive");
+    int W = (int)h->cfg.sweep_workers;
+    if (W == 0) {  // autotuned once per handle, on long sweeps only
+      if (h->tuned_workers == 0 && nf >= 16) {
+        std::vector<double> sorted(freqs, freqs + nf);
+        std::sort(sorted.begin(), sorted.end());
+        autotune(h, sorted[nf / 2], nrhs);
+      }
+      W = h->tuned_workers > 0 ? (int)h->tuned_workers : 1;
     }
-    sync(h);
+    // interleave cheap and expensive frequencies over the workers
+    std::vector<int64_t> idx(nf);
+    for (int64_t i = 0; i < nf; i++) idx[i] = i;
+    run_sweep(h, W, freqs, idx.data(), nf, g, nrhs, p, info, worst);
   });
   return st != BEM_OK ? st : worst;
 }

@@ -10,6 +10,9 @@
 // writes both matrices. Regular pairs (16-point rule) and special pairs
 // (i == j singular rule, near-singular split-polar rule) run in separate
 // kernels so every warp follows one rule.
+#include <mutex>
+#include <set>
+
 #include "bem_kernels.h"
 #include "quadrature.cuh"
 
@@ -17,8 +20,17 @@ namespace bemgpu {
 
 static __constant__ QuadRules c_rules;
 
+// The tables (always the same) go to each device's constant memory once,
+// synchronously, so no later handle rewrites them under running kernels.
 void nearfield_upload_rules(const QuadRules& r, cudaStream_t s) {
-  cudaMemcpyToSymbolAsync(c_rules, &r, sizeof(QuadRules), 0, cudaMemcpyHostToDevice, s);
+  (void)s;
+  static std::mutex mu;
+  static std::set<int> done;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  if (done.count(dev)) return;
+  if (cudaMemcpyToSymbol(c_rules, &r, sizeof(QuadRules)) == cudaSuccess) done.insert(dev);
 }
 
 __device__ __forceinline__ void store(double2* p, int64_t g, double2 v) { p[g] = v; }

@@ -23,6 +23,8 @@
 
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <set>
 #include <vector>
 
 #include "bem_kernels.h"
@@ -893,11 +895,21 @@ uint16_t host_bf16(float x) {
 
 }  // namespace
 
+// The rule tables go to each device's constant memory once (synchronously),
+// so that concurrent sweep workers never rewrite them under running kernels.
 void sel_upload_rules(cudaStream_t s) {
+  (void)s;
+  static std::mutex mu;
+  static std::set<int> done;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  if (done.count(dev)) return;
   static const SelRules R = build_rules();
   static const QuadRules Q = make_rules();
-  cudaMemcpyToSymbolAsync(c_sel, &R, sizeof(SelRules), 0, cudaMemcpyHostToDevice, s);
-  cudaMemcpyToSymbolAsync(c_rules, &Q, sizeof(QuadRules), 0, cudaMemcpyHostToDevice, s);
+  if (cudaMemcpyToSymbol(c_sel, &R, sizeof(SelRules)) == cudaSuccess &&
+      cudaMemcpyToSymbol(c_rules, &Q, sizeof(QuadRules)) == cudaSuccess)
+    done.insert(dev);
 }
 
 void launch_sel_label(const Elem* P, const Elem* Q, const double* k, int64_t n, double tol,

@@ -187,3 +187,23 @@ def random_patches(tri: np.ndarray, count: int, frac: float, seed: int) -> np.nd
         idx = np.argsort(((c - ctr) ** 2).sum(1))[:k]
         out[idx, r] = rng.uniform(-1.0, 1.0, k)
     return out
+
+
+def box_piston_rhs(tri: np.ndarray, lx=0.3, ly=0.2, lz=0.4, radius=0.05, patches=3,
+                   seed=20260103) -> np.ndarray:
+    """Driving velocities of the box sweep: column 0 is a circular piston of
+    the given radius centred on the z = lz face (unit velocity), columns
+    1..patches are seeded random-velocity patches on ~5 % of the elements."""
+    c = (tri[:, 0:3] + tri[:, 3:6] + tri[:, 6:9]) / 3.0
+    on_face = np.abs(c[:, 2] - lz) < 1e-9 * max(lx, ly, lz)
+    r = np.hypot(c[:, 0] - lx / 2, c[:, 1] - ly / 2)
+    g = np.zeros((tri.shape[0], 1 + patches), np.complex128)
+    g[on_face & (r <= radius), 0] = 1.0
+    if patches:
+        g[:, 1:] = random_patches(tri, patches, 0.05, seed)
+    return g
+
+
+def log_frequencies(count=64, f0=50.0, f1=2000.0) -> np.ndarray:
+    """count log-spaced frequencies from f0 to f1 (Hz)."""
+    return np.exp(np.linspace(np.log(f0), np.log(f1), count))

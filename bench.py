@@ -200,6 +200,45 @@ def time_matvec(torch, pkg, s, n, reps=50):
     return h0.elapsed_time(h1) / reps
 
 
+def box_sweep(pkg, meshes, torch):
+    """The batched sweep on the closed box with a piston: 5,120-triangle
+    surface, 64 log-spaced frequencies 50-2000 Hz x 4 right-hand sides (piston
+    + 3 random patches), mixed precision; sequential vs autotuned workers."""
+    tri = meshes.box(n_target=5120)
+    n = tri.shape[0]
+    g = meshes.box_piston_rhs(tri)
+    freqs = meshes.log_frequencies(64, 50.0, 2000.0)
+    out = {"workload": f"closed box 0.3x0.2x0.4 m, {n} triangles, piston r=0.05 m + 3 patches, "
+                       "64 log-spaced f 50-2000 Hz", "nrhs": int(g.shape[1]), "freqs": 64}
+    for name, workers in (("sequential", 1), ("batched", 0)):
+        s = pkg.Solver(aca_tol=ACA_TOL, gmres_tol=GMRES_TOL, wave_speed=C0, density=RHO,
+                       precision=1, sweep_workers=workers)
+        s.set_mesh(tri)
+        s.set_bc(np.zeros(n), np.ones(n))
+        tune = None
+        if workers == 0:
+            t0 = time.perf_counter()
+            tune = s.autotune(float(freqs[32]), g.shape[1])
+            out["autotune_s"] = round(time.perf_counter() - t0, 3)
+        s.sweep(freqs[:2], g)  # warm-up (allocations)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        p, info = s.sweep(freqs, g)
+        dt = time.perf_counter() - t0
+        out[name] = {"freq_solves_per_s": round(64 / dt, 3), "seconds": round(dt, 3),
+                     "max_iterations": int(max(i["iterations"] for i in info)),
+                     "all_converged": bool(all(i["status"] == 0 for i in info))}
+        if tune:
+            out[name]["tuned"] = tune
+        if name == "sequential":
+            p_seq = p
+        else:
+            out["rel_diff_batched_vs_sequential"] = float(np.linalg.norm(p - p_seq)
+                                                          / np.linalg.norm(p_seq))
+        s.close()
+    return out
+
+
 def run_ours(args):
     import torch
     ws, rank, local = dist_env()
@@ -299,6 +338,8 @@ def run_ours(args):
     }
     if args.selector:
         line["selector_stats"] = s.sel_stats()
+    if not args.no_sweep and ws == 1:
+        line["box_sweep"] = box_sweep(pkg, meshes, torch)
     if not args.no_cpu_baseline and rank == 0 and ws == 1:
         line["cpu_baseline"] = cpu_baseline_sample(args)
     if rank == 0:
@@ -379,6 +420,8 @@ def main():
                     help="mixed arm: truncating SVD recompression tolerance after ACA (0: off)")
     ap.add_argument("--precond", action="store_true",
                     help="mixed arm: H-LU preconditioned GMRES (rank 2)")
+    ap.add_argument("--no-sweep", action="store_true",
+                    help="skip the batched box sweep (64 frequencies x 4 RHS)")
     ap.add_argument("--selector", action="store_true",
                     help="mixed arm: learned quadrature order per near-field pair")
     args = ap.parse_args()

@@ -64,6 +64,10 @@ typedef struct bem_config {
                               block to this relative error after assembly */
   double selector_guard;   /* pairs whose top class probability is below this
                               get the highest order (guard band) */
+  int64_t sweep_workers;   /* bem_sweep: frequencies solved concurrently, each
+                              worker on its own stream (0: autotuned) */
+  int64_t aca_big_mn;      /* ACA size bin: blocks with m + n >= this get the
+                              512-thread kernel (0: 512, or autotuned) */
 } bem_config;
 
 typedef struct bem_solve_info {
@@ -242,6 +246,13 @@ bem_status bem_solve(bem_handle* h, double freq, const double* g, int64_t nrhs, 
 /* Same with device pointers (inputs already resident in GPU memory). */
 bem_status bem_solve_device(bem_handle* h, double freq, const void* g, int64_t nrhs, void* phi,
                             void* dphi, void* p, bem_solve_info* info);
+
+/* Autotuner of the batched sweep at a probe frequency: times the ACA size
+ * bin thresholds 256 / 512 / 1024 on one assembly and sweeps of 1, 2, 3, 4
+ * concurrent workers; keeps the fastest of each in the handle. tuned (may be
+ * NULL) receives {workers, aca_big_mn}. No counterpart in the reference,
+ * whose frequency loop is serial (bemsolvercontroller.cpp:63-72). */
+bem_status bem_autotune(bem_handle* h, double freq, int64_t nrhs, int64_t* tuned);
 
 /* Frequency sweep (BemSolverController::run, bemsolvercontroller.cpp:49-109):
  * nf frequencies x nrhs right-hand sides; p is n x nrhs x nf (caller order).
