@@ -146,10 +146,11 @@ bem_status bem_hmatvec_device_ex(bem_handle* h, int32_t which, const void* x, vo
 
 /* Allocation-free variant of bem_hmatvec_device (no counterpart in the
  * reference). For callers that must not allocate GPU memory during the call:
- * code running while a CUDA stream is being captured into a graph, real-time
- * loops that forbid allocator calls, and hosts whose GPU memory is handed out
- * by an outside pool. x and y are device pointers the caller owns; the
- * per-block projections go to a fixed 32 MiB device array inside the library
+ * real-time loops whose latency budget forbids allocator calls (cudaMalloc
+ * can synchronise the device), and hosts whose GPU memory is handed out by an
+ * outside pool that the library must not bypass. x and y are device pointers
+ * the caller owns; the per-block projections go to a fixed 32 MiB device
+ * array inside the library
  * (2^21 complex-FP64 values: the matrix's total rank reservation times the
  * vectors per pass must fit, or the call returns BEM_EINVAL). The call never
  * calls cudaMalloc / cudaFree. Every call shares that array, so calls that

@@ -1,8 +1,8 @@
 """bem_hmatvec_noalloc: the H-matvec for callers that must not allocate GPU
-memory during the call (code recorded into a CUDA graph while a stream is
-being captured, real-time loops that forbid allocator calls, hosts whose GPU
-memory comes from an outside pool). It keeps its per-block projections in a
-fixed device array inside the library instead of a cudaMalloc'd buffer.
+memory during the call (real-time loops that forbid allocator calls, which can
+synchronise the device; hosts whose GPU memory comes from an outside pool). It
+keeps its per-block projections in a fixed device array inside the library
+instead of a cudaMalloc'd buffer.
 
 The test calls it through the C ABI twice in a row (the second call reuses the
 array the first one left behind) and compares each result with the
