@@ -336,8 +336,12 @@ __device__ void norm_increment(const FarBlock& fb, const T* U, const T* V, const
   __syncthreads();
 }
 
+// Occupancy over registers: the 128-thread kernel is capped at 64 registers
+// (8 CTAs per SM), the 512-thread one at 64 (2 CTAs per SM). Despite the
+// spills this causes, the ACA phase at 20,480 elements drops from 24.4 ms
+// (uncapped, 168 registers, 3 CTAs per SM) to 19.7 ms.
 template <int MODE, typename T, int NT>
-__global__ void __launch_bounds__(NT) aca_kernel(AcaArgs a) {
+__global__ void __launch_bounds__(NT, NT == 128 ? 8 : 2) aca_kernel(AcaArgs a) {
   __shared__ T coef[ACA_MAX_KCAP];
   using R = typename Cx<T>::R;
   __shared__ Red<R> red;

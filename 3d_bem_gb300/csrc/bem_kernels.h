@@ -110,6 +110,10 @@ struct HmvArgs {
   int accumulate;
   float2* xf;  // FP32 scratch copies of x (ldx x nrhs) and t (ldt x nrhs)
   float2* tf;  // for the FP32-arithmetic variant
+  // optional pass-V work list: items (far block, first row), 16 rows each,
+  // built from the block ranks; null = one CTA per far block
+  const int2* vwork;
+  int64_t nvwork;
 };
 
 void nearfield_upload_rules(const QuadRules& r, cudaStream_t s);

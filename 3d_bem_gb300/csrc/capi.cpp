@@ -82,6 +82,8 @@ struct DevHM {
   DBuf<unsigned char> F, U, V, S;
   DBuf<int32_t> rank, flags;
   std::vector<int32_t> h_rank, h_flags;
+  DBuf<int2> vwork;  // H-matvec pass-V work items (block, first row)
+  int64_t nvwork = 0;
   int prec = 0;
   bool assembled = false;
 };
@@ -296,6 +298,14 @@ void fetch_ranks(bem_handle* h, DevHM& m) {
     CK(cudaMemcpyAsync(m.h_rank.data(), m.rank.p, nf * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaMemcpyAsync(m.h_flags.data(), m.flags.p, nf * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
   }
+  sync(h);
+  // pass-V work items of the H-matvec: 16 rows of one block each, so the
+  // largest blocks spread over many CTAs
+  std::vector<int2> vw;
+  for (size_t i = 0; i < nf; i++)
+    for (int32_t l0 = 0; l0 < m.h_rank[i]; l0 += 16) vw.push_back(make_int2((int)i, l0));
+  m.vwork.upload(vw, h->stream);
+  m.nvwork = (int64_t)vw.size();
   sync(h);
   m.assembled = true;
   if (&m == &h->hm[1]) h->have_hlu = false;  // factors of the previous matrix
@@ -530,6 +540,8 @@ void hmatvec_dev(bem_handle* h, int which, const double2* x, double2* y, int64_t
     a.accumulate = acc;
     a.xf = h->dXf.p;
     a.tf = h->dTf.p;
+    a.vwork = m.vwork.p;
+    a.nvwork = m.nvwork;
     h->launches += launch_hmatvec(a, h->stream);
   }
 }

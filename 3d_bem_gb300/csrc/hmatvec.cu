@@ -25,6 +25,7 @@ namespace {
 
 constexpr int VT = 128;  // threads of a pass-V CTA
 constexpr int UT = 512;  // threads of a pass-U CTA (16 warps split a leaf's block list)
+constexpr int VROWS = 16;  // rows of V per pass-V work item (4 warps x 4 rows)
 
 template <typename T, bool F32> struct Acc;
 // FP64 accumulation
@@ -45,6 +46,24 @@ template <typename T> struct Acc<T, true> {
 };
 
 __device__ __forceinline__ float2 ld32(const float2* p) { return __ldg(p); }
+
+// The block and row range of a pass-V CTA: with a work list, item
+// (block, first row) covers up to VROWS rows of V, so the largest blocks are
+// spread over many CTAs; without one, a CTA takes a whole block.
+__device__ __forceinline__ void vrange(const int2* __restrict__ vwork,
+                                       const int32_t* __restrict__ rank, int& b, int& lbeg,
+                                       int& lend) {
+  if (vwork) {
+    const int2 wi = vwork[blockIdx.x];
+    b = wi.x;
+    lbeg = wi.y;
+    lend = min(wi.y + VROWS, rank[b]);
+  } else {
+    b = blockIdx.x;
+    lbeg = 0;
+    lend = rank[b];
+  }
+}
 __device__ __forceinline__ float2 tof(double2 v) { return make_float2((float)v.x, (float)v.y); }
 
 // t[r][soff + l] = s_l * sum_j V[l, j] x[c0 + j, r]
@@ -54,11 +73,13 @@ __global__ void __launch_bounds__(VT) hmv_vpass(const FarBlock* __restrict__ far
                                                 const T* __restrict__ Vp,
                                                 const T* __restrict__ Sp,
                                                 const double2* __restrict__ x, int64_t ldx,
-                                                double2* __restrict__ t, int64_t ldt) {
-  const FarBlock fb = far[blockIdx.x];
-  const int k = rank[blockIdx.x];
+                                                double2* __restrict__ t, int64_t ldt,
+                                                const int2* __restrict__ vwork) {
+  int bi, lbeg, lend;
+  vrange(vwork, rank, bi, lbeg, lend);
+  const FarBlock fb = far[bi];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int l = w; l < k; l += VT / 32) {
+  for (int l = lbeg + w; l < lend; l += VT / 32) {
     const T* Vl = Vp + fb.voff + (int64_t)l * fb.n;
     double ax[R], ay[R];
 #pragma unroll
@@ -217,15 +238,17 @@ __global__ void __launch_bounds__(VT) hmv32_vpass(const FarBlock* __restrict__ f
                                                   const float2* __restrict__ Vp,
                                                   const float2* __restrict__ Sp,
                                                   const float2* __restrict__ x, int64_t ldx,
-                                                  float2* __restrict__ t, int64_t ldt) {
-  const FarBlock fb = far[blockIdx.x];
-  const int k = rank[blockIdx.x];
+                                                  float2* __restrict__ t, int64_t ldt,
+                                                  const int2* __restrict__ vwork) {
+  int bi, lbeg, lend;
+  vrange(vwork, rank, bi, lbeg, lend);
+  const FarBlock fb = far[bi];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // each warp streams G rows of V at once (G independent loads in flight per
   // lane; short rows would otherwise leave one load per reduction chain)
   constexpr int G = 4;
-  for (int l0 = w * G; l0 < k; l0 += (VT / 32) * G) {
-    const int ng = min(G, k - l0);
+  for (int l0 = lbeg + w * G; l0 < lend; l0 += (VT / 32) * G) {
+    const int ng = min(G, lend - l0);
     const float2* V0 = Vp + fb.voff + (int64_t)l0 * fb.n;
     float fx[G][R], fy[G][R];
 #pragma unroll
@@ -361,10 +384,11 @@ __global__ void to_float_kernel(const double2* __restrict__ x, float2* __restric
 template <int R>
 void launch32_r(const HmvArgs& a, cudaStream_t s) {
   to_float_kernel<<<(unsigned)((a.ldx * R + 255) / 256), 256, 0, s>>>(a.x, a.xf, a.ldx * R);
-  if (a.nfar > 0)
-    hmv32_vpass<R><<<(unsigned)a.nfar, VT, 0, s>>>(a.far, a.rank, (const float2*)a.V,
-                                                   (const float2*)a.S, a.xf, a.ldx, a.tf,
-                                                   a.ldt);
+  const int64_t nv = a.vwork ? a.nvwork : a.nfar;
+  if (nv > 0)
+    hmv32_vpass<R><<<(unsigned)nv, VT, 0, s>>>(a.far, a.rank, (const float2*)a.V,
+                                               (const float2*)a.S, a.xf, a.ldx, a.tf, a.ldt,
+                                               a.vwork);
   if (a.nleaves > 0)
     hmv32_upass<R><<<(unsigned)a.nleaves, UT, 0, s>>>(
         a.leaves, a.list_off, a.list, a.far, a.rank, a.nearb, (const float2*)a.U,
@@ -386,9 +410,11 @@ void launch32(const HmvArgs& a, cudaStream_t s) {
 
 template <typename T, bool F32, int R>
 void launch_r(const HmvArgs& a, cudaStream_t s) {
-  if (a.nfar > 0)
-    hmv_vpass<T, F32, R><<<(unsigned)a.nfar, VT, 0, s>>>(a.far, a.rank, (const T*)a.V,
-                                                         (const T*)a.S, a.x, a.ldx, a.t, a.ldt);
+  const int64_t nv = a.vwork ? a.nvwork : a.nfar;
+  if (nv > 0)
+    hmv_vpass<T, F32, R><<<(unsigned)nv, VT, 0, s>>>(a.far, a.rank, (const T*)a.V,
+                                                     (const T*)a.S, a.x, a.ldx, a.t, a.ldt,
+                                                     a.vwork);
   if (a.nleaves > 0)
     hmv_upass<T, F32, R><<<(unsigned)a.nleaves, UT, 0, s>>>(
         a.leaves, a.list_off, a.list, a.far, a.rank, a.nearb, (const T*)a.U, (const T*)a.F, a.x,
@@ -475,11 +501,13 @@ __global__ void __launch_bounds__(VT) hmvdf_vpass(const FarBlock* __restrict__ f
                                                   const float2* __restrict__ Vp,
                                                   const float2* __restrict__ Sp,
                                                   const float4* __restrict__ x, int64_t ldx,
-                                                  float4* __restrict__ t, int64_t ldt) {
-  const FarBlock fb = far[blockIdx.x];
-  const int k = rank[blockIdx.x];
+                                                  float4* __restrict__ t, int64_t ldt,
+                                                  const int2* __restrict__ vwork) {
+  int bi, lbeg, lend;
+  vrange(vwork, rank, bi, lbeg, lend);
+  const FarBlock fb = far[bi];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int l = w; l < k; l += VT / 32) {
+  for (int l = lbeg + w; l < lend; l += VT / 32) {
     const float2* Vl = Vp + fb.voff + (int64_t)l * fb.n;
     CDF acc[R];
 #pragma unroll 2
@@ -571,9 +599,11 @@ void launchdf_r(const HmvArgs& a, cudaStream_t s) {
   float4* xd = (float4*)a.xf;
   float4* td = (float4*)a.tf;
   to_df_kernel<<<(unsigned)((a.ldx * R + 255) / 256), 256, 0, s>>>(a.x, xd, a.ldx * R);
-  if (a.nfar > 0)
-    hmvdf_vpass<R><<<(unsigned)a.nfar, VT, 0, s>>>(a.far, a.rank, (const float2*)a.V,
-                                                   (const float2*)a.S, xd, a.ldx, td, a.ldt);
+  const int64_t nv = a.vwork ? a.nvwork : a.nfar;
+  if (nv > 0)
+    hmvdf_vpass<R><<<(unsigned)nv, VT, 0, s>>>(a.far, a.rank, (const float2*)a.V,
+                                               (const float2*)a.S, xd, a.ldx, td, a.ldt,
+                                               a.vwork);
   if (a.nleaves > 0)
     hmvdf_upass<R><<<(unsigned)a.nleaves, UT, 0, s>>>(
         a.leaves, a.list_off, a.list, a.far, a.rank, a.nearb, (const float2*)a.U,
