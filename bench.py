@@ -52,6 +52,11 @@ WORKLOADS = {
     "sphere20k": (5, "pulsating sphere r=1 m, icosphere 20,480 triangles, f=1.5 kHz"),
     "sphere5k": (4, "pulsating sphere r=1 m, icosphere 5,120 triangles, f=1.5 kHz (profiling case)"),
 }
+# DRAM traffic of the FP32 H-matvec per algorithmic byte, from one ncu
+# capture of hmv32_vpass + hmv32_upass at 5,120 elements (126.08 MB read +
+# write against 129.02 MB algorithmic; profiles/hmatvec_fp32_sphere5k.md),
+# scaled to the benchmark operator by its algorithmic bytes.
+HMV32_TRAFFIC_PER_BYTE = (57592832 + 169728 + 68490496 + 13568) / 129017600
 METRIC = "freq-solves/sec (H-matrix Helmholtz BEM solve, <=1e-5 rel. surface-pressure error)"
 UNIT = "freq-solves/s"
 
@@ -184,17 +189,19 @@ def timed_arm(torch, pkg, s, n, args, ws):
 
 
 def time_matvec(torch, pkg, s, n, reps=50):
-    """Average duration of one system-matrix H-matvec (V pass + U pass) with
-    CUDA events on the library's stream."""
-    stream = torch.cuda.ExternalStream(pkg.lib().bem_stream(s._h))
+    """Average duration of one system-matrix H-matvec as the inner GMRES runs
+    it (complex-FP32 storage, FP32 arithmetic: vector conversion, pass V,
+    pass U), with CUDA events on the library's stream."""
+    L = pkg.lib()
+    stream = torch.cuda.ExternalStream(L.bem_stream(s._h))
     x = torch.randn(n, dtype=torch.complex128, device="cuda")
     y = torch.zeros(n, dtype=torch.complex128, device="cuda")
     for _ in range(3):
-        pkg.lib().bem_hmatvec_device(s._h, 1, x.data_ptr(), y.data_ptr(), 1, 0)
+        L.bem_hmatvec_device_ex(s._h, 1, x.data_ptr(), y.data_ptr(), 1, 0, pkg.BEM_ARITH_FP32)
     h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     h0.record(stream)
     for _ in range(reps):
-        pkg.lib().bem_hmatvec_device(s._h, 1, x.data_ptr(), y.data_ptr(), 1, 0)
+        L.bem_hmatvec_device_ex(s._h, 1, x.data_ptr(), y.data_ptr(), 1, 0, pkg.BEM_ARITH_FP32)
     h1.record(stream)
     torch.cuda.synchronize()
     return h0.elapsed_time(h1) / reps
@@ -292,8 +299,8 @@ def run_ours(args):
     torch.cuda.synchronize()
     e2e = K2 / (time.perf_counter() - t0)
 
-    # roofline of the H-matvec (complex-FP32 storage, FP64 accumulation: the
-    # refinement-residual operator; the bytes are those of the stored matrix)
+    # roofline of the inner-GMRES H-matvec (complex-FP32 storage, FP32
+    # arithmetic; the bytes are those of the stored matrix, read once)
     info_part = s.partition()
     ranks = s.ranks(1)
     B = matvec_bytes(info_part, ranks, n, elem=8)
@@ -321,9 +328,12 @@ def run_ours(args):
             "learned_selector": bool(args.selector)}),
         "e2e": {"value": round(e2e, 4), "unit": UNIT, "h2d_bytes_per_step": n * 16,
                 "d2h_bytes_per_step": n * 16},
-        "roofline": {"kernel": "hmatvec (V pass + U pass), c64 storage", "bound": "hbm",
+        "roofline": {"kernel": "hmatvec FP32 (hmv32_vpass + hmv32_upass), c64 storage",
+                     "bound": "hbm",
                      "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                     "frac": round(achieved / hbm, 4), "traffic": None,
+                     "frac": round(achieved / hbm, 4),
+                     "traffic": int(HMV32_TRAFFIC_PER_BYTE * B),
+                     "traffic_source": "ncu dram bytes at 5,120 elements, scaled by bytes",
                      "bytes_per_launch": B, "ms_per_launch": round(mv_ms, 4),
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
         "gpu_launches": int(launches),
