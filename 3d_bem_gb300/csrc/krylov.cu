@@ -53,19 +53,31 @@ __global__ void __launch_bounds__(DT) dot_partial_kernel(const double2* __restri
   }
 }
 
-// h[r][q] = sum over CTAs (fixed order); H column j += h (first pass sets it)
+// h[r][q] = sum over CTAs; H column j += h (first pass sets it). One warp
+// per (r, q): lane l sums the partials l, l + 32, ... in order, then a fixed
+// shuffle tree, so the result does not depend on scheduling.
 __global__ void dot_reduce_kernel(const double2* __restrict__ partial, int nct, int R, int nq,
                                   int m, int j, int first, const GmresState* __restrict__ st,
                                   double2* __restrict__ h, double2* __restrict__ H) {
-  const int task = blockIdx.x * blockDim.x + threadIdx.x;
+  const int task = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
   if (task >= R * nq) return;
   const int r = task / nq, q = task % nq;
   if (st[r].done) return;
-  double2 s = make_double2(0, 0);
-  for (int c = 0; c < nct; c++) s = cadd(s, partial[((int64_t)c * R + r) * nq + q]);
-  h[r * nq + q] = s;
-  double2* Hc = H + ((int64_t)r * m + j) * (m + 1);
-  Hc[q] = first ? s : cadd(Hc[q], s);
+  double sx = 0, sy = 0;
+  for (int c = lane; c < nct; c += 32) {
+    const double2 v = partial[((int64_t)c * R + r) * nq + q];
+    sx += v.x;
+    sy += v.y;
+  }
+  sx = warp_sum(sx);
+  sy = warp_sum(sy);
+  if (lane == 0) {
+    const double2 s = make_double2(sx, sy);
+    h[r * nq + q] = s;
+    double2* Hc = H + ((int64_t)r * m + j) * (m + 1);
+    Hc[q] = first ? s : cadd(Hc[q], s);
+  }
 }
 
 // w[r][i] -= sum_q h[r][q] V[q][r][i]
@@ -115,12 +127,16 @@ __global__ void finish_step_kernel(const double* __restrict__ partial, int nct, 
                                    double2* __restrict__ H, double2* __restrict__ g,
                                    double2* __restrict__ cs, double2* __restrict__ sn,
                                    double* __restrict__ hnorm) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  // one warp per right-hand side: the lanes sum the CTA partials (fixed
+  // order per lane, fixed shuffle tree), lane 0 applies the rotations
+  const int r = blockIdx.x, lane = threadIdx.x;
   if (r >= R) return;
   GmresState s = st[r];
   if (s.done) return;
   double n2 = 0;
-  for (int c = 0; c < nct; c++) n2 += partial[(int64_t)c * R + r];
+  for (int c = lane; c < nct; c += 32) n2 += partial[(int64_t)c * R + r];
+  n2 = warp_sum(n2);
+  if (lane != 0) return;
   const double hn = sqrt(n2);
   hnorm[r] = hn;
   double2* Hc = H + ((int64_t)r * m + j) * (m + 1);
@@ -224,10 +240,12 @@ __global__ void __launch_bounds__(DT) residual_kernel(const double2* __restrict_
 __global__ void restart_kernel(const double* __restrict__ partial, int nct, int R, int m,
                                double tol, int init, GmresState* __restrict__ st,
                                double2* __restrict__ g, double* __restrict__ hnorm) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.x, lane = threadIdx.x;  // one warp per right-hand side
   if (r >= R) return;
   double n2 = 0;
-  for (int c = 0; c < nct; c++) n2 += partial[(int64_t)c * R + r];
+  for (int c = lane; c < nct; c += 32) n2 += partial[(int64_t)c * R + r];
+  n2 = warp_sum(n2);
+  if (lane != 0) return;
   double beta = sqrt(n2);
   GmresState s = st[r];
   if (init) {
@@ -273,14 +291,14 @@ void krylov_orthogonalize(const KrylovArgs& a, int j, cudaStream_t s) {
   for (int pass = 0; pass < 2; pass++) {
     dot_partial_kernel<<<nct, DT, 0, s>>>(a.Vb, a.w, a.N, a.R, nq, chunk, a.st, a.cpart);
     int tasks = a.R * nq;
-    dot_reduce_kernel<<<(tasks + 127) / 128, 128, 0, s>>>(a.cpart, nct, a.R, nq, a.m, j,
-                                                          pass == 0, a.st, a.h, a.H);
+    dot_reduce_kernel<<<(tasks + 3) / 4, 128, 0, s>>>(a.cpart, nct, a.R, nq, a.m, j, pass == 0,
+                                                      a.st, a.h, a.H);
     dim3 g((unsigned)((a.N + DT - 1) / DT), (unsigned)a.R);
     axpy_kernel<<<g, DT, 0, s>>>(a.Vb, a.w, a.N, a.R, nq, a.h, a.st);
   }
   nrm_partial_kernel<<<nct, DT, 0, s>>>(a.w, a.N, a.R, chunk, a.npart);
-  finish_step_kernel<<<(a.R + 31) / 32, 32, 0, s>>>(a.npart, nct, a.R, a.m, j, a.tol, a.st, a.H,
-                                                   a.g, a.cs, a.sn, a.hnorm);
+  finish_step_kernel<<<a.R, 32, 0, s>>>(a.npart, nct, a.R, a.m, j, a.tol, a.st, a.H, a.g, a.cs,
+                                        a.sn, a.hnorm);
   dim3 g((unsigned)((a.N + DT - 1) / DT), (unsigned)a.R);
   scale_kernel<<<g, DT, 0, s>>>(a.w, a.Vb + (int64_t)(j + 1) * a.R * a.N, a.N, a.hnorm, a.st, j);
 }
@@ -290,8 +308,7 @@ void krylov_restart(const KrylovArgs& a, int init, cudaStream_t s) {
   const int nct = krylov_num_ctas(a.N);
   const int64_t chunk = (a.N + nct - 1) / nct;
   nrm_partial_kernel<<<nct, DT, 0, s>>>(a.w, a.N, a.R, chunk, a.npart);
-  restart_kernel<<<(a.R + 31) / 32, 32, 0, s>>>(a.npart, nct, a.R, a.m, a.tol, init, a.st, a.g,
-                                               a.hnorm);
+  restart_kernel<<<a.R, 32, 0, s>>>(a.npart, nct, a.R, a.m, a.tol, init, a.st, a.g, a.hnorm);
   if (!init) {
     dim3 g((unsigned)((a.N + DT - 1) / DT), (unsigned)a.R);
     copy_scale_kernel<<<g, DT, 0, s>>>(a.w, a.Vb, a.N, a.hnorm);
