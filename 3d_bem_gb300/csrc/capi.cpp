@@ -155,7 +155,9 @@ struct bem_handle {
   FlatFactor hL, hU;
   DBuf<int32_t> dLs, dUs;
   DBuf<int64_t> dLl, dUl;
-  DBuf<double2> dLd, dUd, dP1, dP2;
+  DBuf<unsigned char> dLd, dUd;  // factor data, complex FP64 or FP32 (hlu_prec)
+  int hlu_prec = 0;
+  DBuf<double2> dP1, dP2;
   DBuf<int> dBad;
   QuadRules rules{};
   cudaEvent_t ev[10]{};
@@ -689,12 +691,26 @@ bool build_hlu(bem_handle* h) {
       require((op >= 0 ? op : -(int64_t)op - 1) < f->nleaves(), BEM_EINVAL,
               "H-LU schedule out of range");
   }
-  auto up = [&](const FlatFactor& f, DBuf<int32_t>& ds, DBuf<int64_t>& dl, DBuf<double2>& dd) {
+  // the factors are applied in the system matrix's storage precision
+  h->hlu_prec = m.prec;
+  auto up = [&](const FlatFactor& f, DBuf<int32_t>& ds, DBuf<int64_t>& dl,
+                DBuf<unsigned char>& dd) {
     ds.upload(f.schedule, s);
     dl.upload(f.leaves, s);
-    dd.ensure(f.data.size());
-    if (!f.data.empty())
-      CK(cudaMemcpyAsync(dd.p, f.data.data(), f.data.size() * sizeof(double2), cudaMemcpyHostToDevice, s));
+    if (h->hlu_prec == 0) {
+      dd.ensure(f.data.size() * sizeof(double2));
+      if (!f.data.empty())
+        CK(cudaMemcpyAsync(dd.p, f.data.data(), f.data.size() * sizeof(double2),
+                           cudaMemcpyHostToDevice, s));
+    } else {
+      std::vector<float2> fd(f.data.size());
+      for (size_t i = 0; i < fd.size(); i++)
+        fd[i] = make_float2((float)f.data[i].real(), (float)f.data[i].imag());
+      dd.ensure(fd.size() * sizeof(float2));
+      if (!fd.empty())
+        CK(cudaMemcpyAsync(dd.p, fd.data(), fd.size() * sizeof(float2), cudaMemcpyHostToDevice, s));
+      CK(cudaStreamSynchronize(s));  // fd goes out of scope
+    }
   };
   up(h->hL, h->dLs, h->dLl, h->dLd);
   up(h->hU, h->dUs, h->dUl, h->dUd);
@@ -711,9 +727,9 @@ void apply_precond(bem_handle* h, double2* w, int R) {
   h->dP1.ensure((size_t)R * N);
   h->dP2.ensure((size_t)R * N);
   CK(cudaMemcpyAsync(h->dP1.p, w, (size_t)R * N * sizeof(double2), cudaMemcpyDeviceToDevice, s));
-  h->launches += launch_hlu_sweep(h->dLs.p, (int)h->hL.schedule.size(), h->dLl.p, h->dLd.p,
+  h->launches += launch_hlu_sweep(h->dLs.p, (int)h->hL.schedule.size(), h->dLl.p, h->dLd.p, h->hlu_prec,
                                   h->dP1.p, h->dP2.p, N, R, 0, s);
-  h->launches += launch_hlu_sweep(h->dUs.p, (int)h->hU.schedule.size(), h->dUl.p, h->dUd.p,
+  h->launches += launch_hlu_sweep(h->dUs.p, (int)h->hU.schedule.size(), h->dUl.p, h->dUd.p, h->hlu_prec,
                                   h->dP2.p, w, N, R, 1, s);
 }
 

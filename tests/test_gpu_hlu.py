@@ -136,3 +136,21 @@ def test_facade_preconditioner(bem, meshes):
         sol.calculateBoundarySolution()
         out.append(be.phiSolution)
     assert rel(out[1], out[0]) < 1e-6
+
+
+def test_hlu_solve_fp32_factors_vs_oracle(bem, meshes, orc):
+    """Mixed precision stores the factors in complex FP32 and sweeps in FP32
+    arithmetic: the result is the oracle's FP64 solve with the same factors
+    to FP32 accuracy."""
+    tri, s = setup(bem, meshes, 3, precision=1, precond_rank=2)
+    n = tri.shape[0]
+    s.assemble(FREQ)
+    s.hlu_build()
+    Ll, Ld, _ = s.hlu_export(0)
+    Ul, Ud, _ = s.hlu_export(1)
+    rng = np.random.default_rng(9)
+    B = rng.standard_normal((n, 2)) + 1j * rng.standard_normal((n, 2))
+    X = s.hlu_solve(B)
+    for q in range(2):
+        x = orc.upper_solve(n, Ul, Ud, orc.lower_solve(n, Ll, Ld, B[:, q]))
+        assert rel(X[:, q], x) < 1e-4, q
