@@ -40,6 +40,7 @@ EXPORTS = [
     "bem_hlu_build", "bem_hlu_solve", "bem_hlu_export", "bem_recompress",
     "bem_sel_nparam", "bem_sel_label", "bem_mlp_grad", "bem_mlp_adam", "bem_mlp_forward",
     "bem_sel_infer", "bem_set_selector", "bem_sel_stats", "bem_sel_classes", "bem_autotune",
+    "bem_set_aca_rules",
 ]
 BEM_ARITH_FP64, BEM_ARITH_FP32, BEM_ARITH_TWOFLOAT = 0, 1, 2
 
@@ -126,7 +127,7 @@ def lib():
     L.bem_recompress.argtypes = [vp, i32, i64, dbl]
     L.bem_sel_nparam.argtypes = []
     L.bem_sel_nparam.restype = i64
-    L.bem_sel_label.argtypes = [vp, vp, vp, i64, dbl, dbl, vp, vp, vp]
+    L.bem_sel_label.argtypes = [vp, vp, vp, i64, dbl, dbl, dbl, vp, vp, vp]
     L.bem_mlp_grad.argtypes = [vp, vp, vp, i64, vp, vp, vp, vp]
     L.bem_mlp_adam.argtypes = [vp, vp, vp, vp, i64, ct.c_float, ct.c_float, ct.c_float,
                                ct.c_float, vp]
@@ -136,6 +137,7 @@ def lib():
     L.bem_sel_stats.argtypes = [vp, vp]
     L.bem_sel_classes.argtypes = [vp, vp]
     L.bem_autotune.argtypes = [vp, dbl, i64, vp]
+    L.bem_set_aca_rules.argtypes = [vp, vp, vp]
     L.bem_hlu_build.argtypes = [vp]
     L.bem_hlu_solve.argtypes = [vp, vp, vp, i64]
     L.bem_hlu_export.argtypes = [vp, i32, P(i64), vp, P(i64), vp, P(i64), vp]
@@ -203,7 +205,7 @@ def _status(st, what):
         raise BemError(st, what)
 
 
-def sel_label(ptri, qtri, k, tol=1e-7, near_ratio=1.0, want_err=False):
+def sel_label(ptri, qtri, k, tol=1e-7, near_ratio=1.0, want_err=False, floor_rel=1e-3):
     """Features (n x 24), labels (n) and optionally the per-rule errors (n x 6)
     of n pairs, computed on the GPU (bem_sel_label)."""
     ptri = np.ascontiguousarray(ptri, np.float64).reshape(-1, 9)
@@ -213,7 +215,7 @@ def sel_label(ptri, qtri, k, tol=1e-7, near_ratio=1.0, want_err=False):
     feat = np.zeros((n, SEL_NFEAT), np.float32)
     lab = np.zeros(n, np.uint8)
     err = np.zeros((n, 6), np.float32) if want_err else None
-    _status(lib().bem_sel_label(_ptr(ptri), _ptr(qtri), _ptr(k), n, tol, near_ratio,
+    _status(lib().bem_sel_label(_ptr(ptri), _ptr(qtri), _ptr(k), n, tol, near_ratio, floor_rel,
                                 _ptr(feat), _ptr(lab), _ptr(err)), "bem_sel_label")
     return (feat, lab, err) if want_err else (feat, lab)
 
@@ -302,6 +304,11 @@ class Solver:
         sg = np.ascontiguousarray(w["sigma"], np.float32)
         self._check(lib().bem_set_selector(self._h, _ptr(prm), _ptr(mu), _ptr(sg)),
                     "bem_set_selector")
+        if "aca_table" in w:
+            tab = np.ascontiguousarray(w["aca_table"], np.uint8)
+            axes = np.ascontiguousarray(w["aca_axes"], np.float32)
+            self._check(lib().bem_set_aca_rules(self._h, _ptr(tab), _ptr(axes)),
+                        "bem_set_aca_rules")
 
     def sel_stats(self) -> dict:
         st = np.zeros(4, np.int64)

@@ -23,10 +23,18 @@
 
 #include "bem_kernels.h"
 #include "quadrature.cuh"
+#include "selector.h"
 
 namespace bemgpu {
 
 static __constant__ QuadRules c_rules;
+
+// class rules of the learned rule table (1, 3, 7, 13, 25 points)
+struct AcaClassRules {
+  float x1[SEL_CLASS_POINTS], x2[SEL_CLASS_POINTS], w[SEL_CLASS_POINTS];
+  int off[SEL_C + 1];
+};
+static __constant__ AcaClassRules c_cls;
 
 // The tables (always the same) go to each device's constant memory once,
 // synchronously, so no later handle rewrites them under running kernels.
@@ -38,7 +46,11 @@ void aca_upload_rules(const QuadRules& r, cudaStream_t s) {
   cudaGetDevice(&dev);
   std::lock_guard<std::mutex> lock(mu);
   if (done.count(dev)) return;
-  if (cudaMemcpyToSymbol(c_rules, &r, sizeof(QuadRules)) == cudaSuccess) done.insert(dev);
+  AcaClassRules cr;
+  sel_class_rule_tables(cr.x1, cr.x2, cr.w, cr.off);
+  if (cudaMemcpyToSymbol(c_rules, &r, sizeof(QuadRules)) == cudaSuccess &&
+      cudaMemcpyToSymbol(c_cls, &cr, sizeof(AcaClassRules)) == cudaSuccess)
+    done.insert(dev);
 }
 
 namespace {
@@ -171,7 +183,21 @@ __device__ __forceinline__ T aca_entry(const AcaArgs& a, int64_t row, int64_t co
     if constexpr (sizeof(T) == sizeof(float2)) {
       // mixed precision: FP32 regular rule, FP64 singular / near-singular
       if (row != col && !near_pair32(a.EF, row, col, a.near_r2f)) {
-        OpsF o = ops_regular32(a.EF, row, col, a.kf, c_rules);
+        OpsF o;
+        if (a.rule_tab) {  // learned order: table bin of (d / e_max, k e_max)
+          float dx, dy, dz;
+          centroid_diff(a.EF[row], a.EF[col], dx, dy, dz);
+          const float em = a.EF[col].emax;
+          const float x = __logf(sqrtf(dx * dx + dy * dy + dz * dz) / em);
+          const float y = __logf(a.kf * em);
+          const int ix = min(max((int)floorf((x - a.tab_x0) / a.tab_dx), 0), ACA_TAB_N - 1);
+          const int iy = min(max((int)floorf((y - a.tab_y0) / a.tab_dy), 0), ACA_TAB_N - 1);
+          const int c = min((int)a.rule_tab[ix * ACA_TAB_N + iy], SEL_C - 1);
+          o = ops_rule32_pts(a.EF, row, col, a.kf, c_cls.off[c], c_cls.off[c + 1], c_cls.x1,
+                             c_cls.x2, c_cls.w);
+        } else {
+          o = ops_regular32(a.EF, row, col, a.kf, c_rules);
+        }
         float2 p, d;
         substitute32(o, a.bc[col], a.alphaf, p, d);
         return a.which ? d : p;

@@ -82,7 +82,13 @@ struct AcaArgs {
   const int64_t* piv_off;
   const int32_t* piv_cnt;
   const int32_t* piv_rc;
+  // learned rule table of the FP32 regular entries (null: the 16-point rule):
+  // class (1/3/7/13/25 points) by x = log(d / e_max), y = log(k e_max) bins
+  const uint8_t* rule_tab;
+  float tab_x0, tab_dx, tab_y0, tab_dy;
 };
+
+constexpr int ACA_TAB_N = 12;  // rule-table bins per axis
 
 struct HmvArgs {
   int precision;  // 0: double2 storage, 1: float2 storage

@@ -30,7 +30,7 @@ struct __align__(16) ElemF {
   float area;
   float c_hi[3];
   float c_lo[3];
-  float pad[1];
+  float emax;    // longest edge (rule-table lookup of ACA entries)
 };
 
 // Rule tables: 16-point triangle rule (order 8), 5-point Gauss-Legendre

@@ -144,6 +144,9 @@ struct bem_handle {
   // H-LU preconditioner: host factors and their device copies
   // learned quadrature-order selector (device blob, per-entry classes, counters)
   DBuf<SelBlob> dSel;
+  DBuf<uint8_t> dAcaTab;  // learned rule table of the ACA entries
+  float aca_axes[4] = {0, 0, 0, 0};
+  bool have_aca_tab = false;
   bool have_selector = false;
   DBuf<uint8_t> dCls;
   DBuf<unsigned long long> dSelCnt;
@@ -260,6 +263,15 @@ std::vector<ElemF> make_elemf(const std::vector<Elem>& E) {
       f.c_lo[d] = (float)(e.c[d] - (double)f.c_hi[d]);
     }
     f.area = (float)e.area;
+    double emax = 0;
+    const double* V[3] = {e.n1, e.n2, e.n3};
+    for (int q = 0; q < 3; q++) {
+      const double* A = V[q];
+      const double* B = V[(q + 1) % 3];
+      emax = std::max(emax, std::sqrt((B[0] - A[0]) * (B[0] - A[0]) + (B[1] - A[1]) * (B[1] - A[1]) +
+                                      (B[2] - A[2]) * (B[2] - A[2])));
+    }
+    f.emax = (float)emax;
     F[i] = f;
   }
   return F;
@@ -345,6 +357,14 @@ AcaArgs aca_args(bem_handle* h, DevHM& m, int which, int extra) {
   a.piv_off = h->dPivOff.p;
   a.piv_cnt = h->dPivCnt.p;
   a.piv_rc = h->dPivRc.p;
+  if ((h->cfg.selector & 2) && m.prec == 1 && !h->points_mode) {
+    require(h->have_aca_tab, BEM_EINVAL, "ACA rule table not set (bem_set_aca_rules)");
+    a.rule_tab = h->dAcaTab.p;
+    a.tab_x0 = h->aca_axes[0];
+    a.tab_dx = h->aca_axes[1];
+    a.tab_y0 = h->aca_axes[2];
+    a.tab_dy = h->aca_axes[3];
+  }
   return a;
 }
 
@@ -436,7 +456,7 @@ void assemble(bem_handle* h, double freq, double* t_near, double* t_aca) {
   na.phi = h->hm[0].F.p;
   na.dphi = h->hm[1].F.p;
   CK(cudaEventRecord(h->ev[0], s));
-  const bool learned = h->cfg.selector && na.precision == 1;
+  const bool learned = (h->cfg.selector & 1) && na.precision == 1;
   if (learned) {
     require(h->have_selector, BEM_EINVAL, "selector weights not set (bem_set_selector)");
     h->dCls.ensure(h->L.near_entries);
@@ -990,6 +1010,13 @@ void clone_state(bem_handle* c, bem_handle* p) {
   c->a = p->a;
   c->b = p->b;
   c->have_bc = p->have_bc;
+  c->have_aca_tab = p->have_aca_tab;
+  if (p->have_aca_tab) {
+    c->dAcaTab.ensure(ACA_TAB_N * ACA_TAB_N);
+    CK(cudaMemcpyAsync(c->dAcaTab.p, p->dAcaTab.p, ACA_TAB_N * ACA_TAB_N, cudaMemcpyDeviceToDevice,
+                       c->stream));
+    for (int i = 0; i < 4; i++) c->aca_axes[i] = p->aca_axes[i];
+  }
   c->have_selector = false;
   if (p->have_selector) {
     c->dSel.ensure(1);
@@ -1377,12 +1404,13 @@ bem_status bem_hmatvec(bem_handle* h, int32_t which, const double* x, double* y,
 int64_t bem_sel_nparam(void) { return SEL_NPARAM; }
 
 bem_status bem_sel_label(const double* ptri, const double* qtri, const double* k, int64_t n,
-                         double tol, double near_ratio, float* feat, uint8_t* label,
-                         float* err) {
+                         double tol, double near_ratio, double floor_rel, float* feat,
+                         uint8_t* label, float* err) {
   return guarded(nullptr, [&] {
     require(n >= 0 && (n == 0 || (ptri && qtri && k && feat && label)), BEM_EINVAL,
             "bad arguments");
-    require(tol > 0 && near_ratio >= 0, BEM_EINVAL, "bad tolerance / near ratio");
+    require(tol > 0 && near_ratio >= 0 && floor_rel >= 0, BEM_EINVAL,
+            "bad tolerance / near ratio / error floor");
     const int64_t chunk = 1 << 18;
     DBuf<Elem> dP, dQ;
     DBuf<double> dk;
@@ -1406,7 +1434,8 @@ bem_status bem_sel_label(const double* ptri, const double* qtri, const double* k
       df.ensure(m * SEL_NF);
       dl.ensure(m);
       if (err) de.ensure(m * 6);
-      launch_sel_label(dP.p, dQ.p, dk.p, m, tol, near_ratio, df.p, dl.p, err ? de.p : nullptr, 0);
+      launch_sel_label(dP.p, dQ.p, dk.p, m, tol, near_ratio, floor_rel, df.p, dl.p,
+                       err ? de.p : nullptr, 0);
       CK(cudaGetLastError());
       CK(cudaMemcpy(feat + o * SEL_NF, df.p, m * SEL_NF * sizeof(float), cudaMemcpyDeviceToHost));
       CK(cudaMemcpy(label + o, dl.p, m, cudaMemcpyDeviceToHost));
@@ -1472,6 +1501,24 @@ bem_status bem_set_selector(bem_handle* h, const float* params, const float* mu,
     CK(cudaMemcpyAsync(h->dSel.p, &b, sizeof(SelBlob), cudaMemcpyHostToDevice, h->stream));
     sync(h);
     h->have_selector = true;
+    h->state_gen++;
+  });
+}
+
+bem_status bem_set_aca_rules(bem_handle* h, const uint8_t* table, const float* axes) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] {
+    require(table && axes, BEM_EINVAL, "bad arguments");
+    for (int i = 0; i < ACA_TAB_N * ACA_TAB_N; i++)
+      require(table[i] < SEL_C, BEM_EINVAL, "rule-table classes must be 0..4");
+    require(std::isfinite(axes[0]) && std::isfinite(axes[2]) && axes[1] > 0 && axes[3] > 0,
+            BEM_EINVAL, "bad rule-table axes");
+    h->dAcaTab.ensure(ACA_TAB_N * ACA_TAB_N);
+    CK(cudaMemcpyAsync(h->dAcaTab.p, table, ACA_TAB_N * ACA_TAB_N, cudaMemcpyHostToDevice,
+                       h->stream));
+    for (int i = 0; i < 4; i++) h->aca_axes[i] = axes[i];
+    sync(h);
+    h->have_aca_tab = true;
     h->state_gen++;
   });
 }

@@ -329,12 +329,13 @@ __device__ Ops ops_rule_sub(const Elem& P, const Elem& Q, double k, int rule, in
 
 __device__ __forceinline__ double cabs1(double2 a) { return sqrt(a.x * a.x + a.y * a.y); }
 
-// max over the four operators of |a - ref| / max(|ref|, 1e-3 max |ref|)
-__device__ double ops_err(const Ops& a, const Ops& r) {
+// max over the four operators of |a - ref| / max(|ref|, floor_rel max |ref|)
+// (floor_rel = 1: every operator measured against the pair's largest)
+__device__ double ops_err(const Ops& a, const Ops& r, double floor_rel) {
   const double2 av[4] = {a.L, a.M, a.Mt, a.N}, rv[4] = {r.L, r.M, r.Mt, r.N};
   double mx = 0;
   for (int i = 0; i < 4; i++) mx = fmax(mx, cabs1(rv[i]));
-  const double floor_ = fmax(1e-3 * mx, 1e-300);
+  const double floor_ = fmax(floor_rel * mx, 1e-300);
   double e = 0;
   for (int i = 0; i < 4; i++) e = fmax(e, cabs1(csub(av[i], rv[i])) / fmax(cabs1(rv[i]), floor_));
   return e;
@@ -344,6 +345,7 @@ __global__ void __launch_bounds__(128) sel_label_kernel(const Elem* __restrict__
                                                         const Elem* __restrict__ Q,
                                                         const double* __restrict__ kk, int64_t n,
                                                         double tol, double near_ratio,
+                                                        double floor_rel,
                                                         float* __restrict__ feat,
                                                         uint8_t* __restrict__ label,
                                                         float* __restrict__ err) {
@@ -360,14 +362,14 @@ __global__ void __launch_bounds__(128) sel_label_kernel(const Elem* __restrict__
                                        : ops_rule_sub(p, q, k, SEL_REF, dc < 3.0 * hq ? 8 : 4);
   int lab = SEL_C;
   for (int c = 0; c < SEL_C; c++) {
-    const double e = ops_err(ops_rule_sub(p, q, k, c, 1), ref);
+    const double e = ops_err(ops_rule_sub(p, q, k, c, 1), ref, floor_rel);
     if (err) err[i * 6 + c] = (float)e;
     if (lab == SEL_C && e <= tol) {
       lab = c;
       if (!err) break;
     }
   }
-  if (err) err[i * 6 + 5] = (float)ops_err(ops_rule_sub(p, q, k, SEL_PLAIN, 1), ref);
+  if (err) err[i * 6 + 5] = (float)ops_err(ops_rule_sub(p, q, k, SEL_PLAIN, 1), ref, floor_rel);
   label[i] = (uint8_t)lab;
 }
 
@@ -753,59 +755,6 @@ __global__ void __launch_bounds__(32 * IW) sel_near_classes_kernel(SelNearArgs a
 // ---------------- near-field entries with the selected rules ----------------
 constexpr int SEL_CLASS_PTS = 1 + 3 + 7 + 13 + 25;  // classes 0-4, stored first
 
-// rule points from a shared-memory copy of the class rules (divergent
-// classes within a warp then cost no constant-cache serialisation)
-__device__ __forceinline__ OpsF ops_rule32(const ElemF* __restrict__ EF, int64_t row, int64_t col,
-                                           float k, int b, int e, const float* rx1,
-                                           const float* rx2, const float* rw) {
-  float dx, dy, dz;
-  centroid_diff(EF[row], EF[col], dx, dy, dz);
-  const ElemF& Q = EF[col];
-  const float npx = EF[row].nrm[0], npy = EF[row].nrm[1], npz = EF[row].nrm[2];
-  const float nqx = Q.nrm[0], nqy = Q.nrm[1], nqz = Q.nrm[2];
-  const float upNq = npx * nqx + npy * nqy + npz * nqz;
-  const float inv4pi = 0.0795774715459476679f;
-  float Lx = 0, Ly = 0, Mx = 0, My = 0, Tx = 0, Ty = 0, Nx = 0, Ny = 0;
-  for (int i = b; i < e; i++) {
-    const float a1 = rx1[i], a2 = rx2[i], a3 = 1.0f - a2 - a1, w = rw[i];
-    const float rx = dx - (a1 * Q.v[0] + a2 * Q.v[3] + a3 * Q.v[6]);
-    const float ry = dy - (a1 * Q.v[1] + a2 * Q.v[4] + a3 * Q.v[7]);
-    const float rz = dz - (a1 * Q.v[2] + a2 * Q.v[5] + a3 * Q.v[8]);
-    const float rr = rx * rx + ry * ry + rz * rz;
-    const float ir = rsqrtf(rr);
-    const float r = rr * ir;
-    const float rnq = -(rx * nqx + ry * nqy + rz * nqz) * ir;
-    const float rnp = (rx * npx + ry * npy + rz * npz) * ir;
-    const float kr = k * r;
-    float s, c;
-    sincosf(kr, &s, &c);
-    const float g0 = ir * inv4pi;
-    const float Gx = c * g0, Gy = s * g0;
-    const float Grx = Gx * ir, Gry = Gy * ir;
-    const float dGx = -Grx - kr * Gry, dGy = -Gry + kr * Grx;
-    const float Grrx = Grx * ir, Grry = Gry * ir;
-    const float a2c = 2.0f - kr * kr, b2c = -2.0f * kr;
-    const float d2Gx = Grrx * a2c - Grry * b2c, d2Gy = Grrx * b2c + Grry * a2c;
-    Lx += w * Gx;
-    Ly += w * Gy;
-    const float wm = w * rnq, wt = w * rnp;
-    Mx += wm * dGx;
-    My += wm * dGy;
-    Tx += wt * dGx;
-    Ty += wt * dGy;
-    const float f1 = -(upNq + rnp * rnq) * ir, f2 = rnp * rnq;
-    Nx += w * (f1 * dGx + f2 * d2Gx);
-    Ny += w * (f1 * dGy + f2 * d2Gy);
-  }
-  const float A = Q.area;
-  OpsF o;
-  o.L = fmk(A * Lx, A * Ly);
-  o.M = fmk(A * Mx, A * My);
-  o.Mt = fmk(A * Tx, A * Ty);
-  o.N = fmk(A * Nx, A * Ny);
-  return o;
-}
-
 __device__ __forceinline__ float fabs2(float2 a) { return sqrtf(a.x * a.x + a.y * a.y); }
 
 // One CTA per near-field tile. The tile's regular entries are first grouped
@@ -849,13 +798,13 @@ __global__ void __launch_bounds__(256) sel_nearfield32_kernel(SelNearfieldArgs a
     const int64_t row = b.r0 + r, col = b.c0 + c;
     const int cls = min((int)a.cls[g], SEL_C - 1);
     float2 p, d;
-    substitute32(ops_rule32(a.EF, row, col, a.k, roff[cls], roff[cls + 1], rx1, rx2, rw),
+    substitute32(ops_rule32_pts(a.EF, row, col, a.k, roff[cls], roff[cls + 1], rx1, rx2, rw),
                  a.bc[col], a.alpha, p, d);
     pts = roff[cls + 1] - roff[cls];
     const uint32_t hsh = (uint32_t)((uint64_t)g * 2654435761ull >> 7);
     if (cls < SEL_C - 1 && a.check_every > 0 && hsh % (uint32_t)a.check_every == 0) {
       float2 p4, d4;
-      substitute32(ops_rule32(a.EF, row, col, a.k, roff[SEL_C - 1], roff[SEL_C], rx1, rx2, rw),
+      substitute32(ops_rule32_pts(a.EF, row, col, a.k, roff[SEL_C - 1], roff[SEL_C], rx1, rx2, rw),
                    a.bc[col], a.alpha, p4, d4);
       pts += roff[SEL_C] - roff[SEL_C - 1];
       chk = 1;
@@ -913,12 +862,12 @@ void sel_upload_rules(cudaStream_t s) {
 }
 
 void launch_sel_label(const Elem* P, const Elem* Q, const double* k, int64_t n, double tol,
-                      double near_ratio, float* feat, uint8_t* label, float* err,
-                      cudaStream_t s) {
+                      double near_ratio, double floor_rel, float* feat, uint8_t* label,
+                      float* err, cudaStream_t s) {
   if (n <= 0) return;
   sel_upload_rules(s);
-  sel_label_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(P, Q, k, n, tol, near_ratio, feat,
-                                                               label, err);
+  sel_label_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(P, Q, k, n, tol, near_ratio,
+                                                               floor_rel, feat, label, err);
 }
 
 void launch_mlp_grad(const float* params, const float* X, const uint8_t* y, int64_t B,
@@ -959,6 +908,17 @@ void launch_sel_nearfield32(const SelNearfieldArgs& a, cudaStream_t s) {
   if (a.ntiles <= 0) return;
   sel_upload_rules(s);
   sel_nearfield32_kernel<<<(unsigned)a.ntiles, 256, 0, s>>>(a);
+}
+
+void sel_class_rule_tables(float* x1, float* x2, float* w, int* off) {
+  static const SelRules R = build_rules();
+  for (int i = 0; i < SEL_CLASS_PTS; i++) {
+    x1[i] = R.fx1[i];
+    x2[i] = R.fx2[i];
+    w[i] = R.fw[i];
+  }
+  for (int c = 0; c < SEL_C; c++) off[c] = R.off[c];
+  off[SEL_C] = SEL_CLASS_PTS;
 }
 
 void sel_make_blob(const float* prm, const float* mu, const float* sigma, SelBlob& B) {

@@ -53,11 +53,12 @@ void sel_upload_rules(cudaStream_t s);
 // class whose rule reaches relative error tol against the reference (the
 // 64-point rule on a subdivision of Q, or the split-polar near-singular rule
 // when the centroid distance is below near_ratio * sqrt(area_Q)); 5 when
-// none does. err (may be null): npairs x 6 relative errors of the 5 classes
-// and the plain 16-point rule.
+// none does. The error of an operator is relative to max(|ref|, floor_rel
+// times the pair's largest operator). err (may be null): npairs x 6 relative
+// errors of the 5 classes and the plain 16-point rule.
 void launch_sel_label(const Elem* P, const Elem* Q, const double* k, int64_t n, double tol,
-                      double near_ratio, float* feat, uint8_t* label, float* err,
-                      cudaStream_t s);
+                      double near_ratio, double floor_rel, float* feat, uint8_t* label,
+                      float* err, cudaStream_t s);
 
 // FP32 training: forward + softmax cross-entropy, backward, parameter
 // gradients (deterministic: one thread per parameter, samples in order) and
@@ -111,6 +112,11 @@ struct SelNearfieldArgs {
   unsigned long long* counters;
 };
 void launch_sel_nearfield32(const SelNearfieldArgs& a, cudaStream_t s);
+
+// FP32 copies of the class rules (1, 3, 7, 13, 25 points, in this order,
+// 49 points) and their offsets (off[5] = 49), for other kernels' tables.
+constexpr int SEL_CLASS_POINTS = 49;
+void sel_class_rule_tables(float* x1, float* x2, float* w, int* off);
 
 // Convert flat FP32 parameters + normalisation into the device blob layout.
 void sel_make_blob(const float* params, const float* mu, const float* sigma, SelBlob& out);

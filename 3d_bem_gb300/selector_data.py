@@ -137,3 +137,34 @@ def pairs(n, seed=SEED, near_frac=2 / 3, max_patches=100000):
                                       axis=1))
     kh = np.exp(rng.uniform(np.log(0.01), np.log(1.5), len(dh)))
     return np.ascontiguousarray(Pt), np.ascontiguousarray(Qt), kh / hq, dh
+
+
+def far_pairs(n, seed=SEED + 1, dmin=2.0, dmax=200.0):
+    """n well-separated pairs for the rule table of ACA entries: a source
+    triangle Q from a jittered patch and a collocation triangle P from
+    another, translated so that the centroid distance over sqrt(area Q) is
+    log-uniform in [dmin, dmax], in a random direction; kh log-uniform in
+    [0.01, 1.5]. Returns (P n x 9, Q n x 9, k n, d/h n)."""
+    rng = np.random.default_rng(seed)
+    Ps, Qs = [], []
+    got = 0
+    while got < n:
+        A, B = patch(rng), patch(rng)
+        m = min(256, n - got)
+        ia = rng.integers(0, len(A), m)
+        ib = rng.integers(0, len(B), m)
+        Ps.append(A[ia])
+        Qs.append(B[ib])
+        got += m
+    P = np.concatenate(Ps)
+    Q = np.concatenate(Qs)
+    aq = 0.5 * np.linalg.norm(np.cross(Q[:, 1] - Q[:, 0], Q[:, 2] - Q[:, 0]), axis=1)
+    hq = np.sqrt(aq)
+    dh = np.exp(rng.uniform(np.log(dmin), np.log(dmax), n))
+    u = rng.standard_normal((n, 3))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    target = Q.mean(1) + u * (dh * hq)[:, None]
+    P = P + (target - P.mean(1))[:, None, :]
+    kh = np.exp(rng.uniform(np.log(0.01), np.log(1.5), n))
+    return (np.ascontiguousarray(P.reshape(-1, 9)), np.ascontiguousarray(Q.reshape(-1, 9)),
+            kh / hq, dh)

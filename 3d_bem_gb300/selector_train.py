@@ -90,6 +90,56 @@ def evaluate(pkg, params, mu, sigma, feat, lab, err, tol, guard):
     }
 
 
+# Rule table of the ACA entries (far pairs): class as a function of
+# x = log(d / e_max) and y = log(k e_max), d the centroid distance, e_max the
+# source triangle's longest edge.
+TAB_N = 12
+TAB_AXES = (np.log(0.25), (np.log(200.0) - np.log(0.25)) / TAB_N,
+            np.log(0.005), (np.log(15.0) - np.log(0.005)) / TAB_N)
+
+
+def table_coords(feat):
+    """Bin indices of pairs from their features (f0 = d/h, f8 = kh,
+    f13 = e_max/h)."""
+    x = np.log(feat[:, 0] / feat[:, 13])
+    y = np.log(feat[:, 8] * feat[:, 13])
+    x0, dx, y0, dy = TAB_AXES
+    ix = np.clip(np.floor((x - x0) / dx).astype(int), 0, TAB_N - 1)
+    iy = np.clip(np.floor((y - y0) / dy).astype(int), 0, TAB_N - 1)
+    return ix, iy
+
+
+def build_rule_table(feat, lab):
+    """Largest class needed by any training pair of a bin (label 5, no rule
+    reaches the tolerance, counts as the highest class), closed so that a bin
+    never needs less than a farther bin or one with smaller k e_max; bins
+    without pairs get the highest class."""
+    ix, iy = table_coords(feat)
+    need = np.minimum(lab, C - 1).astype(int)
+    tab = np.full((TAB_N, TAB_N), -1, int)
+    np.maximum.at(tab, (ix, iy), need)
+    for i in range(TAB_N - 2, -1, -1):  # nearer needs at least what farther needs
+        tab[i] = np.maximum(tab[i], tab[i + 1])
+    for j in range(1, TAB_N):  # larger k e_max needs at least what smaller needs
+        tab[:, j] = np.maximum(tab[:, j], tab[:, j - 1])
+    tab[tab < 0] = C - 1
+    return tab.astype(np.uint8)
+
+
+def eval_rule_table(tab, feat, lab, err, tol):
+    ix, iy = table_coords(feat)
+    cls = tab[ix, iy].astype(int)
+    ok = err[np.arange(len(cls)), cls] <= tol
+    reach = lab < C
+    return {"pairs": int(len(cls)),
+            "within_tol_table": float(np.mean(ok)),
+            "within_tol_plain16": float(np.mean(err[:, 5] <= tol)),
+            "achievable_within_tol_table": float(np.mean(ok[reach])) if reach.any() else 1.0,
+            "under_integrated": float(np.mean(cls < np.minimum(lab, C - 1))),
+            "mean_points_table": float(np.mean(POINTS[cls])),
+            "mean_points_plain": float(PLAIN_POINTS)}
+
+
 def train(pkg, X, y, *, epochs, batch, lr, seed, log=print):
     """FP32 training with the library kernels; X normalised (n x 24)."""
     import torch
@@ -143,6 +193,10 @@ def main(argv=None):
     ap.add_argument("--tol", type=float, default=1e-7)
     ap.add_argument("--guard", type=float, default=0.9)
     ap.add_argument("--seed", type=int, default=20260105)
+    ap.add_argument("--aca-pairs", type=int, default=1_000_000)
+    ap.add_argument("--aca-tol", type=float, default=1e-6)
+    ap.add_argument("--aca-floor", type=float, default=1.0,
+                    help="ACA labels: operator errors relative to the pair's largest")
     ap.add_argument("--out", default=os.path.join(os.path.dirname(os.path.abspath(__file__)),
                                                   "selector_weights.npz"))
     args = ap.parse_args(argv)
@@ -166,14 +220,27 @@ def main(argv=None):
     reg = dh[ntr:] >= 2.0
     ev_reg = evaluate(pkg, params, mu, sigma, feat[ntr:][reg], lab[ntr:][reg], err[ntr:][reg],
                       args.tol, args.guard)
+    # rule table of the ACA entries, from far pairs labelled at the ACA-level
+    # tolerance; evaluated on far pairs of another seed
+    Pf, Qf, kf, dhf = data.far_pairs(args.aca_pairs, seed=args.seed + 1)
+    ff, lf, ef = pkg.sel_label(Pf, Qf, kf, tol=args.aca_tol, want_err=True,
+                               floor_rel=args.aca_floor)
+    table = build_rule_table(ff, lf)
+    Pv, Qv, kv, dhv = data.far_pairs(200_000, seed=args.seed + 2)
+    fv, lv, ev_ = pkg.sel_label(Pv, Qv, kv, tol=args.aca_tol, want_err=True,
+                                floor_rel=args.aca_floor)
+    tab_eval = eval_rule_table(table, fv, lv, ev_, args.aca_tol)
     report = {"pairs": int(len(lab)), "train": ntr, "test": int(len(lab) - ntr),
+              "aca_table": table.tolist(), "aca_tol": args.aca_tol,
+              "aca_floor": args.aca_floor,
+              "aca_table_eval": tab_eval,
               "label_hist": np.bincount(lab, minlength=C + 1).tolist(), "tol": args.tol,
               "guard": args.guard, "epochs": args.epochs, "batch": args.batch,
               "loss_history": hist, "seconds": {"pairs": t1 - t0, "labels": t2 - t1,
                                                 "train": t3 - t2}, "test_metrics": ev,
               "test_metrics_regular_pairs": ev_reg}
-    np.savez(args.out, params=params, mu=mu, sigma=sigma,
-             report=np.array(json.dumps(report)))
+    np.savez(args.out, params=params, mu=mu, sigma=sigma, aca_table=table,
+             aca_axes=np.array(TAB_AXES, np.float32), report=np.array(json.dumps(report)))
     print(json.dumps(report))
 
 

@@ -15,7 +15,9 @@ larger than the 129 MB L2, so no explicit flush is needed.
 Two arms of the same method run on the GPU:
   mixed (headline) -- FP32 regular quadrature with FP64-formed centroid
       differences, FP64 singular/near-singular rules, complex-FP32 storage,
-      FP32-arithmetic inner GMRES inside FP64 iterative refinement;
+      FP32-arithmetic inner GMRES inside FP64 iterative refinement, and the
+      learned rule table for the ACA entries (--no-aca-rules: 16 points);
+      --selector adds the learned per-pair order of the near field;
   plain            -- complex FP64 throughout.
 The line reports the mixed arm; the plain arm's rate and the relative surface-
 pressure difference between the two ride along.
@@ -273,8 +275,9 @@ def run_ours(args):
         extra["recompress_tol"] = args.recompress
     if args.precond:
         extra.update(use_preconditioner=1, precond_rank=2)
-    if args.selector:
-        extra["selector"] = 1
+    learned = (1 if args.selector else 0) | (0 if args.no_aca_rules else 2)
+    if learned:
+        extra["selector"] = learned
     s, n = make_solver(pkg, meshes, sub, 1, **extra)
     clk = Clocks(local)
     clk.start()
@@ -325,7 +328,8 @@ def run_ours(args):
         "config": workload_config(args.workload, {
             "precision": "mixed", "parallelism": f"replicas{ws}" if ws > 1 else "single-gpu",
             "recompress_tol": args.recompress, "hlu_preconditioner": bool(args.precond),
-            "learned_selector": bool(args.selector)}),
+            "learned_selector": bool(args.selector),
+            "learned_aca_rules": not args.no_aca_rules}),
         "e2e": {"value": round(e2e, 4), "unit": UNIT, "h2d_bytes_per_step": n * 16,
                 "d2h_bytes_per_step": n * 16},
         "roofline": {"kernel": "hmatvec FP32 (hmv32_vpass + hmv32_upass), c64 storage",
@@ -434,6 +438,9 @@ def main():
                     help="skip the batched box sweep (64 frequencies x 4 RHS)")
     ap.add_argument("--selector", action="store_true",
                     help="mixed arm: learned quadrature order per near-field pair")
+    ap.add_argument("--no-aca-rules", action="store_true",
+                    help="mixed arm: the 16-point rule for the ACA entries instead of the "
+                         "learned rule table")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

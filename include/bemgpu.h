@@ -56,8 +56,10 @@ typedef struct bem_config {
   double density;          /* rho (p = i rho omega phi) */
   uint64_t seed;           /* seeds the ACA start columns / pivot members */
   int32_t use_preconditioner; /* usePreconditioner: H-LU left preconditioning */
-  int32_t selector;         /* 1: learned quadrature order per near-field pair
-                              (mixed precision; weights via bem_set_selector) */
+  int32_t selector;         /* learned quadrature orders (mixed precision):
+                              bit 0 (1): per near-field pair, the network
+                              (bem_set_selector); bit 1 (2): per ACA entry,
+                              the rule table (bem_set_aca_rules) */
   int64_t precond_rank;    /* preconditionerRank (ref default 2) */
   double precond_tol;      /* preconditionerRelError (ref default 0) */
   double recompress_tol;   /* > 0: truncating SVD recompression of every ACA
@@ -195,11 +197,14 @@ int64_t bem_sel_nparam(void); /* 6085: W1 24x64, b1, W2 64x64, b2, W3 64x5, b3 *
  * doubles each; wavenumber k) -> features (n x 24), label = cheapest class
  * whose L, M, Mt, N are within tol (relative) of the reference (the 64-point
  * product rule on a subdivision of Q; the split-polar near-singular rule when
- * the centroid distance is below near_ratio * sqrt(area Q)), 5 if none;
+ * the centroid distance is below near_ratio * sqrt(area Q)), 5 if none; an
+ * operator's error is relative to max(|its reference|, floor_rel times the
+ * pair's largest operator) (1e-3: per operator; 1: against the largest);
  * err (n x 6, may be NULL): relative errors of the 5 classes and of the
  * plain 16-point rule. Host buffers; runs on the current device. */
 bem_status bem_sel_label(const double* ptri, const double* qtri, const double* k, int64_t n,
-                         double tol, double near_ratio, float* feat, uint8_t* label, float* err);
+                         double tol, double near_ratio, double floor_rel, float* feat,
+                         uint8_t* label, float* err);
 /* FP32 training on device buffers: gradient of the mean softmax cross-entropy
  * (bitwise reproducible) with work = B * 265 floats; an Adam step; FP32
  * logits (B x 5). stream: cudaStream_t or NULL. */
@@ -218,6 +223,12 @@ bem_status bem_sel_infer(const float* params, const float* mu, const float* sigm
 /* Install trained weights in a handle (used when cfg.selector = 1). */
 bem_status bem_set_selector(bem_handle* h, const float* params, const float* mu,
                             const float* sigma);
+/* Rule table of the ACA entries (cfg.selector bit 1): 12 x 12 classes
+ * (0..4 = 1, 3, 7, 13, 25 points), row = bin of log(d / e_max), column = bin
+ * of log(k e_max), d the centroid distance, e_max the source's longest edge;
+ * axes = {x0, dx, y0, dy} of the bins. Fitted to labels of the same kind as
+ * the network's, at the ACA-level tolerance. */
+bem_status bem_set_aca_rules(bem_handle* h, const uint8_t* table, const float* axes);
 /* After an assembly with the selector: stats[0] quadrature points used,
  * [1] entries re-integrated by the check, [2] entries that fell back to the
  * highest order, [3] regular near-field entries. */

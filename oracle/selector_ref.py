@@ -91,9 +91,9 @@ def label_reference(ptri, qtri, k):
     return out
 
 
-def rel_err(o, ref):
+def rel_err(o, ref, floor=1e-3):
     mx = np.abs(ref).max(1, keepdims=True)
-    return (np.abs(o - ref) / np.maximum(np.abs(ref), 1e-3 * mx)).max(1)
+    return (np.abs(o - ref) / np.maximum(np.abs(ref), floor * mx)).max(1)
 
 
 def errors_and_labels(ptri, qtri, k, rules, tol, ref=None):

@@ -253,3 +253,45 @@ def test_mesh_classes_match_rows_inference(bem, meshes, torch):
                                    sg.ctypes.data_as(ct.c_void_p), ct.c_void_p(Fd.data_ptr()),
                                    len(k), None, ct.c_void_p(cr.data_ptr()), None) == 0
     assert np.mean(cls[reg] == cr.cpu().numpy()) > 0.99
+
+
+def test_aca_rule_table_gain(bem, sd, st):
+    """The committed rule table of the ACA entries on far pairs it never saw:
+    the chosen rule reaches the table's tolerance on (nearly) every pair, with
+    fewer points on average than the plain 16-point rule."""
+    w = bem.load_selector_weights()
+    rep = json_report(w)
+    tol, floor = float(rep["aca_tol"]), float(rep["aca_floor"])
+    P, Q, k, dh = sd.far_pairs(40000, seed=77)
+    feat, lab, err = bem.sel_label(P, Q, k, tol=tol, want_err=True, floor_rel=floor)
+    ev = st.eval_rule_table(w["aca_table"], feat, lab, err, tol)
+    assert ev["under_integrated"] < 0.002
+    assert ev["achievable_within_tol_table"] > 0.995
+    assert ev["mean_points_table"] < 16
+
+
+def json_report(w):
+    import json
+    return json.loads(str(w["report"]))
+
+
+@pytest.mark.parametrize("sub,freq", [(3, 500.0), (4, 1500.0)])
+def test_solve_with_aca_rule_table(bem, meshes, sub, freq):
+    tri = meshes.icosphere(sub, 1.0)
+    n = tri.shape[0]
+    out, ranks = {}, {}
+    for sel in (0, 2):
+        s = bem.Solver(aca_tol=1e-5, gmres_tol=1e-10, precision=1, selector=sel)
+        s.set_mesh(tri)
+        s.set_bc(np.zeros(n), np.ones(n))
+        phi, dphi, p, info = s.solve(freq, np.ones(n))
+        assert info["status"] == 0
+        out[sel] = p[:, 0]
+        adm = s.partition()[:, 4] == 1
+        ranks[sel] = s.ranks(1)[adm]
+    # cheaper rules only where they meet the ACA-level tolerance: two ACA
+    # approximations at 1e-5 of the same matrix (their pressures differ by a
+    # few 1e-6, within the 1e-5 target), ranks within +-2 (ACA's stopping
+    # test reacts to entry changes at the 1e-6 level)
+    assert rel(out[2], out[0]) < 1e-5
+    assert np.mean(np.abs(ranks[2] - ranks[0]) <= 2) > 0.97
