@@ -40,7 +40,7 @@ EXPORTS = [
     "bem_hlu_build", "bem_hlu_solve", "bem_hlu_export", "bem_recompress",
     "bem_sel_nparam", "bem_sel_label", "bem_mlp_grad", "bem_mlp_adam", "bem_mlp_forward",
     "bem_sel_infer", "bem_set_selector", "bem_sel_stats", "bem_sel_classes", "bem_autotune",
-    "bem_set_aca_rules",
+    "bem_set_aca_rules", "bem_set_bc_impedance",
 ]
 BEM_ARITH_FP64, BEM_ARITH_FP32, BEM_ARITH_TWOFLOAT = 0, 1, 2
 
@@ -138,6 +138,7 @@ def lib():
     L.bem_sel_classes.argtypes = [vp, vp]
     L.bem_autotune.argtypes = [vp, dbl, i64, vp]
     L.bem_set_aca_rules.argtypes = [vp, vp, vp]
+    L.bem_set_bc_impedance.argtypes = [vp, vp]
     L.bem_hlu_build.argtypes = [vp]
     L.bem_hlu_solve.argtypes = [vp, vp, vp, i64]
     L.bem_hlu_export.argtypes = [vp, i32, P(i64), vp, P(i64), vp, P(i64), vp]
@@ -267,6 +268,11 @@ class Solver:
         info = np.zeros((nb.value, 5), np.int64)
         self._check(lib().bem_get_partition(self._h, ct.byref(nb), _ptr(info)), "bem_get_partition")
         return info
+
+    def set_bc_impedance(self, beta):
+        """Impedance walls: a = i k beta (beta = rho c / Z per element), b = 1."""
+        beta = np.ascontiguousarray(np.asarray(beta, np.complex128).ravel())
+        self._check(lib().bem_set_bc_impedance(self._h, _ptr(beta)), "bem_set_bc_impedance")
 
     def set_bc(self, a, b):
         a = _c128(a)

@@ -130,6 +130,9 @@ struct bem_handle {
   DBuf<int64_t> dSpEntry, dPivOff, dPerm;
   DBuf<LeafRows> dLeaves;
   DBuf<double> dRowPts, dColPts;
+  // impedance walls (bem_set_bc_impedance): a = i k beta, b = 1
+  std::vector<cplx> beta;
+  bool impedance = false;
   // boundary conditions (cluster order)
   bool have_bc = false;
   std::vector<cplx> a, b;
@@ -283,7 +286,8 @@ void set_frequency(bem_handle* h, double k) {
   std::vector<BcCoef> bc(N);
   std::vector<double2> av(N), bv(N);
   for (int64_t i = 0; i < N; i++) {
-    const cplx a = h->a[i], b = h->b[i];
+    // impedance walls: a = i k beta (beta = rho c / Z), rescaled per frequency
+    const cplx a = h->impedance ? cplx(0.0, k) * h->beta[i] : h->a[i], b = h->b[i];
     BcCoef c{};
     c.subst = std::abs(a) < std::abs(b) ? 1 : 0;
     cplx inv = c.subst ? 1.0 / b : 1.0 / a;
@@ -1009,6 +1013,8 @@ void clone_state(bem_handle* c, bem_handle* p) {
   c->have_mesh = true;
   c->a = p->a;
   c->b = p->b;
+  c->beta = p->beta;
+  c->impedance = p->impedance;
   c->have_bc = p->have_bc;
   c->have_aca_tab = p->have_aca_tab;
   if (p->have_aca_tab) {
@@ -1346,6 +1352,29 @@ bem_status bem_set_bc(bem_handle* h, const double* a, const double* b) {
       h->a[i] = av;
       h->b[i] = bv;
     }
+    h->impedance = false;
+    h->have_bc = true;
+    h->state_gen++;
+  });
+}
+
+bem_status bem_set_bc_impedance(bem_handle* h, const double* beta) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] {
+    require(h->have_mesh && !h->points_mode, BEM_EINVAL, "mesh not set (bem_set_mesh)");
+    require(beta, BEM_EINVAL, "beta is required");
+    const int64_t N = h->N;
+    h->beta.resize(N);
+    h->a.assign(N, cplx(0.0, 0.0));
+    h->b.assign(N, cplx(1.0, 0.0));
+    for (int64_t i = 0; i < N; i++) {
+      const int64_t o = h->rows.perm[i];
+      const cplx bv(beta[2 * o], beta[2 * o + 1]);
+      require(std::isfinite(bv.real()) && std::isfinite(bv.imag()), BEM_ENONFINITE,
+              "non-finite wall admittance");
+      h->beta[i] = bv;
+    }
+    h->impedance = true;
     h->have_bc = true;
     h->state_gen++;
   });

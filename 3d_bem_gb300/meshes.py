@@ -207,3 +207,25 @@ def box_piston_rhs(tri: np.ndarray, lx=0.3, ly=0.2, lz=0.4, radius=0.05, patches
 def log_frequencies(count=64, f0=50.0, f1=2000.0) -> np.ndarray:
     """count log-spaced frequencies from f0 to f1 (Hz)."""
     return np.exp(np.linspace(np.log(f0), np.log(f1), count))
+
+
+def pencil_rhs(tri: np.ndarray, radius=0.004, patches=7, seed=20260105) -> np.ndarray:
+    """Driving data of the pencil sweep: column 0 is g = 1 on the outer ring
+    of the back cap (z = 0, r > radius / 2), columns 1..patches are seeded
+    random-velocity patches on ~5 % of the elements."""
+    c = (tri[:, 0:3] + tri[:, 3:6] + tri[:, 6:9]) / 3.0
+    on_cap = np.abs(c[:, 2]) < 1e-12
+    ring = on_cap & (np.hypot(c[:, 0], c[:, 1]) > 0.5 * radius)
+    g = np.zeros((tri.shape[0], 1 + patches), np.complex128)
+    g[ring, 0] = 1.0
+    if patches:
+        g[:, 1:] = random_patches(tri, patches, 0.05, seed)
+    return g
+
+
+def wall_admittance(n: int, seed=20260105, zmin=0.5, zmax=50.0) -> np.ndarray:
+    """Seeded per-element admittance ratios beta = rho c / Z with the wall
+    impedance Z log-uniform in [zmin, zmax] rho c (real, resistive walls)."""
+    rng = np.random.default_rng(seed)
+    z = np.exp(rng.uniform(np.log(zmin), np.log(zmax), n))
+    return (1.0 / z).astype(np.complex128)

@@ -248,6 +248,62 @@ def box_sweep(pkg, meshes, torch):
     return out
 
 
+def pencil_sweep(pkg, meshes, torch, every=8, plain_freqs=2):
+    """The large-body sweep: pencil (cylinder r = 4 mm, L = 0.2 m, conical tip),
+    81,760 triangles, impedance walls Z log-uniform in [0.5, 50] rho c,
+    8 right-hand sides (back-cap ring + 7 random patches), 64 log-spaced
+    frequencies 200 Hz - 8 kHz. The mixed arm (learned ACA rules, autotuned
+    workers) solves every `every`-th frequency; the plain complex-FP64 arm
+    solves `plain_freqs` of those; the 64-frequency times are extrapolated
+    from the per-frequency means, and the pressures of the frequencies both
+    arms solved are compared."""
+    tri = meshes.pencil()
+    n = tri.shape[0]
+    g = meshes.pencil_rhs(tri)
+    beta = meshes.wall_admittance(n)
+    freqs = meshes.log_frequencies(64, 200.0, 8000.0)
+    sub = freqs[::every]
+    out = {"workload": f"pencil r=4 mm L=0.2 m + conical tip, {n} triangles, impedance walls "
+                       "Z in [0.5, 50] rho c, 8 RHS, 64 log-spaced f 200 Hz-8 kHz",
+           "nrhs": int(g.shape[1]), "freqs_total": 64}
+
+    def solver(precision, **extra):
+        s = pkg.Solver(aca_tol=ACA_TOL, gmres_tol=GMRES_TOL, wave_speed=C0, density=RHO,
+                       precision=precision, **extra)
+        s.set_mesh(tri)
+        s.set_bc_impedance(beta)
+        return s
+
+    s = solver(1, selector=2, sweep_workers=0)
+    tune = s.autotune(float(sub[len(sub) // 2]), g.shape[1])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pm, im = s.sweep(sub, g)
+    dt = time.perf_counter() - t0
+    out["mixed"] = {"freqs_solved": int(len(sub)), "seconds": round(dt, 3),
+                    "s_per_freq": round(dt / len(sub), 4),
+                    "sweep_64_s_extrapolated": round(64 * dt / len(sub), 2),
+                    "max_iterations": int(max(i["iterations"] for i in im)),
+                    "all_converged": bool(all(i["status"] == 0 for i in im)),
+                    "tuned": tune}
+    s.close()
+    s64 = solver(0, sweep_workers=1)
+    pick = np.arange(0, len(sub), max(1, len(sub) // plain_freqs))[:plain_freqs]
+    t0 = time.perf_counter()
+    pp, ip = s64.sweep(sub[pick], g)
+    dt64 = time.perf_counter() - t0
+    s64.close()
+    out["plain_fp64"] = {"freqs_solved": int(len(pick)), "seconds": round(dt64, 3),
+                         "s_per_freq": round(dt64 / len(pick), 4),
+                         "sweep_64_s_extrapolated": round(64 * dt64 / len(pick), 2),
+                         "all_converged": bool(all(i["status"] == 0 for i in ip))}
+    errs = [float(np.linalg.norm(pm[:, r, f] - pp[:, r, j]) / np.linalg.norm(pp[:, r, j]))
+            for j, f in enumerate(pick) for r in range(g.shape[1])]
+    out["max_rel_err_mixed_vs_fp64"] = max(errs)
+    out["speedup_mixed_vs_fp64"] = round((dt64 / len(pick)) / (dt / len(sub)), 2)
+    return out
+
+
 def run_ours(args):
     import torch
     ws, rank, local = dist_env()
@@ -354,6 +410,8 @@ def run_ours(args):
         line["selector_stats"] = s.sel_stats()
     if not args.no_sweep and ws == 1:
         line["box_sweep"] = box_sweep(pkg, meshes, torch)
+    if args.pencil and ws == 1:
+        line["pencil_sweep"] = pencil_sweep(pkg, meshes, torch)
     if not args.no_cpu_baseline and rank == 0 and ws == 1:
         line["cpu_baseline"] = cpu_baseline_sample(args)
     if rank == 0:
@@ -434,6 +492,8 @@ def main():
                     help="mixed arm: truncating SVD recompression tolerance after ACA (0: off)")
     ap.add_argument("--precond", action="store_true",
                     help="mixed arm: H-LU preconditioned GMRES (rank 2)")
+    ap.add_argument("--pencil", action="store_true",
+                    help="also measure the 81,760-triangle pencil sweep (minutes)")
     ap.add_argument("--no-sweep", action="store_true",
                     help="skip the batched box sweep (64 frequencies x 4 RHS)")
     ap.add_argument("--selector", action="store_true",

@@ -115,6 +115,12 @@ bem_status bem_plan_mesh(const bem_config* cfg, const double* tri, int64_t n, in
 /* Robin coefficients a, b per element, caller order
  * (calculateBoundaryConditionAndSourceTermVector, :3386-3429). */
 bem_status bem_set_bc(bem_handle* h, const double* a, const double* b);
+/* Impedance walls: per element the admittance ratio beta = rho c / Z_e
+ * (complex, caller order), i.e. the Robin data a = i k beta, b = 1 at every
+ * frequency k of a solve or sweep (the wall-impedance section of the
+ * reference's solving script, wallimpedancesection.cpp:360-407, with the
+ * physical rho c and the current k; see the design notes). */
+bem_status bem_set_bc_impedance(bem_handle* h, const double* beta);
 
 /* Collocation operators L, M, Mt, N for (row, col) pairs in cluster order
  * (BemOperatorsConst, boundaryelementsolver.cpp:844-894); out: count x 4

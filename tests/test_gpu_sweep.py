@@ -80,3 +80,25 @@ def test_box_piston_sweep(bem, meshes):
     on = g[:, 0] != 0
     amp = np.abs(p[on, 0, :]).mean(0)
     assert amp[-1] > amp[0]
+
+
+def test_impedance_walls_match_robin_data(bem, meshes):
+    """bem_set_bc_impedance (a = i k beta, b = 1 at every frequency) solves
+    exactly what per-frequency Robin data a, b would."""
+    tri = meshes.box(n_target=1200, seed=5)
+    n = tri.shape[0]
+    beta = meshes.wall_admittance(n, seed=3)
+    g = np.ones(n)
+    freqs = np.array([300.0, 700.0])
+    s = bem.Solver(aca_tol=1e-5, gmres_tol=1e-10, precision=1, sweep_workers=2)
+    s.set_mesh(tri)
+    s.set_bc_impedance(beta)
+    p, info = s.sweep(freqs, g)
+    assert all(i["status"] == 0 for i in info)
+    for q, f in enumerate(freqs):
+        r = bem.Solver(aca_tol=1e-5, gmres_tol=1e-10, precision=1)
+        r.set_mesh(tri)
+        k = 2 * np.pi * f / 343.0
+        r.set_bc(1j * k * beta, np.ones(n))
+        _, _, pr, _ = r.solve(f, g)
+        assert np.array_equal(p[:, :, q], pr)
