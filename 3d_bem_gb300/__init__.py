@@ -37,7 +37,7 @@ EXPORTS = [
     "bem_assemble", "bem_hmatvec", "bem_hmatvec_device", "bem_get_block", "bem_get_ranks",
     "bem_gmres", "bem_solve", "bem_solve_device", "bem_sweep", "bem_points_assemble",
     "bem_launch_count", "bem_stream", "bem_hmatvec_noalloc", "bem_hmatvec_device_ex",
-    "bem_hlu_build", "bem_hlu_solve", "bem_hlu_export", "bem_recompress",
+    "bem_hlu_build", "bem_hlu_solve", "bem_hlu_export", "bem_hlu_sweep_kind", "bem_recompress",
     "bem_sel_nparam", "bem_sel_label", "bem_mlp_grad", "bem_mlp_adam", "bem_mlp_forward",
     "bem_sel_infer", "bem_set_selector", "bem_sel_stats", "bem_sel_classes", "bem_autotune",
     "bem_set_aca_rules", "bem_set_bc_impedance",
@@ -142,6 +142,7 @@ def lib():
     L.bem_hlu_build.argtypes = [vp]
     L.bem_hlu_solve.argtypes = [vp, vp, vp, i64]
     L.bem_hlu_export.argtypes = [vp, i32, P(i64), vp, P(i64), vp, P(i64), vp]
+    L.bem_hlu_sweep_kind.argtypes = [vp, P(i32)]
     L.bem_launch_count.argtypes = [vp]
     L.bem_launch_count.restype = i64
     L.bem_stream.argtypes = [vp]
@@ -350,6 +351,12 @@ class Solver:
         x = np.zeros_like(b)
         self._check(lib().bem_hlu_solve(self._h, _ptr(b), _ptr(x), R), "bem_hlu_solve")
         return x
+
+    def hlu_sweep_kind(self) -> int:
+        """1: dataflow sweeps (driver + helper CTAs), 0: sequential sweeps."""
+        k = ct.c_int32()
+        self._check(lib().bem_hlu_sweep_kind(self._h, ct.byref(k)), "bem_hlu_sweep_kind")
+        return k.value
 
     def hlu_export(self, which: int):
         """Flat factor ``which`` (0 L, 1 U): (leaves n x 7, data, schedule)."""

@@ -11,6 +11,7 @@
 #include <chrono>
 #include <cmath>
 #include <complex>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <mutex>
@@ -164,6 +165,17 @@ struct bem_handle {
   DBuf<unsigned char> dLd, dUd;  // factor data, complex FP64 or FP32 (hlu_prec)
   int hlu_prec = 0;
   DBuf<double2> dP1, dP2;
+  // dataflow form of the sweeps (one plan per factor) and its workspace
+  struct DfDev {
+    DBuf<unsigned char> chunks, rows, erows, cols, diag;
+    DBuf<int64_t> slot;
+    HluDfDev view;
+  } dfL, dfU;
+  bool df_ok = false;
+  std::string df_why;
+  DBuf<unsigned char> dfXi, dfAcc, dfEacc;  // factor-type vectors
+  DBuf<unsigned char> dfPre, dfFin;
+  DBuf<int> dfCtrl, dfErr;
   DBuf<int> dBad;
   QuadRules rules{};
   cudaEvent_t ev[10]{};
@@ -647,6 +659,83 @@ void pool_to_host(const DevHM& m, const DBuf<unsigned char>& src, size_t total,
   for (size_t i = 0; i < total; i++) out[i] = cplx(tmp[i].x, tmp[i].y);
 }
 
+template <typename T>
+void upload_bytes(DBuf<unsigned char>& d, const std::vector<T>& v, cudaStream_t s) {
+  d.ensure(v.size() * sizeof(T));
+  if (!v.empty())
+    CK(cudaMemcpyAsync(d.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+
+// Plans of the dataflow sweeps for both factors; when either factor lacks
+// their structure both sweeps stay on the sequential kernel (df_why says why).
+void upload_df_plans(bem_handle* h) {
+  h->df_ok = false;
+  h->df_why.clear();
+  HluDfPlan pl, pu;
+  const int eb = h->hlu_prec == 0 ? (int)sizeof(double2) : (int)sizeof(float2);
+  if (!hlu_df_plan(h->hL, h->N, eb, pl, &h->df_why) ||
+      !hlu_df_plan(h->hU, h->N, eb, pu, &h->df_why))
+    return;
+  cudaStream_t s = h->stream;
+  const size_t cs = h->hlu_prec == 0 ? sizeof(double2) : sizeof(float2);
+  int64_t nslot = 0;
+  int D = 0;
+  for (int q = 0; q < 2; q++) {
+    const HluDfPlan& p = q ? pu : pl;
+    bem_handle::DfDev& d = q ? h->dfU : h->dfL;
+    upload_bytes(d.chunks, p.chunks, s);
+    upload_bytes(d.rows, p.rows, s);
+    upload_bytes(d.erows, p.erows, s);
+    upload_bytes(d.cols, p.cols, s);
+    d.slot.upload(p.slot, s);
+    if (h->hlu_prec == 0) {
+      upload_bytes(d.diag, p.diag, s);
+    } else {
+      std::vector<float2> fd(p.diag.size());
+      for (size_t i = 0; i < fd.size(); i++)
+        fd[i] = make_float2((float)p.diag[i].real(), (float)p.diag[i].imag());
+      upload_bytes(d.diag, fd, s);
+      CK(cudaStreamSynchronize(s));  // fd goes out of scope
+    }
+    d.view.chunks = (const HluDfChunk*)d.chunks.p;
+    d.view.rows = (const HluDfRow*)d.rows.p;
+    d.view.erows = (const HluDfRow*)d.erows.p;
+    d.view.cols = (const HluDfCol*)d.cols.p;
+    d.view.slot = d.slot.p;
+    d.view.diag = d.diag.p;
+    d.view.D = p.D();
+    nslot = std::max(nslot, p.nslot);
+    D = std::max(D, p.D());
+  }
+  h->dfXi.ensure((size_t)HLU_DF_MAX_R * h->N * cs);
+  h->dfAcc.ensure((size_t)HLU_DF_MAX_R * h->N * cs);
+  h->dfEacc.ensure((size_t)HLU_DF_MAX_R * h->N * cs);
+  h->dfPre.ensure((size_t)std::max<int64_t>(nslot, 1) * cs);
+  h->dfFin.ensure((size_t)std::max<int64_t>(nslot, 1) * cs);
+  h->dfCtrl.ensure((size_t)(4 + 3 * D));
+  h->dfErr.ensure(1);
+  CK(cudaMemsetAsync(h->dfErr.p, 0, sizeof(int), s));
+  h->df_ok = true;
+}
+
+int df_helpers() {
+  const char* e = std::getenv("BEM_HLU_HELPERS");
+  const int v = e ? std::atoi(e) : 0;
+  return v > 0 ? v : 32;
+}
+
+// nonzero sticky error word of the dataflow sweeps: a wait ran out of time
+void check_df_error(bem_handle* h) {
+  if (!h->df_ok) return;
+  int e = 0;
+  CK(cudaMemcpyAsync(&e, h->dfErr.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (e) {
+    CK(cudaMemsetAsync(h->dfErr.p, 0, sizeof(int), h->stream));
+    throw BemError{BEM_ECUDA, "H-LU sweep: a dataflow wait ran out of time"};
+  }
+}
+
 // Truncated copy of the assembled dPhi matrix (HMatrix(const HMatrix&, rank,
 // err), hmatrix.cpp:770-776) factorized on the host; factors uploaded.
 // Returns false, keeping no factors, when they hold NaN or Inf: the solve
@@ -738,6 +827,7 @@ bool build_hlu(bem_handle* h) {
   };
   up(h->hL, h->dLs, h->dLl, h->dLd);
   up(h->hU, h->dUs, h->dUl, h->dUd);
+  upload_df_plans(h);
   CK(cudaStreamSynchronize(s));
   h->have_hlu = true;
   return true;
@@ -748,6 +838,20 @@ bool build_hlu(bem_handle* h) {
 void apply_precond(bem_handle* h, double2* w, int R) {
   const int64_t N = h->N;
   cudaStream_t s = h->stream;
+  if (h->df_ok) {  // dataflow sweeps: w -> dP2 -> w, up to 8 vectors per launch
+    h->dP2.ensure((size_t)std::min(R, HLU_DF_MAX_R) * N);
+    HluDfWork ws{h->dfXi.p, h->dfAcc.p, h->dfEacc.p, h->dfPre.p, h->dfFin.p, h->dfCtrl.p, h->dfErr.p};
+    const int hp = df_helpers();
+    for (int r0 = 0; r0 < R; r0 += HLU_DF_MAX_R) {
+      const int rc = std::min(HLU_DF_MAX_R, R - r0);
+      double2* wr = w + (size_t)r0 * N;
+      h->launches += launch_hlu_df(h->dfL.view, h->dLl.p, h->dLd.p, h->hlu_prec, wr, h->dP2.p, N,
+                                   rc, ws, hp, s);
+      h->launches += launch_hlu_df(h->dfU.view, h->dUl.p, h->dUd.p, h->hlu_prec, h->dP2.p, wr, N,
+                                   rc, ws, hp, s);
+    }
+    return;
+  }
   h->dP1.ensure((size_t)R * N);
   h->dP2.ensure((size_t)R * N);
   CK(cudaMemcpyAsync(h->dP1.p, w, (size_t)R * N * sizeof(double2), cudaMemcpyDeviceToDevice, s));
@@ -974,6 +1078,7 @@ void solve_dev(bem_handle* h, double freq, const double2* g_caller, int64_t R, d
   int bad = 0;
   CK(cudaMemcpyAsync(&bad, h->dBad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   sync(h);
+  if (use_precond(h)) check_df_error(h);
   loc.t_rhs = elapsed(h->ev[3], h->ev[4]);
   loc.t_gmres = elapsed(h->ev[4], h->ev[5]);
   loc.t_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -1595,6 +1700,17 @@ bem_status bem_hlu_solve(bem_handle* h, const double* b, double* x, int64_t nrhs
     CK(cudaGetLastError());
     copy_out(h, x, h->dIn.p, (size_t)h->N * nrhs);
     sync(h);
+    check_df_error(h);
+  });
+}
+
+bem_status bem_hlu_sweep_kind(const bem_handle* hc, int32_t* kind) {
+  if (!hc) return BEM_EINVAL;
+  bem_handle* h = const_cast<bem_handle*>(hc);
+  return guarded(h, [&] {
+    require(kind != nullptr, BEM_EINVAL, "bad arguments");
+    require(h->have_hlu, BEM_EINVAL, "preconditioner not built (bem_hlu_build)");
+    *kind = h->df_ok ? 1 : 0;
   });
 }
 

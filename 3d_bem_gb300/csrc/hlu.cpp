@@ -741,4 +741,170 @@ void hlu_factor(const HTree& tree, const std::vector<HBlockDesc>& blocks, std::v
   flatten_upper(Un, U);
 }
 
+bool hlu_df_plan(const FlatFactor& f, int64_t N, int elem_bytes, HluDfPlan& p,
+                 std::string* why) {
+  p = HluDfPlan();
+  auto fail = [&](const char* s) {
+    if (why) *why = s;
+    p = HluDfPlan();
+    return false;
+  };
+  const int64_t nl = f.nleaves();
+  const int64_t* lv = f.leaves.data();
+  std::vector<int32_t> diag;
+  for (int32_t op : f.schedule)
+    if (op >= 0) diag.push_back(op);
+  const int D = (int)diag.size();
+  if (D == 0 || N <= 0) return fail("no diagonal leaves");
+  std::vector<int32_t> chunk_of(N, -1);
+  std::vector<int64_t> cr0(D), cm(D);
+  for (int i = 0; i < D; i++) {
+    const int64_t* L = lv + 7 * (int64_t)diag[i];
+    if (L[0] != L[2] || L[1] != L[3] || L[1] < 1 || L[1] > HLU_DF_MAX_M || L[0] < 0 ||
+        L[0] + L[1] > N)
+      return fail("diagonal leaf shape");
+    for (int64_t r = L[0]; r < L[0] + L[1]; r++) {
+      if (chunk_of[r] >= 0) return fail("diagonal leaves overlap");
+      chunk_of[r] = i;
+    }
+    cr0[i] = L[0];
+    cm[i] = L[1];
+  }
+  for (int64_t r = 0; r < N; r++)
+    if (chunk_of[r] < 0) return fail("diagonal leaves do not cover the rows");
+  // chunks [lo, hi] (solve order) that tile [a, a + len) exactly
+  auto span = [&](int64_t a, int64_t len, int& lo, int& hi) {
+    if (len < 1 || a < 0 || a + len > N) return false;
+    const int c1 = chunk_of[a], c2 = chunk_of[a + len - 1];
+    lo = std::min(c1, c2);
+    hi = std::max(c1, c2);
+    int64_t tot = 0;
+    for (int c = lo; c <= hi; c++) {
+      if (cr0[c] < a || cr0[c] + cm[c] > a + len) return false;
+      tot += cm[c];
+    }
+    return tot == len;
+  };
+  std::vector<std::vector<HluDfRow>> rl(D), el(D);  // late, early
+  std::vector<std::vector<HluDfCol>> cl(D);
+  std::vector<HluDfChunk> ch(D + 1);
+  for (int i = 0; i <= D; i++) {
+    ch[i] = HluDfChunk{};
+    ch[i].corner = -1;
+  }
+  p.slot.assign(nl, -1);
+  for (int32_t op : f.schedule) {
+    if (op >= 0) continue;
+    const int32_t o = -op - 1;
+    const int64_t* L = lv + 7 * (int64_t)o;
+    const int64_t kind = L[4], k = L[5];
+    if (kind != 0 && kind != 1) return fail("off-diagonal leaf kind");
+    const bool lr = kind == 1;
+    if (lr && (k < 1 || k > HLU_DF_MAX_RANK)) return fail("low-rank leaf rank");
+    int ra, rb, ca, cb;
+    if (!span(L[0], L[1], ra, rb) || !span(L[2], L[3], ca, cb))
+      return fail("leaf not aligned with the diagonal leaves");
+    if (cb >= ra) return fail("leaf not below the diagonal in solve order");
+    bool uses_fin = false;
+    for (int i = ra; i <= rb; i++) {
+      const int32_t ro = (int32_t)(cr0[i] - L[0]);
+      if (cb == i - 1) {
+        if (ch[i].corner >= 0) return fail("two corner leaves");
+        ch[i].corner = o;
+        ch[i].cro = ro;
+        ch[i].cco = (int32_t)(cr0[i - 1] - L[2]);
+        ch[i].cflags = (lr ? 1 : 0) | (lr && ca < cb ? 2 : 0) | (!lr && ca == cb ? 4 : 0);
+        ch[i].cm = (int32_t)L[1];
+        ch[i].cn = (int32_t)L[3];
+        ch[i].ck = (int32_t)k;
+        ch[i].cc0 = (int32_t)L[2];
+        ch[i].cdata = L[6];
+      } else {
+        auto& list = cb <= i - HLU_DF_LAG ? el[i] : rl[i];
+        if (!lr) {
+          list.push_back(HluDfRow{o, ro, 0, 0, -1});
+        } else if (cb == i - 2) {
+          list.push_back(HluDfRow{o, ro, ca < cb ? 2 : 3, (int32_t)(cr0[i - 2] - L[2]), -1});
+        } else {
+          list.push_back(HluDfRow{o, ro, 1, 0, -1});
+          uses_fin = true;
+        }
+      }
+    }
+    if (!lr) continue;
+    // the prefix over cols ca..cb-1 is read by the corner (rows cb + 1) and
+    // by mode 2 (rows cb + 2); fin by mode 1
+    const bool uses_pre = ca < cb && ra <= cb + 2;
+    if (!uses_pre && !uses_fin) continue;
+    p.slot[o] = p.nslot;
+    p.nslot += k * HLU_DF_MAX_R;
+    for (int j = ca; j <= cb; j++) {
+      const bool last = j == cb;
+      if (last && !uses_fin) continue;
+      for (int32_t l = 0; l < (int32_t)k; l++)
+        cl[j].push_back(HluDfCol{o, (int32_t)(cr0[j] - L[2]), (j == ca ? 1 : 0) | (last ? 2 : 0), l});
+    }
+  }
+  // CSR lists, apply matrices
+  int64_t moff = 0;
+  for (int i = 0; i < D; i++) {
+    ch[i].r0 = (int32_t)cr0[i];
+    ch[i].m = (int32_t)cm[i];
+    ch[i].moff = moff;
+    // late entries: at most one per column chunk i - LAG + 1 .. i - 2; their
+    // constants (full: F rows, low rank: U rows and V over cols(i - 2)) get
+    // staging offsets, 32 rows per column / rank, within the staging budget
+    if ((int)rl[i].size() > HLU_DF_NLATE) return fail("too many late leaves");
+    int64_t so = 0;
+    const int64_t budget = HLU_DF_STAGE_BYTES / elem_bytes;
+    for (HluDfRow& r : rl[i]) {
+      const int64_t* L = lv + 7 * (int64_t)r.leaf;
+      const int64_t need = L[4] == 0 ? (L[3] <= 2 * HLU_DF_MAX_M ? 32 * L[3] : budget + 1)
+                                     : 32 * L[5] * (r.mode >= 2 ? 2 : 1);
+      if (so + need <= budget) {
+        r.soff = (int32_t)so;
+        so += need;
+      }
+    }
+    ch[i].rbeg = (int32_t)p.rows.size();
+    p.rows.insert(p.rows.end(), rl[i].begin(), rl[i].end());
+    ch[i].ebeg = (int32_t)p.erows.size();
+    p.erows.insert(p.erows.end(), el[i].begin(), el[i].end());
+    ch[i].cbeg = (int32_t)p.cols.size();
+    p.cols.insert(p.cols.end(), cl[i].begin(), cl[i].end());
+    const int64_t* L = lv + 7 * (int64_t)diag[i];
+    const int64_t m = L[1];
+    const cd* Dd = f.data.data() + L[6];
+    if (L[6] < 0 || L[6] + m * m > (int64_t)f.data.size()) return fail("diagonal leaf data");
+    p.diag.resize(moff + m * m);
+    cd* M = p.diag.data() + moff;
+    if (L[4] == 2) {  // Q (column-major): M[row][t] = conj(Q[t, row]) = conj(Q[row * m + t])
+      for (int64_t e = 0; e < m * m; e++) M[e] = std::conj(Dd[e]);
+    } else if (L[4] == 3) {  // R upper (column-major): M = R^{-1} row-major
+      for (int64_t t = 0; t < m; t++) {
+        if (Dd[t + t * m] == cd(0.0)) return fail("zero pivot");
+        for (int64_t row = 0; row < m; row++) M[row * m + t] = 0.0;
+        // column t of R^{-1}: R y = e_t
+        M[t * m + t] = 1.0 / Dd[t + t * m];
+        for (int64_t row = t - 1; row >= 0; row--) {
+          cd acc = 0.0;
+          for (int64_t q = row + 1; q <= t; q++) acc += Dd[row + q * m] * M[q * m + t];
+          M[row * m + t] = -acc / Dd[row + row * m];
+        }
+      }
+    } else {
+      return fail("diagonal leaf kind");
+    }
+    moff += m * m;
+  }
+  ch[D].r0 = (int32_t)N;
+  ch[D].rbeg = (int32_t)p.rows.size();
+  ch[D].ebeg = (int32_t)p.erows.size();
+  ch[D].cbeg = (int32_t)p.cols.size();
+  ch[D].moff = moff;
+  p.chunks = std::move(ch);
+  return true;
+}
+
 }  // namespace bemgpu
+

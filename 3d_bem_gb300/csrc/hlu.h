@@ -5,8 +5,10 @@
 
 #include <complex>
 #include <memory>
+#include <string>
 #include <vector>
 
+#include "hlu_solve.h"
 #include "host_tree.h"
 
 namespace bemgpu {
@@ -49,5 +51,28 @@ struct InBlock {
 void hlu_factor(const HTree& tree, const std::vector<HBlockDesc>& blocks,
                 std::vector<InBlock>& in, int64_t max_rank, double tol, FlatFactor& L,
                 FlatFactor& U);
+
+// Plan of the dataflow sweep (hlu_solve.h) for one flattened factor: chunks
+// in solve order with their corner leaves, row and column lists, pre/fin slot
+// offsets, and the m x m apply matrix of every diagonal leaf, row-major:
+// conj(Q) stored like Q (y = Q^H s) for L, R^{-1} for U (back substitution
+// done once here, per column of the identity, instead of once per sweep).
+struct HluDfPlan {
+  std::vector<HluDfChunk> chunks;  // D + 1, the last one a sentinel
+  std::vector<HluDfRow> rows, erows;  // late and early row lists
+  std::vector<HluDfCol> cols;
+  std::vector<int64_t> slot;       // per leaf, -1 for none
+  int64_t nslot = 0;               // complex values in each of pre and fin
+  std::vector<cd> diag;
+  int D() const { return (int)chunks.size() - 1; }
+};
+
+// False (with the reason) when the factor does not have the dataflow form's
+// structure: diagonal leaves that do not tile [0, N) or exceed 32 rows, a leaf
+// that is not aligned with them or not below the diagonal in solve order, a
+// rank above 32, a zero pivot. The sweep then runs on launch_hlu_sweep.
+// elem_bytes: size of one factor element (16 complex FP64, 8 complex FP32),
+// for the staging offsets of the late entries.
+bool hlu_df_plan(const FlatFactor& f, int64_t N, int elem_bytes, HluDfPlan& p, std::string* why);
 
 }  // namespace bemgpu

@@ -191,6 +191,12 @@ bem_status bem_hlu_build(bem_handle* h);
 /* x = U^{-1} L^{-1} b on the GPU for nrhs vectors (cluster order, host
  * buffers): HArithm::LUSubstitutionSolve (harithm.cpp:1168-1190). */
 bem_status bem_hlu_solve(bem_handle* h, const double* b, double* x, int64_t nrhs);
+/* Form of the sweeps of the built factors: 1 = dataflow (one driver CTA on
+ * the chain of diagonal leaves, helper CTAs applying the off-diagonal leaves
+ * as their columns are solved; needs diagonal leaves <= 32 rows and ranks
+ * <= 32), 0 = one CTA per right-hand side walking the leaf schedule in the
+ * reference's order. Both give the same solve to rounding. */
+bem_status bem_hlu_sweep_kind(const bem_handle* h, int32_t* kind);
 /* ---- Learned quadrature-order selector (no counterpart in the reference,
  * which integrates every regular pair with one 16-point rule,
  * boundaryelementsolver.cpp:857-893). A 24-64-64-5 ReLU network picks per

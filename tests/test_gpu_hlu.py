@@ -154,3 +154,43 @@ def test_hlu_solve_fp32_factors_vs_oracle(bem, meshes, orc):
     for q in range(2):
         x = orc.upper_solve(n, Ul, Ud, orc.lower_solve(n, Ll, Ld, B[:, q]))
         assert rel(X[:, q], x) < 1e-4, q
+
+
+def oracle_solve(orc, s, n, B):
+    Ll, Ld, _ = s.hlu_export(0)
+    Ul, Ud, _ = s.hlu_export(1)
+    return np.stack([orc.upper_solve(n, Ul, Ud, orc.lower_solve(n, Ll, Ld, B[:, q]))
+                     for q in range(B.shape[1])], axis=1)
+
+
+def test_dataflow_sweep_many_rhs_and_helpers(bem, meshes, orc, monkeypatch):
+    """The dataflow sweep (default for leaf 32, rank <= 32): 11 right-hand
+    sides take two launches (8 + 3); the result matches the oracle's
+    leaf-by-leaf solve, and is bitwise the same for any number of helper
+    blocks (each sum has one fixed order)."""
+    tri, s = setup(bem, meshes, 3, precond_rank=4)
+    n = tri.shape[0]
+    s.assemble(FREQ)
+    s.hlu_build()
+    assert s.hlu_sweep_kind() == 1
+    rng = np.random.default_rng(4)
+    B = rng.standard_normal((n, 11)) + 1j * rng.standard_normal((n, 11))
+    X = s.hlu_solve(B)
+    assert rel(X, oracle_solve(orc, s, n, B)) < 1e-12
+    for h in ("1", "3", "150"):
+        monkeypatch.setenv("BEM_HLU_HELPERS", h)
+        assert np.array_equal(s.hlu_solve(B), X), h
+
+
+def test_sequential_sweep_for_large_leaves(bem, meshes, orc):
+    """Diagonal leaves above 32 rows (leaf_size 64) keep the sequential
+    sweep; it matches the oracle too."""
+    tri, s = setup(bem, meshes, 3, precond_rank=2, leaf_size=64)
+    n = tri.shape[0]
+    s.assemble(FREQ)
+    s.hlu_build()
+    assert s.hlu_sweep_kind() == 0
+    rng = np.random.default_rng(6)
+    B = rng.standard_normal((n, 2)) + 1j * rng.standard_normal((n, 2))
+    assert rel(s.hlu_solve(B), oracle_solve(orc, s, n, B)) < 1e-12
+
