@@ -61,7 +61,8 @@ class Config(ct.Structure):
                 ("use_preconditioner", ct.c_int32), ("selector", ct.c_int32),
                 ("precond_rank", ct.c_int64), ("precond_tol", ct.c_double),
                 ("recompress_tol", ct.c_double), ("selector_guard", ct.c_double),
-                ("sweep_workers", ct.c_int64), ("aca_big_mn", ct.c_int64)]
+                ("sweep_workers", ct.c_int64), ("aca_big_mn", ct.c_int64),
+                ("precond_reuse", ct.c_double)]
 
 
 class SolveInfo(ct.Structure):
@@ -69,11 +70,11 @@ class SolveInfo(ct.Structure):
                 ("true_residual", ct.c_double), ("max_rank", ct.c_int64),
                 ("capped_blocks", ct.c_int64), ("t_nearfield", ct.c_double),
                 ("t_aca", ct.c_double), ("t_rhs", ct.c_double), ("t_gmres", ct.c_double),
-                ("t_total", ct.c_double), ("status", ct.c_int32), ("pad", ct.c_int32),
+                ("t_total", ct.c_double), ("status", ct.c_int32), ("precond_reused", ct.c_int32),
                 ("t_precond", ct.c_double)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 _lib = None

@@ -159,6 +159,8 @@ struct bem_handle {
   DBuf<unsigned char> rcA, rcB, rcC;
   DBuf<int64_t> dCoff;
   bool have_hlu = false;
+  double mat_freq = 0;  // frequency of the assembled matrices
+  double hlu_freq = 0;  // frequency of the matrix the factors came from
   FlatFactor hL, hU;
   DBuf<int32_t> dLs, dUs;
   DBuf<int64_t> dLl, dUl;
@@ -338,7 +340,9 @@ void fetch_ranks(bem_handle* h, DevHM& m) {
   m.nvwork = (int64_t)vw.size();
   sync(h);
   m.assembled = true;
-  if (&m == &h->hm[1]) h->have_hlu = false;  // factors of the previous matrix
+  // factors of the previous matrix: dropped, unless they are kept as the
+  // preconditioner of nearby frequencies
+  if (&m == &h->hm[1] && !(h->cfg.precond_reuse > 1.0)) h->have_hlu = false;
 }
 
 AcaArgs aca_args(bem_handle* h, DevHM& m, int which, int extra) {
@@ -451,6 +455,7 @@ void assemble(bem_handle* h, double freq, double* t_near, double* t_aca) {
   const double k = 2.0 * M_PI * freq / h->cfg.wave_speed;
   require(k > 0 && std::isfinite(k), BEM_EINVAL, "frequency must be positive and finite");
   set_frequency(h, k);
+  h->mat_freq = freq;
   for (auto& m : h->hm) alloc_hm(h, m);
   cudaStream_t s = h->stream;
   cplx al = coupling_parameter(h->cfg.coupling, k);
@@ -830,6 +835,7 @@ bool build_hlu(bem_handle* h) {
   upload_df_plans(h);
   CK(cudaStreamSynchronize(s));
   h->have_hlu = true;
+  h->hlu_freq = h->mat_freq;
   return true;
 }
 
@@ -1045,9 +1051,14 @@ void solve_dev(bem_handle* h, double freq, const double2* g_caller, int64_t R, d
   bem_solve_info loc{};
   assemble(h, freq, &loc.t_nearfield, &loc.t_aca);
   if (h->cfg.use_preconditioner) {
-    const auto tp = std::chrono::steady_clock::now();
-    build_hlu(h);  // non-finite factors: continue without the preconditioner
-    loc.t_precond = std::chrono::duration<double>(std::chrono::steady_clock::now() - tp).count();
+    const double r = h->hlu_freq > 0 ? std::max(freq / h->hlu_freq, h->hlu_freq / freq) : 0.0;
+    if (h->have_hlu && h->cfg.precond_reuse > 1.0 && r > 0 && r <= h->cfg.precond_reuse) {
+      loc.precond_reused = 1;
+    } else {
+      const auto tp = std::chrono::steady_clock::now();
+      build_hlu(h);  // non-finite factors: continue without the preconditioner
+      loc.t_precond = std::chrono::duration<double>(std::chrono::steady_clock::now() - tp).count();
+    }
   }
   h->dG.ensure((size_t)R * N);
   h->dRhs.ensure((size_t)R * N);
@@ -1164,7 +1175,7 @@ void ensure_workers(bem_handle* h, int nw) {
 
 // Frequencies idx[0..n) of a sweep on W handles (h and W - 1 workers), one
 // host thread per handle, each on its own stream; frequency i goes to handle
-// i mod W. p (caller order, n_freq slices) gets each frequency's pressure.
+// i mod W (with H-LU factor reuse: contiguous blocks of ascending frequencies). p (caller order, n_freq slices) gets each frequency's pressure.
 void run_sweep(bem_handle* h, int W, const double* freqs, const int64_t* idx, int64_t n,
                const double* g, int64_t nrhs, double* p, bem_solve_info* info,
                bem_status& worst) {
@@ -1182,7 +1193,11 @@ void run_sweep(bem_handle* h, int W, const double* freqs, const int64_t* idx, in
       CK(cudaSetDevice(h->device));
       copy_in(x, x->dIn, g, cnt);
       x->dOut3.ensure(cnt);
-      for (int64_t i = w; i < n; i += W) {
+      // with factor reuse, each handle takes a contiguous block of the
+      // (sorted) frequencies, so its consecutive solves are close
+      const bool blocks = h->cfg.use_preconditioner && h->cfg.precond_reuse > 1.0;
+      const int64_t i0 = blocks ? n * w / W : w, i1 = blocks ? n * (w + 1) / W : n;
+      for (int64_t i = i0; i < i1; i += blocks ? 1 : W) {
         const int64_t f = idx[i];
         bem_solve_info loc{};
         solve_dev(x, freqs[f], x->dIn.p, nrhs, nullptr, nullptr, x->dOut3.p, &loc);
@@ -1291,6 +1306,7 @@ void bem_config_default(bem_config* c) {
   c->selector_guard = 0.9;
   c->sweep_workers = 0;
   c->aca_big_mn = 0;
+  c->precond_reuse = 0.0;
 }
 
 bem_status bem_create(const bem_config* cfg, bem_handle** out) {
@@ -1315,6 +1331,8 @@ bem_status bem_create(const bem_config* cfg, bem_handle** out) {
     require(h->cfg.sweep_workers >= 0 && h->cfg.sweep_workers <= 16, BEM_EINVAL,
             "sweep_workers must be 0 (auto) .. 16");
     require(h->cfg.aca_big_mn >= 0, BEM_EINVAL, "aca_big_mn must be >= 0");
+    require(h->cfg.precond_reuse >= 0 && std::isfinite(h->cfg.precond_reuse), BEM_EINVAL,
+            "precond_reuse must be finite and >= 0");
     CK(cudaGetDevice(&h->device));
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     CK(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
@@ -1458,6 +1476,7 @@ bem_status bem_set_bc(bem_handle* h, const double* a, const double* b) {
       h->b[i] = bv;
     }
     h->impedance = false;
+    h->have_hlu = false;  // factors of another operator
     h->have_bc = true;
     h->state_gen++;
   });
@@ -1480,6 +1499,7 @@ bem_status bem_set_bc_impedance(bem_handle* h, const double* beta) {
       h->beta[i] = bv;
     }
     h->impedance = true;
+    h->have_hlu = false;  // factors of another operator
     h->have_bc = true;
     h->state_gen++;
   });
@@ -1947,9 +1967,13 @@ bem_status bem_sweep(bem_handle* h, const double* freqs, int64_t nf, const doubl
       }
       W = h->tuned_workers > 0 ? (int)h->tuned_workers : 1;
     }
-    // interleave cheap and expensive frequencies over the workers
+    // interleave cheap and expensive frequencies over the workers; with
+    // factor reuse, frequencies go in ascending order
     std::vector<int64_t> idx(nf);
     for (int64_t i = 0; i < nf; i++) idx[i] = i;
+    if (h->cfg.use_preconditioner && h->cfg.precond_reuse > 1.0)
+      std::stable_sort(idx.begin(), idx.end(),
+                       [&](int64_t x, int64_t y) { return freqs[x] < freqs[y]; });
     run_sweep(h, W, freqs, idx.data(), nf, g, nrhs, p, info, worst);
   });
   return st != BEM_OK ? st : worst;

@@ -252,11 +252,13 @@ def pencil_sweep(pkg, meshes, torch, every=8, plain_freqs=2):
     """The large-body sweep: pencil (cylinder r = 4 mm, L = 0.2 m, conical tip),
     81,760 triangles, impedance walls Z log-uniform in [0.5, 50] rho c,
     8 right-hand sides (back-cap ring + 7 random patches), 64 log-spaced
-    frequencies 200 Hz - 8 kHz. The mixed arm (learned ACA rules, autotuned
-    workers) solves every `every`-th frequency; the plain complex-FP64 arm
-    solves `plain_freqs` of those; the 64-frequency times are extrapolated
-    from the per-frequency means, and the pressures of the frequencies both
-    arms solved are compared."""
+    frequencies 200 Hz - 8 kHz. Both arms use the H-LU preconditioner (rank 2,
+    rebuilt for every frequency as in the reference; unpreconditioned GMRES
+    does not reach 1e-10 on this body in 1000 steps). The mixed arm (learned
+    ACA rules) solves every `every`-th frequency; the plain complex-FP64 arm
+    solves `plain_freqs` of those; the 64-frequency times are extrapolated from
+    the per-frequency means. The host-side factorization (the same code in both
+    arms) is reported apart from the GPU work."""
     tri = meshes.pencil()
     n = tri.shape[0]
     g = meshes.pencil_rhs(tri)
@@ -264,43 +266,44 @@ def pencil_sweep(pkg, meshes, torch, every=8, plain_freqs=2):
     freqs = meshes.log_frequencies(64, 200.0, 8000.0)
     sub = freqs[::every]
     out = {"workload": f"pencil r=4 mm L=0.2 m + conical tip, {n} triangles, impedance walls "
-                       "Z in [0.5, 50] rho c, 8 RHS, 64 log-spaced f 200 Hz-8 kHz",
+                       "Z in [0.5, 50] rho c, 8 RHS, 64 log-spaced f 200 Hz-8 kHz, "
+                       "H-LU preconditioner rank 2",
            "nrhs": int(g.shape[1]), "freqs_total": 64}
 
     def solver(precision, **extra):
         s = pkg.Solver(aca_tol=ACA_TOL, gmres_tol=GMRES_TOL, wave_speed=C0, density=RHO,
-                       precision=precision, **extra)
+                       precision=precision, use_preconditioner=1, precond_rank=2,
+                       gmres_maxit=1000, sweep_workers=1, **extra)
         s.set_mesh(tri)
         s.set_bc_impedance(beta)
         return s
 
-    s = solver(1, selector=2, sweep_workers=0)
-    tune = s.autotune(float(sub[len(sub) // 2]), g.shape[1])
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    pm, im = s.sweep(sub, g)
-    dt = time.perf_counter() - t0
-    out["mixed"] = {"freqs_solved": int(len(sub)), "seconds": round(dt, 3),
-                    "s_per_freq": round(dt / len(sub), 4),
-                    "sweep_64_s_extrapolated": round(64 * dt / len(sub), 2),
-                    "max_iterations": int(max(i["iterations"] for i in im)),
-                    "all_converged": bool(all(i["status"] == 0 for i in im)),
-                    "tuned": tune}
+    def arm(s, fr):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        p, info = s.sweep(fr, g)
+        dt = time.perf_counter() - t0
+        tp = sum(i["t_precond"] for i in info)
+        return p, info, {"freqs_solved": int(len(fr)), "seconds": round(dt, 3),
+                         "s_per_freq": round(dt / len(fr), 4),
+                         "host_factor_s_per_freq": round(tp / len(fr), 4),
+                         "gpu_s_per_freq": round((dt - tp) / len(fr), 4),
+                         "sweep_64_s_extrapolated": round(64 * dt / len(fr), 2),
+                         "max_iterations": int(max(i["iterations"] for i in info)),
+                         "all_converged": bool(all(i["status"] == 0 for i in info))}
+
+    s = solver(1, selector=2)
+    pm, im, out["mixed"] = arm(s, sub)
     s.close()
-    s64 = solver(0, sweep_workers=1)
     pick = np.arange(0, len(sub), max(1, len(sub) // plain_freqs))[:plain_freqs]
-    t0 = time.perf_counter()
-    pp, ip = s64.sweep(sub[pick], g)
-    dt64 = time.perf_counter() - t0
+    s64 = solver(0)
+    pp, ip, out["plain_fp64"] = arm(s64, sub[pick])
     s64.close()
-    out["plain_fp64"] = {"freqs_solved": int(len(pick)), "seconds": round(dt64, 3),
-                         "s_per_freq": round(dt64 / len(pick), 4),
-                         "sweep_64_s_extrapolated": round(64 * dt64 / len(pick), 2),
-                         "all_converged": bool(all(i["status"] == 0 for i in ip))}
     errs = [float(np.linalg.norm(pm[:, r, f] - pp[:, r, j]) / np.linalg.norm(pp[:, r, j]))
             for j, f in enumerate(pick) for r in range(g.shape[1])]
     out["max_rel_err_mixed_vs_fp64"] = max(errs)
-    out["speedup_mixed_vs_fp64"] = round((dt64 / len(pick)) / (dt / len(sub)), 2)
+    out["speedup_mixed_vs_fp64"] = round(out["plain_fp64"]["s_per_freq"] / out["mixed"]["s_per_freq"], 2)
+    out["speedup_gpu_work"] = round(out["plain_fp64"]["gpu_s_per_freq"] / out["mixed"]["gpu_s_per_freq"], 2)
     return out
 
 

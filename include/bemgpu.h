@@ -70,6 +70,11 @@ typedef struct bem_config {
                               worker on its own stream (0: autotuned) */
   int64_t aca_big_mn;      /* ACA size bin: blocks with m + n >= this get the
                               512-thread kernel (0: 512, or autotuned) */
+  double precond_reuse;    /* > 1: a solve keeps the H-LU factors of an earlier
+                              frequency f0 while max(f / f0, f0 / f) <= this
+                              (frequency sweeps; GMRES still converges to the
+                              solution of the current matrix); <= 1: factors
+                              rebuilt for every solve, as the reference does */
 } bem_config;
 
 typedef struct bem_solve_info {
@@ -84,7 +89,7 @@ typedef struct bem_solve_info {
   double t_gmres;
   double t_total;
   int32_t status;
-  int32_t pad;
+  int32_t precond_reused;  /* 1: the solve used factors of an earlier frequency */
   double t_precond;        /* H-LU build (host) including transfers */
 } bem_solve_info;
 

@@ -194,3 +194,27 @@ def test_sequential_sweep_for_large_leaves(bem, meshes, orc):
     B = rng.standard_normal((n, 2)) + 1j * rng.standard_normal((n, 2))
     assert rel(s.hlu_solve(B), oracle_solve(orc, s, n, B)) < 1e-12
 
+
+def test_factor_reuse_over_a_sweep(bem, meshes):
+    """precond_reuse = 1.3: a sweep keeps the H-LU factors while the frequency
+    stays within 1.3x of the one they were built at, and rebuilds them past
+    it; every pressure is the solution of its own matrix (GMRES on
+    (LU)^-1 A x = (LU)^-1 b with the residual of the current A)."""
+    tri = meshes.icosphere(3, 1.0)
+    n = tri.shape[0]
+    freqs = np.array([200.0, 220.0, 250.0, 270.0, 300.0])
+    g = np.ones(n)
+    out = {}
+    for reuse in (0.0, 1.3):
+        s = bem.Solver(aca_tol=1e-6, gmres_tol=1e-10, precision=1, use_preconditioner=1,
+                       precond_rank=2, precond_reuse=reuse, sweep_workers=1)
+        s.set_mesh(tri)
+        s.set_bc(np.zeros(n), np.ones(n))
+        out[reuse] = s.sweep(freqs, g)
+        s.close()
+    (p0, i0), (p1, i1) = out[0.0], out[1.3]
+    assert [i["precond_reused"] for i in i0] == [0, 0, 0, 0, 0]
+    assert [i["precond_reused"] for i in i1] == [0, 1, 1, 0, 1]
+    assert all(i["status"] == 0 and i["true_residual"] < 1e-9 for i in i0 + i1)
+    assert rel(p1, p0) < 1e-7
+
