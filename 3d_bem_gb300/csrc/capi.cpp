@@ -112,6 +112,7 @@ struct bem_handle {
   int64_t tuned_workers = 0;
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;  // second stream for concurrent ACA launches
+  cudaStream_t nearst = nullptr;  // near-field assembly, concurrent with ACA
   cudaEvent_t fork = nullptr, join = nullptr;
   int64_t launches = 0;
   // mesh
@@ -477,12 +478,17 @@ void assemble(bem_handle* h, double freq, double* t_near, double* t_aca) {
   na.phi = h->hm[0].F.p;
   na.dphi = h->hm[1].F.p;
   CK(cudaEventRecord(h->ev[0], s));
+  // the near field (FP64-pipe-bound singular rules, FP32 regular rules) runs
+  // on its own stream beside the barrier-bound ACA kernels; both write
+  // disjoint pools of the same matrices
+  cudaStream_t ns = h->nearst;
+  CK(cudaStreamWaitEvent(ns, h->ev[0], 0));
   const bool learned = (h->cfg.selector & 1) && na.precision == 1;
   if (learned) {
     require(h->have_selector, BEM_EINVAL, "selector weights not set (bem_set_selector)");
     h->dCls.ensure(h->L.near_entries);
     h->dSelCnt.ensure(3);
-    CK(cudaMemsetAsync(h->dSelCnt.p, 0, 3 * sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(h->dSelCnt.p, 0, 3 * sizeof(unsigned long long), ns));
     SelNearArgs ca{};
     ca.blob = h->dSel.p;
     ca.EF = h->dEF.p;
@@ -493,7 +499,7 @@ void assemble(bem_handle* h, double freq, double* t_near, double* t_aca) {
     ca.k = k;
     ca.guard_prob = (float)h->cfg.selector_guard;
     ca.cls = h->dCls.p;
-    launch_sel_near_classes(ca, s);
+    launch_sel_near_classes(ca, ns);
     SelNearfieldArgs fa{};
     fa.EF = h->dEF.p;
     fa.bc = h->dBc.p;
@@ -509,23 +515,26 @@ void assemble(bem_handle* h, double freq, double* t_near, double* t_aca) {
     fa.check_every = 16;
     fa.check_tol = 1e-6f;
     fa.counters = h->dSelCnt.p;
-    launch_sel_nearfield32(fa, s);
+    launch_sel_nearfield32(fa, ns);
     h->launches += 2 * (na.ntiles > 0);
     na.ntiles = 0;  // the special entries only
   }
-  launch_nearfield(na, s);
+  launch_nearfield(na, ns);
   h->launches += (na.ntiles > 0) + (na.nspecial > 0);
-  CK(cudaEventRecord(h->ev[1], s));
   if (learned)
     CK(cudaMemcpyAsync(h->sel_stats, h->dSelCnt.p, 3 * sizeof(unsigned long long),
-                       cudaMemcpyDeviceToHost, s));
+                       cudaMemcpyDeviceToHost, ns));
+  CK(cudaEventRecord(h->ev[1], ns));
   launch_aca_split(h, {aca_args(h, h->hm[0], 0, 0), aca_args(h, h->hm[1], 1, 1)});
   CK(cudaEventRecord(h->ev[2], s));
+  CK(cudaStreamWaitEvent(s, h->ev[1], 0));  // join the near field
   CK(cudaGetLastError());
   fetch_ranks(h, h->hm[0]);
   fetch_ranks(h, h->hm[1]);
+  // overlapping phases: the near field's own span, and the ACA span from the
+  // start of assembly to its last block
   if (t_near) *t_near = elapsed(h->ev[0], h->ev[1]);
-  if (t_aca) *t_aca = elapsed(h->ev[1], h->ev[2]);
+  if (t_aca) *t_aca = elapsed(h->ev[0], h->ev[2]);
   if (h->cfg.recompress_tol > 0) {
     CK(cudaEventRecord(h->ev[1], s));
     for (auto& m : h->hm) recompress(h, m, 0, h->cfg.recompress_tol);
@@ -1334,8 +1343,13 @@ bem_status bem_create(const bem_config* cfg, bem_handle** out) {
     require(h->cfg.precond_reuse >= 0 && std::isfinite(h->cfg.precond_reuse), BEM_EINVAL,
             "precond_reuse must be finite and >= 0");
     CK(cudaGetDevice(&h->device));
+    // the near-field stream at the highest priority: its short, FP64-bound
+    // blocks go first while the ACA blocks fill the remaining slots
+    int prio_low = 0, prio_high = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     CK(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithPriority(&h->nearst, cudaStreamNonBlocking, prio_high));
     CK(cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&h->join, cudaEventDisableTiming));
     for (auto& e : h->ev) CK(cudaEventCreate(&e));
@@ -1359,14 +1373,16 @@ void bem_destroy(bem_handle* h) {
   h->workers.clear();
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->side) cudaStreamSynchronize(h->side);
+  if (h->nearst) cudaStreamSynchronize(h->nearst);
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
   if (h->fork) cudaEventDestroy(h->fork);
   if (h->join) cudaEventDestroy(h->join);
-  cudaStream_t s = h->stream, s2 = h->side;
+  cudaStream_t s = h->stream, s2 = h->side, s3 = h->nearst;
   delete h;  // device buffers are released by their destructors
   if (s) cudaStreamDestroy(s);
   if (s2) cudaStreamDestroy(s2);
+  if (s3) cudaStreamDestroy(s3);
 }
 
 const char* bem_last_error(const bem_handle* h) { return h ? h->err.c_str() : "null handle"; }

@@ -83,8 +83,8 @@ typedef struct bem_solve_info {
   double true_residual;    /* max ||b - A x|| / ||b|| after the solve */
   int64_t max_rank;        /* largest ACA rank of the system matrix */
   int64_t capped_blocks;   /* blocks that hit their rank reservation */
-  double t_nearfield;      /* seconds, device-timed */
-  double t_aca;
+  double t_nearfield;      /* seconds, device-timed; the near field runs beside */
+  double t_aca;            /* ACA (both spans start with the assembly) */
   double t_rhs;
   double t_gmres;
   double t_total;
