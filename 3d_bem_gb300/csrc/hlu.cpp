@@ -174,19 +174,83 @@ int64_t min_rank(const std::vector<double>& sv, int64_t max_rank, double rel) {
 
 }  // namespace
 
+namespace {
+
+// Householder QR of X (rows x cols, column-major, in place): R in the upper
+// triangle, reflector j (unit 2-norm) in v[j * rows + j .. rows), so that
+// X = H_0 ... H_{p-1} [R; 0] with H_j = I - 2 v_j v_j^H.
+void householder_inplace(int64_t rows, int64_t cols, cd* X, cd* v) {
+  const int64_t p = std::min(rows, cols);
+  for (int64_t j = 0; j < p; j++) {
+    cd* x = X + j * rows;
+    double xn = 0;
+    for (int64_t i = j; i < rows; i++) xn += std::norm(x[i]);
+    xn = std::sqrt(xn);
+    cd* vj = v + j * rows;
+    for (int64_t i = j; i < rows; i++) vj[i] = x[i];
+    const cd x0 = x[j];
+    const cd ph = std::abs(x0) > 0 ? x0 / std::abs(x0) : cd(1.0);
+    vj[j] += ph * xn;
+    double vn = 0;
+    for (int64_t i = j; i < rows; i++) vn += std::norm(vj[i]);
+    vn = std::sqrt(vn);
+    if (vn > 0)
+      for (int64_t i = j; i < rows; i++) vj[i] /= vn;
+    for (int64_t c = j; c < cols; c++) {
+      cd* y = X + c * rows;
+      cd d = 0;
+      for (int64_t i = j; i < rows; i++) d += std::conj(vj[i]) * y[i];
+      d *= 2.0;
+      for (int64_t i = j; i < rows; i++) y[i] -= vj[i] * d;
+    }
+  }
+}
+
+// Y (rows x r, column-major) := H_0 ... H_{p-1} Y
+void apply_q(int64_t rows, int64_t p, const cd* v, int64_t r, cd* Y) {
+  for (int64_t j = p - 1; j >= 0; j--) {
+    const cd* vj = v + j * rows;
+    for (int64_t c = 0; c < r; c++) {
+      cd* y = Y + c * rows;
+      cd d = 0;
+      for (int64_t i = j; i < rows; i++) d += std::conj(vj[i]) * y[i];
+      d *= 2.0;
+      for (int64_t i = j; i < rows; i++) y[i] -= vj[i] * d;
+    }
+  }
+}
+
+// grow-only scratch of one thread (no allocation per truncation)
+struct TruncScratch {
+  std::vector<cd> xa, va, xb, vb, core, ct;
+  cd* get(std::vector<cd>& b, size_t n) {
+    if (b.size() < n) b.resize(n);
+    return b.data();
+  }
+};
+
+}  // namespace
+
 void rk_truncate(int64_t m, int64_t n, int64_t& k, std::vector<cd>& A, std::vector<cd>& B,
                  int64_t max_rank, double tol) {
   if (k == 0) return;
-  std::vector<cd> Qa, Ra, Qb, Rb;
-  qr_thin(m, k, A, Qa, Ra);
-  qr_thin(n, k, B, Qb, Rb);
+  thread_local TruncScratch ws;
+  // A = Qa Ra, B = Qb Rb (Householder, Q kept as reflectors)
+  cd* xa = ws.get(ws.xa, (size_t)(m * k));
+  cd* va = ws.get(ws.va, (size_t)(m * k));
+  cd* xb = ws.get(ws.xb, (size_t)(n * k));
+  cd* vb = ws.get(ws.vb, (size_t)(n * k));
+  std::copy(A.begin(), A.begin() + m * k, xa);
+  std::copy(B.begin(), B.begin() + n * k, xb);
+  householder_inplace(m, k, xa, va);
+  householder_inplace(n, k, xb, vb);
   const int64_t pa = std::min(m, k), pb = std::min(n, k);
-  // core = Ra Rb^T (pa x pb)
-  std::vector<cd> C(pa * pb, 0.0);
+  // core = Ra Rb^T (pa x pb); R entries (r, l) with r <= l
+  cd* C = ws.get(ws.core, (size_t)(pa * pb));
   for (int64_t c = 0; c < pb; c++)
     for (int64_t r = 0; r < pa; r++) {
       cd acc = 0;
-      for (int64_t l = 0; l < k; l++) acc += Ra[l * pa + r] * Rb[l * pb + c];
+      for (int64_t l = std::max(r, c); l < k; l++) acc += xa[l * m + r] * xb[l * n + c];
       C[c * pa + r] = acc;
     }
   // core = W diag(sig) Z^H with W pa x q, Z pb x q, q = min(pa, pb)
@@ -194,13 +258,13 @@ void rk_truncate(int64_t m, int64_t n, int64_t& k, std::vector<cd>& A, std::vect
   std::vector<cd> W, Z;
   const int64_t q = std::min(pa, pb);
   if (pa >= pb) {
-    jacobi_svd(pa, pb, C.data(), sig, W, Z);
+    jacobi_svd(pa, pb, C, sig, W, Z);
   } else {  // C^T = U' S V'^H  ->  C = conj(V') S U'^T
-    std::vector<cd> Ct(pb * pa);
+    cd* Ct = ws.get(ws.ct, (size_t)(pb * pa));
     for (int64_t c = 0; c < pb; c++)
       for (int64_t r = 0; r < pa; r++) Ct[r * pb + c] = C[c * pa + r];
     std::vector<cd> Up, Vp;
-    jacobi_svd(pb, pa, Ct.data(), sig, Up, Vp);
+    jacobi_svd(pb, pa, Ct, sig, Up, Vp);
     W.resize(pa * q);
     Z.resize(pb * q);
     for (size_t i = 0; i < W.size(); i++) W[i] = std::conj(Vp[i]);
@@ -208,20 +272,14 @@ void rk_truncate(int64_t m, int64_t n, int64_t& k, std::vector<cd>& A, std::vect
   }
   int64_t r = min_rank(sig, max_rank, tol);
   while (r > 0 && sig[r - 1] == 0.0) r--;  // exact zeros carry nothing
+  // A' = Qa [W S; 0], B' = Qb [conj(Z); 0] (A B^T = Qa W S Z^H Qb^T)
   std::vector<cd> An(m * r, 0.0), Bn(n * r, 0.0);
   for (int64_t l = 0; l < r; l++) {
-    for (int64_t i = 0; i < m; i++) {
-      cd acc = 0;
-      for (int64_t t = 0; t < pa; t++) acc += Qa[t * m + i] * W[l * pa + t];
-      An[l * m + i] = acc * sig[l];
-    }
-    // A B^T = Qa W S Z^H Qb^T, so column l of B is Qb conj(Z e_l)
-    for (int64_t j = 0; j < n; j++) {
-      cd acc = 0;
-      for (int64_t t = 0; t < pb; t++) acc += Qb[t * n + j] * std::conj(Z[l * pb + t]);
-      Bn[l * n + j] = acc;
-    }
+    for (int64_t t = 0; t < pa; t++) An[l * m + t] = W[l * pa + t] * sig[l];
+    for (int64_t t = 0; t < pb; t++) Bn[l * n + t] = std::conj(Z[l * pb + t]);
   }
+  apply_q(m, pa, va, r, An.data());
+  apply_q(n, pb, vb, r, Bn.data());
   A = std::move(An);
   B = std::move(Bn);
   k = r;
