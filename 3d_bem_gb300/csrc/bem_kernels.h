@@ -90,6 +90,23 @@ struct AcaArgs {
 
 constexpr int ACA_TAB_N = 12;  // rule-table bins per axis
 
+// Optional early exit of a launch: when every flag f[i * stride] (i < n) is
+// nonzero the kernels return at once. GMRES gates the operator products of its
+// Arnoldi steps with the right-hand sides' converged flags, so the steps it
+// runs past convergence (it checks on the host every few steps) cost no work.
+struct HmvGate {
+  const int* f;
+  int stride, n;
+};
+#ifdef __CUDACC__
+__device__ __forceinline__ bool gate_closed(const HmvGate& g) {
+  if (!g.f) return false;
+  for (int i = 0; i < g.n; i++)
+    if (!g.f[(int64_t)i * g.stride]) return false;
+  return true;
+}
+#endif
+
 struct HmvArgs {
   int precision;  // 0: double2 storage, 1: float2 storage
   int fp32_math;  // float2 storage only: 0 FP64 arithmetic, 1 FP32 products with
@@ -120,6 +137,7 @@ struct HmvArgs {
   // built from the block ranks; null = one CTA per far block
   const int2* vwork;
   int64_t nvwork;
+  HmvGate gate;  // null f: always run
 };
 
 void nearfield_upload_rules(const QuadRules& r, cudaStream_t s);

@@ -551,8 +551,11 @@ enum Arith { ARITH_FP64 = 0, ARITH_FP32 = 1, ARITH_TWOFLOAT = 2 };
 // products, FP32 products with compensated sums (inner GMRES operator), or
 // two-float products on the FP32 units (FP64-accurate refinement residual).
 // Complex-FP64 storage always uses FP64 arithmetic.
+// gate_flags: optional converged flags of the R right-hand sides (stride
+// GATE_STRIDE ints); the launch does no work when all are set (HmvGate).
+constexpr int GATE_STRIDE = (int)(sizeof(GmresState) / sizeof(int));
 void hmatvec_dev(bem_handle* h, int which, const double2* x, double2* y, int64_t R, int acc,
-                 int arith = ARITH_FP64) {
+                 int arith = ARITH_FP64, const int* gate_flags = nullptr) {
   require(which == 0 || which == 1, BEM_EINVAL, "which must be 0 (phi) or 1 (dPhi)");
   DevHM& m = h->hm[which];
   require(m.assembled, BEM_EINVAL, "matrix not assembled");
@@ -594,6 +597,7 @@ void hmatvec_dev(bem_handle* h, int which, const double2* x, double2* y, int64_t
     a.tf = h->dTf.p;
     a.vwork = m.vwork.p;
     a.nvwork = m.nvwork;
+    if (gate_flags) a.gate = HmvGate{gate_flags + r0 * GATE_STRIDE, GATE_STRIDE, (int)a.nrhs};
     h->launches += launch_hmatvec(a, h->stream);
   }
 }
@@ -850,7 +854,7 @@ bool build_hlu(bem_handle* h) {
 
 // w := U^{-1} L^{-1} w for R device vectors (LUPrecondidionedHMatrixWrapper's
 // two substitutions, gmres.h:134-147)
-void apply_precond(bem_handle* h, double2* w, int R) {
+void apply_precond(bem_handle* h, double2* w, int R, const int* gate_flags = nullptr) {
   const int64_t N = h->N;
   cudaStream_t s = h->stream;
   if (h->df_ok) {  // dataflow sweeps: w -> dP2 -> w, up to 8 vectors per launch
@@ -860,10 +864,12 @@ void apply_precond(bem_handle* h, double2* w, int R) {
     for (int r0 = 0; r0 < R; r0 += HLU_DF_MAX_R) {
       const int rc = std::min(HLU_DF_MAX_R, R - r0);
       double2* wr = w + (size_t)r0 * N;
+      const HmvGate gate = gate_flags ? HmvGate{gate_flags + r0 * GATE_STRIDE, GATE_STRIDE, rc}
+                                      : HmvGate{nullptr, 0, 0};
       h->launches += launch_hlu_df(h->dfL.view, h->dLl.p, h->dLd.p, h->hlu_prec, wr, h->dP2.p, N,
-                                   rc, ws, hp, s);
+                                   rc, ws, hp, s, gate);
       h->launches += launch_hlu_df(h->dfU.view, h->dUl.p, h->dUd.p, h->hlu_prec, h->dP2.p, wr, N,
-                                   rc, ws, hp, s);
+                                   rc, ws, hp, s, gate);
     }
     return;
   }
@@ -918,9 +924,13 @@ GmresResult gmres_core(bem_handle* h, const double2* b, double2* x, int R, doubl
     krylov_restart(a, 0, s);
     h->launches += 2;
     if (read_states(h) || total >= maxit) break;
+    // the operator products of an Arnoldi step are gated by the converged
+    // flags: the steps run past convergence before the next host check
+    // (every 8 steps) do no work
+    const int* done_flags = &g.st.p[0].done;
     for (int j = 0; j < g.m; j++) {
-      hmatvec_dev(h, 1, g.Vb.p + (int64_t)j * R * N, g.w.p, R, 0, f32);
-      if (pc) apply_precond(h, g.w.p, R);
+      hmatvec_dev(h, 1, g.Vb.p + (int64_t)j * R * N, g.w.p, R, 0, f32, done_flags);
+      if (pc) apply_precond(h, g.w.p, R, done_flags);
       krylov_orthogonalize(a, j, s);
       h->launches += 9;
       total++;

@@ -360,6 +360,7 @@ struct DfArgs {
   int* err;
   int64_t N;
   int R;
+  HmvGate gate;
   __device__ int* flagR(int i) const { return ctrl + 4 + i; }
   __device__ int* flagC(int j) const { return ctrl + 4 + p.D + j; }
   __device__ int* flagE(int i) const { return ctrl + 4 + 2 * p.D + i; }
@@ -882,6 +883,7 @@ template <typename T2>
 __global__ void __launch_bounds__(DT, 1) hlu_df_kernel(DfArgs a) {
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ int sq;
+  if (gate_closed(a.gate)) return;  // every block reads the same flags
   if (blockIdx.x == 0)
     df_driver<T2>(a, sm);
   else
@@ -908,7 +910,7 @@ int df_prepare() {  // max resident blocks, after raising the shared-memory limi
 
 int launch_hlu_df(const HluDfDev& p, const int64_t* leaves, const void* data, int precision,
                   const double2* w, double2* x, int64_t N, int R, const HluDfWork& ws, int helpers,
-                  cudaStream_t s) {
+                  cudaStream_t s, HmvGate gate) {
   if (p.D <= 0 || R <= 0) return 0;
   if (R > HLU_DF_MAX_R) throw std::runtime_error("launch_hlu_df: more than 8 right-hand sides");
   CUDA_OK(cudaMemsetAsync(ws.ctrl, 0, (size_t)(4 + 3 * p.D) * sizeof(int), s));
@@ -927,6 +929,7 @@ int launch_hlu_df(const HluDfDev& p, const int64_t* leaves, const void* data, in
   a.err = ws.err;
   a.N = N;
   a.R = R;
+  a.gate = gate;
   void* args[] = {&a};
   const int cap = precision == 0 ? df_prepare<double2>() : df_prepare<float2>();
   const int grid = std::max(2, std::min(1 + std::max(1, helpers), cap));

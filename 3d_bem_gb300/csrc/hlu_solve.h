@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "bem_kernels.h"
+
 namespace bemgpu {
 
 constexpr int HLU_MAX_RANK = 512;  // largest low-rank leaf of a factor
@@ -100,8 +102,9 @@ struct HluDfWork {
 
 // w (R x N) -> x (R x N) with one cooperative launch of 1 driver + `helpers`
 // CTAs (R <= HLU_DF_MAX_R; w is only read). Returns the kernels launched.
+// gate: optional early exit (bem_kernels.h HmvGate; all its flags set -> no work)
 int launch_hlu_df(const HluDfDev& p, const int64_t* leaves, const void* data, int precision,
                   const double2* w, double2* x, int64_t N, int R, const HluDfWork& ws, int helpers,
-                  cudaStream_t s);
+                  cudaStream_t s, HmvGate gate = HmvGate{nullptr, 0, 0});
 
 }  // namespace bemgpu

@@ -74,7 +74,8 @@ __global__ void __launch_bounds__(VT) hmv_vpass(const FarBlock* __restrict__ far
                                                 const T* __restrict__ Sp,
                                                 const double2* __restrict__ x, int64_t ldx,
                                                 double2* __restrict__ t, int64_t ldt,
-                                                const int2* __restrict__ vwork) {
+                                                const int2* __restrict__ vwork, HmvGate gate) {
+  if (gate_closed(gate)) return;
   int bi, lbeg, lend;
   vrange(vwork, rank, bi, lbeg, lend);
   const FarBlock fb = far[bi];
@@ -140,7 +141,8 @@ __global__ void __launch_bounds__(UT) hmv_upass(
     const int32_t* __restrict__ rank, const NearBlock* __restrict__ nearb,
     const T* __restrict__ Up, const T* __restrict__ F, const double2* __restrict__ x,
     int64_t ldx, const double2* __restrict__ t, int64_t ldt, double2* __restrict__ y,
-    int64_t ldy, int accumulate) {
+    int64_t ldy, int accumulate, HmvGate gate) {
+  if (gate_closed(gate)) return;
   __shared__ double2 part[UT / 32][32];
   const LeafRows lf = leaves[blockIdx.x];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -239,7 +241,8 @@ __global__ void __launch_bounds__(VT) hmv32_vpass(const FarBlock* __restrict__ f
                                                   const float2* __restrict__ Sp,
                                                   const float2* __restrict__ x, int64_t ldx,
                                                   float2* __restrict__ t, int64_t ldt,
-                                                  const int2* __restrict__ vwork) {
+                                                  const int2* __restrict__ vwork, HmvGate gate) {
+  if (gate_closed(gate)) return;
   int bi, lbeg, lend;
   vrange(vwork, rank, bi, lbeg, lend);
   const FarBlock fb = far[bi];
@@ -299,7 +302,8 @@ __global__ void __launch_bounds__(UT) hmv32_upass(
     const int32_t* __restrict__ rank, const NearBlock* __restrict__ nearb,
     const float2* __restrict__ Up, const float2* __restrict__ F, const float2* __restrict__ x,
     int64_t ldx, const float2* __restrict__ t, int64_t ldt, double2* __restrict__ y,
-    int64_t ldy, int accumulate) {
+    int64_t ldy, int accumulate, HmvGate gate) {
+  if (gate_closed(gate)) return;
   __shared__ float4 part[UT / 32][32];
   const LeafRows lf = leaves[blockIdx.x];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -376,23 +380,25 @@ __global__ void __launch_bounds__(UT) hmv32_upass(
 }
 
 __global__ void to_float_kernel(const double2* __restrict__ x, float2* __restrict__ xf,
-                                int64_t n) {
+                                int64_t n, HmvGate gate) {
+  if (gate_closed(gate)) return;
   const int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x;
   if (i < n) xf[i] = make_float2((float)x[i].x, (float)x[i].y);
 }
 
 template <int R>
 void launch32_r(const HmvArgs& a, cudaStream_t s) {
-  to_float_kernel<<<(unsigned)((a.ldx * R + 255) / 256), 256, 0, s>>>(a.x, a.xf, a.ldx * R);
+  to_float_kernel<<<(unsigned)((a.ldx * R + 255) / 256), 256, 0, s>>>(a.x, a.xf, a.ldx * R,
+                                                                      a.gate);
   const int64_t nv = a.vwork ? a.nvwork : a.nfar;
   if (nv > 0)
     hmv32_vpass<R><<<(unsigned)nv, VT, 0, s>>>(a.far, a.rank, (const float2*)a.V,
                                                (const float2*)a.S, a.xf, a.ldx, a.tf, a.ldt,
-                                               a.vwork);
+                                               a.vwork, a.gate);
   if (a.nleaves > 0)
     hmv32_upass<R><<<(unsigned)a.nleaves, UT, 0, s>>>(
         a.leaves, a.list_off, a.list, a.far, a.rank, a.nearb, (const float2*)a.U,
-        (const float2*)a.F, a.xf, a.ldx, a.tf, a.ldt, a.y, a.ldy, a.accumulate);
+        (const float2*)a.F, a.xf, a.ldx, a.tf, a.ldt, a.y, a.ldy, a.accumulate, a.gate);
 }
 
 void launch32(const HmvArgs& a, cudaStream_t s) {
@@ -414,11 +420,11 @@ void launch_r(const HmvArgs& a, cudaStream_t s) {
   if (nv > 0)
     hmv_vpass<T, F32, R><<<(unsigned)nv, VT, 0, s>>>(a.far, a.rank, (const T*)a.V,
                                                      (const T*)a.S, a.x, a.ldx, a.t, a.ldt,
-                                                     a.vwork);
+                                                     a.vwork, a.gate);
   if (a.nleaves > 0)
     hmv_upass<T, F32, R><<<(unsigned)a.nleaves, UT, 0, s>>>(
         a.leaves, a.list_off, a.list, a.far, a.rank, a.nearb, (const T*)a.U, (const T*)a.F, a.x,
-        a.ldx, a.t, a.ldt, a.y, a.ldy, a.accumulate);
+        a.ldx, a.t, a.ldt, a.y, a.ldy, a.accumulate, a.gate);
 }
 
 template <typename T, bool F32>
