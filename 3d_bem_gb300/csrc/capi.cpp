@@ -618,7 +618,9 @@ void ensure_gmres(bem_handle* h, int R) {
   g.h.ensure((size_t)R * (m + 1));
   g.y.ensure((size_t)R * m);
   g.cpart.ensure((size_t)nct * R * (m + 1));
-  g.npart.ensure((size_t)nct * R);
+  // norm partials: one per partial-sum CTA, or one per 256 elements (the
+  // fused Arnoldi update writes those)
+  g.npart.ensure((size_t)std::max<int64_t>(nct, (h->N + 255) / 256) * R);
   g.hnorm.ensure(R);
   g.st.ensure(R);
   g.hst.resize(R);
@@ -931,8 +933,7 @@ GmresResult gmres_core(bem_handle* h, const double2* b, double2* x, int R, doubl
     for (int j = 0; j < g.m; j++) {
       hmatvec_dev(h, 1, g.Vb.p + (int64_t)j * R * N, g.w.p, R, 0, f32, done_flags);
       if (pc) apply_precond(h, g.w.p, R, done_flags);
-      krylov_orthogonalize(a, j, s);
-      h->launches += 9;
+      h->launches += krylov_orthogonalize(a, j, s);
       total++;
       const bool last = (j == g.m - 1) || total >= maxit;
       if (((j + 1) % 8 == 0) || last) {

@@ -53,51 +53,6 @@ __global__ void __launch_bounds__(DT) dot_partial_kernel(const double2* __restri
   }
 }
 
-// h[r][q] = sum over CTAs; H column j += h (first pass sets it). One warp
-// per (r, q): lane l sums the partials l, l + 32, ... in order, then a fixed
-// shuffle tree, so the result does not depend on scheduling.
-__global__ void dot_reduce_kernel(const double2* __restrict__ partial, int nct, int R, int nq,
-                                  int m, int j, int first, const GmresState* __restrict__ st,
-                                  double2* __restrict__ h, double2* __restrict__ H) {
-  const int task = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (task >= R * nq) return;
-  const int r = task / nq, q = task % nq;
-  if (st[r].done) return;
-  double sx = 0, sy = 0;
-  for (int c = lane; c < nct; c += 32) {
-    const double2 v = partial[((int64_t)c * R + r) * nq + q];
-    sx += v.x;
-    sy += v.y;
-  }
-  sx = warp_sum(sx);
-  sy = warp_sum(sy);
-  if (lane == 0) {
-    const double2 s = make_double2(sx, sy);
-    h[r * nq + q] = s;
-    double2* Hc = H + ((int64_t)r * m + j) * (m + 1);
-    Hc[q] = first ? s : cadd(Hc[q], s);
-  }
-}
-
-// w[r][i] -= sum_q h[r][q] V[q][r][i]
-__global__ void __launch_bounds__(DT) axpy_kernel(const double2* __restrict__ Vb,
-                                                  double2* __restrict__ w, int64_t N, int R,
-                                                  int nq, const double2* __restrict__ h,
-                                                  const GmresState* __restrict__ st) {
-  const int r = blockIdx.y;
-  if (st[r].done) return;
-  const int64_t i = (int64_t)blockIdx.x * DT + threadIdx.x;
-  if (i >= N) return;
-  double2 acc = w[(int64_t)r * N + i];
-  for (int q = 0; q < nq; q++) {
-    double2 hv = h[r * nq + q];
-    double2 v = Vb[((int64_t)q * R + r) * N + i];
-    acc = csub(acc, cmul(hv, v));
-  }
-  w[(int64_t)r * N + i] = acc;
-}
-
 // partial squared norms of R vectors: partial[cta][r]
 __global__ void __launch_bounds__(DT) nrm_partial_kernel(const double2* __restrict__ w, int64_t N,
                                                          int R, int64_t chunk,
@@ -120,74 +75,126 @@ __global__ void __launch_bounds__(DT) nrm_partial_kernel(const double2* __restri
   }
 }
 
-// One thread per RHS: finish Arnoldi step j (subdiagonal, previous and new
-// Givens rotations, residual estimate, convergence flag).
-__global__ void finish_step_kernel(const double* __restrict__ partial, int nct, int R, int m,
-                                   int j, double tol, GmresState* __restrict__ st,
-                                   double2* __restrict__ H, double2* __restrict__ g,
-                                   double2* __restrict__ cs, double2* __restrict__ sn,
-                                   double* __restrict__ hnorm) {
-  // one warp per right-hand side: the lanes sum the CTA partials (fixed
-  // order per lane, fixed shuffle tree), lane 0 applies the rotations
-  const int r = blockIdx.x, lane = threadIdx.x;
-  if (r >= R) return;
-  GmresState s = st[r];
-  if (s.done) return;
+// Fused Arnoldi kernels: grid (ceil(N / DT), R), one right-hand side r per
+// blockIdx.y. Every CTA reduces the dot partials itself (one warp per q, lane
+// l sums partials l, l + 32, ... in order, fixed shuffle tree: the same sums
+// in every CTA), so no separate reduction launch sits between the passes.
+//
+// w[r] -= sum_q h[r][q] V[q][r] with h reduced from the partials; CTA x = 0
+// writes h into the Hessenberg column. With norm_out, the CTA also writes the
+// squared norm of its updated slice of w to norm_out[blockIdx.x * R + r].
+__global__ void __launch_bounds__(DT) reduce_axpy_kernel(
+    const double2* __restrict__ partial, int nct, const double2* __restrict__ Vb,
+    double2* __restrict__ w, int64_t N, int R, int nq, int m, int j, int first,
+    const GmresState* __restrict__ st, double2* __restrict__ H, double* __restrict__ norm_out) {
+  extern __shared__ double2 hs[];  // nq
+  __shared__ double red[DT / 32];
+  const int r = blockIdx.y;
+  if (st[r].done) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int q = warp; q < nq; q += DT / 32) {
+    double sx = 0, sy = 0;
+    for (int c = lane; c < nct; c += 32) {
+      const double2 v = partial[((int64_t)c * R + r) * nq + q];
+      sx += v.x;
+      sy += v.y;
+    }
+    sx = warp_sum(sx);
+    sy = warp_sum(sy);
+    if (lane == 0) {
+      const double2 sv = make_double2(sx, sy);
+      hs[q] = sv;
+      if (blockIdx.x == 0) {
+        double2* Hc = H + ((int64_t)r * m + j) * (m + 1);
+        Hc[q] = first ? sv : cadd(Hc[q], sv);
+      }
+    }
+  }
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * DT + threadIdx.x;
   double n2 = 0;
-  for (int c = lane; c < nct; c += 32) n2 += partial[(int64_t)c * R + r];
-  n2 = warp_sum(n2);
-  if (lane != 0) return;
-  const double hn = sqrt(n2);
-  hnorm[r] = hn;
-  double2* Hc = H + ((int64_t)r * m + j) * (m + 1);
-  double2* cr = cs + (int64_t)r * m;
-  double2* sr = sn + (int64_t)r * m;
-  double2* gr = g + (int64_t)r * (m + 1);
-  Hc[j + 1] = make_double2(hn, 0.0);
-  for (int q = 0; q < j; q++) {
-    double2 a = Hc[q], b = Hc[q + 1];
-    Hc[q] = cadd(cmul(cr[q], a), cmul(sr[q], b));
-    Hc[q + 1] = cadd(cscale(-1.0, cmul(cconj(sr[q]), a)), cmul(cr[q], b));
+  if (i < N) {
+    double2 acc = w[(int64_t)r * N + i];
+    for (int q = 0; q < nq; q++) acc = csub(acc, cmul(hs[q], Vb[((int64_t)q * R + r) * N + i]));
+    w[(int64_t)r * N + i] = acc;
+    n2 = cabs2(acc);
   }
-  double2 a = Hc[j], b = Hc[j + 1];
-  double aa = sqrt(cabs2(a));
-  double rho = sqrt(cabs2(a) + cabs2(b));
-  double2 c, sv;
-  if (aa == 0.0) {
-    c = make_double2(0, 0);
-    sv = make_double2(1, 0);
-  } else {
-    c = make_double2(aa / rho, 0.0);
-    sv = cscale(1.0 / (aa * rho), cmul(a, cconj(b)));
+  if (norm_out) {
+    n2 = warp_sum(n2);
+    if (lane == 0) red[warp] = n2;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0;
+      for (int q = 0; q < DT / 32; q++) t += red[q];
+      norm_out[(int64_t)blockIdx.x * R + r] = t;
+    }
   }
-  cr[j] = c;
-  sr[j] = sv;
-  Hc[j] = cadd(cmul(c, a), cmul(sv, b));
-  Hc[j + 1] = make_double2(0, 0);
-  double2 gj = gr[j];
-  gr[j + 1] = cscale(-1.0, cmul(cconj(sv), gj));
-  gr[j] = cmul(c, gj);
-  s.jcount = j + 1;
-  s.iters += 1;
-  s.resid = sqrt(cabs2(gr[j + 1])) / s.bnorm;
-  if (s.resid < tol || hn == 0.0) s.done = 1;
-  st[r] = s;
 }
 
-// V[j+1][r] = w[r] / hnorm[r]
-__global__ void __launch_bounds__(DT) scale_kernel(const double2* __restrict__ w,
-                                                   double2* __restrict__ vnext, int64_t N,
-                                                   const double* __restrict__ hnorm,
-                                                   const GmresState* __restrict__ st,
-                                                   int j) {
-  const int r = blockIdx.y;
-  // a RHS that converged at this very step (jcount == j+1) still gets its
-  // vector; it is not used afterwards
-  if (st[r].done && st[r].jcount != j + 1) return;
+// Finish Arnoldi step j and write V[j + 1] = w / ||w||: every CTA sums the
+// nct norm partials (warp 0, fixed order) for its scaling; CTA x = 0 also
+// applies the Givens rotations and updates the state (as finish_step_kernel).
+// A right-hand side that converges at this step may or may not get its next
+// vector written; it is not used afterwards.
+__global__ void __launch_bounds__(DT) finish_scale_kernel(
+    const double* __restrict__ partial, int nct, int R, int m, int j, double tol,
+    GmresState* __restrict__ st, double2* __restrict__ H, double2* __restrict__ g,
+    double2* __restrict__ cs, double2* __restrict__ sn, double* __restrict__ hnorm,
+    const double2* __restrict__ w, double2* __restrict__ vnext, int64_t N) {
+  __shared__ double hn_s;
+  const int r = blockIdx.y, lane = threadIdx.x & 31;
+  GmresState s = st[r];
+  if (s.done) return;
+  if (threadIdx.x < 32) {
+    double n2 = 0;
+    for (int c = lane; c < nct; c += 32) n2 += partial[(int64_t)c * R + r];
+    n2 = warp_sum(n2);
+    if (lane == 0) {
+      const double hn = sqrt(n2);
+      hn_s = hn;
+      if (blockIdx.x == 0) {
+        hnorm[r] = hn;
+        double2* Hc = H + ((int64_t)r * m + j) * (m + 1);
+        double2* cr = cs + (int64_t)r * m;
+        double2* sr = sn + (int64_t)r * m;
+        double2* gr = g + (int64_t)r * (m + 1);
+        Hc[j + 1] = make_double2(hn, 0.0);
+        for (int q = 0; q < j; q++) {
+          double2 a = Hc[q], b = Hc[q + 1];
+          Hc[q] = cadd(cmul(cr[q], a), cmul(sr[q], b));
+          Hc[q + 1] = cadd(cscale(-1.0, cmul(cconj(sr[q]), a)), cmul(cr[q], b));
+        }
+        double2 a = Hc[j], b = Hc[j + 1];
+        double aa = sqrt(cabs2(a));
+        double rho = sqrt(cabs2(a) + cabs2(b));
+        double2 c, sv;
+        if (aa == 0.0) {
+          c = make_double2(0, 0);
+          sv = make_double2(1, 0);
+        } else {
+          c = make_double2(aa / rho, 0.0);
+          sv = cscale(1.0 / (aa * rho), cmul(a, cconj(b)));
+        }
+        cr[j] = c;
+        sr[j] = sv;
+        Hc[j] = cadd(cmul(c, a), cmul(sv, b));
+        Hc[j + 1] = make_double2(0, 0);
+        double2 gj = gr[j];
+        gr[j + 1] = cscale(-1.0, cmul(cconj(sv), gj));
+        gr[j] = cmul(c, gj);
+        s.jcount = j + 1;
+        s.iters += 1;
+        s.resid = sqrt(cabs2(gr[j + 1])) / s.bnorm;
+        if (s.resid < tol || hn == 0.0) s.done = 1;
+        st[r] = s;
+      }
+    }
+  }
+  __syncthreads();
   const int64_t i = (int64_t)blockIdx.x * DT + threadIdx.x;
   if (i >= N) return;
-  const double hn = hnorm[r];
-  double2 v = w[(int64_t)r * N + i];
+  const double hn = hn_s;
+  const double2 v = w[(int64_t)r * N + i];
   vnext[(int64_t)r * N + i] = hn > 0 ? cscale(1.0 / hn, v) : make_double2(0, 0);
 }
 
@@ -284,23 +291,23 @@ int krylov_num_ctas(int64_t N) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(c, 608));
 }
 
-void krylov_orthogonalize(const KrylovArgs& a, int j, cudaStream_t s) {
+// CGS2 step j in five launches: dot partials, reduction + update (twice; the
+// second also takes the norm partials of w), then the Givens step + scaling
+int krylov_orthogonalize(const KrylovArgs& a, int j, cudaStream_t s) {
   const int nq = j + 1;
   const int nct = krylov_num_ctas(a.N);
   const int64_t chunk = (a.N + nct - 1) / nct;
+  const dim3 g((unsigned)((a.N + DT - 1) / DT), (unsigned)a.R);
+  const size_t hsm = (size_t)nq * sizeof(double2);
   for (int pass = 0; pass < 2; pass++) {
     dot_partial_kernel<<<nct, DT, 0, s>>>(a.Vb, a.w, a.N, a.R, nq, chunk, a.st, a.cpart);
-    int tasks = a.R * nq;
-    dot_reduce_kernel<<<(tasks + 3) / 4, 128, 0, s>>>(a.cpart, nct, a.R, nq, a.m, j, pass == 0,
-                                                      a.st, a.h, a.H);
-    dim3 g((unsigned)((a.N + DT - 1) / DT), (unsigned)a.R);
-    axpy_kernel<<<g, DT, 0, s>>>(a.Vb, a.w, a.N, a.R, nq, a.h, a.st);
+    reduce_axpy_kernel<<<g, DT, hsm, s>>>(a.cpart, nct, a.Vb, a.w, a.N, a.R, nq, a.m, j,
+                                          pass == 0, a.st, a.H, pass == 1 ? a.npart : nullptr);
   }
-  nrm_partial_kernel<<<nct, DT, 0, s>>>(a.w, a.N, a.R, chunk, a.npart);
-  finish_step_kernel<<<a.R, 32, 0, s>>>(a.npart, nct, a.R, a.m, j, a.tol, a.st, a.H, a.g, a.cs,
-                                        a.sn, a.hnorm);
-  dim3 g((unsigned)((a.N + DT - 1) / DT), (unsigned)a.R);
-  scale_kernel<<<g, DT, 0, s>>>(a.w, a.Vb + (int64_t)(j + 1) * a.R * a.N, a.N, a.hnorm, a.st, j);
+  finish_scale_kernel<<<g, DT, 0, s>>>(a.npart, (int)g.x, a.R, a.m, j, a.tol, a.st, a.H, a.g,
+                                       a.cs, a.sn, a.hnorm, a.w,
+                                       a.Vb + (int64_t)(j + 1) * a.R * a.N, a.N);
+  return 5;
 }
 
 void krylov_restart(const KrylovArgs& a, int init, cudaStream_t s) {

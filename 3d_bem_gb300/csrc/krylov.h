@@ -36,7 +36,8 @@ struct KrylovArgs {
 };
 
 int krylov_num_ctas(int64_t N);
-void krylov_orthogonalize(const KrylovArgs& a, int j, cudaStream_t s);
+// one CGS2 Arnoldi step j on a.w; returns the kernels launched
+int krylov_orthogonalize(const KrylovArgs& a, int j, cudaStream_t s);
 void krylov_restart(const KrylovArgs& a, int init, cudaStream_t s);
 void krylov_residual(const double2* b, double2* w, int64_t n, cudaStream_t s);
 // partial[cta][r] = squared norm of v[r] over the CTA's chunk (krylov_num_ctas CTAs)
