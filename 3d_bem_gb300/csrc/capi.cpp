@@ -113,6 +113,7 @@ struct bem_handle {
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;  // second stream for concurrent ACA launches
   cudaStream_t nearst = nullptr;  // near-field assembly, concurrent with ACA
+  int nsm = 152;                  // streaming multiprocessors of the device
   cudaEvent_t fork = nullptr, join = nullptr;
   int64_t launches = 0;
   // mesh
@@ -221,14 +222,24 @@ cplx coupling_parameter(int kind, double k) {
 }
 
 // ACA size bin: the far blocks (sorted by m + n, largest first) with
-// m + n >= thr get the 512-thread ACA kernel (0: the default threshold)
+// m + n >= thr get the 512-thread ACA kernel. thr <= 0: every block with
+// m + n >= 2048, and besides them the largest blocks with m + n >= 512 up to
+// half the SM count -- the few long rank loops start at once on their own
+// SMs while the 128-thread kernel fills the rest (sphere 20,480: 76 blocks,
+// ACA 19.5 ms; thresholds 512 / 1024 / 3072: 21.1 / 20.4 / 34.6 ms).
 void set_big_mn(bem_handle* h, int64_t thr) {
   Layout& L = h->L;
-  if (thr <= 0) thr = ACA_BIG_MN;
-  L.nbig = 0;
-  while (L.nbig < (int64_t)L.far_order.size() &&
-         (int64_t)L.far[L.far_order[L.nbig]].m + L.far[L.far_order[L.nbig]].n >= thr)
-    L.nbig++;
+  const int64_t nf = (int64_t)L.far_order.size();
+  auto count = [&](int64_t t) {
+    int64_t c = 0;
+    while (c < nf && (int64_t)L.far[L.far_order[c]].m + L.far[L.far_order[c]].n >= t) c++;
+    return c;
+  };
+  if (thr > 0) {
+    L.nbig = count(thr);
+    return;
+  }
+  L.nbig = std::max(count(4 * ACA_BIG_MN), std::min<int64_t>(count(ACA_BIG_MN), h->nsm / 2));
 }
 
 void upload_layout(bem_handle* h) {
@@ -1266,9 +1277,9 @@ void autotune(bem_handle* h, double freq, int64_t nrhs) {
           "mesh and boundary conditions must be set");
   require(freq > 0 && std::isfinite(freq) && nrhs >= 1, BEM_EINVAL, "bad probe");
   // ACA size bin: the threshold with the shortest ACA phase (best of two)
-  int64_t best_thr = h->cfg.aca_big_mn > 0 ? h->cfg.aca_big_mn : ACA_BIG_MN;
+  int64_t best_thr = h->cfg.aca_big_mn;
   double best_t = 1e300;
-  for (int64_t thr : {256, 512, 1024}) {
+  for (int64_t thr : {0, 256, 512, 1024, 2048}) {  // 0: the size rule of set_big_mn
     set_big_mn(h, thr);
     double t = 1e300;
     for (int rep = 0; rep < 2; rep++) {
@@ -1354,6 +1365,7 @@ bem_status bem_create(const bem_config* cfg, bem_handle** out) {
     require(h->cfg.precond_reuse >= 0 && std::isfinite(h->cfg.precond_reuse), BEM_EINVAL,
             "precond_reuse must be finite and >= 0");
     CK(cudaGetDevice(&h->device));
+    CK(cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->device));
     // the near-field stream at the highest priority: its short, FP64-bound
     // blocks go first while the ACA blocks fill the remaining slots
     int prio_low = 0, prio_high = 0;

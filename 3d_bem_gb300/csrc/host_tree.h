@@ -62,7 +62,7 @@ struct Layout {
   std::vector<NearBlock> near;
   std::vector<FarBlock> far;
   std::vector<int32_t> far_order;   // launch order (largest first)
-  int64_t nbig = 0;                 // leading far_order entries with m + n >= ACA_BIG_MN
+  int64_t nbig = 0;                 // leading far_order entries on the 512-thread ACA kernel
   std::vector<NearTile> tiles;
   std::vector<uint32_t> special_bits;
   std::vector<int64_t> sp_entry;

@@ -69,7 +69,9 @@ typedef struct bem_config {
   int64_t sweep_workers;   /* bem_sweep: frequencies solved concurrently, each
                               worker on its own stream (0: autotuned) */
   int64_t aca_big_mn;      /* ACA size bin: blocks with m + n >= this get the
-                              512-thread kernel (0: 512, or autotuned) */
+                              512-thread kernel (0: the blocks with m + n >=
+                              2048 plus the largest ones with m + n >= 512
+                              up to half the SM count; or autotuned) */
   double precond_reuse;    /* > 1: a solve keeps the H-LU factors of an earlier
                               frequency f0 while max(f / f0, f0 / f) <= this
                               (frequency sweeps; GMRES still converges to the
