@@ -14,6 +14,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -674,20 +675,29 @@ bool read_states(bem_handle* h) {
 
 // ---- H-LU preconditioner ----
 
-// copy of the stored pool [off, off + cnt) as complex FP64
-void pool_to_host(const DevHM& m, const DBuf<unsigned char>& src, size_t total,
-                  std::vector<cplx>& out, cudaStream_t s) {
-  out.resize(total);
-  if (!total) return;
-  if (m.prec == 0) {
-    CK(cudaMemcpyAsync(out.data(), src.p, total * sizeof(double2), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    return;
+// host copy of a stored pool in its storage type (complex FP64 or FP32),
+// left uninitialized before the copy; at() reads one value as complex FP64
+struct HostPool {
+  std::unique_ptr<unsigned char[]> buf;
+  int prec = 0;
+  cplx at(int64_t i) const {
+    if (prec == 0) {
+      const double2 v = reinterpret_cast<const double2*>(buf.get())[i];
+      return cplx(v.x, v.y);
+    }
+    const float2 v = reinterpret_cast<const float2*>(buf.get())[i];
+    return cplx(v.x, v.y);
   }
-  std::vector<float2> tmp(total);
-  CK(cudaMemcpyAsync(tmp.data(), src.p, total * sizeof(float2), cudaMemcpyDeviceToHost, s));
+};
+
+void pool_to_host(const DevHM& m, const DBuf<unsigned char>& src, size_t total, HostPool& out,
+                  cudaStream_t s) {
+  out.prec = m.prec;
+  const size_t bytes = total * (m.prec == 0 ? sizeof(double2) : sizeof(float2));
+  out.buf.reset(new unsigned char[std::max<size_t>(bytes, 1)]);
+  if (!total) return;
+  CK(cudaMemcpyAsync(out.buf.get(), src.p, bytes, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
-  for (size_t i = 0; i < total; i++) out[i] = cplx(tmp[i].x, tmp[i].y);
 }
 
 template <typename T>
@@ -723,7 +733,8 @@ void upload_df_plans(bem_handle* h) {
       upload_bytes(d.diag, p.diag, s);
     } else {
       std::vector<float2> fd(p.diag.size());
-      for (size_t i = 0; i < fd.size(); i++)
+#pragma omp parallel for schedule(static)
+      for (int64_t i = 0; i < (int64_t)fd.size(); i++)
         fd[i] = make_float2((float)p.diag[i].real(), (float)p.diag[i].imag());
       upload_bytes(d.diag, fd, s);
       CK(cudaStreamSynchronize(s));  // fd goes out of scope
@@ -780,7 +791,7 @@ bool build_hlu(bem_handle* h) {
   DevHM& m = h->hm[1];
   const Layout& L = h->L;
   cudaStream_t s = h->stream;
-  std::vector<cplx> F, U, V, S;
+  HostPool F, U, V, S;
   pool_to_host(m, m.F, L.near_entries, F, s);
   pool_to_host(m, m.U, L.u_size, U, s);
   pool_to_host(m, m.V, L.v_size, V, s);
@@ -796,7 +807,8 @@ bool build_hlu(bem_handle* h) {
     InBlock& ib = in[i];
     if (!b.adm) {
       const NearBlock& nbk = L.near[near_of[i]];
-      ib.F.assign(F.begin() + nbk.off, F.begin() + nbk.off + b.m * b.n);
+      ib.F.resize(b.m * b.n);
+      for (int64_t e = 0; e < b.m * b.n; e++) ib.F[e] = F.at(nbk.off + e);
       continue;
     }
     const FarBlock& fb = L.far[far_of[i]];
@@ -806,9 +818,9 @@ bool build_hlu(bem_handle* h) {
     ib.A.resize(b.m * k);
     ib.B.resize(b.n * k);
     for (int64_t l = 0; l < k; l++) {
-      const cplx sl = S[fb.soff + l];
-      for (int64_t r = 0; r < b.m; r++) ib.A[l * b.m + r] = U[fb.uoff + l * b.m + r] * sl;
-      for (int64_t c = 0; c < b.n; c++) ib.B[l * b.n + c] = V[fb.voff + l * b.n + c];
+      const cplx sl = S.at(fb.soff + l);
+      for (int64_t r = 0; r < b.m; r++) ib.A[l * b.m + r] = U.at(fb.uoff + l * b.m + r) * sl;
+      for (int64_t c = 0; c < b.n; c++) ib.B[l * b.n + c] = V.at(fb.voff + l * b.n + c);
     }
     rk_truncate(b.m, b.n, ib.k, ib.A, ib.B, h->cfg.precond_rank, h->cfg.precond_tol);
   }
@@ -848,7 +860,8 @@ bool build_hlu(bem_handle* h) {
                            cudaMemcpyHostToDevice, s));
     } else {
       std::vector<float2> fd(f.data.size());
-      for (size_t i = 0; i < fd.size(); i++)
+#pragma omp parallel for schedule(static)
+      for (int64_t i = 0; i < (int64_t)fd.size(); i++)
         fd[i] = make_float2((float)f.data[i].real(), (float)f.data[i].imag());
       dd.ensure(fd.size() * sizeof(float2));
       if (!fd.empty())
