@@ -75,9 +75,10 @@ __global__ void __launch_bounds__(VT) hmv_vpass(const FarBlock* __restrict__ far
                                                 const double2* __restrict__ x, int64_t ldx,
                                                 double2* __restrict__ t, int64_t ldt,
                                                 const int2* __restrict__ vwork, HmvGate gate) {
-  if (gate_closed(gate)) return;
   int bi, lbeg, lend;
   vrange(vwork, rank, bi, lbeg, lend);
+  if (gate_closed(gate)) lend = lbeg;  // an empty range, not an early return: the
+                                       // kernel keeps its load scheduling
   const FarBlock fb = far[bi];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int l = lbeg + w; l < lend; l += VT / 32) {
@@ -142,9 +143,9 @@ __global__ void __launch_bounds__(UT) hmv_upass(
     const T* __restrict__ Up, const T* __restrict__ F, const double2* __restrict__ x,
     int64_t ldx, const double2* __restrict__ t, int64_t ldt, double2* __restrict__ y,
     int64_t ldy, int accumulate, HmvGate gate) {
-  if (gate_closed(gate)) return;
   __shared__ double2 part[UT / 32][32];
-  const LeafRows lf = leaves[blockIdx.x];
+  LeafRows lf = leaves[blockIdx.x];
+  if (gate_closed(gate)) lf.size = 0;  // no rows (see the V pass)
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int beg = list_off[blockIdx.x], end = list_off[blockIdx.x + 1];
   for (int base = 0; base < lf.size; base += 32) {
@@ -242,9 +243,10 @@ __global__ void __launch_bounds__(VT) hmv32_vpass(const FarBlock* __restrict__ f
                                                   const float2* __restrict__ x, int64_t ldx,
                                                   float2* __restrict__ t, int64_t ldt,
                                                   const int2* __restrict__ vwork, HmvGate gate) {
-  if (gate_closed(gate)) return;
   int bi, lbeg, lend;
   vrange(vwork, rank, bi, lbeg, lend);
+  if (gate_closed(gate)) lend = lbeg;  // an empty range, not an early return: the
+                                       // kernel keeps its load scheduling
   const FarBlock fb = far[bi];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // each warp streams G rows of V at once (G independent loads in flight per
@@ -303,9 +305,9 @@ __global__ void __launch_bounds__(UT) hmv32_upass(
     const float2* __restrict__ Up, const float2* __restrict__ F, const float2* __restrict__ x,
     int64_t ldx, const float2* __restrict__ t, int64_t ldt, double2* __restrict__ y,
     int64_t ldy, int accumulate, HmvGate gate) {
-  if (gate_closed(gate)) return;
   __shared__ float4 part[UT / 32][32];
-  const LeafRows lf = leaves[blockIdx.x];
+  LeafRows lf = leaves[blockIdx.x];
+  if (gate_closed(gate)) lf.size = 0;  // no rows (see the V pass)
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int beg = list_off[blockIdx.x], end = list_off[blockIdx.x + 1];
   for (int base = 0; base < lf.size; base += 32) {
@@ -381,9 +383,8 @@ __global__ void __launch_bounds__(UT) hmv32_upass(
 
 __global__ void to_float_kernel(const double2* __restrict__ x, float2* __restrict__ xf,
                                 int64_t n, HmvGate gate) {
-  if (gate_closed(gate)) return;
   const int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x;
-  if (i < n) xf[i] = make_float2((float)x[i].x, (float)x[i].y);
+  if (i < n && !gate_closed(gate)) xf[i] = make_float2((float)x[i].x, (float)x[i].y);
 }
 
 template <int R>
