@@ -13,6 +13,8 @@
 // Hessenberg column j of RHS r: H[(r * m + j) * (m + 1) + i].
 #include "bem_kernels.h"
 #include "krylov.h"
+
+#include <algorithm>
 #include "quadrature.cuh"
 
 namespace bemgpu {
@@ -26,7 +28,10 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// partial[cta][r][q] = sum_{i in chunk} conj(V[q][r][i]) w[r][i]
+// partial[cta][r][q] = sum_{i in chunk} conj(V[q][r][i]) w[r][i]; grid
+// (chunks, task groups): the (q, r) dot products of a chunk are spread over
+// gridDim.y CTAs, one warp each, so long bases (many q) at small N do not
+// queue on the few CTAs of the chunks
 __global__ void __launch_bounds__(DT) dot_partial_kernel(const double2* __restrict__ Vb,
                                                          const double2* __restrict__ w, int64_t N,
                                                          int R, int nq, int64_t chunk,
@@ -35,7 +40,7 @@ __global__ void __launch_bounds__(DT) dot_partial_kernel(const double2* __restri
   const int64_t i0 = (int64_t)blockIdx.x * chunk;
   const int64_t i1 = min(N, i0 + chunk);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int task = warp; task < nq * R; task += DT / 32) {
+  for (int task = blockIdx.y * (DT / 32) + warp; task < nq * R; task += gridDim.y * (DT / 32)) {
     const int q = task / R, r = task % R;
     double sx = 0, sy = 0;
     if (!st[r].done) {
@@ -92,23 +97,59 @@ __global__ void __launch_bounds__(DT) reduce_axpy_kernel(
   const int r = blockIdx.y;
   if (st[r].done) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int q = warp; q < nq; q += DT / 32) {
-    double sx = 0, sy = 0;
-    for (int c = lane; c < nct; c += 32) {
-      const double2 v = partial[((int64_t)c * R + r) * nq + q];
-      sx += v.x;
-      sy += v.y;
-    }
-    sx = warp_sum(sx);
-    sy = warp_sum(sy);
-    if (lane == 0) {
-      const double2 sv = make_double2(sx, sy);
-      hs[q] = sv;
-      if (blockIdx.x == 0) {
-        double2* Hc = H + ((int64_t)r * m + j) * (m + 1);
-        Hc[q] = first ? sv : cadd(Hc[q], sv);
+  // many partials: one warp per q, lanes over the partials, fixed shuffle
+  // tree; few partials (small N): one thread per q, four interleaved
+  // accumulators in a fixed order (coalesced over q), so long bases do not
+  // queue q by q on the warps
+  const int64_t cstride = (int64_t)R * nq;
+  if (nct >= 64) {
+    for (int q = warp; q < nq; q += DT / 32) {
+      double sx = 0, sy = 0;
+      for (int c = lane; c < nct; c += 32) {
+        const double2 v = partial[c * cstride + (int64_t)r * nq + q];
+        sx += v.x;
+        sy += v.y;
+      }
+      sx = warp_sum(sx);
+      sy = warp_sum(sy);
+      if (lane == 0) {
+        const double2 sv = make_double2(sx, sy);
+        hs[q] = sv;
+        if (blockIdx.x == 0) {
+          double2* Hc = H + ((int64_t)r * m + j) * (m + 1);
+          Hc[q] = first ? sv : cadd(Hc[q], sv);
+        }
       }
     }
+  } else {
+  for (int q = threadIdx.x; q < nq; q += DT) {
+    const double2* pq = partial + (int64_t)r * nq + q;
+    double a0 = 0, a1 = 0, a2 = 0, a3 = 0, b0 = 0, b1 = 0, b2 = 0, b3 = 0;
+    int c = 0;
+    for (; c + 4 <= nct; c += 4) {
+      const double2 v0 = pq[c * cstride], v1 = pq[(c + 1) * cstride];
+      const double2 v2 = pq[(c + 2) * cstride], v3 = pq[(c + 3) * cstride];
+      a0 += v0.x;
+      b0 += v0.y;
+      a1 += v1.x;
+      b1 += v1.y;
+      a2 += v2.x;
+      b2 += v2.y;
+      a3 += v3.x;
+      b3 += v3.y;
+    }
+    for (; c < nct; c++) {
+      const double2 v = pq[c * cstride];
+      a0 += v.x;
+      b0 += v.y;
+    }
+    const double2 sv = make_double2((a0 + a1) + (a2 + a3), (b0 + b1) + (b2 + b3));
+    hs[q] = sv;
+    if (blockIdx.x == 0) {
+      double2* Hc = H + ((int64_t)r * m + j) * (m + 1);
+      Hc[q] = first ? sv : cadd(Hc[q], sv);
+    }
+  }
   }
   __syncthreads();
   const int64_t i = (int64_t)blockIdx.x * DT + threadIdx.x;
@@ -299,8 +340,11 @@ int krylov_orthogonalize(const KrylovArgs& a, int j, cudaStream_t s) {
   const int64_t chunk = (a.N + nct - 1) / nct;
   const dim3 g((unsigned)((a.N + DT - 1) / DT), (unsigned)a.R);
   const size_t hsm = (size_t)nq * sizeof(double2);
+  // task groups: about two (q, r) dot products per warp
+  const int tg = std::max(1, std::min(128, (nq * a.R + 2 * (DT / 32) - 1) / (2 * (DT / 32))));
   for (int pass = 0; pass < 2; pass++) {
-    dot_partial_kernel<<<nct, DT, 0, s>>>(a.Vb, a.w, a.N, a.R, nq, chunk, a.st, a.cpart);
+    dot_partial_kernel<<<dim3((unsigned)nct, (unsigned)tg), DT, 0, s>>>(a.Vb, a.w, a.N, a.R, nq,
+                                                                        chunk, a.st, a.cpart);
     reduce_axpy_kernel<<<g, DT, hsm, s>>>(a.cpart, nct, a.Vb, a.w, a.N, a.R, nq, a.m, j,
                                           pass == 0, a.st, a.H, pass == 1 ? a.npart : nullptr);
   }
