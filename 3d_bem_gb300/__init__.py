@@ -40,7 +40,7 @@ EXPORTS = [
     "bem_hlu_build", "bem_hlu_solve", "bem_hlu_export", "bem_hlu_sweep_kind", "bem_recompress",
     "bem_sel_nparam", "bem_sel_label", "bem_mlp_grad", "bem_mlp_adam", "bem_mlp_forward",
     "bem_sel_infer", "bem_set_selector", "bem_sel_stats", "bem_sel_classes", "bem_autotune",
-    "bem_set_aca_rules", "bem_set_bc_impedance",
+    "bem_set_aca_rules", "bem_set_bc_impedance", "bem_field", "bem_field_device",
 ]
 BEM_ARITH_FP64, BEM_ARITH_FP32, BEM_ARITH_TWOFLOAT = 0, 1, 2
 
@@ -140,6 +140,8 @@ def lib():
     L.bem_autotune.argtypes = [vp, dbl, i64, vp]
     L.bem_set_aca_rules.argtypes = [vp, vp, vp]
     L.bem_set_bc_impedance.argtypes = [vp, vp]
+    L.bem_field.argtypes = [vp, dbl, vp, i64, vp, vp, i64, vp, i64, vp, vp]
+    L.bem_field_device.argtypes = [vp, dbl, vp, i64, vp, vp, i64, vp, i64, vp, vp]
     L.bem_hlu_build.argtypes = [vp]
     L.bem_hlu_solve.argtypes = [vp, vp, vp, i64]
     L.bem_hlu_export.argtypes = [vp, i32, P(i64), vp, P(i64), vp, P(i64), vp]
@@ -454,6 +456,35 @@ class Solver:
             self._check(st, "bem_sweep")
         return p, [i.as_dict() for i in infos]
 
+    def field(self, freq: float, pts, phi, dphi, sources=None):
+        """Velocity potential and sound pressure (npts x R each) at the
+        observation points ``pts`` from a boundary solution phi, dphi (n x R,
+        caller order); ``sources``: rows (x, y, z, complex weight)."""
+        pts = np.ascontiguousarray(pts, np.float64).reshape(-1, 3)
+        phi = np.asarray(phi, np.complex128)
+        n = self.n or phi.shape[0]
+        phi = np.asfortranarray(phi.reshape(n, -1))
+        dphi = np.asfortranarray(np.asarray(dphi, np.complex128).reshape(n, -1))
+        R = phi.shape[1]
+        src = _sources(sources)
+        pf = np.zeros((pts.shape[0], R), np.complex128, order="F")
+        pp = np.zeros((pts.shape[0], R), np.complex128, order="F")
+        self._check(lib().bem_field(self._h, freq, _ptr(pts), pts.shape[0], _ptr(phi), _ptr(dphi),
+                                    R, _ptr(src) if src.shape[0] else None, src.shape[0],
+                                    _ptr(pf), _ptr(pp)), "bem_field")
+        return pf, pp
+
+    def field_device(self, freq: float, pts_ptr: int, npts: int, phi_ptr: int, dphi_ptr: int,
+                     R: int, phi_f_ptr=0, p_f_ptr=0, sources=None):
+        """bem_field_device on raw device pointers (asynchronous on the
+        handle's stream)."""
+        src = _sources(sources)
+        self._check(lib().bem_field_device(
+            self._h, freq, ct.c_void_p(pts_ptr), npts, ct.c_void_p(phi_ptr),
+            ct.c_void_p(dphi_ptr), R, _ptr(src) if src.shape[0] else None, src.shape[0],
+            ct.c_void_p(phi_f_ptr) if phi_f_ptr else None,
+            ct.c_void_p(p_f_ptr) if p_f_ptr else None), "bem_field_device")
+
     def points_assemble(self, rowpts, colpts, k):
         rowpts = np.ascontiguousarray(rowpts, np.float64)
         colpts = np.ascontiguousarray(colpts, np.float64)
@@ -466,6 +497,14 @@ class Solver:
 
     def launch_count(self) -> int:
         return int(lib().bem_launch_count(self._h))
+
+
+def _sources(sources) -> np.ndarray:
+    """Point sources (x, y, z, complex weight) as the C-ABI's nsrc x 5 rows."""
+    if sources is None or len(sources) == 0:
+        return np.zeros((0, 5))
+    s = np.asarray(sources, np.complex128).reshape(-1, 4)
+    return np.ascontiguousarray(np.column_stack([s[:, :3].real, s[:, 3].real, s[:, 3].imag]))
 
 
 # ---------------------------------------------------------------------------
@@ -501,18 +540,40 @@ class BoundaryElements:
 
 
 @dataclass
+class ObservationField:
+    """ObservationField (ObservationScript/observationfield.h): observation
+    triangles (M x 9); the field is evaluated at their midpoints."""
+    triangles: np.ndarray
+    phiSolution: np.ndarray | None = None
+    soundPressure: np.ndarray | None = None
+
+    def calculateTrianglesMidpoints(self) -> np.ndarray:
+        """observationfield.cpp:4-11 with global::midpointOfTriangle
+        (global.cpp:910-913): (node1 + node2 + node3) / 3."""
+        t = np.asarray(self.triangles, np.float64).reshape(-1, 9)
+        return (t[:, 0:3] + t[:, 3:6] + t[:, 6:9]) / 3.0
+
+
+@dataclass
 class BoundaryElementSolver:
     """Mirror of BoundaryElementSolver (boundaryelementsolver.h) for the
     H-matrix path: set ``boundaryElements``, ``frequency``, ``waveSpeed``,
-    ``airDensity`` and call :meth:`calculateBoundarySolution`."""
+    ``airDensity`` and call :meth:`calculateBoundarySolution`; then
+    :meth:`calculateFieldSolution` fills ``observationFields``.
+    ``pointSources``: rows (x, y, z, complex weight)."""
     boundaryElements: BoundaryElements
     frequency: float
     waveSpeed: float = 343.0
     airDensity: float = 1.2041
     bemSolverParameters: BemSolverParameters = field(default_factory=BemSolverParameters)
+    observationFields: list = field(default_factory=list)
+    pointSources: list = field(default_factory=list)
     info: dict | None = None
+    _s: "Solver | None" = field(default=None, repr=False)
 
     def _solver(self) -> Solver:
+        if self._s is not None:
+            return self._s
         p = self.bemSolverParameters
         if not p.hMatSolving:
             raise BemError(BEM_EINVAL, "only the H-matrix path is accelerated")
@@ -525,6 +586,7 @@ class BoundaryElementSolver:
                    precond_rank=p.preconditionerRank, precond_tol=p.preconditionerRelError)
         s.set_mesh(self.boundaryElements.triangles)
         s.set_bc(self.boundaryElements.a, self.boundaryElements.b)
+        self._s = s
         return s
 
     def calculateBoundarySolution(self):
@@ -533,10 +595,27 @@ class BoundaryElementSolver:
         be = self.boundaryElements
         be.phiSolution, be.dPhiSolution, be.soundPressure = phi[:, 0], dphi[:, 0], p[:, 0]
         self.info = info
-        s.close()
         return info
 
     hMatrixSolve = calculateBoundarySolution
+
+    def calculateFieldSolution(self):
+        """calculateFieldSolution (boundaryelementsolver.cpp:2192-2249):
+        phiSolution and soundPressure of every observation field from the
+        boundary solution and the point sources (bem_field)."""
+        be = self.boundaryElements
+        if be.phiSolution is None or be.dPhiSolution is None:
+            raise BemError(BEM_EINVAL, "no boundary solution")
+        s = self._solver()
+        for f in self.observationFields:
+            pf, pp = s.field(self.frequency, f.calculateTrianglesMidpoints(), be.phiSolution,
+                             be.dPhiSolution, self.pointSources)
+            f.phiSolution, f.soundPressure = pf[:, 0], pp[:, 0]
+
+    def close(self):
+        if self._s is not None:
+            self._s.close()
+            self._s = None
 
 
 class HMatrix:

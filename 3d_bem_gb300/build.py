@@ -25,7 +25,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["nearfield.cu", "aca.cu", "hmatvec.cu", "krylov.cu", "post.cu", "hlu_solve.cu", "recompress.cu",
-              "selector.cu"]
+              "selector.cu", "field.cu"]
 CPP_SOURCES = ["host_tree.cpp", "hlu.cpp", "capi.cpp"]
 
 

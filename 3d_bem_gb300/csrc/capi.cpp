@@ -28,6 +28,7 @@
 #include "selector.h"
 #include "host_tree.h"
 #include "krylov.h"
+#include "field.h"
 #include "post.h"
 
 using namespace bemgpu;
@@ -182,6 +183,12 @@ struct bem_handle {
   DBuf<unsigned char> dfPre, dfFin;
   DBuf<int> dfCtrl, dfErr;
   DBuf<int> dBad;
+  // field evaluation (bem_field): element records, coefficients, partial
+  // sums, copies of the caller's points / boundary data / sources
+  DBuf<FieldElemF> dFe;
+  DBuf<unsigned char> dFcoef;
+  DBuf<double2> dFpart, dFphi, dFdphi, dFout1, dFout2;
+  DBuf<double> dFpts, dFsrc;
   QuadRules rules{};
   cudaEvent_t ev[10]{};
 };
@@ -1953,6 +1960,91 @@ bem_status bem_gmres(bem_handle* h, const double* b, double* x, int64_t nrhs, be
   });
   if (info) *info = loc;
   return st != BEM_OK ? st : loc.status;
+}
+
+namespace {
+
+// ---- field evaluation ----
+
+// Element chunks of the field sum: enough CTAs for about eight per SM, chunks
+// of at least 512 elements.
+int field_split(const bem_handle* h, int64_t M) {
+  const int64_t bx = (M + FIELD_PTS - 1) / FIELD_PTS;
+  const int64_t want = (8LL * h->nsm + bx - 1) / bx;
+  const int64_t most = std::max<int64_t>(1, h->N / 512);
+  return (int)std::max<int64_t>(1, std::min<int64_t>({want, most, 256}));
+}
+
+// calculateFieldSolution (boundaryelementsolver.cpp:2192-2249) on device
+// buffers: pts M x 3, phi / dphi N x R (caller order), src nsrc x 5 on the
+// host; phi_f / p_f M x R (either may be null).
+void field_dev(bem_handle* h, double freq, const double* pts, int64_t M, const double2* phi,
+               const double2* dphi, int64_t R, const double* src, int64_t nsrc, double2* phi_f,
+               double2* p_f) {
+  require(h->have_mesh && !h->points_mode, BEM_EINVAL, "mesh not set");
+  require(std::isfinite(freq) && freq >= 0, BEM_EINVAL, "frequency must be >= 0");
+  require(M >= 0 && R >= 1 && R <= (1 << 20) && nsrc >= 0 && nsrc <= (1 << 20), BEM_EINVAL,
+          "bad sizes");
+  require(phi && dphi && (M == 0 || pts) && (nsrc == 0 || src), BEM_EINVAL, "bad arguments");
+  if (M == 0) return;
+  const int64_t N = h->N;
+  const int prec = h->cfg.precision != 0 ? 1 : 0;
+  const double k = 2.0 * M_PI * freq / h->cfg.wave_speed;
+  // sound pressure i rho 2 pi f phi; 2 pi at f = 0 (:2236-2243)
+  const double2 pfac = make_double2(0.0, h->cfg.density * 2.0 * M_PI * (freq != 0 ? freq : 1.0));
+  cudaStream_t s = h->stream;
+  if (nsrc > 0) {
+    h->dFsrc.ensure((size_t)nsrc * 5);
+    CK(cudaMemcpyAsync(h->dFsrc.p, src, (size_t)nsrc * 5 * sizeof(double), cudaMemcpyHostToDevice, s));
+  }
+  if (prec == 1) h->dFe.ensure((size_t)N);
+  h->dFcoef.ensure((size_t)N * R * (prec == 1 ? sizeof(FieldCoefF) : sizeof(FieldCoef)));
+  const int S = field_split(h, M);
+  h->dFpart.ensure((size_t)S * R * M);
+  h->launches += launch_field_prep(h->dE.p, h->dPerm.p, N, phi, dphi, (int)R, prec, h->dFe.p,
+                                   h->dFcoef.p, s);
+  h->launches += launch_field_sum(h->dE.p, h->dFe.p, h->dFcoef.p, N, (int)R, pts, M, k, prec, S,
+                                  h->dFpart.p, s);
+  h->launches += launch_field_finish(h->dFpart.p, S, M, (int)R, pts, nsrc ? h->dFsrc.p : nullptr,
+                                     (int)nsrc, k, pfac, phi_f, p_f, s);
+  CK(cudaGetLastError());
+}
+
+}  // namespace
+
+bem_status bem_field(bem_handle* h, double freq, const double* pts, int64_t npts,
+                     const double* phi, const double* dphi, int64_t nrhs, const double* sources,
+                     int64_t nsrc, double* phi_f, double* p_f) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] {
+    require(h->have_mesh && !h->points_mode, BEM_EINVAL, "mesh not set");
+    require(phi && dphi && nrhs >= 1 && npts >= 0 && (npts == 0 || pts), BEM_EINVAL,
+            "bad arguments");
+    if (npts == 0) return;
+    const size_t cn = (size_t)h->N * nrhs, cm = (size_t)npts * nrhs;
+    h->dFpts.ensure((size_t)npts * 3);
+    CK(cudaMemcpyAsync(h->dFpts.p, pts, (size_t)npts * 3 * sizeof(double), cudaMemcpyHostToDevice,
+                       h->stream));
+    copy_in(h, h->dFphi, phi, cn);
+    copy_in(h, h->dFdphi, dphi, cn);
+    if (phi_f) h->dFout1.ensure(cm);
+    if (p_f) h->dFout2.ensure(cm);
+    field_dev(h, freq, h->dFpts.p, npts, h->dFphi.p, h->dFdphi.p, nrhs, sources, nsrc,
+              phi_f ? h->dFout1.p : nullptr, p_f ? h->dFout2.p : nullptr);
+    copy_out(h, phi_f, h->dFout1.p, cm);
+    copy_out(h, p_f, h->dFout2.p, cm);
+    sync(h);
+  });
+}
+
+bem_status bem_field_device(bem_handle* h, double freq, const void* pts, int64_t npts,
+                            const void* phi, const void* dphi, int64_t nrhs,
+                            const double* sources, int64_t nsrc, void* phi_f, void* p_f) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] {
+    field_dev(h, freq, (const double*)pts, npts, (const double2*)phi, (const double2*)dphi, nrhs,
+              sources, nsrc, (double2*)phi_f, (double2*)p_f);
+  });
 }
 
 bem_status bem_solve_device(bem_handle* h, double freq, const void* g, int64_t nrhs, void* phi,

@@ -307,6 +307,78 @@ def pencil_sweep(pkg, meshes, torch, every=8, plain_freqs=2):
     return out
 
 
+def field_eval(pkg, meshes, torch, s, n, sub, cpu=True, reps=10):
+    """Field evaluation after the solve (bem_field; calculateFieldSolution,
+    boundaryelementsolver.cpp:2192-2249): sound pressure at the 20,480
+    triangle midpoints of a radius-2 m observation sphere from the mixed-
+    precision boundary solution at 1.5 kHz. Kernel time with the data
+    resident (bem_field_device, CUDA events on the library's stream), end to
+    end through bem_field with host buffers, the analytic field
+    p(r) = p(a) (a / r) exp(ik(r - a)) as accuracy check, and the oracle's
+    dense FP64 sum on all host cores over a 256-point sample."""
+    L = pkg.lib()
+    tri = meshes.icosphere(sub, 1.0)
+    obs = meshes.icosphere(5, 2.0)
+    pts = np.ascontiguousarray((obs[:, 0:3] + obs[:, 3:6] + obs[:, 6:9]) / 3.0)
+    M = pts.shape[0]
+    phi, dphi, _, _ = s.solve(FREQ, np.ones(n))
+    stream = torch.cuda.ExternalStream(L.bem_stream(s._h))
+    dpts = torch.from_numpy(pts).to("cuda")
+    dph = torch.from_numpy(phi[:, 0].copy()).to("cuda")
+    ddph = torch.from_numpy(dphi[:, 0].copy()).to("cuda")
+    dpf = torch.zeros(M, dtype=torch.complex128, device="cuda")
+    dpp = torch.zeros(M, dtype=torch.complex128, device="cuda")
+    torch.cuda.synchronize()
+
+    def run():
+        s.field_device(FREQ, dpts.data_ptr(), M, dph.data_ptr(), ddph.data_ptr(), 1,
+                       dpf.data_ptr(), dpp.data_ptr())
+    for _ in range(3):
+        run()
+    torch.cuda.synchronize()
+    l0 = s.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        run()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    launches = (s.launch_count() - l0) // reps
+    t0 = time.perf_counter()
+    for _ in range(3):
+        _, pp = s.field(FREQ, pts, phi[:, 0], dphi[:, 0])
+    e2e_ms = (time.perf_counter() - t0) / 3 * 1e3
+    k = 2 * np.pi * FREQ / C0
+    pa = RHO * C0 * (1j * k) / (1j * k - 1)
+    r = np.linalg.norm(pts, axis=1)
+    ex = pa * (1.0 / r) * np.exp(1j * k * (r - 1.0))
+    pairs = float(n) * M
+    out = {
+        "workload": f"{n}-element boundary solution -> {M} observation points "
+                    "(midpoints of an r=2 m icosphere), 7-point rule, mixed precision",
+        "kernel_ms": round(ms, 4), "launches_per_eval": int(launches),
+        "gpairs_per_s": round(pairs / (ms * 1e-3) / 1e9, 2),
+        "e2e_ms": round(e2e_ms, 3),
+        "h2d_bytes": int(M * 24 + 2 * n * 16), "d2h_bytes": int(2 * M * 16),
+        "analytic_rel_err": float(np.abs(pp[:, 0] - ex).max() / np.abs(ex).max()),
+    }
+    if cpu:
+        import oracle
+        sample = 256
+        cores = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        _, op = oracle.field(tri, FREQ, pts[:sample], phi[:, 0], dphi[:, 0], c=C0, rho=RHO,
+                             nthreads=cores)
+        cpu_s = (time.perf_counter() - t0) * M / sample
+        out["rel_err_vs_oracle_sample"] = float(np.linalg.norm(pp[:sample, 0] - op[:, 0])
+                                                / np.linalg.norm(op[:, 0]))
+        out["cpu_oracle"] = {"s_per_eval": round(cpu_s, 3), "cores": cores, "kind": "port",
+                             "sample": f"{sample} of {M} points, scaled"}
+        out["speedup_vs_cpu_oracle"] = round(cpu_s / (e2e_ms * 1e-3), 1)
+    return out
+
+
 def run_ours(args):
     import torch
     ws, rank, local = dist_env()
@@ -411,6 +483,9 @@ def run_ours(args):
     }
     if args.selector:
         line["selector_stats"] = s.sel_stats()
+    if not args.no_field and ws == 1:
+        line["field_eval"] = field_eval(pkg, meshes, torch, s, n, sub,
+                                        cpu=not args.no_cpu_baseline and rank == 0)
     if not args.no_sweep and ws == 1:
         line["box_sweep"] = box_sweep(pkg, meshes, torch)
     if args.pencil and ws == 1:
@@ -497,6 +572,8 @@ def main():
                     help="mixed arm: H-LU preconditioned GMRES (rank 2)")
     ap.add_argument("--pencil", action="store_true",
                     help="also measure the 81,760-triangle pencil sweep (minutes)")
+    ap.add_argument("--no-field", action="store_true",
+                    help="skip the field evaluation at 20,480 observation points")
     ap.add_argument("--no-sweep", action="store_true",
                     help="skip the batched box sweep (64 frequencies x 4 RHS)")
     ap.add_argument("--selector", action="store_true",

@@ -291,6 +291,30 @@ bem_status bem_autotune(bem_handle* h, double freq, int64_t nrhs, int64_t* tuned
 bem_status bem_sweep(bem_handle* h, const double* freqs, int64_t nf, const double* g,
                      int64_t nrhs, double* p, bem_solve_info* info);
 
+/* Field evaluation (BoundaryElementSolver::calculateFieldSolution,
+ * boundaryelementsolver.cpp:2192-2249, as its regular sum
+ * calculateFieldSolutionRegular :2263-2316 with BemOperatorField :2318-2353):
+ * velocity potential phi_f and sound pressure p_f = i rho 2 pi f phi_f (2 pi
+ * in place of 2 pi f at f = 0) at npts observation points pts (npts x 3, e.g.
+ * the triangle midpoints of an observation field, ObservationField::
+ * calculateTrianglesMidpoints) from a boundary solution phi, dphi (n x nrhs,
+ * caller order, as bem_solve returns them). Per element the 7-point triangle
+ * rule of order 5 (orderLow, boundaryelementsolver.h:653-654), evaluated in
+ * the configured precision. sources: nsrc point sources, rows x, y, z, Re w,
+ * Im w, host memory (sourcePhiTerm :3443-3450), added to every column; may be
+ * NULL when nsrc = 0. phi_f and p_f (npts x nrhs) may be NULL. The reference's
+ * default (hMatFieldSolving, bemparameters.h:29) approximates the same sum
+ * with on-the-fly ACA at fieldACARelativeError = 1e-2 (:2397-2570); this call
+ * evaluates it without approximation. No impedance plane terms. */
+bem_status bem_field(bem_handle* h, double freq, const double* pts, int64_t npts,
+                     const double* phi, const double* dphi, int64_t nrhs, const double* sources,
+                     int64_t nsrc, double* phi_f, double* p_f);
+/* Same with device pointers for pts, phi, dphi, phi_f and p_f (sources stay
+ * in host memory); asynchronous on bem_stream. */
+bem_status bem_field_device(bem_handle* h, double freq, const void* pts, int64_t npts,
+                            const void* phi, const void* dphi, int64_t nrhs,
+                            const double* sources, int64_t nsrc, void* phi_f, void* p_f);
+
 /* Point-cloud H-matrix with the reference's test kernel exp(ikr)/(4 pi r)
  * (Tests/tests.h:30-42): rows and columns get their own cluster trees.
  * Afterwards which = 0 addresses this matrix in bem_hmatvec / bem_get_block

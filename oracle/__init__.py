@@ -21,9 +21,11 @@ F64P = ct.POINTER(ct.c_double)
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle with its Makefile (a few seconds)."""
-    if force or not os.path.exists(_LIB_PATH):
-        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    """Compile the oracle with its Makefile (a few seconds; make skips an
+    up-to-date library)."""
+    if force:
+        subprocess.run(["make", "-s", "-C", _HERE, "clean"], check=True)
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
 
 
@@ -77,6 +79,9 @@ def lib():
         L.orc_triangle_rule.argtypes = [ct.c_int64, F64P]
         L.orc_line_rule.restype = ct.c_int64
         L.orc_line_rule.argtypes = [ct.c_int64, F64P]
+        L.orc_field.argtypes = [F64P, ct.c_int64, ct.c_double, ct.c_double, ct.c_double,
+                                F64P, ct.c_int64, F64P, F64P, ct.c_int64, F64P, ct.c_int64,
+                                ct.c_int, F64P, F64P]
         L.orc_pivot_hash.restype = ct.c_uint64
         L.orc_pivot_hash.argtypes = [ct.c_uint64, ct.c_uint64, ct.c_uint64]
         _lib = L
@@ -278,6 +283,29 @@ def line_rule(n):
     out = np.zeros((32, 2))
     k = lib().orc_line_rule(n, _f(out))
     return out[:k].copy()
+
+
+def field(tri, freq, pts, phi, dphi, sources=None, c=343.0, rho=1.2041, nthreads=0):
+    """Velocity potential and sound pressure at observation points (npts x R
+    each) from a boundary solution phi, dphi (n x R, caller order); sources:
+    rows (x, y, z, complex weight)."""
+    tri = np.ascontiguousarray(tri, np.float64)
+    n = tri.shape[0]
+    pts = np.ascontiguousarray(pts, np.float64).reshape(-1, 3)
+    phi = np.asfortranarray(np.asarray(phi, np.complex128).reshape(n, -1))
+    dphi = np.asfortranarray(np.asarray(dphi, np.complex128).reshape(n, -1))
+    R = phi.shape[1]
+    src = np.zeros((0, 5))
+    if sources is not None and len(sources):
+        s = np.asarray(sources, np.complex128).reshape(-1, 4)
+        src = np.column_stack([s[:, :3].real, s[:, 3].real, s[:, 3].imag])
+    src = np.ascontiguousarray(src, np.float64)
+    pf = np.zeros((pts.shape[0], R), np.complex128, order="F")
+    pp = np.zeros((pts.shape[0], R), np.complex128, order="F")
+    # complex arrays are passed by their data pointers (interleaved re, im)
+    lib().orc_field(_f(tri), n, freq, c, rho, _f(pts), pts.shape[0], _f(phi), _f(dphi), R,
+                    _f(src), src.shape[0], nthreads, _f(pf), _f(pp))
+    return pf, pp
 
 
 def pivot_hash(seed, a, b):

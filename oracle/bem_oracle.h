@@ -29,6 +29,8 @@
  *   - GMRES: HMatrix/gmres.h:170-207 (Eigen GMRES, restated from Saad &
  *     Schultz 1986 with Householder-free CGS2 Arnoldi + Givens rotations)
  *   - solve orchestration: boundaryelementsolver.cpp:526-744, :2251-2261
+ *   - field evaluation: boundaryelementsolver.cpp:2192-2249, :2263-2353,
+ *     :3443-3450 (field.cpp)
  *
  * Deliberate, documented differences from the reference (shared with the GPU
  * library so the two stay comparable):
@@ -136,6 +138,16 @@ int orc_solve(const orc_problem* p, double freq, double c, double rho,
 /* Dense reference matrices (small N): both N x N column-major, cluster order. */
 void orc_dense(const orc_problem* p, double k, int coupling, const double* a,
                const double* b, double* phi, double* dphi, int nthreads);
+
+/* Field evaluation (calculateFieldSolutionRegular, boundaryelementsolver.cpp:
+ * 2263-2316; BemOperatorField :2318-2353; sourcePhiTerm :3443-3450): tri is
+ * n x 9 in the caller's order, phi / dphi n x nrhs complex, pts npts x 3,
+ * src nsrc x 5 (x, y, z, Re w, Im w); phi_f and p_f (npts x nrhs complex) may
+ * be NULL. p_f = i rho 2 pi f phi_f (2 pi at f = 0). */
+void orc_field(const double* tri, int64_t n, double freq, double c, double rho,
+               const double* pts, int64_t npts, const double* phi, const double* dphi,
+               int64_t nrhs, const double* src, int64_t nsrc, int nthreads,
+               double* phi_f, double* p_f);
 
 /* Quadrature tables used (for cross-checking the GPU library's copy). */
 int64_t orc_triangle_rule(int64_t order, double* out /* npts x 3 */);

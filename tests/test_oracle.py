@@ -179,3 +179,102 @@ def test_block_triangular_solves(orc):
     assert rel(LD @ y, b) < 1e-12
     x = orc.upper_solve(n, Ub, Ud, y)
     assert rel(UD @ x, y) < 1e-12
+
+
+def _monopole_data(tri, k):
+    """Boundary data of a unit monopole at the origin: phi and dphi/dn at the
+    element centroids (normals from the node order, as the reference)."""
+    c = (tri[:, 0:3] + tri[:, 3:6] + tri[:, 6:9]) / 3.0
+    nrm = np.cross(tri[:, 3:6] - tri[:, 0:3], tri[:, 6:9] - tri[:, 0:3])
+    nrm /= np.linalg.norm(nrm, axis=1)[:, None]
+    r = np.linalg.norm(c, axis=1)
+    phi = np.exp(1j * k * r) / (4 * np.pi * r)
+    dphi = phi * (1j * k - 1 / r) * np.sum(nrm * c, 1) / r
+    return phi, dphi
+
+
+def test_field_reproduces_monopole(orc, meshes):
+    """Kirchhoff-Helmholtz representation (calculateFieldSolutionRegular):
+    exterior monopole data give the monopole outside the surface (O(h^2)
+    faceting error) and zero inside."""
+    tri = meshes.icosphere(3, 0.5)
+    f = 400.0
+    k = 2 * np.pi * f / 343.0
+    phi, dphi = _monopole_data(tri, k)
+    out = np.array([[1.0, 0, 0], [0, 1.5, 0.3], [2, 2, 2], [-0.4, 0.7, -0.9]])
+    inside = np.array([[0.1, 0.05, 0.0], [0.0, -0.2, 0.1]])
+    pf, pp = orc.field(tri, f, np.vstack([out, inside]), phi, dphi)
+    r = np.linalg.norm(out, axis=1)
+    ex = np.exp(1j * k * r) / (4 * np.pi * r)
+    assert (np.abs(pf[:4, 0] - ex) / np.abs(ex)).max() < 0.01
+    assert np.abs(pf[4:, 0]).max() < 0.01 * np.abs(ex).max()
+    # sound pressure i rho 2 pi f phi (calculateFieldSolution :2236-2243)
+    assert np.allclose(pp, 1j * 1.2041 * 2 * np.pi * f * pf, rtol=1e-14, atol=0)
+
+
+def test_field_point_sources(orc, meshes):
+    """sourcePhiTerm: with zero boundary data the field is the point sources'
+    w exp(ikr) / (4 pi r), summed; at f = 0 the pressure factor is 2 pi."""
+    tri = meshes.icosphere(1, 0.5)
+    n = tri.shape[0]
+    pts = np.array([[1.0, 0.2, 0.0], [0.3, -2.0, 0.5]])
+    src = [[0, 0, 0, 1.0], [0.1, 0.2, -0.1, 0.5 - 2j]]
+    for f in (250.0, 0.0):
+        k = 2 * np.pi * f / 343.0
+        pf, pp = orc.field(tri, f, pts, np.zeros(n), np.zeros(n), sources=src)
+        ex = 0
+        for s in src:
+            r = np.linalg.norm(pts - np.array(s[:3]).real, axis=1)
+            ex = ex + s[3] * np.exp(1j * k * r) / (4 * np.pi * r)
+        assert rel(pf[:, 0], ex) < 1e-14
+        fac = 2 * np.pi * (f if f else 1.0)
+        assert np.allclose(pp[:, 0], 1j * 1.2041 * fac * pf[:, 0], rtol=1e-14, atol=0)
+
+
+def test_field_matches_vectorised_restatement(orc, meshes):
+    """The oracle's loop against an independent numpy evaluation of the same
+    sum (7-point rule of order 5, BemOperatorField :2318-2353), two columns."""
+    tri = meshes.icosphere(1, 0.7)
+    n = tri.shape[0]
+    rng = np.random.default_rng(5)
+    phi = rng.standard_normal((n, 2)) + 1j * rng.standard_normal((n, 2))
+    dphi = rng.standard_normal((n, 2)) + 1j * rng.standard_normal((n, 2))
+    pts = rng.uniform(-2, 2, (7, 3))
+    f = 700.0
+    k = 2 * np.pi * f / 343.0
+    pf, _ = orc.field(tri, f, pts, phi, dphi)
+    rule = orc.triangle_rule(5)
+    assert rule.shape == (7, 3)
+    n1, n2, n3 = tri[:, 0:3], tri[:, 3:6], tri[:, 6:9]
+    cr = np.cross(n2 - n1, n3 - n1)
+    area = np.linalg.norm(cr, axis=1) / 2
+    nq = cr / np.linalg.norm(cr, axis=1)[:, None]
+    q = (rule[:, 0, None, None] * n1 + rule[:, 1, None, None] * n2
+         + (1 - rule[:, 0] - rule[:, 1])[:, None, None] * n3)      # 7 x n x 3
+    rv = pts[:, None, None, :] - q[None]                           # P x 7 x n x 3
+    r = np.linalg.norm(rv, axis=-1)
+    G = np.exp(1j * k * r) / (4 * np.pi * r)
+    rnq = -np.sum(rv * nq[None, None], -1) / r
+    w = rule[:, 2][None, :, None]
+    Lk = (w * G).sum(1) * area
+    Mk = (w * G / r * (1j * k * r - 1) * rnq).sum(1) * area
+    ref = Mk @ phi - Lk @ dphi
+    assert rel(pf, ref) < 1e-13
+
+
+def test_field_pulsating_sphere(orc, meshes):
+    """Solve then field: p(r) = p(a) (a / r) exp(ik(r - a)) outside a sphere
+    with uniform normal velocity."""
+    a = 1.0
+    tri = meshes.icosphere(3, a)
+    P = orc.Problem(tri, 32, 2.0)
+    n = P.n
+    f, c, rho = 200.0, 343.0, 1.2
+    k = 2 * np.pi * f / c
+    phi, dphi, p, st = P.solve(f, c, rho, 2, np.zeros(n), np.ones(n), np.ones(n), 1e-4, 1e-8)
+    r = np.array([1.5, 2.0, 4.0])
+    pts = np.column_stack([r * 0.6, r * 0.0, r * 0.8])
+    _, pp = orc.field(tri, f, pts, phi[:, 0], dphi[:, 0], c=c, rho=rho)
+    pa = rho * c * (1j * k * a) / (1j * k * a - 1)
+    ex = pa * (a / r) * np.exp(1j * k * (r - a))
+    assert np.abs(pp[:, 0] - ex).max() / abs(pa) < 0.03
