@@ -379,6 +379,19 @@ def field_eval(pkg, meshes, torch, s, n, sub, cpu=True, reps=10):
     return out
 
 
+def run_field_only(args):
+    """The field leg alone on one GPU (for profiling its kernels)."""
+    import torch
+    pkg = importlib.import_module("3d_bem_gb300")
+    meshes = importlib.import_module("3d_bem_gb300.meshes")
+    pkg.build()
+    sub = WORKLOADS[args.workload][0]
+    s, n = make_solver(pkg, meshes, sub, 1)
+    out = field_eval(pkg, meshes, torch, s, n, sub, cpu=not args.no_cpu_baseline)
+    print(json.dumps({"field_eval": out}), flush=True)
+    s.close()
+
+
 def run_ours(args):
     import torch
     ws, rank, local = dist_env()
@@ -574,6 +587,8 @@ def main():
                     help="also measure the 81,760-triangle pencil sweep (minutes)")
     ap.add_argument("--no-field", action="store_true",
                     help="skip the field evaluation at 20,480 observation points")
+    ap.add_argument("--field-only", action="store_true",
+                    help="only the field evaluation leg (one mixed solve first); profiling")
     ap.add_argument("--no-sweep", action="store_true",
                     help="skip the batched box sweep (64 frequencies x 4 RHS)")
     ap.add_argument("--selector", action="store_true",
@@ -582,7 +597,9 @@ def main():
                     help="mixed arm: the 16-point rule for the ACA entries instead of the "
                          "learned rule table")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.field_only:
+        run_field_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
