@@ -41,6 +41,8 @@ EXPORTS = [
     "bem_sel_nparam", "bem_sel_label", "bem_mlp_grad", "bem_mlp_adam", "bem_mlp_forward",
     "bem_sel_infer", "bem_set_selector", "bem_sel_stats", "bem_sel_classes", "bem_autotune",
     "bem_set_aca_rules", "bem_set_bc_impedance", "bem_field", "bem_field_device",
+    "bem_msh_read", "bem_msh_free", "bem_msh_num_physical", "bem_msh_physical", "bem_msh_select",
+    "bem_msh_elements", "bem_quads_to_triangles", "bem_wall_beta",
 ]
 BEM_ARITH_FP64, BEM_ARITH_FP32, BEM_ARITH_TWOFLOAT = 0, 1, 2
 
@@ -141,6 +143,16 @@ def lib():
     L.bem_set_aca_rules.argtypes = [vp, vp, vp]
     L.bem_set_bc_impedance.argtypes = [vp, vp]
     L.bem_field.argtypes = [vp, dbl, vp, i64, vp, vp, i64, vp, i64, vp, vp]
+    L.bem_msh_read.argtypes = [ct.c_char_p, P(vp), ct.c_char_p, i64]
+    L.bem_msh_free.argtypes = [vp]
+    L.bem_msh_free.restype = None
+    L.bem_msh_num_physical.argtypes = [vp]
+    L.bem_msh_num_physical.restype = i64
+    L.bem_msh_physical.argtypes = [vp, i64, P(i32), P(i32), ct.c_char_p, i64]
+    L.bem_msh_select.argtypes = [vp, ct.c_char_p, ct.c_char_p, P(i64), P(i64)]
+    L.bem_msh_elements.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    L.bem_quads_to_triangles.argtypes = [vp, i64, vp]
+    L.bem_wall_beta.argtypes = [i32, i32, vp, dbl, vp]
     L.bem_field_device.argtypes = [vp, dbl, vp, i64, vp, vp, i64, vp, i64, vp, vp]
     L.bem_hlu_build.argtypes = [vp]
     L.bem_hlu_solve.argtypes = [vp, vp, vp, i64]
@@ -505,6 +517,127 @@ def _sources(sources) -> np.ndarray:
         return np.zeros((0, 5))
     s = np.asarray(sources, np.complex128).reshape(-1, 4)
     return np.ascontiguousarray(np.column_stack([s[:, :3].real, s[:, 3].real, s[:, 3].imag]))
+
+
+# ---------------------------------------------------------------------------
+# Mesh input and boundary data (host only)
+# ---------------------------------------------------------------------------
+class MshFile:
+    """A GMSH ASCII mesh (formats 2.2 and 4.1) read by the library
+    (bem_msh_read); :meth:`select` applies the reference's include / exclude
+    lists."""
+
+    def __init__(self, path):
+        err = ct.create_string_buffer(512)
+        h = ct.c_void_p()
+        st = lib().bem_msh_read(os.fsencode(path), ct.byref(h), err, 512)
+        if st != BEM_OK:
+            raise BemError(st, f"bem_msh_read: {err.value.decode(errors='replace')}")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().bem_msh_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def physical_names(self) -> list:
+        """[(dim, number, name)] from $PhysicalNames."""
+        out = []
+        name = ct.create_string_buffer(256)
+        d, t = ct.c_int32(), ct.c_int32()
+        for i in range(lib().bem_msh_num_physical(self._h)):
+            _raise(lib().bem_msh_physical(self._h, i, ct.byref(d), ct.byref(t), name, 256),
+                   "bem_msh_physical")
+            out.append((d.value, t.value, name.value.decode(errors="replace")))
+        return out
+
+    def select(self, include="all", exclude="") -> dict:
+        """Triangles (N x 9), quadrilaterals (M x 12) and their physical /
+        geometric numbers after the include / exclude selection."""
+        inc = " ".join(include) if isinstance(include, (list, tuple)) else str(include)
+        exc = " ".join(exclude) if isinstance(exclude, (list, tuple)) else str(exclude)
+        nt, nq = ct.c_int64(), ct.c_int64()
+        _raise(lib().bem_msh_select(self._h, inc.encode(), exc.encode(), ct.byref(nt),
+                                    ct.byref(nq)), "bem_msh_select")
+        out = {"tri": np.zeros((nt.value, 9)), "tri_phys": np.zeros(nt.value, np.int32),
+               "tri_geom": np.zeros(nt.value, np.int32), "quad": np.zeros((nq.value, 12)),
+               "quad_phys": np.zeros(nq.value, np.int32),
+               "quad_geom": np.zeros(nq.value, np.int32)}
+        _raise(lib().bem_msh_elements(self._h, *(_ptr(out[k]) for k in (
+            "tri", "tri_phys", "tri_geom", "quad", "quad_phys", "quad_geom"))), "bem_msh_elements")
+        return out
+
+
+def _raise(st, what):
+    if st != BEM_OK:
+        raise BemError(st, what)
+
+
+def quads_to_triangles(quads) -> np.ndarray:
+    """global::quadrilateralsToTriangles: M x 12 -> 2M x 9 (shorter diagonal)."""
+    q = np.ascontiguousarray(quads, np.float64).reshape(-1, 12)
+    out = np.zeros((2 * q.shape[0], 9))
+    _raise(lib().bem_quads_to_triangles(_ptr(q), q.shape[0], _ptr(out)), "bem_quads_to_triangles")
+    return out
+
+
+def read_msh(path, include="all", exclude=""):
+    """Triangles of a .msh file as the solver takes them: the selected
+    triangles, then the selected quadrilaterals split in two; returns
+    (tri, phys, geom)."""
+    m = MshFile(path)
+    sel = m.select(include, exclude)
+    m.close()
+    tri = np.vstack([sel["tri"], quads_to_triangles(sel["quad"])])
+    phys = np.concatenate([sel["tri_phys"], np.repeat(sel["quad_phys"], 2)])
+    geom = np.concatenate([sel["tri_geom"], np.repeat(sel["quad_geom"], 2)])
+    return tri, phys, geom
+
+
+IMP_REFLECTION, IMP_DAMPING, IMP_IMPEDANCE, IMP_ADMITTANCE = 0, 1, 2, 3
+
+
+def wall_beta(imp_type: int, value, normalized: bool = True, medium_impedance: float = 0.0):
+    """beta of a wall section (a = i k beta, b = 1), WallImpedanceSection::setUpValues."""
+    v = np.array([complex(value).real, complex(value).imag])
+    b = np.zeros(2)
+    _raise(lib().bem_wall_beta(imp_type, int(bool(normalized)), _ptr(v), medium_impedance,
+                               _ptr(b)), "bem_wall_beta")
+    return complex(b[0], b[1])
+
+
+class mshReader:
+    """Mirror of mshReader (mshreader.h): ``readMsh(filename, elementIndex,
+    includeAll, include, exclude)`` fills ``triangles`` (N x 9),
+    ``quadrilaterals`` (M x 12), ``physicalGroupsNames`` and
+    ``physicalGroupsNumbers``; ``elementIndex`` is kept as the index the
+    reference stamps on every element."""
+
+    def __init__(self):
+        self.triangles = np.zeros((0, 9))
+        self.quadrilaterals = np.zeros((0, 12))
+        self.physicalGroupsNames: list = []
+        self.physicalGroupsNumbers: list = []
+        self.elementIndex = 0
+
+    def readMsh(self, filename, elementIndex=0, includeAll=True, include=(), exclude=()):
+        self.elementIndex = elementIndex
+        m = MshFile(filename)
+        inc = list(include) + (["all"] if includeAll and not include else [])
+        sel = m.select(inc, list(exclude))
+        names = m.physical_names
+        m.close()
+        self.triangles, self.quadrilaterals = sel["tri"], sel["quad"]
+        self.physicalGroupsNames = [n for _, _, n in names]
+        self.physicalGroupsNumbers = [t for _, t, _ in names]
+        return self
 
 
 # ---------------------------------------------------------------------------

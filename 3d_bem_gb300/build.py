@@ -26,7 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["nearfield.cu", "aca.cu", "hmatvec.cu", "krylov.cu", "post.cu", "hlu_solve.cu", "recompress.cu",
               "selector.cu", "field.cu"]
-CPP_SOURCES = ["host_tree.cpp", "hlu.cpp", "capi.cpp"]
+CPP_SOURCES = ["host_tree.cpp", "hlu.cpp", "capi.cpp", "msh.cpp"]
 
 
 def _sources():

@@ -315,6 +315,51 @@ bem_status bem_field_device(bem_handle* h, double freq, const void* pts, int64_t
                             const void* phi, const void* dphi, int64_t nrhs,
                             const double* sources, int64_t nsrc, void* phi_f, void* p_f);
 
+/* ---- mesh input and boundary data (host only, no GPU needed) ---- */
+
+/* A GMSH ASCII mesh: format 2.2 as mshReader::readSections reads it
+ * (mshreader.cpp:200-376: $Nodes, $Elements with number / type / tags,
+ * $PhysicalNames), or format 4.1 (block-structured $Nodes / $Elements; an
+ * element's geometric number is its entity tag, its physical number the
+ * entity's first physical tag from $Entities). Triangles (type 2) and
+ * quadrilaterals (type 3) are kept, other element types skipped. On failure
+ * *out is NULL and err (errcap bytes, may be NULL) holds the reason. */
+typedef struct bem_msh bem_msh;
+bem_status bem_msh_read(const char* path, bem_msh** out, char* err, int64_t errcap);
+void bem_msh_free(bem_msh* m);
+/* $PhysicalNames entries: dimension, number and name (NUL-terminated, cap bytes). */
+int64_t bem_msh_num_physical(const bem_msh* m);
+bem_status bem_msh_physical(const bem_msh* m, int64_t i, int32_t* dim, int32_t* tag, char* name,
+                            int64_t cap);
+/* Element selection (mshReader::sortOutIncludesAndExcludes / elementIsIncluded,
+ * mshreader.cpp:22-198, :378-428). include / exclude: lists separated by
+ * blanks, commas or semicolons of physical group names (case-insensitive),
+ * geometric numbers and ranges "a..b" / "a...b" (open ends allowed). An include
+ * list that is empty or only "all" keeps everything except the excluded
+ * physical groups and geometric numbers; otherwise it keeps the named physical
+ * groups plus the included minus the excluded geometric numbers. Returns the
+ * selected triangle and quadrilateral counts (either pointer may be NULL);
+ * after bem_msh_read everything is selected. */
+bem_status bem_msh_select(bem_msh* m, const char* include, const char* exclude, int64_t* ntri,
+                          int64_t* nquad);
+/* The selection, in file order: triangles (ntri x 9: node1, node2, node3 xyz),
+ * quadrilaterals (nquad x 12) and their physical / geometric numbers. Any
+ * pointer may be NULL. */
+bem_status bem_msh_elements(const bem_msh* m, double* tri, int32_t* tri_phys, int32_t* tri_geom,
+                            double* quad, int32_t* quad_phys, int32_t* quad_geom);
+/* global::quadrilateralsToTriangles (global.cpp:841-870): each quadrilateral
+ * (12 doubles) becomes two triangles (18 doubles) split along the shorter
+ * diagonal, node orders as the reference. */
+bem_status bem_quads_to_triangles(const double* quad, int64_t nq, double* tri);
+/* WallImpedanceSection::setUpValues (SolvingScript/wallimpedancesection.cpp:
+ * 308-405): the beta of bem_set_bc_impedance (a = i k beta, b = 1, g = 0) for
+ * imp_type 0 reflection factor R (beta = (1 - R) / (1 + R), real part of R),
+ * 1 damping d (d / (2 - d)), 2 impedance Z (normalized: 1 / Z, else
+ * medium_impedance / Z), 3 admittance Y (normalized: Y, else
+ * medium_impedance Y). value and beta are complex (re, im). */
+bem_status bem_wall_beta(int32_t imp_type, int32_t normalized, const double* value,
+                         double medium_impedance, double* beta);
+
 /* Point-cloud H-matrix with the reference's test kernel exp(ikr)/(4 pi r)
  * (Tests/tests.h:30-42): rows and columns get their own cluster trees.
  * Afterwards which = 0 addresses this matrix in bem_hmatvec / bem_get_block
