@@ -11,8 +11,9 @@
 //
 // Mixed precision (precision 1): the integrand in FP32 with two-float
 // centroids (p - c_j keeps ~7 digits, the rule points are offsets from c_j),
-// exp(ikr) from the hardware sin / cos after an exact reduction of (k / pi) r
-// to [-1, 1] (absolute error ~4e-7 on [-pi, pi]), per-tile sums in FP32
+// exp(ikr) from the hardware sin / cos after an exact reduction of
+// k r / (2 pi) to [-1/2, 1/2] (absolute error ~4e-7 on [-pi, pi]), per-tile
+// sums in FP32
 // folded into FP64 accumulators every FIELD_TILE elements. Precision 0: the
 // same sum in FP64.
 #include "field.h"
@@ -67,11 +68,16 @@ __global__ void field_prep_kernel(const Elem* __restrict__ E, const int64_t* __r
 #pragma unroll
     for (int i = 0; i < 7; i++) {
       const double a1 = cR7x1[i], a2 = cR7x2[i], a3 = 1.0 - a2 - a1;
+      double on = 0.0;
 #pragma unroll
-      for (int d = 0; d < 3; d++)
-        f.q[3 * i + d] = (float)((a1 * e.n1[d] + a2 * e.n2[d] + a3 * e.n3[d]) - e.c[d]);
+      for (int d = 0; d < 3; d++) {
+        const double o = (a1 * e.n1[d] + a2 * e.n2[d] + a3 * e.n3[d]) - e.c[d];
+        f.q[3 * i + d] = (float)o;
+        on += o * e.nrm[d];
+      }
+      f.qn[i] = (float)on;
     }
-    f.pad[0] = f.pad[1] = 0.0f;
+    f.pad[0] = f.pad[1] = f.pad[2] = 0.0f;
     fe[j] = f;
   }
   const int64_t cj = perm[j];
@@ -97,7 +103,7 @@ template <int RB>
 __global__ void __launch_bounds__(FIELD_PTS)
     field_sum32_kernel(const FieldElemF* __restrict__ fe, const FieldCoefF* __restrict__ coef,
                        int64_t N, int64_t chunk, const double* __restrict__ pts, int64_t M,
-                       float k, float kpi, int r0, int R, double2* __restrict__ partial) {
+                       float k, float kc, int r0, int R, double2* __restrict__ partial) {
   __shared__ FieldElemF se[FIELD_TILE];
   __shared__ FieldCoefF sc[RB][FIELD_TILE];
   const int64_t ip = (int64_t)blockIdx.x * FIELD_PTS + threadIdx.x;
@@ -120,7 +126,8 @@ __global__ void __launch_bounds__(FIELD_PTS)
     __syncthreads();
     const float4* src = reinterpret_cast<const float4*>(fe + t0);
     float4* dst = reinterpret_cast<float4*>(se);
-    for (int i = threadIdx.x; i < nt * 8; i += FIELD_PTS) dst[i] = src[i];
+    constexpr int PIECES = (int)(sizeof(FieldElemF) / sizeof(float4));
+    for (int i = threadIdx.x; i < nt * PIECES; i += FIELD_PTS) dst[i] = src[i];
     for (int i = threadIdx.x; i < RB * nt; i += FIELD_PTS) {
       const int r = i / nt, j = i - r * nt;
       sc[r][j] = coef[(int64_t)(r0 + r) * N + t0 + j];
@@ -134,7 +141,7 @@ __global__ void __launch_bounds__(FIELD_PTS)
       const float dx = (ph[0] - E.c_hi[0]) + (pl[0] - E.c_lo[0]);
       const float dy = (ph[1] - E.c_hi[1]) + (pl[1] - E.c_lo[1]);
       const float dz = (ph[2] - E.c_hi[2]) + (pl[2] - E.c_lo[2]);
-      const float nx = E.nrm[0], ny = E.nrm[1], nz = E.nrm[2];
+      const float dn = dx * E.nrm[0] + dy * E.nrm[1] + dz * E.nrm[2];
       float Lx = 0.0f, Ly = 0.0f, Mx = 0.0f, My = 0.0f;
 #pragma unroll
       for (int i = 0; i < 7; i++) {
@@ -142,21 +149,20 @@ __global__ void __launch_bounds__(FIELD_PTS)
         const float rr = rx * rx + ry * ry + rz * rz;
         const float ir = rsqrtf(rr);
         const float r = rr * ir;
-        // exp(ikr): x = k r / pi reduced exactly to t in [-1, 1] (x - 2 rint(x / 2)
-        // has no rounding), then the hardware sin / cos on pi t in [-pi, pi]
-        const float x = kpi * r;
-        const float xr = x - 2.0f * rintf(0.5f * x);
+        // exp(ikr): x = k r / (2 pi) reduced exactly to [-1/2, 1/2] (x - rint(x)
+        // has no rounding), then the hardware sin / cos on 2 pi (x - rint(x))
+        const float x = kc * r;
+        const float xr = x - rintf(x);
         float sn, cs;
-        __sincosf(3.14159265358979f * xr, &sn, &cs);
-        const float g0 = ir * cR7gf[i];
-        const float Gx = cs * g0, Gy = sn * g0;
+        __sincosf(6.28318530717959f * xr, &sn, &cs);
         const float kr = k * r;
-        // w dG/dr rnq = w G (ikr - 1) / r * (-(p - q) . n / r)
-        const float t = -(rx * nx + ry * ny + rz * nz) * (ir * ir);
-        Lx += Gx;
-        Ly += Gy;
-        Mx += t * (-Gx - kr * Gy);
-        My += t * (kr * Gx - Gy);
+        const float g0 = ir * cR7gf[i];  // w / (4 pi r)
+        Lx = fmaf(g0, cs, Lx);
+        Ly = fmaf(g0, sn, Ly);
+        // w dG/dr rnq = g0 (p - q_i) . n / r^2 (cos + kr sin, sin - kr cos)
+        const float tg = (dn - E.qn[i]) * (ir * ir * g0);
+        Mx = fmaf(tg, fmaf(kr, sn, cs), Mx);
+        My = fmaf(tg, fmaf(-kr, cs, sn), My);
       }
 #pragma unroll
       for (int r = 0; r < RB; r++) {
@@ -280,9 +286,9 @@ void sum_pass(const Elem* E, const FieldElemF* fe, const void* coef, int64_t N, 
               int r0, double2* partial, cudaStream_t s) {
   const dim3 grid((unsigned)((M + FIELD_PTS - 1) / FIELD_PTS), (unsigned)S);
   if (precision == 1) {
-    const double kpi = k / 3.14159265358979323846;
+    const double kc = k / (2.0 * 3.14159265358979323846);
     field_sum32_kernel<RB><<<grid, FIELD_PTS, 0, s>>>(fe, static_cast<const FieldCoefF*>(coef), N,
-                                                      chunk, pts, M, (float)k, (float)kpi, r0, R,
+                                                      chunk, pts, M, (float)k, (float)kc, r0, R,
                                                       partial);
   } else {
     field_sum64_kernel<RB><<<grid, FIELD_PTS, 0, s>>>(E, static_cast<const FieldCoef*>(coef), N,

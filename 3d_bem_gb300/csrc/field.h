@@ -11,16 +11,18 @@
 
 namespace bemgpu {
 
-// FP32 element record of the mixed-precision field kernel, one 128-byte line:
-// centroid as two floats (c_hi + c_lo), the 7 rule points as offsets from the
-// centroid, unit normal.
+// FP32 element record of the mixed-precision field kernel (160 bytes):
+// centroid as two floats (c_hi + c_lo), the 7 rule points as offsets o_i from
+// the centroid, unit normal n, and n . o_i (so (p - q_i) . n costs one
+// subtraction per rule point).
 struct __align__(16) FieldElemF {
   float c_hi[3], c_lo[3];
   float q[21];
   float nrm[3];
-  float pad[2];
+  float qn[7];
+  float pad[3];
 };
-static_assert(sizeof(FieldElemF) == 128, "FieldElemF is one 128-byte line");
+static_assert(sizeof(FieldElemF) == 160, "FieldElemF is ten 16-byte pieces");
 
 // Coefficients of one element and right-hand side: a = A phi, b = A dphi
 // (A the element area), complex.
