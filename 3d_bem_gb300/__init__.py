@@ -42,7 +42,7 @@ EXPORTS = [
     "bem_sel_infer", "bem_set_selector", "bem_sel_stats", "bem_sel_classes", "bem_autotune",
     "bem_set_aca_rules", "bem_set_bc_impedance", "bem_field", "bem_field_device",
     "bem_msh_read", "bem_msh_free", "bem_msh_num_physical", "bem_msh_physical", "bem_msh_select",
-    "bem_msh_elements", "bem_quads_to_triangles", "bem_wall_beta",
+    "bem_msh_elements", "bem_quads_to_triangles", "bem_wall_beta", "bem_set_impedance_plane",
 ]
 BEM_ARITH_FP64, BEM_ARITH_FP32, BEM_ARITH_TWOFLOAT = 0, 1, 2
 
@@ -153,6 +153,7 @@ def lib():
     L.bem_msh_elements.argtypes = [vp, vp, vp, vp, vp, vp, vp]
     L.bem_quads_to_triangles.argtypes = [vp, i64, vp]
     L.bem_wall_beta.argtypes = [i32, i32, vp, dbl, vp]
+    L.bem_set_impedance_plane.argtypes = [vp, vp, vp]
     L.bem_field_device.argtypes = [vp, dbl, vp, i64, vp, vp, i64, vp, i64, vp, vp]
     L.bem_hlu_build.argtypes = [vp]
     L.bem_hlu_solve.argtypes = [vp, vp, vp, i64]
@@ -467,6 +468,17 @@ class Solver:
         if st not in (BEM_OK, BEM_EMAXIT):
             self._check(st, "bem_sweep")
         return p, [i.as_dict() for i in infos]
+
+    def set_impedance_plane(self, point=None, normal=None):
+        """One infinite rigid plane (impedance plane); None removes it."""
+        if normal is None:
+            self._check(lib().bem_set_impedance_plane(self._h, None, None),
+                        "bem_set_impedance_plane")
+            return
+        p = np.ascontiguousarray(point, np.float64).reshape(3)
+        n = np.ascontiguousarray(normal, np.float64).reshape(3)
+        self._check(lib().bem_set_impedance_plane(self._h, _ptr(p), _ptr(n)),
+                    "bem_set_impedance_plane")
 
     def field(self, freq: float, pts, phi, dphi, sources=None):
         """Velocity potential and sound pressure (npts x R each) at the

@@ -167,6 +167,9 @@ __device__ __forceinline__ bool near_pair32(const ElemF* __restrict__ EF, int64_
 // not carry its registers
 __device__ __noinline__ double2 entry64(const AcaArgs& a, int64_t row, int64_t col) {
   Ops o = ops_eval(a.E, row, col, a.k, a.near_r, c_rules);
+  // impedance plane: the reflected element with the regular rule
+  // (implicitPhiMatrixPlusReflected, boundaryelementsolver.cpp:2042-2050)
+  if (a.Er) ops_add(o, ops_regular(a.E[row], a.Er[col], a.k, c_rules));
   double2 p, d;
   substitute(o, row == col, a.bc[col], a.alpha, p, d);
   return a.which ? d : p;
@@ -177,9 +180,11 @@ __device__ __noinline__ float2 entry64f(const AcaArgs& a, int64_t row, int64_t c
   return make_float2((float)v.x, (float)v.y);
 }
 
+// MODE 0: BEM entries; 2: BEM entries with an impedance plane (the
+// reflected element's operators added); 1: point-cloud test kernel.
 template <int MODE, typename T>
 __device__ __forceinline__ T aca_entry(const AcaArgs& a, int64_t row, int64_t col) {
-  if constexpr (MODE == 0) {
+  if constexpr (MODE == 0 || MODE == 2) {
     if constexpr (sizeof(T) == sizeof(float2)) {
       // mixed precision: FP32 regular rule, FP64 singular / near-singular
       if (row != col && !near_pair32(a.EF, row, col, a.near_r2f)) {
@@ -198,6 +203,7 @@ __device__ __forceinline__ T aca_entry(const AcaArgs& a, int64_t row, int64_t co
         } else {
           o = ops_regular32(a.EF, row, col, a.kf, c_rules);
         }
+        if constexpr (MODE == 2) ops_add(o, ops_regular32_pq(a.EF[row], a.EFr[col], a.kf, c_rules));
         float2 p, d;
         substitute32(o, a.bc[col], a.alphaf, p, d);
         return a.which ? d : p;
@@ -483,11 +489,14 @@ __global__ void __launch_bounds__(NT, NT == 128 ? 8 : 2) aca_kernel(AcaArgs a) {
 template <int NT>
 void launch_nt(const AcaArgs& a, cudaStream_t s) {
   const unsigned g = (unsigned)a.nfar;
+  const bool plane = a.mode == 0 && a.Er != nullptr;
   if (a.precision == 0) {
-    if (a.mode == 0) aca_kernel<0, double2, NT><<<g, NT, 0, s>>>(a);
+    if (plane) aca_kernel<2, double2, NT><<<g, NT, 0, s>>>(a);
+    else if (a.mode == 0) aca_kernel<0, double2, NT><<<g, NT, 0, s>>>(a);
     else aca_kernel<1, double2, NT><<<g, NT, 0, s>>>(a);
   } else {
-    if (a.mode == 0) aca_kernel<0, float2, NT><<<g, NT, 0, s>>>(a);
+    if (plane) aca_kernel<2, float2, NT><<<g, NT, 0, s>>>(a);
+    else if (a.mode == 0) aca_kernel<0, float2, NT><<<g, NT, 0, s>>>(a);
     else aca_kernel<1, float2, NT><<<g, NT, 0, s>>>(a);
   }
 }

@@ -50,6 +50,10 @@ struct NearfieldArgs {
   double2 alpha;
   void* phi;   // double2 or float2 per precision
   void* dphi;
+  // impedance plane: the elements reflected in it (cluster order), null
+  // without a plane; every entry adds the reflected element's operators
+  const Elem* Er = nullptr;
+  const ElemF* EFr = nullptr;
 };
 
 struct AcaArgs {
@@ -86,6 +90,9 @@ struct AcaArgs {
   // class (1/3/7/13/25 points) by x = log(d / e_max), y = log(k e_max) bins
   const uint8_t* rule_tab;
   float tab_x0, tab_dx, tab_y0, tab_dy;
+  // impedance plane (mode 0 only): reflected elements, null without a plane
+  const Elem* Er;
+  const ElemF* EFr;
 };
 
 constexpr int ACA_TAB_N = 12;  // rule-table bins per axis

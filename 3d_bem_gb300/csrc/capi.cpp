@@ -183,6 +183,14 @@ struct bem_handle {
   DBuf<unsigned char> dfPre, dfFin;
   DBuf<int> dfCtrl, dfErr;
   DBuf<int> dBad;
+  // impedance plane (bem_set_impedance_plane): point, unit normal and the
+  // elements reflected in it (cluster order)
+  bool have_plane = false;
+  double plane_p[3] = {0, 0, 0}, plane_n[3] = {0, 0, 0};
+  std::vector<Elem> Er;
+  DBuf<Elem> dEr;
+  DBuf<ElemF> dEFr;
+  DBuf<FieldElemF> dFeR;
   // field evaluation (bem_field): element records, coefficients, partial
   // sums, copies of the caller's points / boundary data / sources
   DBuf<FieldElemF> dFe;
@@ -371,6 +379,8 @@ AcaArgs aca_args(bem_handle* h, DevHM& m, int which, int extra) {
   a.precision = m.prec;
   a.E = h->dE.p;
   a.EF = h->dEF.p;
+  a.Er = h->have_plane && !h->points_mode ? h->dEr.p : nullptr;
+  a.EFr = h->have_plane && !h->points_mode ? h->dEFr.p : nullptr;
   a.bc = h->dBc.p;
   a.k = h->k;
   a.near_r = h->near_r;
@@ -483,6 +493,8 @@ void assemble(bem_handle* h, double freq, double* t_near, double* t_aca) {
   na.precision = h->hm[0].prec;
   na.E = h->dE.p;
   na.EF = h->dEF.p;
+  na.Er = h->have_plane ? h->dEr.p : nullptr;
+  na.EFr = h->have_plane ? h->dEFr.p : nullptr;
   na.bc = h->dBc.p;
   na.blocks = h->dNear.p;
   na.tiles = h->dTiles.p;
@@ -502,7 +514,9 @@ void assemble(bem_handle* h, double freq, double* t_near, double* t_aca) {
   // disjoint pools of the same matrices
   cudaStream_t ns = h->nearst;
   CK(cudaStreamWaitEvent(ns, h->ev[0], 0));
-  const bool learned = (h->cfg.selector & 1) && na.precision == 1;
+  // the learned near-field orders were trained on free-space pairs: with an
+  // impedance plane the near field keeps the 16-point rule
+  const bool learned = (h->cfg.selector & 1) && na.precision == 1 && !h->have_plane;
   if (learned) {
     require(h->have_selector, BEM_EINVAL, "selector weights not set (bem_set_selector)");
     h->dCls.ensure(h->L.near_entries);
@@ -1183,6 +1197,16 @@ void clone_state(bem_handle* c, bem_handle* p) {
   c->beta = p->beta;
   c->impedance = p->impedance;
   c->have_bc = p->have_bc;
+  c->have_plane = p->have_plane;
+  if (p->have_plane) {
+    for (int d = 0; d < 3; d++) {
+      c->plane_p[d] = p->plane_p[d];
+      c->plane_n[d] = p->plane_n[d];
+    }
+    c->Er = p->Er;
+    c->dEr.upload(c->Er, c->stream);
+    c->dEFr.upload(make_elemf(c->Er), c->stream);
+  }
   c->have_aca_tab = p->have_aca_tab;
   if (p->have_aca_tab) {
     c->dAcaTab.ensure(ACA_TAB_N * ACA_TAB_N);
@@ -1444,6 +1468,7 @@ bem_status bem_set_mesh(bem_handle* h, const double* tri, int64_t n) {
     h->cols = h->rows;
     h->N = n;
     prepare_elements(tri, h->rows.perm, h->E, h->avgdim);
+    h->have_plane = false;  // a plane belongs to the mesh it was set for
     for (const Elem& e : h->E)
       require(e.area > 0 && std::isfinite(e.nrm[0]), BEM_EINVAL, "degenerate (zero-area) triangle");
     h->near_r = 4.0 * h->avgdim;
@@ -1561,6 +1586,58 @@ bem_status bem_set_bc_impedance(bem_handle* h, const double* beta) {
     h->have_hlu = false;  // factors of another operator
     h->have_bc = true;
     h->state_gen++;
+  });
+}
+
+bem_status bem_set_impedance_plane(bem_handle* h, const double* point, const double* normal) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] {
+    require(h->have_mesh && !h->points_mode, BEM_EINVAL, "mesh not set (bem_set_mesh)");
+    double nn = 0;
+    if (normal)
+      for (int d = 0; d < 3; d++) nn += normal[d] * normal[d];
+    h->have_hlu = false;  // factors of another operator
+    h->state_gen++;
+    if (!normal || nn == 0.0) {  // no plane
+      h->have_plane = false;
+      return;
+    }
+    require(point && std::isfinite(nn), BEM_EINVAL, "plane point and normal required");
+    for (int d = 0; d < 3; d++)
+      require(std::isfinite(point[d]), BEM_EINVAL, "non-finite plane point");
+    // MeshFunctions::reflectTriangles (meshfunctions.cpp:349-380): every node
+    // x -> x - 2 (n . x + d) n with the unit normal n and d = -n . point; node 1
+    // and node 3 swap so the reflected element keeps its orientation
+    const double inv = 1.0 / std::sqrt(nn);
+    double n[3], dd = 0;
+    for (int d = 0; d < 3; d++) {
+      n[d] = normal[d] * inv;
+      dd -= n[d] * point[d];
+    }
+    const int64_t N = h->N;
+    std::vector<double> tri((size_t)9 * N);
+    const auto reflect = [&](const double* x, double* out) {
+      const double t = n[0] * x[0] + n[1] * x[1] + n[2] * x[2] + dd;
+      for (int d = 0; d < 3; d++) out[d] = x[d] - 2.0 * t * n[d];
+    };
+    for (int64_t i = 0; i < N; i++) {
+      const Elem& e = h->E[i];
+      reflect(e.n3, &tri[9 * i]);
+      reflect(e.n2, &tri[9 * i + 3]);
+      reflect(e.n1, &tri[9 * i + 6]);
+    }
+    std::vector<int64_t> ident(N);
+    for (int64_t i = 0; i < N; i++) ident[i] = i;
+    double avg = 0;
+    prepare_elements(tri.data(), ident, h->Er, avg);
+    for (int d = 0; d < 3; d++) {
+      h->plane_p[d] = point[d];
+      h->plane_n[d] = n[d];
+    }
+    h->dEr.upload(h->Er, h->stream);
+    h->dEFr.upload(make_elemf(h->Er), h->stream);
+    h->have_plane = true;
+    sync(h);
   });
 }
 
@@ -2000,13 +2077,26 @@ void field_dev(bem_handle* h, double freq, const double* pts, int64_t M, const d
   if (prec == 1) h->dFe.ensure((size_t)N);
   h->dFcoef.ensure((size_t)N * R * (prec == 1 ? sizeof(FieldCoefF) : sizeof(FieldCoef)));
   const int S = field_split(h, M);
-  h->dFpart.ensure((size_t)S * R * M);
+  // with an impedance plane the reflected elements add a second set of S
+  // partial sums with the same coefficients (:2305-2311)
+  const int passes = h->have_plane ? 2 : 1;
+  h->dFpart.ensure((size_t)passes * S * R * M);
   h->launches += launch_field_prep(h->dE.p, h->dPerm.p, N, phi, dphi, (int)R, prec, h->dFe.p,
                                    h->dFcoef.p, s);
   h->launches += launch_field_sum(h->dE.p, h->dFe.p, h->dFcoef.p, N, (int)R, pts, M, k, prec, S,
                                   h->dFpart.p, s);
-  h->launches += launch_field_finish(h->dFpart.p, S, M, (int)R, pts, nsrc ? h->dFsrc.p : nullptr,
-                                     (int)nsrc, k, pfac, phi_f, p_f, s);
+  if (h->have_plane) {
+    if (prec == 1) {
+      h->dFeR.ensure((size_t)N);
+      h->launches += launch_field_prep(h->dEr.p, nullptr, N, nullptr, nullptr, 0, prec,
+                                       h->dFeR.p, nullptr, s);
+    }
+    h->launches += launch_field_sum(h->dEr.p, h->dFeR.p, h->dFcoef.p, N, (int)R, pts, M, k, prec,
+                                    S, h->dFpart.p + (size_t)S * R * M, s);
+  }
+  h->launches += launch_field_finish(h->dFpart.p, passes * S, M, (int)R, pts,
+                                     nsrc ? h->dFsrc.p : nullptr, (int)nsrc, k, pfac, phi_f, p_f,
+                                     s);
   CK(cudaGetLastError());
 }
 

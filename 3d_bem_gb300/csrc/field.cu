@@ -80,6 +80,7 @@ __global__ void field_prep_kernel(const Elem* __restrict__ E, const int64_t* __r
     f.pad[0] = f.pad[1] = f.pad[2] = 0.0f;
     fe[j] = f;
   }
+  if (R == 0) return;  // element records only (the reflected elements)
   const int64_t cj = perm[j];
   const double A = e.area;
   for (int r = 0; r < R; r++) {

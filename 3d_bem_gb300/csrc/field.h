@@ -40,7 +40,8 @@ constexpr int FIELD_RB = 4;     // right-hand sides per pass
 // Element records (precision 1 only) and the coefficients of R columns:
 // phi, dphi are N x R complex FP64 in the caller's order, perm[j] the caller
 // index of cluster-order element j. coef: R x N FieldCoefF (precision 1) or
-// FieldCoef (precision 0).
+// FieldCoef (precision 0). R = 0: the records only (perm, phi, dphi, coef
+// unused).
 int launch_field_prep(const Elem* E, const int64_t* perm, int64_t N, const double2* phi,
                       const double2* dphi, int R, int precision, FieldElemF* fe, void* coef,
                       cudaStream_t s);

@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(256) nearfield_regular_kernel(
     const Elem* __restrict__ E, const BcCoef* __restrict__ bc,
     const NearBlock* __restrict__ blocks, const NearTile* __restrict__ tiles,
     const uint32_t* __restrict__ special_bits, double k, double2 alpha,
-    double2* __restrict__ phi, double2* __restrict__ dphi) {
+    double2* __restrict__ phi, double2* __restrict__ dphi, const Elem* __restrict__ Er) {
   const NearTile t = tiles[blockIdx.x];
   if ((int)threadIdx.x >= t.count) return;
   const NearBlock b = blocks[t.block];
@@ -54,6 +54,7 @@ __global__ void __launch_bounds__(256) nearfield_regular_kernel(
   const int r = e % b.m, c = e / b.m;
   const int64_t row = b.r0 + r, col = b.c0 + c;
   Ops o = ops_regular(E[row], E[col], k, c_rules);
+  if (Er) ops_add(o, ops_regular(E[row], Er[col], k, c_rules));
   double2 p, d;
   substitute(o, false, bc[col], alpha, p, d);
   phi[g] = p;
@@ -66,7 +67,7 @@ __global__ void __launch_bounds__(256) nearfield_regular32_kernel(
     const Elem* __restrict__ E, const ElemF* __restrict__ EF, const BcCoef* __restrict__ bc,
     const NearBlock* __restrict__ blocks, const NearTile* __restrict__ tiles,
     const uint32_t* __restrict__ special_bits, float k, float2 alpha, float2* __restrict__ phi,
-    float2* __restrict__ dphi) {
+    float2* __restrict__ dphi, const ElemF* __restrict__ EFr) {
   const NearTile t = tiles[blockIdx.x];
   if ((int)threadIdx.x >= t.count) return;
   const NearBlock b = blocks[t.block];
@@ -76,6 +77,7 @@ __global__ void __launch_bounds__(256) nearfield_regular32_kernel(
   const int r = e % b.m, c = e / b.m;
   const int64_t row = b.r0 + r, col = b.c0 + c;
   OpsF o = ops_regular32(EF, row, col, k, c_rules);
+  if (EFr) ops_add(o, ops_regular32_pq(EF[row], EFr[col], k, c_rules));
   float2 p, d;
   substitute32(o, bc[col], alpha, p, d);
   phi[g] = p;
@@ -89,12 +91,15 @@ __global__ void __launch_bounds__(128) nearfield_special_kernel(
     const Elem* __restrict__ E, const BcCoef* __restrict__ bc,
     const int64_t* __restrict__ sp_entry, const int32_t* __restrict__ sp_row,
     const int32_t* __restrict__ sp_col, int64_t count, double k, double2 alpha,
-    T* __restrict__ phi, T* __restrict__ dphi) {
+    T* __restrict__ phi, T* __restrict__ dphi, const Elem* __restrict__ Er) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
   const int64_t row = sp_row[i], col = sp_col[i];
   Ops o = (row == col) ? ops_singular(E[row], k, c_rules)
                        : ops_nearsing(E[row], E[col], k, c_rules);
+  // the reflected element always takes the regular rule (BemOperatorsReflected,
+  // boundaryelementsolver.cpp:1516-1554)
+  if (Er) ops_add(o, ops_regular(E[row], Er[col], k, c_rules));
   double2 p, d;
   substitute(o, row == col, bc[col], alpha, p, d);
   const int64_t g = sp_entry[i];
@@ -158,20 +163,22 @@ void launch_nearfield(const NearfieldArgs& a, cudaStream_t s) {
     if (a.ntiles > 0)
       nearfield_regular_kernel<<<(unsigned)a.ntiles, 256, 0, s>>>(
           a.E, a.bc, a.blocks, a.tiles, a.special_bits, a.k, a.alpha, (double2*)a.phi,
-          (double2*)a.dphi);
+          (double2*)a.dphi, a.Er);
     if (a.nspecial > 0)
       nearfield_special_kernel<double2><<<g, 128, 0, s>>>(a.E, a.bc, a.sp_entry, a.sp_row,
                                                           a.sp_col, a.nspecial, a.k, a.alpha,
-                                                          (double2*)a.phi, (double2*)a.dphi);
+                                                          (double2*)a.phi, (double2*)a.dphi,
+                                                          a.Er);
   } else {
     if (a.ntiles > 0)
       nearfield_regular32_kernel<<<(unsigned)a.ntiles, 256, 0, s>>>(
           a.E, a.EF, a.bc, a.blocks, a.tiles, a.special_bits, (float)a.k,
-          make_float2((float)a.alpha.x, (float)a.alpha.y), (float2*)a.phi, (float2*)a.dphi);
+          make_float2((float)a.alpha.x, (float)a.alpha.y), (float2*)a.phi, (float2*)a.dphi,
+          a.EFr);
     if (a.nspecial > 0)
       nearfield_special_kernel<float2><<<g, 128, 0, s>>>(a.E, a.bc, a.sp_entry, a.sp_row,
                                                          a.sp_col, a.nspecial, a.k, a.alpha,
-                                                         (float2*)a.phi, (float2*)a.dphi);
+                                                         (float2*)a.phi, (float2*)a.dphi, a.Er);
   }
 }
 

@@ -372,12 +372,11 @@ __device__ __forceinline__ void centroid_diff(const ElemF& P, const ElemF& Q, fl
 // centroid difference c_p - c_q keeps ~7 significant digits (two-float
 // centroids); source points are offsets from c_q, so r = |p - q| keeps ~7
 // significant digits even for neighbouring panels.
-__device__ __forceinline__ OpsF ops_regular32(const ElemF* __restrict__ EF, int64_t row,
-                                              int64_t col, float k, const QuadRules& R) {
+__device__ __forceinline__ OpsF ops_regular32_pq(const ElemF& P, const ElemF& Q, float k,
+                                                 const QuadRules& R) {
   float dx, dy, dz;
-  centroid_diff(EF[row], EF[col], dx, dy, dz);
-  const ElemF& Q = EF[col];
-  const float npx = EF[row].nrm[0], npy = EF[row].nrm[1], npz = EF[row].nrm[2];
+  centroid_diff(P, Q, dx, dy, dz);
+  const float npx = P.nrm[0], npy = P.nrm[1], npz = P.nrm[2];
   const float nqx = Q.nrm[0], nqy = Q.nrm[1], nqz = Q.nrm[2];
   const float upNq = npx * nqx + npy * nqy + npz * nqz;
   const float inv4pi = 0.0795774715459476679f;
@@ -421,6 +420,27 @@ __device__ __forceinline__ OpsF ops_regular32(const ElemF* __restrict__ EF, int6
   o.Mt = fmk(A * Tx, A * Ty);
   o.N = fmk(A * Nx, A * Ny);
   return o;
+}
+
+__device__ __forceinline__ OpsF ops_regular32(const ElemF* __restrict__ EF, int64_t row,
+                                              int64_t col, float k, const QuadRules& R) {
+  return ops_regular32_pq(EF[row], EF[col], k, R);
+}
+
+// Sums of operator sets: an entry with an impedance plane adds the operators
+// of the column element reflected in the plane to its own (the substitution
+// is affine in L, M, Mt, N and the reflected part has no jump terms).
+__device__ __forceinline__ void ops_add(OpsF& a, const OpsF& b) {
+  a.L = fadd(a.L, b.L);
+  a.M = fadd(a.M, b.M);
+  a.Mt = fadd(a.Mt, b.Mt);
+  a.N = fadd(a.N, b.N);
+}
+__device__ __forceinline__ void ops_add(Ops& a, const Ops& b) {
+  a.L = cadd(a.L, b.L);
+  a.M = cadd(a.M, b.M);
+  a.Mt = cadd(a.Mt, b.Mt);
+  a.N = cadd(a.N, b.N);
 }
 
 // FP32 BC substitution for off-diagonal regular entries (no jump terms).

@@ -291,6 +291,23 @@ bem_status bem_autotune(bem_handle* h, double freq, int64_t nrhs, int64_t* tuned
 bem_status bem_sweep(bem_handle* h, const double* freqs, int64_t nf, const double* g,
                      int64_t nrhs, double* p, bem_solve_info* info);
 
+/* One impedance plane (BoundaryElements::impedancePlanes with a single entry,
+ * the infinite baffle of the solving scripts): the plane through point with
+ * the given normal. Every matrix entry then adds the operators of the column
+ * element reflected in the plane, integrated with the regular 16-point rule
+ * (implicitPhiMatrixPlusReflected / implicitDPhiMatrixPlusReflected,
+ * boundaryelementsolver.cpp:2042-2050, via implicitPhiMatrixReflected /
+ * implicitDPhiMatrixReflected :1556-1643), on the same block partition; the
+ * reflected element is MeshFunctions::reflectTriangles (meshfunctions.cpp:
+ * 349-380: mirrored nodes, node 1 and node 3 swapped). bem_field adds the
+ * reflected terms as calculateFieldSolutionRegular does (:2305-2311). With a
+ * plane the near field ignores selector bit 0 (the learned near-field orders
+ * were trained on free-space pairs). normal = NULL or zero removes the plane;
+ * bem_set_mesh removes it too. bem_operators keeps returning the free-space
+ * operators. Two planes (the reference's reflection matrices, :746-842) are
+ * not supported. */
+bem_status bem_set_impedance_plane(bem_handle* h, const double* point, const double* normal);
+
 /* Field evaluation (BoundaryElementSolver::calculateFieldSolution,
  * boundaryelementsolver.cpp:2192-2249, as its regular sum
  * calculateFieldSolutionRegular :2263-2316 with BemOperatorField :2318-2353):

@@ -81,7 +81,8 @@ def lib():
         L.orc_line_rule.argtypes = [ct.c_int64, F64P]
         L.orc_field.argtypes = [F64P, ct.c_int64, ct.c_double, ct.c_double, ct.c_double,
                                 F64P, ct.c_int64, F64P, F64P, ct.c_int64, F64P, ct.c_int64,
-                                ct.c_int, F64P, F64P]
+                                F64P, ct.c_int, F64P, F64P]
+        L.orc_set_plane.argtypes = [vp, F64P, F64P]
         L.orc_pivot_hash.restype = ct.c_uint64
         L.orc_pivot_hash.argtypes = [ct.c_uint64, ct.c_uint64, ct.c_uint64]
         _lib = L
@@ -113,6 +114,15 @@ class Problem:
         if getattr(self, "_h", None):
             lib().orc_destroy(self._h)
             self._h = None
+
+    def set_plane(self, point=None, normal=None):
+        """One impedance plane (None removes it)."""
+        if normal is None:
+            lib().orc_set_plane(self._h, None, None)
+            return
+        p = np.ascontiguousarray(point, np.float64)
+        n = np.ascontiguousarray(normal, np.float64)
+        lib().orc_set_plane(self._h, _f(p), _f(n))
 
     @property
     def perm(self):
@@ -285,7 +295,8 @@ def line_rule(n):
     return out[:k].copy()
 
 
-def field(tri, freq, pts, phi, dphi, sources=None, c=343.0, rho=1.2041, nthreads=0):
+def field(tri, freq, pts, phi, dphi, sources=None, c=343.0, rho=1.2041, nthreads=0,
+          plane=None):
     """Velocity potential and sound pressure at observation points (npts x R
     each) from a boundary solution phi, dphi (n x R, caller order); sources:
     rows (x, y, z, complex weight)."""
@@ -303,8 +314,11 @@ def field(tri, freq, pts, phi, dphi, sources=None, c=343.0, rho=1.2041, nthreads
     pf = np.zeros((pts.shape[0], R), np.complex128, order="F")
     pp = np.zeros((pts.shape[0], R), np.complex128, order="F")
     # complex arrays are passed by their data pointers (interleaved re, im)
+    pl = None if plane is None else np.ascontiguousarray(np.concatenate(
+        [np.asarray(plane[0], np.float64).ravel(), np.asarray(plane[1], np.float64).ravel()]))
     lib().orc_field(_f(tri), n, freq, c, rho, _f(pts), pts.shape[0], _f(phi), _f(dphi), R,
-                    _f(src), src.shape[0], nthreads, _f(pf), _f(pp))
+                    _f(src), src.shape[0], _f(pl) if pl is not None else None, nthreads,
+                    _f(pf), _f(pp))
     return pf, pp
 
 

@@ -15,6 +15,9 @@ struct orc_problem {
   Mesh mesh;
   ClusterTree tree;
   std::vector<BlockInfo> blocks;
+  Mesh refl;              // impedance plane: reflected elements (cluster order)
+  bool has_refl = false;
+  const Mesh* reflected() const { return has_refl ? &refl : nullptr; }
 };
 
 struct orc_hmatrix {
@@ -46,6 +49,16 @@ orc_problem* orc_create(const double* tri, int64_t n, int64_t leaf, double eta) 
   mesh_prepare(p->mesh);
   p->blocks = build_partition(p->tree, p->tree, eta);
   return p;
+}
+
+void orc_set_plane(orc_problem* p, const double* point, const double* normal) {
+  if (!normal || (normal[0] == 0 && normal[1] == 0 && normal[2] == 0)) {
+    p->has_refl = false;
+    return;
+  }
+  p->refl = reflect_mesh(p->mesh, V3(point[0], point[1], point[2]),
+                         V3(normal[0], normal[1], normal[2]));
+  p->has_refl = true;
 }
 
 void orc_destroy(orc_problem* p) { delete p; }
@@ -86,7 +99,7 @@ void orc_geometry(const orc_problem* p, double* normals, double* areas, double* 
 
 void orc_operators(const orc_problem* p, double k, const int64_t* rows, const int64_t* cols,
                    int64_t cnt, double* out) {
-  OperatorCtx ctx(&p->mesh, k);
+  OperatorCtx ctx(&p->mesh, k, p->reflected());
   cd* o = C(out);
 #pragma omp parallel for schedule(dynamic, 64)
   for (int64_t e = 0; e < cnt; e++) {
@@ -101,7 +114,7 @@ void orc_operators(const orc_problem* p, double k, const int64_t* rows, const in
 void orc_entries(const orc_problem* p, double k, int coupling, const double* a,
                  const double* b, const int64_t* rows, const int64_t* cols, int64_t cnt,
                  double* phi, double* dphi) {
-  OperatorCtx ctx(&p->mesh, k);
+  OperatorCtx ctx(&p->mesh, k, p->reflected());
   Coupling cp = coupling_parameter(coupling, k);
   EntryGen g{&ctx, cp.alpha, cp.alpha_half, C(a), C(b), 0};
 #pragma omp parallel for schedule(dynamic, 64)
@@ -146,7 +159,7 @@ static orc_hmatrix* assemble(const std::vector<BlockInfo>& blocks, int64_t nr, i
 orc_hmatrix* orc_hassemble(const orc_problem* p, double k, int coupling, const double* a,
                            const double* b, int which, double tol, int64_t max_rank,
                            uint64_t seed, int nthreads) {
-  OperatorCtx ctx(&p->mesh, k);
+  OperatorCtx ctx(&p->mesh, k, p->reflected());
   Coupling cp = coupling_parameter(coupling, k);
   EntryGen g{&ctx, cp.alpha, cp.alpha_half, C(a), C(b), which};
   EntryFn f = [&g](int64_t r, int64_t c) { return g(r, c); };
@@ -546,7 +559,7 @@ int orc_solve(const orc_problem* p, double freq, double c, double rho, int coupl
 
 void orc_dense(const orc_problem* p, double k, int coupling, const double* a, const double* b,
                double* phi, double* dphi, int nthreads) {
-  OperatorCtx ctx(&p->mesh, k);
+  OperatorCtx ctx(&p->mesh, k, p->reflected());
   Coupling cp = coupling_parameter(coupling, k);
   EntryGen g{&ctx, cp.alpha, cp.alpha_half, C(a), C(b), 0};
   int64_t N = p->mesh.n;

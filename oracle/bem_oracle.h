@@ -62,6 +62,12 @@ typedef struct orc_hmatrix orc_hmatrix;
 /* Mesh + cluster tree + block partition (triangles reordered internally). */
 orc_problem* orc_create(const double* tri, int64_t n, int64_t leaf, double eta);
 void orc_destroy(orc_problem* p);
+/* One impedance plane (point, normal; normal NULL or zero removes it): every
+ * operator evaluation adds the reflected column element's regular-rule
+ * operators (implicitPhiMatrixPlusReflected, boundaryelementsolver.cpp:
+ * 2042-2050; BemOperatorsReflected :1516-1554; MeshFunctions::reflectTriangles
+ * meshfunctions.cpp:349-380). */
+void orc_set_plane(orc_problem* p, const double* point, const double* normal);
 int64_t orc_n(const orc_problem* p);
 /* perm[new_index] = caller index */
 void orc_perm(const orc_problem* p, int64_t* perm);
@@ -143,11 +149,13 @@ void orc_dense(const orc_problem* p, double k, int coupling, const double* a,
  * 2263-2316; BemOperatorField :2318-2353; sourcePhiTerm :3443-3450): tri is
  * n x 9 in the caller's order, phi / dphi n x nrhs complex, pts npts x 3,
  * src nsrc x 5 (x, y, z, Re w, Im w); phi_f and p_f (npts x nrhs complex) may
- * be NULL. p_f = i rho 2 pi f phi_f (2 pi at f = 0). */
+ * be NULL. p_f = i rho 2 pi f phi_f (2 pi at f = 0). plane: NULL or 6 doubles
+ * (point, normal) of one impedance plane, whose reflected elements add their
+ * terms with the same boundary data (:2305-2311). */
 void orc_field(const double* tri, int64_t n, double freq, double c, double rho,
                const double* pts, int64_t npts, const double* phi, const double* dphi,
-               int64_t nrhs, const double* src, int64_t nsrc, int nthreads,
-               double* phi_f, double* p_f);
+               int64_t nrhs, const double* src, int64_t nsrc, const double* plane,
+               int nthreads, double* phi_f, double* p_f);
 
 /* Quadrature tables used (for cross-checking the GPU library's copy). */
 int64_t orc_triangle_rule(int64_t order, double* out /* npts x 3 */);

@@ -9,7 +9,9 @@
 // boundaryelementsolver.h:653-654), Lk = A sum w G, Mk = A sum w dG/dr rnq,
 // G = exp(ikr) / (4 pi r), dG/dr = (G / r)(ikr - 1), rnq = -((p - q) . n_q) / r.
 // Sound pressure: i rho 2 pi f phi, with 2 pi in place of 2 pi f at f = 0
-// (calculateFieldSolution, :2232-2244). k = 2 pi f / c (:2199).
+// (calculateFieldSolution, :2232-2244). k = 2 pi f / c (:2199). With one
+// impedance plane the reflected elements add the same terms with the same
+// boundary data (:2305-2311).
 #include "bem_oracle.h"
 #include "oracle_core.hpp"
 
@@ -21,8 +23,8 @@ using namespace orc;
 
 extern "C" void orc_field(const double* tri, int64_t n, double freq, double c, double rho,
                           const double* pts, int64_t npts, const double* phi, const double* dphi,
-                          int64_t nrhs, const double* src, int64_t nsrc, int nthreads,
-                          double* phi_f, double* p_f) {
+                          int64_t nrhs, const double* src, int64_t nsrc, const double* plane,
+                          int nthreads, double* phi_f, double* p_f) {
   Mesh m;
   m.tri.resize(n);
   for (int64_t i = 0; i < n; i++) {
@@ -30,6 +32,12 @@ extern "C" void orc_field(const double* tri, int64_t n, double freq, double c, d
     m.tri[i] = Tri{V3(t[0], t[1], t[2]), V3(t[3], t[4], t[5]), V3(t[6], t[7], t[8])};
   }
   mesh_prepare(m);
+  std::vector<const Mesh*> parts{&m};
+  Mesh mirrored;
+  if (plane && (plane[3] != 0 || plane[4] != 0 || plane[5] != 0)) {
+    mirrored = reflect_mesh(m, V3(plane[0], plane[1], plane[2]), V3(plane[3], plane[4], plane[5]));
+    parts.push_back(&mirrored);
+  }
   const Rule2D rule = triangle_rule(5);
   const double k = PI2 * freq / c;
   const cd ik(0.0, k);
@@ -51,9 +59,10 @@ extern "C" void orc_field(const double* tri, int64_t n, double freq, double c, d
       s0 += cd(sq[3], sq[4]) * std::exp(ik * r) / (PI4 * r);
     }
     std::vector<cd> acc(nrhs, s0);
+    for (const Mesh* g : parts)
     for (int64_t j = 0; j < n; j++) {  // BemOperatorField
-      const Tri& t = m.tri[j];
-      const V3 nq = m.normal[j];
+      const Tri& t = g->tri[j];
+      const V3 nq = g->normal[j];
       cd Lk = 0.0, Mk = 0.0;
       for (int i = 0; i < rule.size(); i++) {
         const double a1 = rule.x1[i], a2 = rule.x2[i], a3 = 1.0 - a2 - a1;
@@ -66,8 +75,8 @@ extern "C" void orc_field(const double* tri, int64_t n, double freq, double c, d
         Lk += rule.w[i] * G;
         Mk += rule.w[i] * ((G / r) * (ikr - 1.0)) * rnq;
       }
-      Lk *= m.area[j];
-      Mk *= m.area[j];
+      Lk *= g->area[j];
+      Mk *= g->area[j];
       for (int64_t r = 0; r < nrhs; r++) acc[r] += Mk * ph[r * n + j] - Lk * dph[r * n + j];
     }
     for (int64_t r = 0; r < nrhs; r++) {

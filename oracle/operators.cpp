@@ -274,7 +274,30 @@ void mesh_prepare(Mesh& m) {
   m.avgdim = m.n > 0 ? acc / m.n / 2.0 : 0.0;
 }
 
-OperatorCtx::OperatorCtx(const Mesh* m, double k_) : mesh(m), k(k_) {
+Mesh reflect_mesh(const Mesh& m, const V3& point, V3 normal) {
+  const double nn = norm(normal);
+  normal = V3(normal.x / nn, normal.y / nn, normal.z / nn);
+  const double d = -dot(normal, point);
+  double R[3][4];
+  for (int i = 0; i < 3; i++) {
+    for (int j = 0; j < 3; j++) R[i][j] = (i == j ? 1.0 : 0.0) - 2.0 * normal[i] * normal[j];
+    R[i][3] = -2.0 * normal[i] * d;
+  }
+  const auto apply = [&](const V3& x) {
+    V3 y;
+    for (int i = 0; i < 3; i++) y[i] = R[i][0] * x.x + R[i][1] * x.y + R[i][2] * x.z + R[i][3];
+    return y;
+  };
+  Mesh r;
+  r.tri.resize(m.tri.size());
+  for (size_t i = 0; i < m.tri.size(); i++)
+    r.tri[i] = Tri{apply(m.tri[i].n3), apply(m.tri[i].n2), apply(m.tri[i].n1)};
+  mesh_prepare(r);
+  return r;
+}
+
+OperatorCtx::OperatorCtx(const Mesh* m, double k_, const Mesh* reflected)
+    : mesh(m), k(k_), refl(reflected) {
   reg = triangle_rule(8);  // orderRegular = 8 (boundaryelementsolver.h:655-660)
   line = line_rule(5);     // orderLineQuadrature = 5 (:662-664)
   Rule1D g32 = gauss_legendre(32);
@@ -286,10 +309,19 @@ OperatorCtx::OperatorCtx(const Mesh* m, double k_) : mesh(m), k(k_) {
 
 // BemOperatorsConst dispatch (boundaryelementsolver.cpp:844-856).
 Ops OperatorCtx::eval(int64_t row, int64_t col) const {
-  if (row == col) return singular(row);
-  if (norm(mesh->colloc[row] - mesh->colloc[col]) < 4.0 * mesh->avgdim)
-    return near_singular(row, col);
-  return regular(row, col);
+  Ops o;
+  if (row == col) o = singular(row);
+  else if (norm(mesh->colloc[row] - mesh->colloc[col]) < 4.0 * mesh->avgdim)
+    o = near_singular(row, col);
+  else o = regular(row, col);
+  if (refl) {
+    const Ops r = regular_from(row, *refl, col);
+    o.L += r.L;
+    o.M += r.M;
+    o.Mt += r.Mt;
+    o.N += r.N;
+  }
+  return o;
 }
 
 namespace {
@@ -314,17 +346,19 @@ inline void accumulate(Ops& o, double w, V3 p, V3 q, V3 np, V3 nq, double upNq, 
 }  // namespace
 
 // Regular 16-point rule (boundaryelementsolver.cpp:857-893).
-Ops OperatorCtx::regular(int64_t row, int64_t col) const {
+Ops OperatorCtx::regular(int64_t row, int64_t col) const { return regular_from(row, *mesh, col); }
+
+Ops OperatorCtx::regular_from(int64_t row, const Mesh& cm, int64_t col) const {
   Ops o{};
-  const Tri& t = mesh->tri[col];
-  V3 p = mesh->colloc[row], np = mesh->normal[row], nq = mesh->normal[col];
+  const Tri& t = cm.tri[col];
+  V3 p = mesh->colloc[row], np = mesh->normal[row], nq = cm.normal[col];
   double upNq = dot(np, nq);
   for (int i = 0; i < reg.size(); i++) {
     double a1 = reg.x1[i], a2 = reg.x2[i], a3 = 1.0 - a2 - a1;
     V3 q = (a1 * t.n1) + (a2 * t.n2) + (a3 * t.n3);
     accumulate(o, reg.w[i], p, q, np, nq, upNq, k);
   }
-  double A = mesh->area[col];
+  double A = cm.area[col];
   o.L *= A;
   o.M *= A;
   o.Mt *= A;

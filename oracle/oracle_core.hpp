@@ -61,6 +61,10 @@ struct Mesh {
   double avgdim = 0;
 };
 void mesh_prepare(Mesh& m);
+// MeshFunctions::reflectTriangles (meshfunctions.cpp:349-380): the mesh
+// mirrored in the plane through point with normal (4 x 4 reflection matrix,
+// node 1 and node 3 swapped), prepared (normals, centroids, areas)
+Mesh reflect_mesh(const Mesh& m, const V3& point, V3 normal);
 
 struct Ops {
   cd L, M, Mt, N;
@@ -72,9 +76,15 @@ struct OperatorCtx {
   Rule2D reg;   // 16-point rule (order 8)
   Rule1D line;  // 5-point Gauss-Legendre
   Rule1D gl16;  // positive half of the 32-point Gauss-Legendre rule
-  OperatorCtx(const Mesh* m, double k_);
+  const Mesh* refl = nullptr;  // impedance plane: the reflected elements, same order
+  OperatorCtx(const Mesh* m, double k_, const Mesh* reflected = nullptr);
+  // operators of the pair, plus those of the reflected column element when a
+  // plane is set (implicitPhiMatrixPlusReflected, boundaryelementsolver.cpp:2042-2050)
   Ops eval(int64_t row, int64_t col) const;
   Ops regular(int64_t row, int64_t col) const;
+  // regular rule with the column element taken from another mesh
+  // (BemOperatorsReflected, :1516-1554)
+  Ops regular_from(int64_t row, const Mesh& cols, int64_t col) const;
   Ops singular(int64_t t) const;
   Ops near_singular(int64_t row, int64_t col) const;
 };

@@ -278,3 +278,63 @@ def test_field_pulsating_sphere(orc, meshes):
     pa = rho * c * (1j * k * a) / (1j * k * a - 1)
     ex = pa * (a / r) * np.exp(1j * k * (r - a))
     assert np.abs(pp[:, 0] - ex).max() / abs(pa) < 0.03
+
+
+def _mirror(tri, point, normal):
+    """MeshFunctions::reflectTriangles: mirrored nodes, node 1 and node 3 swapped."""
+    nrm = np.asarray(normal, float) / np.linalg.norm(normal)
+    d = -nrm @ np.asarray(point, float)
+    R = lambda x: x - 2.0 * (x @ nrm + d)[:, None] * nrm
+    return np.hstack([R(tri[:, 6:9]), R(tri[:, 3:6]), R(tri[:, 0:3])])
+
+
+def _caller(D, perm):
+    out = np.empty_like(D)
+    out[np.ix_(perm, perm)] = D
+    return out
+
+
+def test_half_space_equals_mirrored_full_space(orc, meshes):
+    """One impedance plane (implicitPhiMatrixPlusReflected): the half-space
+    matrices equal the free-space matrices of the body plus its mirror image,
+    folded onto the body's elements (mirror far enough that no mirrored pair
+    is near-singular, so both use the regular rule)."""
+    tri = meshes.icosphere(2, 0.5)
+    tri[:, 2::3] += 0.9
+    n = tri.shape[0]
+    point, normal = [0.0, 0.0, 0.0], [0.0, 0.0, 2.0]
+    full = np.vstack([tri, _mirror(tri, point, normal)])
+    rng = np.random.default_rng(2)
+    a = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    k = 2 * np.pi * 300.0 / 343.0
+    P = orc.Problem(tri)
+    P.set_plane(point, normal)
+    F = orc.Problem(full)
+    hp, hd = P.dense(k, 2, a[P.perm], b[P.perm])
+    a2, b2 = np.concatenate([a, a]), np.concatenate([b, b])
+    fp, fd = F.dense(k, 2, a2[F.perm], b2[F.perm])
+    for H, Fm in ((hp, fp), (hd, fd)):
+        Hc, Fc = _caller(H, P.perm), _caller(Fm, F.perm)
+        assert rel(Hc, Fc[:n, :n] + Fc[:n, n:]) < 1e-13
+    # removing the plane gives the free-space matrices back
+    P.set_plane()
+    fp1, _ = orc.Problem(tri).dense(k, 2, a[P.perm], b[P.perm])
+    hp1, _ = P.dense(k, 2, a[P.perm], b[P.perm])
+    assert np.array_equal(hp1, fp1)
+
+
+def test_half_space_field_equals_mirrored_data(orc, meshes):
+    tri = meshes.icosphere(1, 0.5)
+    tri[:, 2::3] += 0.8
+    n = tri.shape[0]
+    rng = np.random.default_rng(6)
+    phi = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    dphi = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    pts = np.column_stack([rng.uniform(-2, 2, 9), rng.uniform(-2, 2, 9), rng.uniform(0.1, 3, 9)])
+    plane = ([0.0, 0.0, 0.0], [0.0, 0.0, 1.0])
+    f_half, _ = orc.field(tri, 500.0, pts, phi, dphi, plane=plane)
+    full = np.vstack([tri, _mirror(tri, *plane)])
+    f_full, _ = orc.field(full, 500.0, pts, np.concatenate([phi, phi]),
+                          np.concatenate([dphi, dphi]))
+    assert rel(f_half, f_full) < 1e-13
