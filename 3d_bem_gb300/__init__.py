@@ -43,6 +43,7 @@ EXPORTS = [
     "bem_set_aca_rules", "bem_set_bc_impedance", "bem_field", "bem_field_device",
     "bem_msh_read", "bem_msh_free", "bem_msh_num_physical", "bem_msh_physical", "bem_msh_select",
     "bem_msh_elements", "bem_quads_to_triangles", "bem_wall_beta", "bem_set_impedance_plane",
+    "bem_set_point_sources",
 ]
 BEM_ARITH_FP64, BEM_ARITH_FP32, BEM_ARITH_TWOFLOAT = 0, 1, 2
 
@@ -154,6 +155,7 @@ def lib():
     L.bem_quads_to_triangles.argtypes = [vp, i64, vp]
     L.bem_wall_beta.argtypes = [i32, i32, vp, dbl, vp]
     L.bem_set_impedance_plane.argtypes = [vp, vp, vp]
+    L.bem_set_point_sources.argtypes = [vp, vp, i64]
     L.bem_field_device.argtypes = [vp, dbl, vp, i64, vp, vp, i64, vp, i64, vp, vp]
     L.bem_hlu_build.argtypes = [vp]
     L.bem_hlu_solve.argtypes = [vp, vp, vp, i64]
@@ -469,6 +471,13 @@ class Solver:
             self._check(st, "bem_sweep")
         return p, [i.as_dict() for i in infos]
 
+    def set_point_sources(self, sources=None):
+        """Point sources of the right-hand side: rows (x, y, z, complex weight);
+        None clears them."""
+        src = _sources(sources)
+        self._check(lib().bem_set_point_sources(self._h, _ptr(src) if src.shape[0] else None,
+                                                src.shape[0]), "bem_set_point_sources")
+
     def set_impedance_plane(self, point=None, normal=None):
         """One infinite rigid plane (impedance plane); None removes it."""
         if normal is None:
@@ -731,6 +740,8 @@ class BoundaryElementSolver:
                    precond_rank=p.preconditionerRank, precond_tol=p.preconditionerRelError)
         s.set_mesh(self.boundaryElements.triangles)
         s.set_bc(self.boundaryElements.a, self.boundaryElements.b)
+        if self.pointSources:
+            s.set_point_sources(self.pointSources)
         self._s = s
         return s
 

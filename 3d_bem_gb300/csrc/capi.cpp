@@ -185,6 +185,9 @@ struct bem_handle {
   DBuf<int> dBad;
   // impedance plane (bem_set_impedance_plane): point, unit normal and the
   // elements reflected in it (cluster order)
+  // point sources of the right-hand side (bem_set_point_sources)
+  std::vector<double> src;
+  DBuf<double> dSrc;
   bool have_plane = false;
   double plane_p[3] = {0, 0, 0}, plane_n[3] = {0, 0, 0};
   std::vector<Elem> Er;
@@ -1131,8 +1134,13 @@ void solve_dev(bem_handle* h, double freq, const double2* g_caller, int64_t R, d
   launch_gather(g_caller, h->dG.p, h->dPerm.p, N, (int)R, s);
   h->launches++;
   CK(cudaEventRecord(h->ev[3], s));
-  // rhs = source term (none) + phi * g  (boundaryelementsolver.cpp:578-579)
+  // rhs = source term + phi * g  (boundaryelementsolver.cpp:578-579)
   hmatvec_dev(h, 0, h->dG.p, h->dRhs.p, R, 0, ARITH_TWOFLOAT);  // FP64-accurate, FP32 units
+  if (!h->src.empty()) {
+    const cplx al = coupling_parameter(h->cfg.coupling, h->k);
+    h->launches += launch_source_rhs(h->dE.p, N, h->dSrc.p, (int)(h->src.size() / 5), h->k,
+                                     make_double2(al.real(), al.imag()), h->dRhs.p, (int)R, s);
+  }
   CK(cudaEventRecord(h->ev[4], s));
   if (use_precond(h)) {  // initial guess (LU)^{-1} rhs (boundaryelementsolver.cpp:688)
     CK(cudaMemcpyAsync(h->dX.p, h->dRhs.p, (size_t)R * N * sizeof(double2), cudaMemcpyDeviceToDevice, s));
@@ -1197,6 +1205,8 @@ void clone_state(bem_handle* c, bem_handle* p) {
   c->beta = p->beta;
   c->impedance = p->impedance;
   c->have_bc = p->have_bc;
+  c->src = p->src;
+  if (!c->src.empty()) c->dSrc.upload(c->src, c->stream);
   c->have_plane = p->have_plane;
   if (p->have_plane) {
     for (int d = 0; d < 3; d++) {
@@ -1469,6 +1479,7 @@ bem_status bem_set_mesh(bem_handle* h, const double* tri, int64_t n) {
     h->N = n;
     prepare_elements(tri, h->rows.perm, h->E, h->avgdim);
     h->have_plane = false;  // a plane belongs to the mesh it was set for
+    h->src.clear();
     for (const Elem& e : h->E)
       require(e.area > 0 && std::isfinite(e.nrm[0]), BEM_EINVAL, "degenerate (zero-area) triangle");
     h->near_r = 4.0 * h->avgdim;
@@ -1586,6 +1597,20 @@ bem_status bem_set_bc_impedance(bem_handle* h, const double* beta) {
     h->have_hlu = false;  // factors of another operator
     h->have_bc = true;
     h->state_gen++;
+  });
+}
+
+bem_status bem_set_point_sources(bem_handle* h, const double* src, int64_t nsrc) {
+  if (!h) return BEM_EINVAL;
+  return guarded(h, [&] {
+    require(h->have_mesh && !h->points_mode, BEM_EINVAL, "mesh not set (bem_set_mesh)");
+    require(nsrc >= 0 && nsrc <= (1 << 20) && (nsrc == 0 || src), BEM_EINVAL, "bad sources");
+    for (int64_t i = 0; i < 5 * nsrc; i++)
+      require(std::isfinite(src[i]), BEM_ENONFINITE, "non-finite point source");
+    h->src.assign(src, src + 5 * nsrc);
+    if (nsrc > 0) h->dSrc.upload(h->src, h->stream);
+    h->state_gen++;
+    sync(h);
   });
 }
 

@@ -50,6 +50,51 @@ __global__ void finite_kernel(const double2* __restrict__ v, int64_t n, int* __r
 }
 }  // namespace
 
+// sourceTermVector of the right-hand side (BoundaryElementSolver::
+// calculateBoundaryConditionAndSourceTermVector, boundaryelementsolver.cpp:
+// 3386-3429, with sourceTerm :3431-3441): per collocation point (cluster
+// order) the sum over the point sources of G + alpha dG rup, G = w exp(ikr) /
+// (4 pi r), r = |p - s|, rup = (p - s) . n_p / r and dG = (G / r) / (ikr - 1)
+// -- the reference divides by (ikr - 1) where the radial derivative would
+// multiply, and this keeps its formula. Added to all R columns of rhs.
+__global__ void source_rhs_kernel(const Elem* __restrict__ E, int64_t N,
+                                  const double* __restrict__ src, int nsrc, double k,
+                                  double2 alpha, double2* __restrict__ rhs, int R) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const Elem& e = E[i];
+  double sx = 0.0, sy = 0.0;
+  for (int q = 0; q < nsrc; q++) {
+    const double* sq = src + 5 * q;
+    const double dx = e.c[0] - sq[0], dy = e.c[1] - sq[1], dz = e.c[2] - sq[2];
+    const double r = sqrt(dx * dx + dy * dy + dz * dz);
+    const double rup = (dx * e.nrm[0] + dy * e.nrm[1] + dz * e.nrm[2]) / r;
+    double sn, cs;
+    sincos(k * r, &sn, &cs);
+    const double g0 = 1.0 / (4.0 * 3.14159265358979323846 * r);
+    // G = w (cos + i sin) / (4 pi r)
+    const double Gx = (sq[3] * cs - sq[4] * sn) * g0, Gy = (sq[3] * sn + sq[4] * cs) * g0;
+    // dG = (G / r) / (-1 + i k r)
+    const double kr = k * r, den = r * (1.0 + kr * kr);
+    const double dGx = (-Gx + kr * Gy) / den, dGy = (-Gy - kr * Gx) / den;
+    sx += Gx + (alpha.x * dGx - alpha.y * dGy) * rup;
+    sy += Gy + (alpha.x * dGy + alpha.y * dGx) * rup;
+  }
+  for (int r = 0; r < R; r++) {
+    double2& v = rhs[(int64_t)r * N + i];
+    v.x += sx;
+    v.y += sy;
+  }
+}
+
+int launch_source_rhs(const Elem* E, int64_t N, const double* src, int nsrc, double k,
+                      double2 alpha, double2* rhs, int R, cudaStream_t s) {
+  if (N <= 0 || nsrc <= 0) return 0;
+  source_rhs_kernel<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(E, N, src, nsrc, k, alpha, rhs,
+                                                                R);
+  return 1;
+}
+
 int launch_gather(const double2* in, double2* out, const int64_t* perm, int64_t N, int R,
                   cudaStream_t s) {
   dim3 g((unsigned)((N + PT - 1) / PT), (unsigned)R);

@@ -126,7 +126,8 @@ bem_status bem_set_bc(bem_handle* h, const double* a, const double* b);
  * (complex, caller order), i.e. the Robin data a = i k beta, b = 1 at every
  * frequency k of a solve or sweep (the wall-impedance section of the
  * reference's solving script, wallimpedancesection.cpp:360-407, with the
- * physical rho c and the current k; see the design notes). */
+ * physical rho c and each solve's own k, where the reference's script reader
+ * uses the last frequency's k and (last frequency) x rho). */
 bem_status bem_set_bc_impedance(bem_handle* h, const double* beta);
 
 /* Collocation operators L, M, Mt, N for (row, col) pairs in cluster order
@@ -290,6 +291,15 @@ bem_status bem_autotune(bem_handle* h, double freq, int64_t nrhs, int64_t* tuned
  * info may be NULL or hold nf records. */
 bem_status bem_sweep(bem_handle* h, const double* freqs, int64_t nf, const double* g,
                      int64_t nrhs, double* p, bem_solve_info* info);
+
+/* Point sources of the boundary solve (BoundaryElementSolver::pointSources):
+ * nsrc rows x, y, z, Re w, Im w (nsrc = 0 clears; bem_set_mesh clears too).
+ * Every solve adds their source term at each collocation point to the
+ * right-hand side, rhs = sourceTermVector + phi g (boundaryelementsolver.cpp:
+ * 578-579), with sourceTerm (:3431-3441) as written there, including its
+ * division of the radial term by (ikr - 1); bem_field adds the sources'
+ * incident field through its own sources argument. */
+bem_status bem_set_point_sources(bem_handle* h, const double* src, int64_t nsrc);
 
 /* One impedance plane (BoundaryElements::impedancePlanes with a single entry,
  * the infinite baffle of the solving scripts): the plane through point with

@@ -83,6 +83,7 @@ def lib():
                                 F64P, ct.c_int64, F64P, F64P, ct.c_int64, F64P, ct.c_int64,
                                 F64P, ct.c_int, F64P, F64P]
         L.orc_set_plane.argtypes = [vp, F64P, F64P]
+        L.orc_set_sources.argtypes = [vp, F64P, ct.c_int64]
         L.orc_pivot_hash.restype = ct.c_uint64
         L.orc_pivot_hash.argtypes = [ct.c_uint64, ct.c_uint64, ct.c_uint64]
         _lib = L
@@ -114,6 +115,15 @@ class Problem:
         if getattr(self, "_h", None):
             lib().orc_destroy(self._h)
             self._h = None
+
+    def set_sources(self, sources=None):
+        """Point sources of the right-hand side: rows (x, y, z, complex weight)."""
+        src = np.zeros((0, 5))
+        if sources is not None and len(sources):
+            q = np.asarray(sources, np.complex128).reshape(-1, 4)
+            src = np.column_stack([q[:, :3].real, q[:, 3].real, q[:, 3].imag])
+        src = np.ascontiguousarray(src, np.float64)
+        lib().orc_set_sources(self._h, _f(src), src.shape[0])
 
     def set_plane(self, point=None, normal=None):
         """One impedance plane (None removes it)."""

@@ -17,6 +17,7 @@ struct orc_problem {
   std::vector<BlockInfo> blocks;
   Mesh refl;              // impedance plane: reflected elements (cluster order)
   bool has_refl = false;
+  std::vector<double> src;  // point sources, rows x, y, z, Re w, Im w
   const Mesh* reflected() const { return has_refl ? &refl : nullptr; }
 };
 
@@ -49,6 +50,10 @@ orc_problem* orc_create(const double* tri, int64_t n, int64_t leaf, double eta) 
   mesh_prepare(p->mesh);
   p->blocks = build_partition(p->tree, p->tree, eta);
   return p;
+}
+
+void orc_set_sources(orc_problem* p, const double* src, int64_t nsrc) {
+  p->src.assign(src, src + (nsrc > 0 ? 5 * nsrc : 0));
 }
 
 void orc_set_plane(orc_problem* p, const double* point, const double* normal) {
@@ -505,7 +510,27 @@ int orc_solve(const orc_problem* p, double freq, double c, double rho, int coupl
   orc_hmatrix* hphi = orc_hassemble(p, k, coupling, (double*)a.data(), (double*)b.data(), 0,
                                     aca_tol, max_rank, seed, nthreads);
   auto t2 = clk::now();
+  // rhs = sourceTermVector + phi g (boundaryelementsolver.cpp:578-579); the
+  // source term of each collocation point restates sourceTerm (:3431-3441),
+  // whose derivative factor divides by (ikr - 1) as written there
   std::vector<cd> rhs(N * R, 0.0);
+  if (!p->src.empty()) {
+    const Coupling cp = coupling_parameter(coupling, k);
+    const cd ik(0.0, k);
+    for (int64_t i = 0; i < N; i++) {
+      cd sum = 0.0;
+      for (size_t q = 0; q + 4 < p->src.size(); q += 5) {
+        const V3 rv = p->mesh.colloc[i] - V3(p->src[q], p->src[q + 1], p->src[q + 2]);
+        const double r = norm(rv);
+        const double rup = dot(rv, p->mesh.normal[i]) / r;
+        const cd ikr = ik * r;
+        const cd G = cd(p->src[q + 3], p->src[q + 4]) * std::exp(ikr) / (PI4 * r);
+        const cd dG = (G / r) / (ikr - 1.0);
+        sum += G + cp.alpha * dG * rup;
+      }
+      for (int64_t r = 0; r < R; r++) rhs[r * N + i] = sum;
+    }
+  }
   for (int64_t r = 0; r < R; r++) orc_hmatvec(hphi, (double*)&g[r * N], (double*)&rhs[r * N]);
   orc_hdestroy(hphi);
   auto t3 = clk::now();

@@ -68,6 +68,10 @@ void orc_destroy(orc_problem* p);
  * 2042-2050; BemOperatorsReflected :1516-1554; MeshFunctions::reflectTriangles
  * meshfunctions.cpp:349-380). */
 void orc_set_plane(orc_problem* p, const double* point, const double* normal);
+/* Point sources of the solve's right-hand side (nsrc rows x, y, z, Re w, Im w;
+ * nsrc = 0 clears): rhs = sourceTermVector + phi g (boundaryelementsolver.cpp:
+ * 578-579, sourceTerm :3431-3441). */
+void orc_set_sources(orc_problem* p, const double* src, int64_t nsrc);
 int64_t orc_n(const orc_problem* p);
 /* perm[new_index] = caller index */
 void orc_perm(const orc_problem* p, int64_t* perm);

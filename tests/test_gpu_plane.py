@@ -106,3 +106,30 @@ def test_half_space_field_vs_oracle(bem, meshes, orc):
     s.set_impedance_plane()
     pf0, _ = s.field(400.0, pts, phi, dphi)
     assert rel(pf0, pf) > 0.05
+
+
+@pytest.mark.parametrize("coupling", [0, 2])
+def test_point_sources_vs_oracle(bem, meshes, orc, coupling):
+    """bem_set_point_sources: rhs = sourceTermVector + phi g with the
+    reference's sourceTerm; a box with Robin walls and two sources, alone and
+    with a driven face, against the oracle."""
+    tri = meshes.box(n_target=1200, seed=4)
+    n = tri.shape[0]
+    rng = np.random.default_rng(12)
+    a = 0.3j * rng.random(n)
+    b = np.ones(n, complex)
+    g = np.where(rng.random(n) < 0.2, 1.0, 0.0) + 0j
+    src = [[0.6, 0.1, 0.2, 1.0 + 0.5j], [-0.4, -0.3, 0.5, 0.7j]]
+    s = bem.Solver(aca_tol=1e-5, gmres_tol=1e-10, precision=1, coupling=coupling)
+    s.set_mesh(tri)
+    s.set_bc(a, b)
+    s.set_point_sources(src)
+    phi, dphi, p, info = s.solve(700.0, g)
+    P = orc.Problem(tri, 32, 2.0)
+    P.set_sources(src)
+    po, dpo, ppo, st = P.solve(700.0, 343.0, 1.2, coupling, a, b, g, 1e-5, 1e-10,
+                               seed=s.config.seed)
+    assert rel(phi[:, 0], po[:, 0]) < 2e-5
+    s.set_point_sources()
+    _, _, p0, _ = s.solve(700.0, g)
+    assert rel(p0[:, 0], p[:, 0]) > 1e-2  # the sources matter

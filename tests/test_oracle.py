@@ -338,3 +338,33 @@ def test_half_space_field_equals_mirrored_data(orc, meshes):
     f_full, _ = orc.field(full, 500.0, pts, np.concatenate([phi, phi]),
                           np.concatenate([dphi, dphi]))
     assert rel(f_half, f_full) < 1e-13
+
+
+def test_point_source_rhs_kelvin_image(orc, meshes):
+    """rhs = sourceTermVector + phi g (boundaryelementsolver.cpp:578-579): a
+    unit point source at distance 2 from a sound-soft unit sphere (phi = 0,
+    a = 1, b = 0, g = 0) at 1 Hz is the Laplace problem whose exact normal
+    derivative comes from the Kelvin image (-a/d at a^2/d). Without coupling
+    the source term is the plain Green's function; flat-panel discretisation
+    error ~1 %."""
+    tri = meshes.icosphere(4, 1.0)
+    n = tri.shape[0]
+    c = (tri[:, 0:3] + tri[:, 3:6] + tri[:, 6:9]) / 3
+    nrm = np.cross(tri[:, 3:6] - tri[:, 0:3], tri[:, 6:9] - tri[:, 0:3])
+    nrm /= np.linalg.norm(nrm, axis=1)[:, None]
+
+    def grad(y, w):
+        r = c - y
+        return -w * r / (4 * np.pi * np.linalg.norm(r, axis=1)[:, None] ** 3)
+
+    exact = np.sum((grad(np.array([0, 0, 2.0]), 1.0) + grad(np.array([0, 0, 0.5]), -0.5)) * nrm, 1)
+    P = orc.Problem(tri, 32, 2.0)
+    P.set_sources([[0, 0, 2.0, 1.0]])
+    phi, dphi, p, st = P.solve(1.0, 343.0, 1.2, 0, np.ones(n), np.zeros(n), np.zeros(n),
+                               1e-6, 1e-10)
+    assert np.abs(phi).max() == 0.0
+    assert rel(dphi[:, 0], exact) < 0.02
+    # clearing the sources gives the zero solution back
+    P.set_sources()
+    _, dphi0, _, _ = P.solve(1.0, 343.0, 1.2, 0, np.ones(n), np.zeros(n), np.zeros(n), 1e-6, 1e-10)
+    assert np.abs(dphi0).max() == 0.0
