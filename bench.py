@@ -26,6 +26,12 @@ pressure difference between the two ride along.
   e2e   : freq-solves/s through bem_solve with host buffers (g copied in, p
           copied out inside the timed region)
 
+Legs riding along in the same line (single GPU): the plain complex-FP64 arm,
+the field at 20,480 observation points (``field_eval``), the same sphere above
+a rigid plane (``half_space``), the 64-frequency box sweep (``box_sweep``) and
+the CPU baseline; ``--no-plain``, ``--no-field``, ``--no-half-space``,
+``--no-sweep``, ``--no-cpu-baseline`` skip them.
+
 ``--impl reference`` times the CPU restatement of the reference path (the
 oracle: FP64 C++/OpenMP, all host cores) on the same workload.
 """
