@@ -297,6 +297,36 @@ void alloc_hm(bem_handle* h, DevHM& m) {
   m.flags.ensure(L.far.size());
 }
 
+// Doubles the rank reservation (up to min(m, n) and ACA_MAX_KCAP) of every
+// admissible block whose ACA stopped at it in either matrix, and lays the
+// low-rank pools out again. Returns whether any block grew.
+bool grow_capped(bem_handle* h) {
+  Layout& L = h->L;
+  const size_t nf = L.far.size();
+  if (h->hm[0].h_flags.size() != nf || h->hm[1].h_flags.size() != nf) return false;
+  bool grew = false;
+  for (size_t i = 0; i < nf; i++) {
+    FarBlock& f = L.far[i];
+    const int64_t lim = std::min<int64_t>(std::min(f.m, f.n), ACA_MAX_KCAP);
+    if ((h->hm[0].h_flags[i] || h->hm[1].h_flags[i]) && f.kcap < lim) {
+      f.kcap = (int32_t)std::min<int64_t>(2 * (int64_t)f.kcap, lim);
+      grew = true;
+    }
+  }
+  if (!grew) return false;
+  L.u_size = L.v_size = L.s_size = 0;
+  for (FarBlock& f : L.far) {
+    f.uoff = L.u_size;
+    f.voff = L.v_size;
+    f.soff = L.s_size;
+    L.u_size += (int64_t)f.kcap * f.m;
+    L.v_size += (int64_t)f.kcap * f.n;
+    L.s_size += f.kcap;
+  }
+  h->dFar.upload(L.far, h->stream);
+  return true;
+}
+
 std::vector<ElemF> make_elemf(const std::vector<Elem>& E) {
   std::vector<ElemF> F(E.size());
   for (size_t i = 0; i < E.size(); i++) {
@@ -567,6 +597,18 @@ void assemble(bem_handle* h, double freq, double* t_near, double* t_aca) {
   CK(cudaGetLastError());
   fetch_ranks(h, h->hm[0]);
   fetch_ranks(h, h->hm[1]);
+  // The reference's ACA doubles its reservation whenever a block needs more
+  // rank (hmatrix.cpp:557-563) and stops only at the tolerance or acaMaxRank:
+  // blocks that reached their device reservation get twice the room (kept
+  // for later frequencies) and the ACA of both matrices runs again.
+  for (int round = 0; round < 8 && h->cfg.aca_max_rank == 0 && grow_capped(h); round++) {
+    for (auto& m : h->hm) alloc_hm(h, m);
+    launch_aca_split(h, {aca_args(h, h->hm[0], 0, 0), aca_args(h, h->hm[1], 1, 1)});
+    CK(cudaEventRecord(h->ev[2], s));
+    CK(cudaGetLastError());
+    fetch_ranks(h, h->hm[0]);
+    fetch_ranks(h, h->hm[1]);
+  }
   // overlapping phases: the near field's own span, and the ACA span from the
   // start of assembly to its last block
   if (t_near) *t_near = elapsed(h->ev[0], h->ev[1]);

@@ -46,7 +46,9 @@ typedef struct bem_config {
   double eta;              /* admissible iff min(diam)/dist < eta (ref: 3) */
   double aca_tol;          /* acaRelativeError */
   int64_t aca_max_rank;    /* acaMaxRank, 0 = unlimited */
-  int64_t rank_reserve;    /* device rank reservation per admissible block */
+  int64_t rank_reserve;    /* initial device rank reservation per admissible
+                              block; blocks whose ACA reaches it get it doubled
+                              and are assembled again (aca_max_rank = 0) */
   double gmres_tol;        /* relative residual (ref: 1e-3 * aca_tol) */
   int64_t gmres_restart;   /* ref: 300 */
   int64_t gmres_maxit;     /* total Arnoldi steps allowed */

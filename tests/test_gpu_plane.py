@@ -133,3 +133,25 @@ def test_point_sources_vs_oracle(bem, meshes, orc, coupling):
     s.set_point_sources()
     _, _, p0, _ = s.solve(700.0, g)
     assert rel(p0[:, 0], p[:, 0]) > 1e-2  # the sources matter
+
+
+def test_rank_reservation_grows(bem, meshes):
+    """The reference's ACA doubles its reservation until the tolerance is met
+    (hmatrix.cpp:557-563): a handle created with a reservation of 4 ends with
+    no capped block and the pressures of the default reservation; a user rank
+    cap (acaMaxRank) still limits the ranks."""
+    tri = body(meshes)
+    n = tri.shape[0]
+    g = np.ones(n)
+    _, _, p96, i96 = solver(bem, tri, 1).solve(400.0, g)
+    s4 = solver(bem, tri, 1, rank_reserve=4)
+    _, _, p4, i4 = s4.solve(400.0, g)
+    assert i96["capped_blocks"] == 0 and i4["capped_blocks"] == 0
+    assert i4["max_rank"] == i96["max_rank"]
+    assert rel(p4[:, 0], p96[:, 0]) < 1e-12
+    _, _, p4b, _ = s4.solve(400.0, g)  # the grown reservation is kept
+    assert np.array_equal(p4b, p4)
+    # a user rank cap (acaMaxRank) is a limit, not a reservation to grow
+    capped = solver(bem, tri, 1, rank_reserve=4, aca_max_rank=4)
+    _, _, pc, ic = capped.solve(400.0, g)
+    assert ic["max_rank"] <= 4 and rel(pc[:, 0], p96[:, 0]) > 1e-6
