@@ -143,6 +143,16 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(torch, value, ws, device="cuda"):
+    """The slowest rank's time (replicas: every rank solves the same
+    workload; the job takes as long as its slowest GPU)."""
+    if ws <= 1:
+        return float(value)
+    t = torch.tensor([float(value)], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def matvec_bytes(info, ranks, n, elem, R=1):
     """Algorithmic bytes of one H-matvec: stored entries once (near-field
     m*n, low-rank (m+n)*k + k), plus each block's x segment and y once."""
@@ -188,11 +198,7 @@ def timed_arm(torch, pkg, s, n, args, ws):
     torch.cuda.synchronize()
     if ws > 1:
         torch.distributed.barrier()
-    ms = e0.elapsed_time(e1)
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(torch, e0.elapsed_time(e1), ws)
     return ms, infos, p.cpu().numpy(), s.launch_count() - l0
 
 
