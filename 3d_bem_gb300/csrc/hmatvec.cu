@@ -24,7 +24,12 @@ namespace bemgpu {
 namespace {
 
 constexpr int VT = 128;  // threads of a pass-V CTA
-constexpr int UT = 512;  // threads of a pass-U CTA (16 warps split a leaf's block list)
+constexpr int UT = 256;  // threads of a pass-U CTA (8 warps split a leaf's block list)
+// The FP32 U pass runs with at most 40 registers (6 CTAs of 256 threads per
+// SM, 48 warps): at 20,480 elements 0.241 -> 0.222 ms per product against 60
+// registers and 32 warps with 512-thread CTAs; 128-thread CTAs (0.291 ms) and
+// a 32-register cap (0.226 ms, more spills) were slower.
+constexpr int UT32_MIN_CTAS = 6;
 constexpr int VROWS = 16;  // rows of V per pass-V work item (4 warps x 4 rows)
 
 template <typename T, bool F32> struct Acc;
@@ -298,7 +303,7 @@ __global__ void __launch_bounds__(VT) hmv32_vpass(const FarBlock* __restrict__ f
 }
 
 template <int R>
-__global__ void __launch_bounds__(UT) hmv32_upass(
+__global__ void __launch_bounds__(UT, UT32_MIN_CTAS) hmv32_upass(
     const LeafRows* __restrict__ leaves, const int32_t* __restrict__ list_off,
     const int32_t* __restrict__ list, const FarBlock* __restrict__ far,
     const int32_t* __restrict__ rank, const NearBlock* __restrict__ nearb,
