@@ -24,12 +24,16 @@ namespace bemgpu {
 namespace {
 
 constexpr int VT = 128;  // threads of a pass-V CTA
-constexpr int UT = 256;  // threads of a pass-U CTA (8 warps split a leaf's block list)
-// The FP32 U pass runs with at most 40 registers (6 CTAs of 256 threads per
-// SM, 48 warps): at 20,480 elements 0.241 -> 0.222 ms per product against 60
-// registers and 32 warps with 512-thread CTAs; 128-thread CTAs (0.291 ms) and
-// a 32-register cap (0.226 ms, more spills) were slower.
-constexpr int UT32_MIN_CTAS = 6;
+constexpr int UT = 512;  // threads of a pass-U CTA (16 warps split a leaf's block list)
+// The FP32 U pass has two launch shapes. With many leaves (at least 4 per SM)
+// 256-thread CTAs capped at 40 registers (6 per SM, 48 warps) stream faster:
+// 20,480 elements 0.241 -> 0.222 ms per product against 512-thread CTAs with 60
+// registers (2 per SM); 128-thread CTAs (0.291 ms) and a 32-register cap
+// (0.226 ms, more spills) were slower. With few leaves the 512-thread CTAs
+// keep more warps busy: 5,120 elements 0.074 against 0.107 ms, 1,280 elements
+// 0.030 against 0.038 ms.
+constexpr int UT32_NARROW = 256, UT32_NARROW_MIN_CTAS = 6;
+constexpr int UT32_NARROW_LEAVES_PER_SM = 4;
 constexpr int VROWS = 16;  // rows of V per pass-V work item (4 warps x 4 rows)
 
 template <typename T, bool F32> struct Acc;
@@ -302,15 +306,15 @@ __global__ void __launch_bounds__(VT) hmv32_vpass(const FarBlock* __restrict__ f
   }
 }
 
-template <int R>
-__global__ void __launch_bounds__(UT, UT32_MIN_CTAS) hmv32_upass(
+template <int R, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) hmv32_upass(
     const LeafRows* __restrict__ leaves, const int32_t* __restrict__ list_off,
     const int32_t* __restrict__ list, const FarBlock* __restrict__ far,
     const int32_t* __restrict__ rank, const NearBlock* __restrict__ nearb,
     const float2* __restrict__ Up, const float2* __restrict__ F, const float2* __restrict__ x,
     int64_t ldx, const float2* __restrict__ t, int64_t ldt, double2* __restrict__ y,
     int64_t ldy, int accumulate, HmvGate gate) {
-  __shared__ float4 part[UT / 32][32];
+  __shared__ float4 part[NT / 32][32];
   LeafRows lf = leaves[blockIdx.x];
   if (gate_closed(gate)) lf.size = 0;  // no rows (see the V pass)
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -320,7 +324,7 @@ __global__ void __launch_bounds__(UT, UT32_MIN_CTAS) hmv32_upass(
     const bool active = ri < lf.size;
     const int64_t grow = lf.start + ri;
     TwoSum sx[R], sy[R];
-    for (int e = beg + w; e < end; e += UT / 32) {
+    for (int e = beg + w; e < end; e += NT / 32) {
       const int32_t code = list[e];
       float ax[R], ay[R];
 #pragma unroll
@@ -370,7 +374,7 @@ __global__ void __launch_bounds__(UT, UT32_MIN_CTAS) hmv32_upass(
       if (w == 0 && active) {
         TwoSum ux, uy;  // combine the warps' partials in FP32, then one FP64 add
 #pragma unroll
-        for (int q = 0; q < UT / 32; q++) {
+        for (int q = 0; q < NT / 32; q++) {
           const float4 p = part[q][lane];
           ux.add(p.x);
           ux.add(p.y);
@@ -392,6 +396,20 @@ __global__ void to_float_kernel(const double2* __restrict__ x, float2* __restric
   if (i < n && !gate_closed(gate)) xf[i] = make_float2((float)x[i].x, (float)x[i].y);
 }
 
+// streaming multiprocessors of the current device (cached per device)
+int sm_count() {
+  static int cached[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+  if (!cached[dev]) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+      n = 152;
+    cached[dev] = n;
+  }
+  return cached[dev];
+}
+
 template <int R>
 void launch32_r(const HmvArgs& a, cudaStream_t s) {
   to_float_kernel<<<(unsigned)((a.ldx * R + 255) / 256), 256, 0, s>>>(a.x, a.xf, a.ldx * R,
@@ -401,10 +419,16 @@ void launch32_r(const HmvArgs& a, cudaStream_t s) {
     hmv32_vpass<R><<<(unsigned)nv, VT, 0, s>>>(a.far, a.rank, (const float2*)a.V,
                                                (const float2*)a.S, a.xf, a.ldx, a.tf, a.ldt,
                                                a.vwork, a.gate);
-  if (a.nleaves > 0)
-    hmv32_upass<R><<<(unsigned)a.nleaves, UT, 0, s>>>(
-        a.leaves, a.list_off, a.list, a.far, a.rank, a.nearb, (const float2*)a.U,
-        (const float2*)a.F, a.xf, a.ldx, a.tf, a.ldt, a.y, a.ldy, a.accumulate, a.gate);
+  if (a.nleaves > 0) {
+    if (a.nleaves >= (int64_t)UT32_NARROW_LEAVES_PER_SM * sm_count())
+      hmv32_upass<R, UT32_NARROW, UT32_NARROW_MIN_CTAS><<<(unsigned)a.nleaves, UT32_NARROW, 0, s>>>(
+          a.leaves, a.list_off, a.list, a.far, a.rank, a.nearb, (const float2*)a.U,
+          (const float2*)a.F, a.xf, a.ldx, a.tf, a.ldt, a.y, a.ldy, a.accumulate, a.gate);
+    else
+      hmv32_upass<R, UT, 2><<<(unsigned)a.nleaves, UT, 0, s>>>(
+          a.leaves, a.list_off, a.list, a.far, a.rank, a.nearb, (const float2*)a.U,
+          (const float2*)a.F, a.xf, a.ldx, a.tf, a.ldt, a.y, a.ldy, a.accumulate, a.gate);
+  }
 }
 
 void launch32(const HmvArgs& a, cudaStream_t s) {
