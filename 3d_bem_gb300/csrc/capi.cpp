@@ -200,6 +200,7 @@ struct bem_handle {
   DBuf<unsigned char> dFcoef;
   DBuf<double2> dFpart, dFphi, dFdphi, dFout1, dFout2;
   DBuf<double> dFpts, dFsrc;
+  std::vector<double> field_src;
   QuadRules rules{};
   cudaEvent_t ev[10]{};
 };
@@ -2138,8 +2139,10 @@ void field_dev(bem_handle* h, double freq, const double* pts, int64_t M, const d
   const double2 pfac = make_double2(0.0, h->cfg.density * 2.0 * M_PI * (freq != 0 ? freq : 1.0));
   cudaStream_t s = h->stream;
   if (nsrc > 0) {
-    h->dFsrc.ensure((size_t)nsrc * 5);
-    CK(cudaMemcpyAsync(h->dFsrc.p, src, (size_t)nsrc * 5 * sizeof(double), cudaMemcpyHostToDevice, s));
+    // staged through the handle's pageable copy, so the caller's array may be
+    // reused as soon as the call returns even when it is pinned
+    h->field_src.assign(src, src + 5 * nsrc);
+    h->dFsrc.upload(h->field_src, s);
   }
   if (prec == 1) h->dFe.ensure((size_t)N);
   h->dFcoef.ensure((size_t)N * R * (prec == 1 ? sizeof(FieldCoefF) : sizeof(FieldCoef)));
