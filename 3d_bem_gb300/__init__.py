@@ -43,7 +43,7 @@ EXPORTS = [
     "bem_set_aca_rules", "bem_set_bc_impedance", "bem_field", "bem_field_device",
     "bem_msh_read", "bem_msh_free", "bem_msh_num_physical", "bem_msh_physical", "bem_msh_select",
     "bem_msh_elements", "bem_quads_to_triangles", "bem_wall_beta", "bem_set_impedance_plane",
-    "bem_set_point_sources",
+    "bem_set_point_sources", "bem_refine_triangles",
 ]
 BEM_ARITH_FP64, BEM_ARITH_FP32, BEM_ARITH_TWOFLOAT = 0, 1, 2
 
@@ -156,6 +156,7 @@ def lib():
     L.bem_wall_beta.argtypes = [i32, i32, vp, dbl, vp]
     L.bem_set_impedance_plane.argtypes = [vp, vp, vp]
     L.bem_set_point_sources.argtypes = [vp, vp, i64]
+    L.bem_refine_triangles.argtypes = [vp, i64, dbl, vp, i64, P(i64), vp]
     L.bem_field_device.argtypes = [vp, dbl, vp, i64, vp, vp, i64, vp, i64, vp, vp]
     L.bem_hlu_build.argtypes = [vp]
     L.bem_hlu_solve.argtypes = [vp, vp, vp, i64]
@@ -620,6 +621,27 @@ def read_msh(path, include="all", exclude=""):
     phys = np.concatenate([sel["tri_phys"], np.repeat(sel["quad_phys"], 2)])
     geom = np.concatenate([sel["tri_geom"], np.repeat(sel["quad_geom"], 2)])
     return tri, phys, geom
+
+
+def refine_triangles(tri, edge_length=None, mesh_frequency=None, c=343.0):
+    """Longest-edge bisection of an Elements section (elementSection.cpp:
+    688-800) to edge_length, or to (c / mesh_frequency) / 2 as
+    solvingscriptreader.cpp:1113-1116 derives it; returns (triangles,
+    parent index of each)."""
+    if edge_length is None:
+        if not mesh_frequency:
+            raise BemError(BEM_EINVAL, "edge_length or mesh_frequency required")
+        edge_length = (c / mesh_frequency) / 2
+    t = np.ascontiguousarray(tri, np.float64).reshape(-1, 9)
+    cnt = ct.c_int64()
+    _raise(lib().bem_refine_triangles(_ptr(t), t.shape[0], float(edge_length), None, 0,
+                                      ct.byref(cnt), None), "bem_refine_triangles")
+    out = np.zeros((cnt.value, 9))
+    parent = np.zeros(cnt.value, np.int64)
+    _raise(lib().bem_refine_triangles(_ptr(t), t.shape[0], float(edge_length), _ptr(out),
+                                      cnt.value, ct.byref(cnt), _ptr(parent)),
+           "bem_refine_triangles")
+    return out, parent
 
 
 IMP_REFLECTION, IMP_DAMPING, IMP_IMPEDANCE, IMP_ADMITTANCE = 0, 1, 2, 3

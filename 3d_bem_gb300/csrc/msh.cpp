@@ -7,6 +7,7 @@
 // wall-impedance Robin data (WallImpedanceSection::setUpValues,
 // SolvingScript/wallimpedancesection.cpp:308-405).
 #include <algorithm>
+#include <array>
 #include <cctype>
 #include <cmath>
 #include <complex>
@@ -572,6 +573,80 @@ bem_status bem_quads_to_triangles(const double* quad, int64_t nq, double* tri) {
         for (int d = 0; d < 3; d++) tri[18 * i + 9 * t + 3 * v + d] = q[3 * s[t][v] + d];
   }
   return BEM_OK;
+}
+
+bem_status bem_refine_triangles(const double* tri, int64_t n, double edge_length, double* out,
+                                int64_t cap, int64_t* nout, int64_t* parent) {
+  if (n < 0 || (n > 0 && !tri) || !nout || !(edge_length > 0) || !std::isfinite(edge_length))
+    return BEM_EINVAL;
+  // ElementSection::refineTriangles / recursiveRefineTriangle
+  // (SolvingScript/elementSection.cpp:688-800): a triangle whose longest edge
+  // (indexOfMaxOfThree, :912, ties to the later edge) exceeds edge_length is
+  // bisected at that edge's midpoint, node orders as the reference, and both
+  // halves are refined in turn (depth first, first half first).
+  const auto len = [](const double* a, const double* b) {
+    return std::sqrt((a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) +
+                     (a[2] - b[2]) * (a[2] - b[2]));
+  };
+  const auto longest = [&](const double* t, double& e) {
+    const double a = len(t, t + 3), b = len(t + 3, t + 6), c = len(t + 6, t);
+    const int i = a > b ? (a > c ? 1 : 3) : (b > c ? 2 : 3);
+    e = i == 1 ? a : (i == 2 ? b : c);
+    return i;
+  };
+  int64_t count = 0;
+  std::vector<std::array<double, 9>> stack;
+  for (int64_t i = 0; i < n; i++) {
+    stack.clear();
+    std::array<double, 9> t0;
+    for (int d = 0; d < 9; d++) t0[d] = tri[9 * i + d];
+    stack.push_back(t0);
+    while (!stack.empty()) {
+      const std::array<double, 9> t = stack.back();
+      stack.pop_back();
+      double e = 0;
+      const int k = longest(t.data(), e);
+      if (!(e > edge_length)) {  // keep it
+        if (out && count < cap) {
+          for (int d = 0; d < 9; d++) out[9 * count + d] = t[d];
+          if (parent) parent[count] = i;
+        }
+        count++;
+        continue;
+      }
+      if (stack.size() > (size_t)1 << 20) return BEM_EINVAL;  // degenerate input
+      const double* n1 = t.data();
+      const double* n2 = t.data() + 3;
+      const double* n3 = t.data() + 6;
+      double m[3];
+      const double* pa = k == 1 ? n1 : (k == 2 ? n2 : n3);
+      const double* pb = k == 1 ? n2 : (k == 2 ? n3 : n1);
+      for (int d = 0; d < 3; d++) m[d] = (pa[d] + pb[d]) / 2;
+      std::array<double, 9> h1, h2;
+      const auto put = [](std::array<double, 9>& h, const double* a, const double* b,
+                          const double* c) {
+        for (int d = 0; d < 3; d++) {
+          h[d] = a[d];
+          h[3 + d] = b[d];
+          h[6 + d] = c[d];
+        }
+      };
+      if (k == 1) {
+        put(h1, n1, m, n3);
+        put(h2, m, n2, n3);
+      } else if (k == 2) {
+        put(h1, n1, n2, m);
+        put(h2, m, n3, n1);
+      } else {
+        put(h1, n1, n2, m);
+        put(h2, m, n2, n3);
+      }
+      stack.push_back(h2);  // refined after h1
+      stack.push_back(h1);
+    }
+  }
+  *nout = count;
+  return out && count > cap ? BEM_EINVAL : BEM_OK;
 }
 
 bem_status bem_wall_beta(int32_t imp_type, int32_t normalized, const double* value,

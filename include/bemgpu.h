@@ -380,6 +380,16 @@ bem_status bem_msh_elements(const bem_msh* m, double* tri, int32_t* tri_phys, in
  * (12 doubles) becomes two triangles (18 doubles) split along the shorter
  * diagonal, node orders as the reference. */
 bem_status bem_quads_to_triangles(const double* quad, int64_t nq, double* tri);
+/* Mesh refinement of an Elements section (SolvingScript::refineElements,
+ * solvingscriptreader.cpp:1104-1127: edge length = (c / MeshFrequency) / 2,
+ * or EdgeLength; ElementSection::refineTriangles / recursiveRefineTriangle,
+ * elementSection.cpp:688-800): every triangle whose longest edge exceeds
+ * edge_length is bisected at that edge, recursively, in the reference's order
+ * and node orders. out (cap x 9, may be NULL to count) receives the triangles,
+ * parent (may be NULL) the index of the input triangle each came from; *nout
+ * the count (BEM_EINVAL when it exceeds cap). */
+bem_status bem_refine_triangles(const double* tri, int64_t n, double edge_length, double* out,
+                                int64_t cap, int64_t* nout, int64_t* parent);
 /* WallImpedanceSection::setUpValues (SolvingScript/wallimpedancesection.cpp:
  * 308-405): the beta of bem_set_bc_impedance (a = i k beta, b = 1, g = 0) for
  * imp_type 0 reflection factor R (beta = (1 - R) / (1 + R), real part of R),

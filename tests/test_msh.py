@@ -260,3 +260,76 @@ def test_reference_example_meshes(bem, rel):
     t = sel["tri"].reshape(-1, 3, 3)
     area = np.linalg.norm(np.cross(t[:, 1] - t[:, 0], t[:, 2] - t[:, 0]), axis=1)
     assert np.isfinite(area).all() and (area > 0).all()
+
+
+def _refine_restated(tri, L):
+    """ElementSection::refineTriangles / recursiveRefineTriangle
+    (elementSection.cpp:688-800) restated recursively."""
+    out, par = [], []
+
+    def length(a, b):
+        return np.sqrt((a[0] - b[0]) ** 2 + (a[1] - b[1]) ** 2 + (a[2] - b[2]) ** 2)
+
+    def rec(t, i):
+        n1, n2, n3 = t[0:3], t[3:6], t[6:9]
+        a, b, c = length(n1, n2), length(n2, n3), length(n3, n1)
+        k = (1 if a > c else 3) if a > b else (2 if b > c else 3)
+        e = (a, b, c)[k - 1]
+        if e <= L:
+            out.append(t)
+            par.append(i)
+            return
+        if k == 1:
+            m = (n1 + n2) / 2
+            h1, h2 = (n1, m, n3), (m, n2, n3)
+        elif k == 2:
+            m = (n2 + n3) / 2
+            h1, h2 = (n1, n2, m), (m, n3, n1)
+        else:
+            m = (n3 + n1) / 2
+            h1, h2 = (n1, n2, m), (m, n2, n3)
+        rec(np.concatenate(h1), i)
+        rec(np.concatenate(h2), i)
+
+    for i, t in enumerate(np.asarray(tri, float).reshape(-1, 9)):
+        rec(t, i)
+    return np.array(out).reshape(-1, 9), np.array(par)
+
+
+def _areas(t):
+    t = t.reshape(-1, 3, 3)
+    return 0.5 * np.linalg.norm(np.cross(t[:, 1] - t[:, 0], t[:, 2] - t[:, 0]), axis=1)
+
+
+def test_refine_triangles_matches_restatement(bem, meshes):
+    rng = np.random.default_rng(3)
+    tri = np.vstack([rng.uniform(-1, 1, (40, 9)), meshes.icosphere(1, 2.0),
+                     np.array([[0, 0, 0, 1, 0, 0, 0, 1, 0.0]])])  # a right isosceles (ties)
+    for L in (0.9, 0.35, 0.12):
+        out, par = bem.refine_triangles(tri, L)
+        ref, rpar = _refine_restated(tri, L)
+        assert np.array_equal(out, ref) and np.array_equal(par, rpar)
+        t = out.reshape(-1, 3, 3)
+        edges = np.linalg.norm(t - np.roll(t, -1, axis=1), axis=2)
+        assert edges.max() <= L
+        # halves tile their parent: areas add up, normals keep their direction
+        tot = np.bincount(par, weights=_areas(out), minlength=tri.shape[0])
+        assert np.allclose(tot, _areas(tri), rtol=1e-12, atol=0)
+        def nrm(x):
+            x = x.reshape(-1, 3, 3)
+            c = np.cross(x[:, 1] - x[:, 0], x[:, 2] - x[:, 0])
+            return c / np.linalg.norm(c, axis=1)[:, None]
+        assert np.allclose(nrm(out), nrm(tri)[par], atol=1e-12)
+
+
+def test_refine_by_mesh_frequency_and_errors(bem, meshes):
+    tri = meshes.icosphere(2, 1.0)
+    out, _ = bem.refine_triangles(tri, mesh_frequency=1000.0, c=343.0)
+    ref, _ = _refine_restated(tri, 343.0 / 1000.0 / 2)
+    assert np.array_equal(out, ref) and out.shape[0] > tri.shape[0]
+    same, par = bem.refine_triangles(tri, 10.0)  # already fine enough: unchanged
+    assert np.array_equal(same, tri) and np.array_equal(par, np.arange(tri.shape[0]))
+    with pytest.raises(bem.BemError):
+        bem.refine_triangles(tri, 0.0)
+    with pytest.raises(bem.BemError):
+        bem.refine_triangles(tri)
