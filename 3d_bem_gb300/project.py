@@ -23,11 +23,15 @@ Follows SolvingScriptReader (SolvingScript/solvingscriptreader.cpp) for:
   section becomes an impedance wall (WallImpedanceSection::setUpValues) with
   the medium impedance rho c;
 * ``Infinite_Baffle``: Position, Normal: one impedance plane;
+* ``Nodes`` (Scale / Shift / Rotate, ``<index> x y z`` lines) and
+  ``Pressure_Points`` (DrvWeight, RefNodes, ``<index> <node> [Weight=w]``):
+  point sources of the right-hand side (setupPressurePoints,
+  solvingscriptreader.cpp:1016-1050);
 * sections prefixed with ``off`` are skipped; ``//`` starts a comment.
 
-Not read: Pressure_Points / Nodes (point sources), two baffles or
-distanceToParallelPlane, per-mesh-file swap flags, interior ElType, the
-single-precision aspect-ratio pre-split of quadrilaterals.
+Not read: two baffles or distanceToParallelPlane, per-mesh-file swap flags,
+interior ElType, the single-precision aspect-ratio pre-split of
+quadrilaterals.
 """
 from __future__ import annotations
 
@@ -73,6 +77,34 @@ def _rotation(deg: float, axis: int) -> np.ndarray:
     i, j = [(1, 2), (2, 0), (0, 1)][axis]
     R[i, i], R[i, j], R[j, i], R[j, j] = c, -s, s, c
     return R
+
+
+def _transform(params):
+    """Scale (3 factors) and the 4 x 4 transform of a section's Scale / Shift /
+    Rotate lines: scale first, then every Shift / Rotate post-multiplies the
+    transform in the order written (QMatrix4x4::translate / rotate)."""
+    scale = np.ones(3)
+    M = np.eye(4)
+    for k, v in params:
+        if k == "scale":
+            vals = _values(v, "m", 3)
+            scale = np.array(vals + [1.0] * (3 - len(vals))) if len(vals) > 1 else \
+                np.full(3, vals[0])
+        elif k == "shift":
+            vals = _values(v, "m", 3) + [0.0, 0.0]
+            T = np.eye(4)
+            T[:3, 3] = vals[:3]
+            M = M @ T
+        elif k == "rotate":
+            vals = [float(x) for x in re.split(r"[ \t,]+", v.strip()) if x] + [0.0, 0.0]
+            for ax in range(3):
+                M = M @ _rotation(vals[ax], ax)
+    return scale, M
+
+
+def _apply(points, scale, M):
+    p = np.asarray(points, float).reshape(-1, 3) * scale
+    return (np.hstack([p, np.ones((p.shape[0], 1))]) @ M.T)[:, :3]
 
 
 @dataclass
@@ -125,6 +157,7 @@ class Project:
     plane: tuple | None
     element_index: np.ndarray
     section: list
+    sources: list = field(default_factory=list)  # rows x, y, z, weight
 
     @classmethod
     def load(cls, abec_path: str) -> "Project":
@@ -170,26 +203,12 @@ class Project:
         for s in sections:
             if s.kind != "elements":
                 continue
-            scale = np.ones(3)
-            M = np.eye(4)
+            scale, M = _transform(s.params)
             swap = False
             alias = None
             mf, edge = 0.0, 0.0
             for k, v in s.params:
-                if k == "scale":
-                    vals = _values(v, "m", 3)
-                    scale = np.array(vals + [1.0] * (3 - len(vals))) if len(vals) > 1 else \
-                        np.full(3, vals[0])
-                elif k == "shift":
-                    vals = _values(v, "m", 3) + [0.0, 0.0]
-                    T = np.eye(4)
-                    T[:3, 3] = vals[:3]
-                    M = M @ T
-                elif k == "rotate":
-                    vals = [float(x) for x in re.split(r"[ \t,]+", v.strip()) if x] + [0.0, 0.0]
-                    for ax in range(3):
-                        M = M @ _rotation(vals[ax], ax)
-                elif k == "swapnormals":
+                if k == "swapnormals":
                     swap = v == "" or v.lower() in ("1", "true")
                 elif k == "meshfilealias":
                     alias = v.strip("\"'").lower()
@@ -213,9 +232,7 @@ class Project:
                 sel = msh.select(inc or "all", exc)
                 msh.close()
                 t = np.vstack([sel["tri"], quads_to_triangles(sel["quad"])])
-                t = t * np.tile(scale * alias_scale.get(a, 1.0), 3)
-                h = np.hstack([t.reshape(-1, 3), np.ones((t.size // 3, 1))]) @ M.T
-                t = h[:, :3].reshape(-1, 9)
+                t = _apply(t, scale * alias_scale.get(a, 1.0), M).reshape(-1, 9)
                 if swap:
                     t = np.hstack([t[:, 6:9], t[:, 3:6], t[:, 0:3]])
                 e = edge if edge > 0 else ((c / mf) / 2 if mf > 0 else
@@ -259,6 +276,34 @@ class Project:
                     g[sel] = w
                     if beta is not None:
                         beta[sel] = 0.0
+        # point sources: Pressure_Points lines "<index> <node> [Weight=w]
+        # [RefNodes=name]" at the nodes of a Nodes section (setupPressurePoints,
+        # solvingscriptreader.cpp:1016-1050; the weight defaults to DrvWeight)
+        nodes = {}
+        for s in sections:
+            if s.kind == "nodes":
+                scale_n, M_n = _transform(s.params)
+                pts = {}
+                for line in s.lines:
+                    tok = line.split()
+                    if len(tok) >= 4:
+                        pts[int(tok[0])] = _apply([float(x) for x in tok[1:4]], scale_n, M_n)[0]
+                nodes[s.name.lower()] = pts
+        sources = []
+        for s in sections:
+            if s.kind == "pressure_points":
+                p = dict(s.params)
+                dw = float(p.get("drvweight", "1"))
+                for line in s.lines:
+                    m = re.match(r"(\d+)\s+(\d+)(.*)$", line)
+                    if not m:
+                        continue
+                    wm = re.search(r"Weight\s*=\s*(\S+)", m.group(3), re.I)
+                    rm = re.search(r"RefNodes\s*=\s*(\S+)", m.group(3), re.I)
+                    ref = (rm.group(1) if rm else p.get("refnodes", "")).strip("\"'").lower()
+                    if ref in nodes and int(m.group(2)) in nodes[ref]:
+                        x = nodes[ref][int(m.group(2))]
+                        sources.append([x[0], x[1], x[2], float(wm.group(1)) if wm else dw])
         plane = None
         for s in sections:
             if s.kind == "infinite_baffle":
@@ -266,7 +311,7 @@ class Project:
                 plane = (np.array(_values(p.get("position", "0 0 0"), "m", 3)),
                          np.array([float(x) for x in re.split(r"[ \t,]+", p["normal"]) if x]))
                 break
-        return cls(tri, g, beta, freqs, c, rho, plane, eidx, sec_of)
+        return cls(tri, g, beta, freqs, c, rho, plane, eidx, sec_of, sources)
 
     def solver(self, **cfg):
         """A Solver with this project's mesh, boundary data and plane."""
@@ -280,6 +325,8 @@ class Project:
             s.set_bc(np.zeros(n), np.ones(n))
         if self.plane is not None:
             s.set_impedance_plane(*self.plane)
+        if self.sources:
+            s.set_point_sources(self.sources)
         return s
 
     def sweep(self, **cfg):

@@ -125,3 +125,41 @@ def test_reference_example_projects(bem, project, rel, sections):
     assert np.all(P.g[~(front | rear)] == 0)
     assert P.plane is None and P.beta is None       # their baffles and walls are "off"
     assert len(P.frequencies) >= 1 and P.frequencies.min() > 0
+
+
+def test_point_sources_from_nodes(bem, project, tmp_path):
+    write_v2(str(tmp_path / "cube.msh"), cube_faces(n=1))
+    (tmp_path / "p.abec").write_text("[Solving]\nScriptname_Solving=S.txt\n"
+                                     "[MeshFiles]\nC0=cube.msh,A\n")
+    (tmp_path / "S.txt").write_text("""Control_Solver
+    f1=200
+Elements E
+    MeshFileAlias=A
+    1 Mesh Include all
+Nodes "Src"
+    scale=10mm
+    shift=0 0 1
+    1  100 0 0
+    2  0 50 0
+Pressure_Points P
+    DrvWeight=3
+    RefNodes="Src"
+    10  1  Weight=0.5
+    11  2
+""")
+    P = project.Project.load(str(tmp_path / "p.abec"))
+    assert np.allclose(P.sources, [[1.0, 0.0, 1.0, 0.5], [0.0, 0.5, 1.0, 3.0]])
+    assert np.all(P.g == 0) and P.beta is None and P.plane is None
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference examples not present")
+def test_reference_sphere_project(bem, project):
+    """Example/Sphere: a GMSH 4.1 sphere, a point source 20 m away and an
+    active rigid baffle."""
+    P = project.Project.load(os.path.join(REF_EXAMPLES, "Sphere/sphere.abec"))
+    assert P.triangles.shape[0] > 0 and set(P.section) == {"Spere"}
+    assert np.allclose(P.sources, [[20.0, 0.0, 0.0, 1.0]])
+    assert np.allclose(P.plane[0], [0, 0, -10]) and np.allclose(P.plane[1], [0, 0, 1])
+    assert P.c == 344.0 and np.allclose(P.frequencies, [100.0])
+    c = P.triangles.reshape(-1, 3, 3).mean(axis=1)
+    assert np.allclose(c.mean(axis=0), [6.1, 1.5, 1.5], atol=0.2)  # shift applied
