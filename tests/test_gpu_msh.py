@@ -64,3 +64,55 @@ def test_solve_from_msh_file(bem, meshes, tmp_path):
     p_arr = solve(tri, np.where(face == 0, beta_wall, 0.0), (face == 1).astype(np.complex128))
     assert np.array_equal(p_file, p_arr)
     assert np.abs(p_file[face == 1]).mean() > 0
+
+
+def test_project_sweep_matches_library_calls(bem, tmp_path):
+    """3d_bem_gb300/project.py end to end: a project with an admittance wall,
+    a driven face, a point source and a baffle sweeps to the same pressures as
+    the same library calls made by hand."""
+    import importlib
+    from test_msh import cube_faces, write_v2
+    project = importlib.import_module("3d_bem_gb300.project")
+    write_v2(str(tmp_path / "cube.msh"), cube_faces(n=3))
+    (tmp_path / "p.abec").write_text("[Solving]\nScriptname_Solving=S.txt\n"
+                                     "[MeshFiles]\nC0=cube.msh,A\n")
+    (tmp_path / "S.txt").write_text("""Control_Solver
+    f1=200Hz; f2=800Hz; NumFrequencies=3; Abscissa=log
+Elements Box
+    Scale=200mm
+    Shift=0 0 0.5
+    MeshFileAlias=A
+    1 Mesh Include front back left right bottom
+Elements Top
+    Scale=200mm
+    Shift=0 0 0.5
+    MeshFileAlias=A
+    2 Mesh Include top
+Driving D
+    RefElements=Top
+    1 2 Weight=1
+Wallimpedance W
+    RefElements=Box
+    ImpType=admittance
+    value=0.2
+Nodes N
+    1  0.1 0.1 2.0
+Pressure_Points S
+    RefNodes=N
+    5 1 Weight=0.3
+Infinite_Baffle B
+    Position = 0,0,0
+    Normal = 0,0,1
+""")
+    P = project.Project.load(str(tmp_path / "p.abec"))
+    assert P.beta is not None and P.plane is not None and len(P.sources) == 1
+    p, info = P.sweep(precision=1, aca_tol=1e-5, gmres_tol=1e-9)
+    assert p.shape == (P.triangles.shape[0], 3) and np.isfinite(p).all()
+    assert all(i["status"] == 0 for i in info)
+    s = bem.Solver(wave_speed=P.c, density=P.rho, precision=1, aca_tol=1e-5, gmres_tol=1e-9)
+    s.set_mesh(P.triangles)
+    s.set_bc_impedance(P.beta)
+    s.set_impedance_plane(*P.plane)
+    s.set_point_sources(P.sources)
+    q, _ = s.sweep(P.frequencies, P.g)
+    assert np.array_equal(p, q[:, 0, :])
