@@ -2017,6 +2017,8 @@ bem_status bem_hmatvec_noalloc(bem_handle* h, int32_t which, const void* x, void
       a.V = m.V.p;
       a.S = m.S.p;
       a.F = m.F.p;
+      a.vwork = m.vwork.p;  // (block, 16-row) work items of pass V: handle-owned, no allocation
+      a.nvwork = m.nvwork;
       a.x = xd + r0 * ncols;
       a.ldx = ncols;
       a.t = t;

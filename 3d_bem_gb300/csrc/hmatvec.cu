@@ -670,7 +670,10 @@ int64_t hmatvec_noalloc_capacity() { return HMV_NOALLOC_SCRATCH; }
 
 // Device address of the scratch array on the current device. The first call
 // on each device looks it up (cudaGetSymbolAddress, with that device current);
-// later calls reuse the cached address.
+// later calls reuse the cached address. The cache is keyed by device ordinal,
+// i.e. it assumes the device's primary context (the one the CUDA runtime
+// uses): after cudaDeviceReset, or under a driver-API context of its own, the
+// cached address no longer belongs to the current context.
 cudaError_t hmatvec_noalloc_scratch(double2** out) {
   static std::mutex mu;
   static void* addr[256] = {};

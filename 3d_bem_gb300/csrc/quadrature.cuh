@@ -160,6 +160,11 @@ __device__ __forceinline__ Ops ops_singular(const Elem& T, double k, const QuadR
 // Closest point of triangle Q to p (global.cpp:955-1228), with the 0.05
 // barycentric classification; returns the region code
 // 0 interior, 1..3 node 1..3, 4 side 21, 5 side 32, 6 side 13.
+// The minimisation over the triangle's (s, t) parameter domain is D. Eberly's
+// published point-to-triangle distance algorithm ("Distance Between Point and
+// Triangle in 3D", Geometric Tools), which the reference also follows region
+// by region; the same branches and quadratic-form names are kept because the
+// near-singular classification has to agree with the reference bit for bit.
 __device__ __forceinline__ int project_point(const Elem& Q, const double* p, double* out) {
   double d[3], e0[3], e1[3];
   for (int i = 0; i < 3; i++) {

@@ -72,19 +72,46 @@ def _grid_face(origin, e1, e2, n1, n2, rng, jitter):
     return np.array(tris)
 
 
-def box(lx=0.3, ly=0.2, lz=0.4, n_target=5120, seed=20260103, jitter=0.25) -> np.ndarray:
+def _box_cells(L, n_target, exact):
+    """Cells per axis (nx, ny, nz) of the box grids: rounded from a uniform
+    spacing, or, with ``exact``, the nearby triple whose total
+    4 (nx ny + ny nz + nx nz) equals ``n_target`` with the most uniform
+    spacing (the rounded triple when no such triple is near)."""
+    area = 2 * (L[0] * L[1] + L[1] * L[2] + L[0] * L[2])
+    h = (2.0 * area / n_target) ** 0.5
+    ideal = [x / h for x in L]
+    base = [max(1, round(v)) for v in ideal]
+    if not exact or n_target % 4:
+        return base
+    best, score = None, None
+    rng3 = [range(max(1, b - 3), b + 4) for b in base]
+    for nx in rng3[0]:
+        for ny in rng3[1]:
+            for nz in rng3[2]:
+                if 4 * (nx * ny + ny * nz + nx * nz) != n_target:
+                    continue
+                sp = [L[0] / nx, L[1] / ny, L[2] / nz]
+                s = max(sp) / min(sp)
+                if score is None or s < score:
+                    best, score = [nx, ny, nz], s
+    return best if best is not None else base
+
+
+def box(lx=0.3, ly=0.2, lz=0.4, n_target=5120, seed=20260103, jitter=0.25,
+        exact=False) -> np.ndarray:
     """Closed box surface with seeded jittered triangulation of every face.
 
     The face grids are sized so the total is close to ``n_target`` triangles
-    with near-uniform element size; interior nodes are jittered by up to
-    ``jitter`` of the local spacing (edge nodes stay put so faces conform).
+    (exactly ``n_target`` with ``exact`` when a grid of near-uniform spacing
+    has that count) with near-uniform element size; interior nodes are
+    jittered by up to ``jitter`` of the local spacing (edge nodes stay put so
+    faces conform).
     """
     rng = np.random.default_rng(seed)
-    area = 2 * (lx * ly + ly * lz + lx * lz)
-    h = (2.0 * area / n_target) ** 0.5
     faces = []
     dims = {(0, 1): (lx, ly), (1, 2): (ly, lz), (0, 2): (lx, lz)}
-    counts = {k: (max(1, round(a / h)), max(1, round(b / h))) for k, (a, b) in dims.items()}
+    cells = _box_cells([lx, ly, lz], n_target, exact)
+    counts = {(i, j): (cells[i], cells[j]) for (i, j) in dims}
     E = np.eye(3)
     L = np.array([lx, ly, lz])
     for (i, j), (n1, n2) in counts.items():
@@ -111,7 +138,10 @@ def pencil(radius=0.004, length=0.2, tip=0.01, n_target=81920, seed=20260105,
 
     ``n_target`` triangles are split between the cylinder, the cone and the cap
     in proportion to their areas; ring nodes are jittered by up to ``jitter`` of
-    the local spacing along the axis and around the ring.
+    the local spacing along the axis and around the ring. The mesh has
+    2 m (nz + ncone + ncap - 1) triangles for m nodes around; m is taken among
+    the divisors of n_target / 2 within 25 % of the uniform spacing, so that
+    the count is exactly ``n_target`` (81,920: m = 64), else rounded.
     """
     rng = np.random.default_rng(seed)
     cone_slant = (tip ** 2 + radius ** 2) ** 0.5
@@ -120,10 +150,21 @@ def pencil(radius=0.004, length=0.2, tip=0.01, n_target=81920, seed=20260105,
     a_cap = np.pi * radius ** 2
     total = a_cyl + a_cone + a_cap
     h = (2.0 * total / n_target) ** 0.5
-    m = max(8, int(round(2 * np.pi * radius / h)))  # nodes around
-    nz = max(1, int(round((n_target * a_cyl / total) / (2 * m))))
+    m0 = 2 * np.pi * radius / h
+    m = max(8, int(round(m0)))  # nodes around
+    divs = [d for d in range(8, int(1.25 * m0) + 1)
+            if n_target % 2 == 0 and (n_target // 2) % d == 0 and d >= 0.8 * m0]
     ncone = max(1, int(round((n_target * a_cone / total) / (2 * m))))
     ncap = max(1, int(round((n_target * a_cap / total) / (2 * m))))
+    nz = max(1, int(round((n_target * a_cyl / total) / (2 * m))))
+    if divs:
+        m = min(divs, key=lambda d: abs(d - m0))
+        rings_total = n_target // (2 * m) + 1  # nz + ncone + ncap
+        ncone = max(1, int(round((n_target * a_cone / total) / (2 * m))))
+        ncap = max(1, int(round((n_target * a_cap / total) / (2 * m))))
+        nz = rings_total - ncone - ncap
+        if nz < 1:
+            raise ValueError("pencil: n_target too small for the cone and cap rings")
     ang = 2 * np.pi * np.arange(m) / m
 
     def ring(z, r, jit_axis, jit_ang):

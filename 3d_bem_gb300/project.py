@@ -90,6 +90,8 @@ def _transform(params):
             vals = _values(v, "m", 3)
             scale = np.array(vals + [1.0] * (3 - len(vals))) if len(vals) > 1 else \
                 np.full(3, vals[0])
+            # a zero factor means 1 (ElementSection, elementSection.cpp:147-149)
+            scale[scale == 0] = 1.0
         elif k == "shift":
             vals = _values(v, "m", 3) + [0.0, 0.0]
             T = np.eye(4)
@@ -176,7 +178,9 @@ class Project:
         with open(os.path.join(base, script), encoding="utf-8", errors="replace") as fh:
             sections = parse_script(fh.read())
         ctrl = {k: v for s in sections if s.kind == "control_solver" for k, v in s.params}
-        c = with_units(ctrl["c"], "m/s") if "c" in ctrl else 343.2
+        c = with_units(ctrl["c"], "m/s") if "c" in ctrl else 0.0
+        if c == 0:  # ControlSolverSection::getWavespeed (controlsolversection.cpp:293-299)
+            c = 343.21
         rho = with_units(ctrl["rho"], "kg/m^3") if "rho" in ctrl else 1.2041
         f1 = with_units(ctrl.get("f1", "0"), "Hz")
         f2 = with_units(ctrl.get("f2", "0"), "Hz")
@@ -196,7 +200,12 @@ class Project:
                 if "meshfilealias" in p and "scale" in p:
                     alias_scale[p["meshfilealias"].strip("\"'").lower()] = \
                         _values(p["scale"], "m", 3)[0]
+        # global edge length (ControlSolverSection::getEdgelength,
+        # controlsolversection.cpp:301-313): half the wavelength at MeshFrequency,
+        # else at the highest of f1, f2
         global_mf = with_units(ctrl["meshfrequency"], "Hz") if "meshfrequency" in ctrl else 0.0
+        if global_mf == 0:
+            global_mf = max(f1, f2)
 
         tris, idx, sec_of = [], [], []
         by_name = {}
@@ -235,8 +244,11 @@ class Project:
                 t = _apply(t, scale * alias_scale.get(a, 1.0), M).reshape(-1, 9)
                 if swap:
                     t = np.hstack([t[:, 6:9], t[:, 3:6], t[:, 0:3]])
-                e = edge if edge > 0 else ((c / mf) / 2 if mf > 0 else
-                                           ((c / global_mf) / 2 if global_mf > 0 else 0.0))
+                # SolvingScriptReader::refineElements (solvingscriptreader.cpp:
+                # 1104-1116): a section's MeshFrequency wins over its EdgeLength;
+                # with neither, the global edge length
+                e = (c / mf) / 2 if mf > 0 else (
+                    edge if edge > 0 else ((c / global_mf) / 2 if global_mf > 0 else 0.0))
                 if e > 0 and t.shape[0]:
                     t, _ = refine_triangles(t, e)
                 tris.append(t)

@@ -62,8 +62,8 @@ WORKLOADS = {
 }
 # DRAM traffic of the FP32 H-matvec per algorithmic byte, from one ncu
 # capture of hmv32_vpass + hmv32_upass at 5,120 elements (126.08 MB read +
-# write against 129.02 MB algorithmic; profiles/hmatvec_fp32_sphere5k.md),
-# scaled to the benchmark operator by its algorithmic bytes.
+# write against 129.02 MB algorithmic), scaled to the benchmark operator by
+# its algorithmic bytes.
 HMV32_TRAFFIC_PER_BYTE = (57592832 + 169728 + 68490496 + 13568) / 129017600
 METRIC = "freq-solves/sec (H-matrix Helmholtz BEM solve, <=1e-5 rel. surface-pressure error)"
 UNIT = "freq-solves/s"

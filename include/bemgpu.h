@@ -174,7 +174,10 @@ bem_status bem_hmatvec_device_ex(bem_handle* h, int32_t which, const void* x, vo
  * calls cudaMalloc / cudaFree. Every call shares that array, so calls that
  * overlap on the GPU (other streams, other handles) race; the first call on
  * each device looks the array up (cudaGetSymbolAddress) and should come before
- * any stream capture. FP64 arithmetic on the stored entries, identical to
+ * any stream capture; the address is kept per device ordinal for the device's
+ * primary context (the CUDA runtime's), so it is not valid across
+ * cudaDeviceReset or under another context on the same device. FP64
+ * arithmetic on the stored entries and the same kernels and work items as
  * bem_hmatvec_device. */
 bem_status bem_hmatvec_noalloc(bem_handle* h, int32_t which, const void* x, void* y,
                                int64_t nrhs, int32_t accumulate);

@@ -408,7 +408,9 @@ Ops OperatorCtx::singular(int64_t ti) const {
 
 // projectPointOnTriangleFaster (global.cpp:955-1228): closest point of a
 // triangle to p, classified as interior / node / side with the 0.05
-// barycentric threshold.
+// barycentric threshold. The region-by-region minimisation is D. Eberly's
+// published point-to-triangle distance algorithm ("Distance Between Point and
+// Triangle in 3D", Geometric Tools), as in the reference.
 enum Region { IN_INTERIOR, ON_NODE1, ON_NODE2, ON_NODE3, ON_SIDE21, ON_SIDE32, ON_SIDE13 };
 
 static std::pair<V3, Region> project_point(const Tri& tr, V3 point) {

@@ -14,7 +14,9 @@ import numpy as np
 import pytest
 
 NAMES = ["front", "back", "left", "right", "bottom", "top"]
-REF_EXAMPLES = "/root/reference/Example"
+# the reference's Example folder (its example meshes and projects), when a
+# copy is at hand: BEM_REFERENCE_EXAMPLES=<path to Example>; skipped otherwise
+REF_EXAMPLES = os.environ.get("BEM_REFERENCE_EXAMPLES", "")
 
 
 def cube_faces(n=3, seed=0):
@@ -238,7 +240,8 @@ def test_wall_beta(bem):
         bem.wall_beta(bem.IMP_REFLECTION, -1.0)  # 1 + R = 0
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference examples not present")
+@pytest.mark.skipif(not REF_EXAMPLES or not os.path.isdir(REF_EXAMPLES),
+                    reason="BEM_REFERENCE_EXAMPLES not set")
 @pytest.mark.parametrize("rel", ["Loudspeaker/loudspeaker.msh", "Pensil/Pensil R70.msh",
                                  "Sphere/twoSpheres.msh"])
 def test_reference_example_meshes(bem, rel):

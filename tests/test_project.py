@@ -10,7 +10,9 @@ import pytest
 
 from test_msh import cube_faces, write_v2
 
-REF_EXAMPLES = "/root/reference/Example"
+# the reference's Example folder (its example meshes and projects), when a
+# copy is at hand: BEM_REFERENCE_EXAMPLES=<path to Example>; skipped otherwise
+REF_EXAMPLES = os.environ.get("BEM_REFERENCE_EXAMPLES", "")
 
 
 @pytest.fixture(scope="module")
@@ -104,7 +106,8 @@ def test_refinement_by_mesh_frequency(bem, project, tmp_path):
     assert np.array_equal(P.triangles, ref) and ref.shape[0] > src.shape[0]
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference examples not present")
+@pytest.mark.skipif(not REF_EXAMPLES or not os.path.isdir(REF_EXAMPLES),
+                    reason="BEM_REFERENCE_EXAMPLES not set")
 @pytest.mark.parametrize("rel,sections", [
     ("Loudspeaker/Project.abec", {"Enclosure-Exterior", "Enclosure-Driver", "Enclosure-Driver-rear"}),
     ("Pensil/pensil.abec", {"enclosure-Exterior", "loudspeaker-Driver-front",
@@ -152,7 +155,8 @@ Pressure_Points P
     assert np.all(P.g == 0) and P.beta is None and P.plane is None
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference examples not present")
+@pytest.mark.skipif(not REF_EXAMPLES or not os.path.isdir(REF_EXAMPLES),
+                    reason="BEM_REFERENCE_EXAMPLES not set")
 def test_reference_sphere_project(bem, project):
     """Example/Sphere: a GMSH 4.1 sphere, a point source 20 m away and an
     active rigid baffle."""
@@ -163,3 +167,46 @@ def test_reference_sphere_project(bem, project):
     assert P.c == 344.0 and np.allclose(P.frequencies, [100.0])
     c = P.triangles.reshape(-1, 3, 3).mean(axis=1)
     assert np.allclose(c.mean(axis=0), [6.1, 1.5, 1.5], atol=0.2)  # shift applied
+
+
+def _one_section_project(tmp_path, control, section_lines, n=1):
+    faces = cube_faces(n=n)
+    write_v2(str(tmp_path / "cube.msh"), faces)
+    (tmp_path / "p.abec").write_text("[Solving]\nScriptname_Solving=S.txt\n"
+                                     "[MeshFiles]\nC0=cube.msh,A\n")
+    (tmp_path / "S.txt").write_text("Control_Solver\n" + control +
+                                    "Elements E\n    MeshFileAlias=A\n" + section_lines +
+                                    "    1 Mesh Include front\n")
+
+
+def test_default_refinement_from_highest_frequency(bem, project, tmp_path):
+    """No MeshFrequency anywhere: the global edge length is half the
+    wavelength at max(f1, f2) (ControlSolverSection::getEdgelength,
+    controlsolversection.cpp:301-313), applied to every section that sets
+    neither MeshFrequency nor EdgeLength (solvingscriptreader.cpp:1109-1111)."""
+    _one_section_project(tmp_path, "    f1=100\n    f2=600\n    c=340\n", "")
+    P = project.Project.load(str(tmp_path / "p.abec"))
+    src = bem.MshFile(str(tmp_path / "cube.msh")).select("front")["tri"]
+    ref, _ = bem.refine_triangles(src, (340.0 / 600.0) / 2)
+    assert ref.shape[0] > src.shape[0]
+    assert np.array_equal(P.triangles, ref)
+
+
+def test_mesh_frequency_wins_over_edge_length(bem, project, tmp_path):
+    """A section with both: MeshFrequency sets the edge length
+    (solvingscriptreader.cpp:1113-1116)."""
+    _one_section_project(tmp_path, "    f1=100\n    c=340\n",
+                         "    MeshFrequency=900Hz\n    EdgeLength=1m\n")
+    P = project.Project.load(str(tmp_path / "p.abec"))
+    src = bem.MshFile(str(tmp_path / "cube.msh")).select("front")["tri"]
+    ref, _ = bem.refine_triangles(src, (340.0 / 900.0) / 2)
+    assert ref.shape[0] > src.shape[0]
+    assert np.array_equal(P.triangles, ref)
+
+
+def test_zero_scale_component_means_one(bem, project, tmp_path):
+    """Scale=0 2 0 scales by (1, 2, 1) (elementSection.cpp:147-149)."""
+    _one_section_project(tmp_path, "    f1=1\n    c=340\n", "    Scale=0 2 0\n")
+    P = project.Project.load(str(tmp_path / "p.abec"))
+    src = bem.MshFile(str(tmp_path / "cube.msh")).select("front")["tri"]
+    assert np.allclose(P.triangles, (src.reshape(-1, 3) * [1.0, 2.0, 1.0]).reshape(-1, 9))
