@@ -32,7 +32,7 @@ STATUS_NAMES = {0: "OK", 1: "EINVAL", 2: "ENOMEM", 3: "ENONFINITE", 4: "EMAXIT",
 # the C-ABI symbols declared in include/bemgpu.h
 EXPORTS = [
     "bem_config_default", "bem_create", "bem_destroy", "bem_last_error", "bem_set_mesh",
-    "bem_plan_mesh",
+    "bem_plan_mesh", "bem_hlu_plan",
     "bem_get_permutation", "bem_get_partition", "bem_set_bc", "bem_operators",
     "bem_assemble", "bem_hmatvec", "bem_hmatvec_device", "bem_get_block", "bem_get_ranks",
     "bem_gmres", "bem_solve", "bem_solve_device", "bem_sweep", "bem_points_assemble",
@@ -65,7 +65,7 @@ class Config(ct.Structure):
                 ("precond_rank", ct.c_int64), ("precond_tol", ct.c_double),
                 ("recompress_tol", ct.c_double), ("selector_guard", ct.c_double),
                 ("sweep_workers", ct.c_int64), ("aca_big_mn", ct.c_int64),
-                ("precond_reuse", ct.c_double)]
+                ("precond_reuse", ct.c_double), ("hlu_device", ct.c_int32)]
 
 
 class SolveInfo(ct.Structure):
@@ -112,6 +112,7 @@ def lib():
     L.bem_last_error.restype = ct.c_char_p
     L.bem_set_mesh.argtypes = [vp, vp, i64]
     L.bem_plan_mesh.argtypes = [P(Config), vp, i64, vp, P(i64), vp]
+    L.bem_hlu_plan.argtypes = [P(Config), vp, i64, vp, i64]
     L.bem_get_permutation.argtypes = [vp, vp]
     L.bem_get_partition.argtypes = [vp, P(i64), vp]
     L.bem_set_bc.argtypes = [vp, vp, vp]
@@ -197,6 +198,25 @@ def plan_mesh(tri, config: Config | None = None):
     if st != BEM_OK:
         raise BemError(st, "bem_plan_mesh failed")
     return perm, info
+
+
+HLU_PLAN_KEYS = ("tasks", "arena_elems", "scratch_elems", "levels", "cost_path_us",
+                 "cost_total_us", "max_trunc_width", "dataflow_sweeps", "gemm", "lmul",
+                 "rmul", "qr", "trunc", "copy", "zero", "dep_entries", "big_scratch_elems",
+                 "path_gemm", "path_lmul", "path_rmul", "path_qr", "path_trunc", "path_copy",
+                 "path_zero")
+
+
+def hlu_plan(tri, config: Config | None = None) -> dict:
+    """Host-only statistics of the GPU H-LU task program for a mesh (no GPU
+    needed): task counts, arena size, critical path of the cost model."""
+    tri = np.ascontiguousarray(tri, dtype=np.float64).reshape(-1, 9)
+    cfg = config if config is not None else default_config()
+    out = np.zeros(len(HLU_PLAN_KEYS))
+    st = lib().bem_hlu_plan(ct.byref(cfg), _ptr(tri), tri.shape[0], _ptr(out), out.size)
+    if st != BEM_OK:
+        raise BemError(st, "bem_hlu_plan failed")
+    return dict(zip(HLU_PLAN_KEYS, out.tolist()))
 
 
 def _ptr(a: np.ndarray):

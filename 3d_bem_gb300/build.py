@@ -25,8 +25,8 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["nearfield.cu", "aca.cu", "hmatvec.cu", "krylov.cu", "post.cu", "hlu_solve.cu", "recompress.cu",
-              "selector.cu", "field.cu"]
-CPP_SOURCES = ["host_tree.cpp", "hlu.cpp", "capi.cpp", "msh.cpp"]
+              "selector.cu", "field.cu", "hlu_exec.cu"]
+CPP_SOURCES = ["host_tree.cpp", "hlu.cpp", "hlu_plan.cpp", "capi.cpp", "msh.cpp"]
 
 
 def _sources():

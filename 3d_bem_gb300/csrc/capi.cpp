@@ -14,6 +14,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <numeric>
+#include <cstdio>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -24,6 +26,7 @@
 #include "bem_kernels.h"
 #include "hlu.h"
 #include "hlu_solve.h"
+#include "hlu_gpu.h"
 #include "recompress.h"
 #include "selector.h"
 #include "host_tree.h"
@@ -183,6 +186,24 @@ struct bem_handle {
   DBuf<unsigned char> dfPre, dfFin;
   DBuf<int> dfCtrl, dfErr;
   DBuf<int> dBad;
+  // GPU H-LU factorization (hlu_gpu.h): the task program of the current
+  // layout and rank, its device tables, the arena holding the factors, and
+  // the truncation scratch
+  uint64_t layout_gen = 0;  // bumped whenever the block offsets change
+  bool hlu_dev = false;     // the current factors live in the arena
+  HluProgram hp;
+  bool hp_ok = false;
+  uint64_t hp_gen = ~0ull;
+  int64_t hp_kc = -1;
+  int hp_prec = -1, hp_grid = 0;
+  std::string hp_why;
+  DBuf<HluTask> dHT;
+  DBuf<int32_t> dHDepOff, dHDeps;
+  DBuf<HluTruncPair> dHPairs;
+  DBuf<HluQrOut> dHQr;
+  DBuf<int> dHDone, dHCtrl;
+  DBuf<unsigned char> dArena, dHScr, dHBig;
+  HluDfPlan hpl, hpu;       // sweep plans of the program's factors (structure)
   // impedance plane (bem_set_impedance_plane): point, unit normal and the
   // elements reflected in it (cluster order)
   // point sources of the right-hand side (bem_set_point_sources)
@@ -281,6 +302,7 @@ void upload_layout(bem_handle* h) {
   h->dPivRc.upload(L.piv_rc, s);
   for (auto& m : h->hm) m.assembled = false;
   h->have_hlu = false;
+  h->layout_gen++;
 }
 
 // storage precision of the matrices: point clouds (test kernel) stay FP64
@@ -325,6 +347,7 @@ bool grow_capped(bem_handle* h) {
     L.s_size += f.kcap;
   }
   h->dFar.upload(L.far, h->stream);
+  h->layout_gen++;
   return true;
 }
 
@@ -827,6 +850,14 @@ void upload_df_plans(bem_handle* h) {
   h->df_ok = true;
 }
 
+// Bound of one dependency wait of the H-LU executor, in SM clock cycles:
+// 2 s at 2 GHz, or BEM_HLU_WAIT_US microseconds (tests of the timeout path).
+int64_t hlu_wait_cycles() {
+  const char* e = std::getenv("BEM_HLU_WAIT_US");
+  const double us = e ? std::atof(e) : 0.0;
+  return us > 0 ? (int64_t)(us * 2000.0) : (int64_t)4000000000LL;
+}
+
 int df_helpers() {
   const char* e = std::getenv("BEM_HLU_HELPERS");
   const int v = e ? std::atoi(e) : 0;
@@ -841,8 +872,249 @@ void check_df_error(bem_handle* h) {
   CK(cudaStreamSynchronize(h->stream));
   if (e) {
     CK(cudaMemsetAsync(h->dfErr.p, 0, sizeof(int), h->stream));
-    throw BemError{BEM_ECUDA, "H-LU sweep: a dataflow wait ran out of time"};
+    throw BemError{BEM_ETIMEOUT, "H-LU sweep: a dataflow wait ran out of time"};
   }
+}
+
+// ---- GPU H-LU factorization ----
+
+bool hlu_device_eligible(const bem_handle* h) {
+  return h->cfg.hlu_device && !h->points_mode && h->cfg.precond_rank >= 1 &&
+         h->cfg.precond_rank <= 64 && h->cfg.leaf_size <= HLU_GPU_MAX_LEAF + 1;
+}
+
+// The task program of the current layout and rank, its device tables and the
+// structure of the sweeps (leaf lists, dataflow plans); built once per mesh
+// (and again after the rank reservations grow).
+bool prepare_hlu_program(bem_handle* h) {
+  if (h->hp_ok && h->hp_gen == h->layout_gen && h->hp_kc == h->cfg.precond_rank) return true;
+  h->hp_ok = false;
+  h->hp_prec = -1;
+  HluProgram& P = h->hp;
+  std::string why;
+  if (!hlu_gpu_plan(h->rows, h->L, h->cfg.precond_rank, P, &why)) {
+    h->hp_why = why;
+    return false;
+  }
+  require(P.tasks.size() < (size_t)INT32_MAX, BEM_EINVAL, "H-LU program too large");
+  cudaStream_t s = h->stream;
+  h->dHT.upload(P.tasks, s);
+  h->dHDepOff.upload(P.dep_off, s);
+  h->dHDeps.upload(P.deps, s);
+  h->dHPairs.upload(P.pairs, s);
+  h->dHQr.upload(P.qr, s);
+  h->dHDone.ensure(P.tasks.size());
+  h->dHCtrl.ensure(4);
+  sync(h);
+  h->hp_gen = h->layout_gen;
+  h->hp_kc = h->cfg.precond_rank;
+  h->hp_ok = true;
+  return true;
+}
+
+// Arena (zeroed once, so padding never holds stale bits), per-CTA scratch for
+// the co-resident grid and the large truncations' regions, per precision.
+void prepare_hlu_arena(bem_handle* h, int prec) {
+  const HluProgram& P = h->hp;
+  if (h->hp_prec == prec) return;
+  const size_t es = prec ? sizeof(float2) : sizeof(double2);
+  const int occ = hlu_exec_occupancy(prec);
+  require(occ >= 1, BEM_ECUDA, "H-LU executor: no co-resident CTA fits an SM");
+  h->hp_grid = h->nsm * std::min(occ, 4);
+  h->dArena.release();
+  h->dHScr.release();
+  h->dHBig.release();
+  h->dArena.ensure((size_t)P.arena * es);
+  CK(cudaMemsetAsync(h->dArena.p, 0, (size_t)P.arena * es, h->stream));
+  h->dHScr.ensure((size_t)h->hp_grid * P.scratch * es);
+  h->dHBig.ensure((size_t)std::max<int64_t>(P.big_scratch, 1) * es);
+  // sweep plans: the staging offsets of their late leaves depend on the
+  // element size of the factors
+  h->hpl = HluDfPlan();
+  h->hpu = HluDfPlan();
+  if (P.df_ok) {
+    std::string w;
+    const bool ok = hlu_df_plan_structure(P.L, h->N, (int)es, h->hpl, &w) &&
+                    hlu_df_plan_structure(P.U, h->N, (int)es, h->hpu, &w);
+    require(ok, BEM_EINVAL, "H-LU program: sweep plan");
+  }
+  h->hp_prec = prec;
+}
+
+// The dataflow sweeps of the program's factors: plans uploaded without their
+// apply matrices, which the QR tasks write into the arena at the plans'
+// offsets.
+void upload_df_plans_device(bem_handle* h) {
+  h->df_ok = false;
+  h->df_why = h->hp.df_why;
+  if (!h->hp.df_ok) return;
+  cudaStream_t s = h->stream;
+  const size_t cs = h->hlu_prec == 0 ? sizeof(double2) : sizeof(float2);
+  int64_t nslot = 0;
+  int D = 0;
+  for (int q = 0; q < 2; q++) {
+    const HluDfPlan& p = q ? h->hpu : h->hpl;
+    bem_handle::DfDev& d = q ? h->dfU : h->dfL;
+    upload_bytes(d.chunks, p.chunks, s);
+    upload_bytes(d.rows, p.rows, s);
+    upload_bytes(d.erows, p.erows, s);
+    upload_bytes(d.cols, p.cols, s);
+    d.slot.upload(p.slot, s);
+    d.view.chunks = (const HluDfChunk*)d.chunks.p;
+    d.view.rows = (const HluDfRow*)d.rows.p;
+    d.view.erows = (const HluDfRow*)d.erows.p;
+    d.view.cols = (const HluDfCol*)d.cols.p;
+    d.view.slot = d.slot.p;
+    d.view.diag = h->dArena.p + (size_t)(q ? h->hp.rinv_base : h->hp.qh_base) * cs;
+    d.view.D = p.D();
+    nslot = std::max(nslot, p.nslot);
+    D = std::max(D, p.D());
+  }
+  h->dfXi.ensure((size_t)HLU_DF_MAX_R * h->N * cs);
+  h->dfAcc.ensure((size_t)HLU_DF_MAX_R * h->N * cs);
+  h->dfEacc.ensure((size_t)HLU_DF_MAX_R * h->N * cs);
+  h->dfPre.ensure((size_t)std::max<int64_t>(nslot, 1) * cs);
+  h->dfFin.ensure((size_t)std::max<int64_t>(nslot, 1) * cs);
+  h->dfCtrl.ensure((size_t)(4 + 3 * D));
+  h->dfErr.ensure(1);
+  CK(cudaMemsetAsync(h->dfErr.p, 0, sizeof(int), s));
+  h->df_ok = true;
+}
+
+// H-LU of the truncated copy of the assembled dPhi matrix, on the GPU: one
+// launch of the task program (loads of the near-field blocks and truncations
+// of the ACA blocks to the preconditioner rank, then the factorization); the
+// factors stay in the arena. Returns false, keeping no factors, when a pivot
+// is zero or a value is not finite (the solve then runs unpreconditioned, as
+// on the host path); a dependency wait that runs out is BEM_ETIMEOUT.
+// Summary of one traced factorization: makespan, busy time per task type,
+// the measured critical path (longest chain of start-to-end times along the
+// dependencies) and the time tasks waited for their dependencies.
+void hlu_trace_summary(const HluProgram& P, const DBuf<unsigned long long>& tr, int grid,
+                       const char* path) {
+  const size_t nt = P.tasks.size();
+  std::vector<unsigned long long> t(3 * nt);
+  CK(cudaMemcpy(t.data(), tr.p, t.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  unsigned long long t0 = ~0ull, t1 = 0;
+  for (size_t i = 0; i < nt; i++) {
+    t0 = std::min(t0, t[3 * i]);
+    t1 = std::max(t1, t[3 * i + 2]);
+  }
+  double busy[8] = {}, wait[8] = {}, mx[8] = {};
+  int64_t cnt[8] = {};
+  std::vector<double> fin(nt, 0.0);
+  std::vector<int32_t> pred(nt, -1);
+  int64_t last = 0;
+  for (size_t i = 0; i < nt; i++) {
+    const int ty = P.tasks[i].type & 7;
+    const double d = 1e-3 * (double)(t[3 * i + 2] - t[3 * i + 1]);
+    busy[ty] += d;
+    mx[ty] = std::max(mx[ty], d);
+    wait[ty] += 1e-3 * (double)(t[3 * i + 1] - t[3 * i]);
+    cnt[ty]++;
+    double best = 0;
+    for (int32_t k = P.dep_off[i]; k < P.dep_off[i + 1]; k++)
+      if (fin[P.deps[k]] > best) {
+        best = fin[P.deps[k]];
+        pred[i] = P.deps[k];
+      }
+    fin[i] = best + d;
+    if (fin[i] > fin[last]) last = (int64_t)i;
+  }
+  int64_t path_cnt[8] = {};
+  double path_t[8] = {};
+  for (int64_t i = last; i >= 0; i = pred[i]) {
+    const int ty = P.tasks[i].type & 7;
+    path_cnt[ty]++;
+    path_t[ty] += 1e-3 * (double)(t[3 * i + 2] - t[3 * i + 1]);
+  }
+  FILE* f = std::fopen(path, "w");
+  if (!f) return;
+  const char* nm[8] = {"gemm", "lmul", "rmul", "qr", "trunc", "copy", "zero", "?"};
+  std::fprintf(f, "tasks %zu grid %d makespan_us %.1f critical_path_us %.1f\n", nt, grid,
+               1e-3 * (double)(t1 - t0), fin[last]);
+  for (int k = 0; k < 7; k++)
+    std::fprintf(f, "%-6s n %9lld busy_us %12.1f avg_us %8.2f max_us %9.1f wait_us %12.1f "
+                 "path_n %6lld path_us %10.1f\n", nm[k], (long long)cnt[k], busy[k],
+                 cnt[k] ? busy[k] / cnt[k] : 0.0, mx[k], wait[k], (long long)path_cnt[k], path_t[k]);
+  // the slowest tasks
+  std::vector<size_t> ord(nt);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::partial_sort(ord.begin(), ord.begin() + std::min<size_t>(20, nt), ord.end(),
+                    [&](size_t a, size_t b) {
+                      return t[3 * a + 2] - t[3 * a + 1] > t[3 * b + 2] - t[3 * b + 1];
+                    });
+  for (size_t r = 0; r < std::min<size_t>(20, nt); r++) {
+    const HluTask& k = P.tasks[ord[r]];
+    std::fprintf(f, "slow %s m %d n %d q %d pairs %d us %.1f\n", nm[k.type & 7], k.m, k.n, k.q,
+                 k.x1, 1e-3 * (double)(t[3 * ord[r] + 2] - t[3 * ord[r] + 1]));
+  }
+  std::fclose(f);
+}
+
+bool build_hlu_device(bem_handle* h) {
+  DevHM& m = h->hm[1];
+  const HluProgram& P = h->hp;
+  prepare_hlu_arena(h, m.prec);
+  cudaStream_t s = h->stream;
+  CK(cudaMemsetAsync(h->dHDone.p, 0, P.tasks.size() * sizeof(int), s));
+  CK(cudaMemsetAsync(h->dHCtrl.p, 0, 4 * sizeof(int), s));
+  HluExecArgs a{};
+  a.precision = m.prec;
+  a.arena = h->dArena.p;
+  a.F = m.F.p;
+  a.U = m.U.p;
+  a.V = m.V.p;
+  a.S = m.S.p;
+  a.rank = m.rank.p;
+  a.tasks = h->dHT.p;
+  a.ntasks = (int32_t)P.tasks.size();
+  a.dep_off = h->dHDepOff.p;
+  a.deps = h->dHDeps.p;
+  a.pairs = h->dHPairs.p;
+  a.qr = h->dHQr.p;
+  a.done = h->dHDone.p;
+  a.ctrl = h->dHCtrl.p;
+  a.scratch = h->dHScr.p;
+  a.scratch_per_cta = P.scratch;
+  a.big_scratch = h->dHBig.p;
+  a.kc = P.kc;
+  a.tol = h->cfg.precond_tol;
+  a.wait_cycles = hlu_wait_cycles();
+  // BEM_HLU_TRACE=<file>: per-task timestamps, summarised into the file
+  const char* trace_path = std::getenv("BEM_HLU_TRACE");
+  DBuf<unsigned long long> trace;
+  if (trace_path && *trace_path) {
+    trace.ensure(3 * P.tasks.size());
+    CK(cudaMemsetAsync(trace.p, 0, 3 * P.tasks.size() * sizeof(unsigned long long), s));
+    a.trace = trace.p;
+  }
+  const int nl = launch_hlu_exec(a, h->hp_grid, s);
+  require(nl > 0, BEM_ECUDA, "H-LU executor: cooperative launch refused");
+  h->launches += nl;
+  CK(cudaGetLastError());
+  launch_hlu_finite_check(h->dArena.p, P.arena, m.prec, h->dHCtrl.p + 3, h->nsm, s);
+  h->launches++;
+  int ctrl[4] = {0, 0, 0, 0};
+  CK(cudaMemcpyAsync(ctrl, h->dHCtrl.p, sizeof(ctrl), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (a.trace) hlu_trace_summary(P, trace, h->hp_grid, trace_path);
+  if (ctrl[1])
+    throw BemError{BEM_ETIMEOUT, "H-LU factorization: a task dependency wait ran out of time"};
+  if (ctrl[2] || ctrl[3]) return false;
+  h->hlu_prec = m.prec;
+  h->hL = P.L;
+  h->hU = P.U;
+  h->dLs.upload(P.L.schedule, s);
+  h->dLl.upload(P.L.leaves, s);
+  h->dUs.upload(P.U.schedule, s);
+  h->dUl.upload(P.U.leaves, s);
+  upload_df_plans_device(h);
+  CK(cudaStreamSynchronize(s));
+  h->hlu_dev = true;
+  h->have_hlu = true;
+  h->hlu_freq = h->mat_freq;
+  return true;
 }
 
 // Truncated copy of the assembled dPhi matrix (HMatrix(const HMatrix&, rank,
@@ -852,7 +1124,9 @@ void check_df_error(bem_handle* h) {
 // boundaryelementsolver.cpp:661-668).
 bool build_hlu(bem_handle* h) {
   h->have_hlu = false;
+  h->hlu_dev = false;
   require(h->hm[1].assembled && !h->points_mode, BEM_EINVAL, "system matrix not assembled");
+  if (hlu_device_eligible(h) && prepare_hlu_program(h)) return build_hlu_device(h);
   require(h->cfg.leaf_size <= HLU_MAX_LEAF + 1, BEM_EINVAL,
           "the preconditioner needs leaf_size <= 513");
   DevHM& m = h->hm[1];
@@ -945,6 +1219,14 @@ bool build_hlu(bem_handle* h) {
   return true;
 }
 
+// factor data (which = 0 L, 1 U): the arena on the device path (the leaf
+// offsets of the program's leaf lists point into it), else the uploads of the
+// host factors
+const void* hlu_data(const bem_handle* h, int which) {
+  if (h->hlu_dev) return h->dArena.p;
+  return which ? h->dUd.p : h->dLd.p;
+}
+
 // w := U^{-1} L^{-1} w for R device vectors (LUPrecondidionedHMatrixWrapper's
 // two substitutions, gmres.h:134-147)
 void apply_precond(bem_handle* h, double2* w, int R, const int* gate_flags = nullptr) {
@@ -959,20 +1241,20 @@ void apply_precond(bem_handle* h, double2* w, int R, const int* gate_flags = nul
       double2* wr = w + (size_t)r0 * N;
       const HmvGate gate = gate_flags ? HmvGate{gate_flags + r0 * GATE_STRIDE, GATE_STRIDE, rc}
                                       : HmvGate{nullptr, 0, 0};
-      h->launches += launch_hlu_df(h->dfL.view, h->dLl.p, h->dLd.p, h->hlu_prec, wr, h->dP2.p, N,
-                                   rc, ws, hp, s, gate);
-      h->launches += launch_hlu_df(h->dfU.view, h->dUl.p, h->dUd.p, h->hlu_prec, h->dP2.p, wr, N,
-                                   rc, ws, hp, s, gate);
+      h->launches += launch_hlu_df(h->dfL.view, h->dLl.p, hlu_data(h, 0), h->hlu_prec, wr, h->dP2.p,
+                                   N, rc, ws, hp, s, gate);
+      h->launches += launch_hlu_df(h->dfU.view, h->dUl.p, hlu_data(h, 1), h->hlu_prec, h->dP2.p, wr,
+                                   N, rc, ws, hp, s, gate);
     }
     return;
   }
   h->dP1.ensure((size_t)R * N);
   h->dP2.ensure((size_t)R * N);
   CK(cudaMemcpyAsync(h->dP1.p, w, (size_t)R * N * sizeof(double2), cudaMemcpyDeviceToDevice, s));
-  h->launches += launch_hlu_sweep(h->dLs.p, (int)h->hL.schedule.size(), h->dLl.p, h->dLd.p, h->hlu_prec,
-                                  h->dP1.p, h->dP2.p, N, R, 0, s);
-  h->launches += launch_hlu_sweep(h->dUs.p, (int)h->hU.schedule.size(), h->dUl.p, h->dUd.p, h->hlu_prec,
-                                  h->dP2.p, w, N, R, 1, s);
+  h->launches += launch_hlu_sweep(h->dLs.p, (int)h->hL.schedule.size(), h->dLl.p, hlu_data(h, 0),
+                                  h->hlu_prec, h->dP1.p, h->dP2.p, N, R, 0, s);
+  h->launches += launch_hlu_sweep(h->dUs.p, (int)h->hU.schedule.size(), h->dUl.p, hlu_data(h, 1),
+                                  h->hlu_prec, h->dP2.p, w, N, R, 1, s);
 }
 
 bool use_precond(const bem_handle* h) { return h->cfg.use_preconditioner && h->have_hlu; }
@@ -1435,6 +1717,7 @@ void bem_config_default(bem_config* c) {
   c->sweep_workers = 0;
   c->aca_big_mn = 0;
   c->precond_reuse = 0.0;
+  c->hlu_device = 1;
 }
 
 bem_status bem_create(const bem_config* cfg, bem_handle** out) {
@@ -1461,6 +1744,8 @@ bem_status bem_create(const bem_config* cfg, bem_handle** out) {
     require(h->cfg.aca_big_mn >= 0, BEM_EINVAL, "aca_big_mn must be >= 0");
     require(h->cfg.precond_reuse >= 0 && std::isfinite(h->cfg.precond_reuse), BEM_EINVAL,
             "precond_reuse must be finite and >= 0");
+    require(h->cfg.hlu_device == 0 || h->cfg.hlu_device == 1, BEM_EINVAL,
+            "hlu_device must be 0 or 1");
     CK(cudaGetDevice(&h->device));
     CK(cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->device));
     // the near-field stream at the highest priority: its short, FP64-bound
@@ -1566,6 +1851,45 @@ bem_status bem_plan_mesh(const bem_config* cfg, const double* tri, int64_t n, in
         o[4] = blocks[i].adm ? 1 : 0;
       }
     *nblocks = (int64_t)blocks.size();
+  });
+}
+
+bem_status bem_hlu_plan(const bem_config* cfg, const double* tri, int64_t n, double* stats,
+                        int64_t nstats) {
+  return guarded(nullptr, [&] {
+    bem_config c;
+    if (cfg) c = *cfg;
+    else bem_config_default(&c);
+    require(tri != nullptr && n >= 1 && stats != nullptr && nstats >= 1, BEM_EINVAL,
+            "bad arguments");
+    require(c.leaf_size >= 2 && c.eta > 0, BEM_EINVAL, "bad configuration");
+    for (int64_t i = 0; i < 9 * n; i++)
+      require(std::isfinite(tri[i]), BEM_ENONFINITE, "non-finite vertex coordinate");
+    std::vector<double> mids(3 * n);
+    for (int64_t i = 0; i < n; i++)
+      for (int d = 0; d < 3; d++)
+        mids[3 * i + d] = ((tri[9 * i + d] + tri[9 * i + 3 + d]) + tri[9 * i + 6 + d]) / 3.0;
+    HTree t = build_tree(mids, c.leaf_size);
+    std::vector<Elem> E;
+    double avgdim = 0;
+    prepare_elements(tri, t.perm, E, avgdim);
+    Layout L;
+    build_layout(t, t, &E, 4.0 * avgdim, c.eta, c.rank_reserve, c.aca_max_rank, false, c.seed, L);
+    HluProgram P;
+    std::string why;
+    require(hlu_gpu_plan(t, L, c.precond_rank, P, &why), BEM_EINVAL,
+            ("H-LU program: " + why).c_str());
+    int64_t ndeps = (int64_t)P.deps.size();
+    const double v[24] = {(double)P.tasks.size(), (double)P.arena, (double)P.scratch,
+                          (double)P.levels, P.cost_path, P.cost_total, (double)P.max_kt,
+                          P.df_ok ? 1.0 : 0.0, (double)P.counts[0], (double)P.counts[1],
+                          (double)P.counts[2], (double)P.counts[3], (double)P.counts[4],
+                          (double)P.counts[5], (double)P.counts[6], (double)ndeps,
+                          (double)P.big_scratch, (double)P.path_counts[0],
+                          (double)P.path_counts[1], (double)P.path_counts[2],
+                          (double)P.path_counts[3], (double)P.path_counts[4],
+                          (double)P.path_counts[5], (double)P.path_counts[6]};
+    for (int64_t i = 0; i < std::min<int64_t>(nstats, 24); i++) stats[i] = v[i];
   });
 }
 
@@ -1946,6 +2270,50 @@ bem_status bem_hlu_export(const bem_handle* hc, int32_t which, int64_t* nleaves,
     require(which == 0 || which == 1, BEM_EINVAL, "which must be 0 (L) or 1 (U)");
     require(h->have_hlu, BEM_EINVAL, "preconditioner not built (bem_hlu_build)");
     const FlatFactor& f = which ? h->hU : h->hL;
+    if (h->hlu_dev) {  // leaves packed in order, data gathered from the arena
+      const int64_t nl = f.nleaves();
+      std::vector<int64_t> lv(f.leaves);
+      int64_t tot = 0;
+      for (int64_t i = 0; i < nl; i++) {
+        const int64_t* L = &f.leaves[7 * i];
+        tot += L[4] == 1 ? (L[1] + L[3]) * L[5] : L[1] * L[3];
+      }
+      if (nleaves) *nleaves = nl;
+      if (ndata) *ndata = tot;
+      if (nsched) *nsched = (int64_t)f.schedule.size();
+      if (sched) std::memcpy(sched, f.schedule.data(), f.schedule.size() * sizeof(int32_t));
+      if (leaves || data) {
+        std::vector<unsigned char> host;
+        const size_t es = h->hlu_prec ? sizeof(float2) : sizeof(double2);
+        if (data) {
+          host.resize((size_t)h->hp.arena * es);
+          CK(cudaMemcpyAsync(host.data(), h->dArena.p, host.size(), cudaMemcpyDeviceToHost,
+                             h->stream));
+          CK(cudaStreamSynchronize(h->stream));
+        }
+        int64_t o = 0;
+        for (int64_t i = 0; i < nl; i++) {
+          int64_t* L = &lv[7 * i];
+          const int64_t cnt = L[4] == 1 ? (L[1] + L[3]) * L[5] : L[1] * L[3];
+          if (data)
+            for (int64_t e = 0; e < cnt; e++) {
+              if (h->hlu_prec) {
+                const float2 v = reinterpret_cast<const float2*>(host.data())[L[6] + e];
+                data[2 * (o + e)] = v.x;
+                data[2 * (o + e) + 1] = v.y;
+              } else {
+                const double2 v = reinterpret_cast<const double2*>(host.data())[L[6] + e];
+                data[2 * (o + e)] = v.x;
+                data[2 * (o + e) + 1] = v.y;
+              }
+            }
+          L[6] = o;
+          o += cnt;
+        }
+        if (leaves) std::memcpy(leaves, lv.data(), lv.size() * sizeof(int64_t));
+      }
+      return;
+    }
     if (nleaves) *nleaves = f.nleaves();
     if (ndata) *ndata = (int64_t)f.data.size();
     if (nsched) *nsched = (int64_t)f.schedule.size();

@@ -9,6 +9,7 @@
 // preconditioner rank (bemparameters.h:27). The same recursion is written here
 // with this library's own node type and dense helpers.
 #include "hlu.h"
+#include "hlu_gpu.h"
 
 #include <algorithm>
 #include <cmath>
@@ -799,8 +800,9 @@ void hlu_factor(const HTree& tree, const std::vector<HBlockDesc>& blocks, std::v
   flatten_upper(Un, U);
 }
 
-bool hlu_df_plan(const FlatFactor& f, int64_t N, int elem_bytes, HluDfPlan& p,
-                 std::string* why) {
+namespace {
+bool df_plan_impl(const FlatFactor& f, int64_t N, int elem_bytes, HluDfPlan& p,
+                  std::string* why, bool with_diag) {
   p = HluDfPlan();
   auto fail = [&](const char* s) {
     if (why) *why = s;
@@ -932,6 +934,11 @@ bool hlu_df_plan(const FlatFactor& f, int64_t N, int elem_bytes, HluDfPlan& p,
     p.cols.insert(p.cols.end(), cl[i].begin(), cl[i].end());
     const int64_t* L = lv + 7 * (int64_t)diag[i];
     const int64_t m = L[1];
+    if (!with_diag) {
+      if (L[4] != 2 && L[4] != 3) return fail("diagonal leaf kind");
+      moff += m * m;
+      continue;
+    }
     const cd* Dd = f.data.data() + L[6];
     if (L[6] < 0 || L[6] + m * m > (int64_t)f.data.size()) return fail("diagonal leaf data");
     p.diag.resize(moff + m * m);
@@ -962,6 +969,17 @@ bool hlu_df_plan(const FlatFactor& f, int64_t N, int elem_bytes, HluDfPlan& p,
   ch[D].moff = moff;
   p.chunks = std::move(ch);
   return true;
+}
+}  // namespace
+
+bool hlu_df_plan(const FlatFactor& f, int64_t N, int elem_bytes, HluDfPlan& p,
+                 std::string* why) {
+  return df_plan_impl(f, N, elem_bytes, p, why, true);
+}
+
+bool hlu_df_plan_structure(const FlatFactor& f, int64_t N, int elem_bytes, HluDfPlan& p,
+                           std::string* why) {
+  return df_plan_impl(f, N, elem_bytes, p, why, false);
 }
 
 }  // namespace bemgpu

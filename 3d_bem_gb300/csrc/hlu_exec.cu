@@ -1,0 +1,841 @@
+// hlu_exec.cu -- executor of the H-LU task program (hlu_gpu.h): one persistent
+// cooperative kernel. Every CTA claims the next task index (the program's
+// topological order), waits until the tasks it depends on have raised their
+// done flags (acquire loads, a bounded wait), runs the task with all its
+// threads and raises its own flag (release store). Claims in a topological
+// order with all CTAs co-resident cannot deadlock: the earliest unfinished
+// task has every dependency finished.
+//
+// Data that other CTAs wrote during the launch is read through L2
+// (ld.global.cg) and written with st.global.cg, so no SM reads a stale L1
+// line of the arena. The arithmetic is the storage type's: complex FP32
+// factors are computed in FP32, complex FP64 factors in FP64.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include "hlu_gpu.h"
+
+namespace bemgpu {
+
+namespace {
+
+constexpr int HX_THREADS = 256;
+constexpr int HX_WARPS = HX_THREADS / 32;
+constexpr int HX_MAX_PAIRS = 64;  // truncation inputs per task (checked on the host)
+
+template <typename T2>
+struct Cx;
+template <>
+struct Cx<float2> {
+  using R = float;
+  static constexpr int SMEM = 6144;  // complex elements of dynamic shared memory
+  __device__ static float2 mk(float a, float b) { return make_float2(a, b); }
+  __device__ static float sq(float x) { return sqrtf(x); }
+  __device__ static float jacobi_thr() { return 1e-6f; }
+  static constexpr int JACOBI_SWEEPS = 30;
+};
+template <>
+struct Cx<double2> {
+  using R = double;
+  static constexpr int SMEM = 6144;
+  __device__ static double2 mk(double a, double b) { return make_double2(a, b); }
+  __device__ static double sq(double x) { return sqrt(x); }
+  __device__ static double jacobi_thr() { return 1e-15; }
+  static constexpr int JACOBI_SWEEPS = 60;
+};
+
+template <typename T2>
+__device__ __forceinline__ T2 cz() {
+  return Cx<T2>::mk(0, 0);
+}
+template <typename T2>
+__device__ __forceinline__ T2 cadd(T2 a, T2 b) {
+  return Cx<T2>::mk(a.x + b.x, a.y + b.y);
+}
+template <typename T2>
+__device__ __forceinline__ T2 csub(T2 a, T2 b) {
+  return Cx<T2>::mk(a.x - b.x, a.y - b.y);
+}
+template <typename T2>
+__device__ __forceinline__ T2 cmul(T2 a, T2 b) {
+  return Cx<T2>::mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// conj(a) b
+template <typename T2>
+__device__ __forceinline__ T2 cmulc(T2 a, T2 b) {
+  return Cx<T2>::mk(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+template <typename T2>
+__device__ __forceinline__ T2 cconj(T2 a) {
+  return Cx<T2>::mk(a.x, -a.y);
+}
+template <typename T2, typename R>
+__device__ __forceinline__ T2 cscale(T2 a, R s) {
+  return Cx<T2>::mk(a.x * s, a.y * s);
+}
+template <typename T2>
+__device__ __forceinline__ T2 cneg(T2 a) {
+  return Cx<T2>::mk(-a.x, -a.y);
+}
+template <typename T2>
+__device__ __forceinline__ typename Cx<T2>::R cabs2(T2 a) {
+  return a.x * a.x + a.y * a.y;
+}
+
+// arena: written by other CTAs during the launch -> L2 only
+template <typename T2>
+__device__ __forceinline__ T2 ldA(const T2* p) {
+  return __ldcg(p);
+}
+template <typename T2>
+__device__ __forceinline__ void stA(T2* p, T2 v) {
+  __stcg(p, v);
+}
+
+template <typename R>
+__device__ __forceinline__ R warp_sum(R v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// CTA-wide sum of one value per thread; red: >= HX_WARPS + 1 values
+template <typename R>
+__device__ R block_sum(R v, R* red) {
+  v = warp_sum(v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    R x = l < HX_WARPS ? red[l] : R(0);
+    x = warp_sum(x);
+    if (l == 0) red[HX_WARPS] = x;
+  }
+  __syncthreads();
+  const R r = red[HX_WARPS];
+  __syncthreads();
+  return r;
+}
+
+// op(A)(i, l) of a column-major matrix with leading dimension ld
+template <typename T2>
+__device__ __forceinline__ T2 opget(const T2* A, int op, int64_t i, int64_t l, int64_t ld) {
+  if (op == HOP_N) return ldA(A + i + l * ld);
+  const T2 v = ldA(A + l + i * ld);
+  return op == HOP_C ? cconj(v) : v;
+}
+
+// ---------------------------------------------------------------- GEMM
+template <typename T2>
+__device__ void task_gemm(const HluTask& t, T2* arena, T2* sm) {
+  using R = typename Cx<T2>::R;
+  const int m = t.m, n = t.n, q = t.q;
+  const int opa = t.flags & 3, opb = (t.flags >> 2) & 3;
+  const bool accu = t.flags & HF_ACC, neg = t.flags & HF_NEG;
+  const T2* A = arena + t.a;
+  const T2* B = arena + t.b;
+  T2* C = arena + t.c;
+  const int tid = threadIdx.x;
+  if ((int64_t)m * n <= 64 && q >= 64) {  // few long dot products: a warp each
+    const int w = tid >> 5, ln = tid & 31;
+    for (int o = w; o < m * n; o += HX_WARPS) {
+      const int i = o % m, j = o / m;
+      R sr = 0, si = 0;
+      for (int l = ln; l < q; l += 32) {
+        const T2 p = cmul(opget(A, opa, i, l, t.lda), opget(B, opb, l, j, t.ldb));
+        sr += p.x;
+        si += p.y;
+      }
+      sr = warp_sum(sr);
+      si = warp_sum(si);
+      if (ln == 0) {
+        T2 v = Cx<T2>::mk(neg ? -sr : sr, neg ? -si : si);
+        T2* c = C + i + (int64_t)j * t.ldc;
+        if (accu) v = cadd(ldA(c), v);
+        stA(c, v);
+      }
+    }
+    return;
+  }
+  // tiles of TM x TN outputs (4 per thread), q in chunks of 16 staged in
+  // shared memory
+  const int TM = n <= 4 ? 256 : (n <= 16 ? 64 : 32);
+  const int TN = 1024 / TM;
+  const int QC = 16;
+  T2* sa = sm;             // TM x QC
+  T2* sb = sm + TM * QC;   // QC x TN
+  const int ti = tid % TM, tj0 = tid / TM, tjs = HX_THREADS / TM;
+  for (int i0 = 0; i0 < m; i0 += TM)
+    for (int j0 = 0; j0 < n; j0 += TN) {
+      T2 acc[4];
+#pragma unroll
+      for (int k = 0; k < 4; k++) acc[k] = cz<T2>();
+      for (int l0 = 0; l0 < q; l0 += QC) {
+        for (int e = tid; e < TM * QC; e += HX_THREADS) {
+          const int ii = e % TM, ll = e / TM;
+          const int gi = i0 + ii, gl = l0 + ll;
+          sa[e] = (gi < m && gl < q) ? opget(A, opa, gi, gl, t.lda) : cz<T2>();
+        }
+        for (int e = tid; e < QC * TN; e += HX_THREADS) {
+          const int ll = e % QC, jj = e / QC;
+          const int gl = l0 + ll, gj = j0 + jj;
+          sb[e] = (gl < q && gj < n) ? opget(B, opb, gl, gj, t.ldb) : cz<T2>();
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int ll = 0; ll < QC; ll++) {
+          const T2 av = sa[ti + ll * TM];
+#pragma unroll
+          for (int k = 0; k < 4; k++) {
+            const T2 bv = sb[ll + (tj0 + k * tjs) * QC];
+            acc[k].x += av.x * bv.x - av.y * bv.y;
+            acc[k].y += av.x * bv.y + av.y * bv.x;
+          }
+        }
+        __syncthreads();
+      }
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const int gi = i0 + ti, gj = j0 + tj0 + k * tjs;
+        if (gi < m && gj < n) {
+          T2 v = neg ? cneg(acc[k]) : acc[k];
+          T2* c = C + gi + (int64_t)gj * t.ldc;
+          if (accu) v = cadd(ldA(c), v);
+          stA(c, v);
+        }
+      }
+    }
+}
+
+// ---------------------------------------------------------------- LMUL / RMUL
+// X (m x n) := op(M) X, M m x m
+template <typename T2>
+__device__ void task_lmul(const HluTask& t, T2* arena, T2* sm) {
+  const int m = t.m, n = t.n, op = t.flags & 3;
+  const T2* M = arena + t.a;
+  T2* X = arena + t.c;
+  T2* sM = sm;           // op(M), m x m column-major
+  T2* sX = sm + m * m;   // m x cw
+  const int cw = max(1, min(n, (Cx<T2>::SMEM - m * m) / m));
+  for (int e = threadIdx.x; e < m * m; e += HX_THREADS) sM[e] = opget(M, op, e % m, e / m, t.lda);
+  for (int j0 = 0; j0 < n; j0 += cw) {
+    const int w = min(cw, n - j0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < m * w; e += HX_THREADS)
+      sX[e] = ldA(X + (e % m) + (int64_t)(j0 + e / m) * t.ldc);
+    __syncthreads();
+    for (int e = threadIdx.x; e < m * w; e += HX_THREADS) {
+      const int i = e % m, j = e / m;
+      T2 acc = cz<T2>();
+      for (int l = 0; l < m; l++) acc = cadd(acc, cmul(sM[i + l * m], sX[l + j * m]));
+      stA(X + i + (int64_t)(j0 + j) * t.ldc, acc);
+    }
+  }
+}
+
+// X (m x n) := X op(M), M n x n
+template <typename T2>
+__device__ void task_rmul(const HluTask& t, T2* arena, T2* sm) {
+  const int m = t.m, n = t.n, op = t.flags & 3;
+  const T2* M = arena + t.a;
+  T2* X = arena + t.c;
+  T2* sM = sm;          // op(M), n x n column-major
+  T2* sX = sm + n * n;  // rw x n
+  const int rw = max(1, min(m, (Cx<T2>::SMEM - n * n) / n));
+  for (int e = threadIdx.x; e < n * n; e += HX_THREADS) sM[e] = opget(M, op, e % n, e / n, t.lda);
+  for (int i0 = 0; i0 < m; i0 += rw) {
+    const int h = min(rw, m - i0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < h * n; e += HX_THREADS)
+      sX[e] = ldA(X + (i0 + e % h) + (int64_t)(e / h) * t.ldc);
+    __syncthreads();
+    for (int e = threadIdx.x; e < h * n; e += HX_THREADS) {
+      const int i = e % h, j = e / h;
+      T2 acc = cz<T2>();
+      for (int l = 0; l < n; l++) acc = cadd(acc, cmul(sX[i + l * h], sM[l + j * n]));
+      stA(X + (i0 + i) + (int64_t)j * t.ldc, acc);
+    }
+  }
+}
+
+// ---------------------------------------------------------------- COPY / ZERO
+template <typename T2>
+__device__ void task_copy(const HluTask& t, T2* arena, const T2* F) {
+  const int src = (t.flags >> HF_SRC_SHIFT) & 7;
+  const bool accu = t.flags & HF_ACC, neg = t.flags & HF_NEG;
+  T2* C = arena + t.c;
+  const int64_t tot = (int64_t)t.m * t.n;
+  for (int64_t e = threadIdx.x; e < tot; e += HX_THREADS) {
+    const int64_t i = e % t.m, j = e / t.m;
+    T2 v = src == 1 ? __ldg(F + t.a + i + j * t.lda) : ldA(arena + t.a + i + j * t.lda);
+    if (neg) v = cneg(v);
+    T2* c = C + i + j * t.ldc;
+    if (accu) v = cadd(ldA(c), v);
+    stA(c, v);
+  }
+}
+
+template <typename T2>
+__device__ void task_zero(const HluTask& t, T2* arena) {
+  T2* C = arena + t.c;
+  const int64_t tot = (int64_t)t.m * t.n;
+  for (int64_t e = threadIdx.x; e < tot; e += HX_THREADS)
+    stA(C + e % t.m + (e / t.m) * t.ldc, cz<T2>());
+}
+
+// ---------------------------------------------------------------- QR of a diagonal leaf
+// Householder reflectors H_j = I - 2 v v^H (|v| = 1) as in the host H-LU:
+// H_{m-1} .. H_0 A = R, Q = H_0 .. H_{m-1}. W accumulates Q^H = H_{m-1} .. H_0
+// alongside. Outputs: Q, R (column-major), Q^H and R^{-1} (row-major).
+template <typename T2>
+__device__ void task_qr(const HluTask& t, const HluExecArgs& a, T2* arena, T2* sm) {
+  using R = typename Cx<T2>::R;
+  const int m = t.m;
+  T2* sA = sm;              // m x m
+  T2* sW = sm + m * m;      // m x m
+  T2* sv = sm + 2 * m * m;  // current reflector, m
+  __shared__ R s_r[4];
+  for (int e = threadIdx.x; e < m * m; e += HX_THREADS) {
+    sA[e] = ldA(arena + t.a + (e % m) + (int64_t)(e / m) * t.lda);
+    sW[e] = (e % m == e / m) ? Cx<T2>::mk(1, 0) : cz<T2>();
+  }
+  __syncthreads();
+  const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  for (int j = 0; j < m; j++) {
+    if (w == 0) {
+      R xn2 = 0;
+      for (int i = j + ln; i < m; i += 32) xn2 += cabs2(sA[i + j * m]);
+      xn2 = warp_sum(xn2);
+      const R xn = Cx<T2>::sq(xn2);
+      const T2 x0 = sA[j + j * m];
+      const R ax0 = Cx<T2>::sq(cabs2(x0));
+      const T2 ph = ax0 > 0 ? cscale(x0, R(1) / ax0) : Cx<T2>::mk(1, 0);
+      const T2 v0 = cadd(x0, cscale(ph, xn));
+      const R vn2 = xn2 - cabs2(x0) + cabs2(v0);
+      const R inv = vn2 > 0 ? R(1) / Cx<T2>::sq(vn2) : R(0);
+      for (int i = j + ln; i < m; i += 32) sv[i] = cscale(i == j ? v0 : sA[i + j * m], inv);
+    }
+    __syncthreads();
+    // apply H_j to columns j.. of A and to all columns of W (rows j..m-1)
+    for (int c = w; c < 2 * m - j; c += HX_WARPS) {
+      T2* y = c < m - j ? sA + (j + c) * m : sW + (c - (m - j)) * m;
+      R dr = 0, di = 0;
+      for (int i = j + ln; i < m; i += 32) {
+        const T2 p = cmulc(sv[i], y[i]);
+        dr += p.x;
+        di += p.y;
+      }
+      dr = warp_sum(dr);
+      di = warp_sum(di);
+      const T2 d2 = Cx<T2>::mk(2 * dr, 2 * di);
+      for (int i = j + ln; i < m; i += 32) y[i] = csub(y[i], cmul(sv[i], d2));
+    }
+    __syncthreads();
+  }
+  const HluQrOut o = a.qr[t.x0];
+  // Q = W^H, Q^H row-major = W column-major read by rows: Qh[r m + c] = W(r, c)
+  for (int e = threadIdx.x; e < m * m; e += HX_THREADS) {
+    const int i = e % m, j = e / m;
+    stA(arena + o.q + e, cconj(sW[j + i * m]));         // Q(i, j) = conj(W(j, i))
+    stA(arena + o.qh + (int64_t)i * m + j, sW[i + j * m]);  // Q^H(i, j) = W(i, j)
+    stA(arena + o.r + e, i <= j ? sA[e] : cz<T2>());
+  }
+  // R^{-1} row-major, one thread per column t: R y = e_t
+  if (threadIdx.x == 0) s_r[0] = 0;
+  __syncthreads();
+  if (threadIdx.x < m) {
+    const int tc = threadIdx.x;
+    T2* y = sW + tc * m;  // W no longer needed: column tc as scratch
+    bool bad = false;
+    for (int r = m - 1; r >= 0; r--) {
+      if (r > tc) {
+        y[r] = cz<T2>();
+        continue;
+      }
+      T2 acc = r == tc ? Cx<T2>::mk(1, 0) : cz<T2>();
+      for (int q2 = r + 1; q2 <= tc; q2++) acc = csub(acc, cmul(sA[r + q2 * m], y[q2]));
+      const T2 d = sA[r + r * m];
+      const R dd = cabs2(d);
+      if (!(dd > 0) || !isfinite(dd)) {
+        bad = true;
+        y[r] = cz<T2>();
+        continue;
+      }
+      y[r] = cscale(cmulc(d, acc), R(1) / dd);  // acc / d
+    }
+    if (bad) s_r[0] = 1;
+    for (int r = 0; r < m; r++) stA(arena + o.rinv + (int64_t)r * m + tc, y[r]);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && s_r[0] != 0) atomicAdd(&a.ctrl[2], 1);
+}
+
+// ---------------------------------------------------------------- truncation
+// Householder QR of X (rows x cols, column-major, ld = rows) in place: R in
+// the upper triangle, reflector j (unit norm) as head[j] at row j and X rows
+// below the diagonal; p = min(rows, cols) reflectors.
+template <typename T2>
+__device__ void house_qr(T2* X, int64_t rows, int cols, T2* head, typename Cx<T2>::R* red) {
+  using R = typename Cx<T2>::R;
+  const int p = (int)(rows < cols ? rows : (int64_t)cols);
+  const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  __shared__ T2 s_v0, s_ph;
+  __shared__ R s_inv, s_xn;
+  for (int j = 0; j < p; j++) {
+    T2* x = X + (int64_t)j * rows;
+    R part = 0;
+    for (int64_t i = j + threadIdx.x; i < rows; i += HX_THREADS) part += cabs2(x[i]);
+    const R xn2 = block_sum(part, red);
+    if (threadIdx.x == 0) {
+      const R xn = Cx<T2>::sq(xn2);
+      const T2 x0 = x[j];
+      const R ax0 = Cx<T2>::sq(cabs2(x0));
+      const T2 ph = ax0 > 0 ? cscale(x0, R(1) / ax0) : Cx<T2>::mk(1, 0);
+      const T2 v0 = cadd(x0, cscale(ph, xn));
+      const R vn2 = xn2 - cabs2(x0) + cabs2(v0);
+      const R inv = vn2 > 0 ? R(1) / Cx<T2>::sq(vn2) : R(0);
+      s_inv = inv;
+      s_v0 = cscale(v0, inv);
+      head[j] = s_v0;
+      s_xn = -xn;  // R(j, j) = -ph xn, set after the updates
+      s_ph = ph;
+    }
+    __syncthreads();
+    const R inv = s_inv;
+    for (int64_t i = j + 1 + threadIdx.x; i < rows; i += HX_THREADS) x[i] = cscale(x[i], inv);
+    __syncthreads();
+    const T2 v0 = s_v0;
+    for (int c = j + 1 + w; c < cols; c += HX_WARPS) {
+      T2* y = X + (int64_t)c * rows;
+      R dr = 0, di = 0;
+      if (ln == 0) {
+        const T2 pp = cmulc(v0, y[j]);
+        dr = pp.x;
+        di = pp.y;
+      }
+      for (int64_t i = j + 1 + ln; i < rows; i += 32) {
+        const T2 pp = cmulc(x[i], y[i]);
+        dr += pp.x;
+        di += pp.y;
+      }
+      dr = warp_sum(dr);
+      di = warp_sum(di);
+      const T2 d2 = Cx<T2>::mk(2 * dr, 2 * di);
+      if (ln == 0) y[j] = csub(y[j], cmul(v0, d2));
+      for (int64_t i = j + 1 + ln; i < rows; i += 32) y[i] = csub(y[i], cmul(x[i], d2));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) x[j] = cscale(s_ph, s_xn);
+    __syncthreads();
+  }
+}
+
+// Y (rows x nc, column-major, ld) := H_0 .. H_{p-1} Y with the reflectors of house_qr
+template <typename T2>
+__device__ void house_apply(const T2* X, int64_t rows, int p, const T2* head, T2* Y, int64_t ld,
+                            int nc, bool to_arena, typename Cx<T2>::R* red) {
+  using R = typename Cx<T2>::R;
+  for (int j = p - 1; j >= 0; j--) {
+    const T2* x = X + (int64_t)j * rows;
+    const T2 v0 = head[j];
+    for (int c = 0; c < nc; c++) {
+      T2* y = Y + (int64_t)c * ld;
+      R dr = 0, di = 0;
+      for (int64_t i = j + threadIdx.x; i < rows; i += HX_THREADS) {
+        const T2 yi = to_arena ? ldA(y + i) : y[i];
+        const T2 pp = cmulc(i == j ? v0 : x[i], yi);
+        dr += pp.x;
+        di += pp.y;
+      }
+      dr = block_sum(dr, red);
+      di = block_sum(di, red);
+      const T2 d2 = Cx<T2>::mk(2 * dr, 2 * di);
+      for (int64_t i = j + threadIdx.x; i < rows; i += HX_THREADS) {
+        const T2 yi = to_arena ? ldA(y + i) : y[i];
+        const T2 v = csub(yi, cmul(i == j ? v0 : x[i], d2));
+        if (to_arena) stA(y + i, v);
+        else y[i] = v;
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// element (r, l) of a truncation piece (kinds 0, 2, 3; identity handled by the caller)
+template <typename T2>
+__device__ __forceinline__ T2 piece_get(const HluExecArgs& a, int kind, int64_t off, int64_t soff,
+                                        int rs, int cs, int64_t r, int l) {
+  if (kind == 0) return ldA(reinterpret_cast<const T2*>(a.arena) + off + r * rs + (int64_t)l * cs);
+  if (kind == 2) {
+    const T2 u = __ldg(reinterpret_cast<const T2*>(a.U) + off + r * rs + (int64_t)l * cs);
+    const T2 s = __ldg(reinterpret_cast<const T2*>(a.S) + soff + l);
+    return cmul(u, s);
+  }
+  return __ldg(reinterpret_cast<const T2*>(a.V) + off + r * rs + (int64_t)l * cs);
+}
+
+template <typename T2>
+__device__ void task_trunc(const HluTask& t, const HluExecArgs& a, T2* arena, T2* slot, T2* sm) {
+  using R = typename Cx<T2>::R;
+  __shared__ int s_cb[HX_MAX_PAIRS + 1];
+  __shared__ R red[HX_WARPS + 8];
+  __shared__ int s_idx[64];
+  __shared__ int s_r;
+  __shared__ unsigned s_off;
+  const int64_t m = t.m, n = t.n;
+  const int kc = a.kc;
+  T2* S = t.a >= 0 ? reinterpret_cast<T2*>(a.big_scratch) + t.a : slot;
+  const HluTruncPair* P = a.pairs + t.x0;
+  const int np = t.x1;
+  if (threadIdx.x == 0) {
+    int c = 0;
+    for (int p = 0; p < np; p++) {
+      s_cb[p] = c;
+      int w = P[p].cols;
+      if (P[p].rank_idx >= 0) w = min(w, max(0, __ldg(a.rank + P[p].rank_idx)));
+      c += w;
+    }
+    s_cb[np] = c;
+  }
+  __syncthreads();
+  const int kt = s_cb[np];
+  T2* SA = S;
+  T2* SB = S + m * kt;
+  T2* C = SB + n * kt;          // pa x pb core, then the Jacobi matrix X (p x q)
+  T2* V = C + (int64_t)kt * kt;  // q x q
+  T2* hA = V + (int64_t)kt * kt;
+  T2* hB = hA + kt;
+  R* sig = reinterpret_cast<R*>(hB + kt);  // kt singular values, then kt marks
+  R* mark = sig + kt;
+  T2* Ao = arena + t.c;
+  T2* Bo = arena + t.b;
+  if (kt == 0 || m == 0 || n == 0) {
+    for (int64_t e = threadIdx.x; e < m * kc; e += HX_THREADS) stA(Ao + e, cz<T2>());
+    for (int64_t e = threadIdx.x; e < n * kc; e += HX_THREADS) stA(Bo + e, cz<T2>());
+    return;
+  }
+  // gather both sides (placements, zeros elsewhere)
+  for (int p = 0; p < np; p++) {
+    const HluTruncPair pp = P[p];
+    const int c0 = s_cb[p], w = s_cb[p + 1] - c0;
+    const bool na = pp.neg & 1, nb = pp.neg & 2;
+    for (int64_t e = threadIdx.x; e < m * w; e += HX_THREADS) {
+      const int64_t r = e % m;
+      const int l = (int)(e / m);
+      T2 v = cz<T2>();
+      const int64_t rr = r - pp.ra;
+      if (rr >= 0 && rr < pp.ma) {
+        if (pp.akind == 1) v = rr == l ? Cx<T2>::mk(1, 0) : cz<T2>();
+        else v = piece_get<T2>(a, pp.akind, pp.aoff, pp.soff, pp.ars, pp.acs, rr, l);
+        if (na) v = cneg(v);
+      }
+      SA[r + (int64_t)(c0 + l) * m] = v;
+    }
+    for (int64_t e = threadIdx.x; e < n * w; e += HX_THREADS) {
+      const int64_t r = e % n;
+      const int l = (int)(e / n);
+      T2 v = cz<T2>();
+      const int64_t rr = r - pp.rb;
+      if (rr >= 0 && rr < pp.mb) {
+        if (pp.bkind == 1) v = rr == l ? Cx<T2>::mk(1, 0) : cz<T2>();
+        else v = piece_get<T2>(a, pp.bkind, pp.boff, 0, pp.brs, pp.bcs, rr, l);
+        if (nb) v = cneg(v);
+      }
+      SB[r + (int64_t)(c0 + l) * n] = v;
+    }
+  }
+  __syncthreads();
+  house_qr(SA, m, kt, hA, red);
+  house_qr(SB, n, kt, hB, red);
+  const int pa = (int)(m < kt ? m : (int64_t)kt), pb = (int)(n < kt ? n : (int64_t)kt);
+  // core = R_A R_B^T (pa x pb); R entries (r, l) with r <= l
+  const bool tr = pa < pb;  // Jacobi on the orientation with fewer columns
+  const int p = tr ? pb : pa, q = tr ? pa : pb;
+  T2* X = C;  // p x q
+  for (int e = threadIdx.x; e < pa * pb; e += HX_THREADS) {
+    const int r = e % pa, c = e / pa;
+    T2 acc = cz<T2>();
+    for (int l = max(r, c); l < kt; l++) acc = cadd(acc, cmul(SA[r + (int64_t)l * m], SB[c + (int64_t)l * n]));
+    if (tr) X[c + r * p] = acc;  // X = core^T
+    else X[r + c * p] = acc;
+  }
+  for (int e = threadIdx.x; e < q * q; e += HX_THREADS) V[e] = (e % q == e / q) ? Cx<T2>::mk(1, 0) : cz<T2>();
+  __syncthreads();
+  // one-sided Jacobi on the q columns of X: X V = U diag(s)
+  const int qq = q + (q & 1);
+  const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  for (int sweep = 0; sweep < Cx<T2>::JACOBI_SWEEPS && q > 1; sweep++) {
+    if (threadIdx.x == 0) s_off = 0u;
+    __syncthreads();
+    for (int rd = 0; rd < qq - 1; rd++) {
+      for (int k = w; k < qq / 2; k += HX_WARPS) {
+        int i1, i2;
+        if (k == 0) {
+          i1 = rd;
+          i2 = qq - 1;
+        } else {
+          i1 = (rd + k) % (qq - 1);
+          i2 = (rd - k + (qq - 1)) % (qq - 1);
+        }
+        if (i1 > i2) {
+          const int tt = i1;
+          i1 = i2;
+          i2 = tt;
+        }
+        if (i2 >= q) continue;
+        T2* xa = X + (int64_t)i1 * p;
+        T2* xb = X + (int64_t)i2 * p;
+        R na = 0, nb = 0, gr = 0, gi = 0;
+        for (int i = ln; i < p; i += 32) {
+          na += cabs2(xa[i]);
+          nb += cabs2(xb[i]);
+          const T2 g = cmulc(xa[i], xb[i]);
+          gr += g.x;
+          gi += g.y;
+        }
+        na = warp_sum(na);
+        nb = warp_sum(nb);
+        gr = warp_sum(gr);
+        gi = warp_sum(gi);
+        if (na == R(0) || nb == R(0)) continue;
+        const R ga = Cx<T2>::sq(gr * gr + gi * gi);
+        const R rel = ga / Cx<T2>::sq(na * nb);
+        if (ga == R(0) || !(rel > Cx<T2>::jacobi_thr())) continue;
+        if (ln == 0) atomicMax(&s_off, __float_as_uint((float)rel));
+        const R er = gr / ga, ei = gi / ga;
+        const R zeta = (nb - na) / (2 * ga);
+        const R tt = (zeta >= 0 ? R(1) : R(-1)) / (fabs(zeta) + Cx<T2>::sq(1 + zeta * zeta));
+        const R cs = R(1) / Cx<T2>::sq(1 + tt * tt), sn = cs * tt;
+        // x' = c x - s (y conj(e)), y' = s x + c (y conj(e))
+        for (int i = ln; i < p; i += 32) {
+          const T2 x = xa[i], y = xb[i];
+          const T2 ye = Cx<T2>::mk(y.x * er + y.y * ei, y.y * er - y.x * ei);
+          xa[i] = Cx<T2>::mk(cs * x.x - sn * ye.x, cs * x.y - sn * ye.y);
+          xb[i] = Cx<T2>::mk(sn * x.x + cs * ye.x, sn * x.y + cs * ye.y);
+        }
+        T2* va = V + (int64_t)i1 * q;
+        T2* vb = V + (int64_t)i2 * q;
+        for (int i = ln; i < q; i += 32) {
+          const T2 x = va[i], y = vb[i];
+          const T2 ye = Cx<T2>::mk(y.x * er + y.y * ei, y.y * er - y.x * ei);
+          va[i] = Cx<T2>::mk(cs * x.x - sn * ye.x, cs * x.y - sn * ye.y);
+          vb[i] = Cx<T2>::mk(sn * x.x + cs * ye.x, sn * x.y + cs * ye.y);
+        }
+      }
+      __syncthreads();
+    }
+    const bool done = __uint_as_float(s_off) == 0.0f;
+    __syncthreads();
+    if (done) break;
+  }
+  // singular values, the rank of the truncation (minRankforError with a cap)
+  for (int j = w; j < q; j += HX_WARPS) {
+    R s2 = 0;
+    for (int i = ln; i < p; i += 32) s2 += cabs2(X[i + (int64_t)j * p]);
+    s2 = warp_sum(s2);
+    if (ln == 0) {
+      sig[j] = Cx<T2>::sq(s2);
+      mark[j] = 0;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    R full = 0;
+    for (int j = 0; j < q; j++) full += sig[j] * sig[j];
+    const int rmax = min(kc, q);
+    int r = 0;
+    R kept = 0;
+    while (r < rmax) {  // largest first
+      int bj = -1;
+      for (int j = 0; j < q; j++)
+        if (mark[j] == R(0) && (bj < 0 || sig[j] > sig[bj])) bj = j;
+      if (bj < 0 || !(sig[bj] > 0)) break;
+      mark[bj] = 1;
+      s_idx[r++] = bj;
+      kept += sig[bj] * sig[bj];
+      if (a.tol > 0 && full > 0 && (full - kept) / full < R(a.tol * a.tol)) break;
+    }
+    s_r = r;
+  }
+  __syncthreads();
+  const int r = s_r;
+  // top rows of the outputs: A' = [W S; 0], B' = [conj(Z); 0] (hlu rk_truncate)
+  for (int64_t e = threadIdx.x; e < m * kc; e += HX_THREADS) {
+    const int64_t i = e % m;
+    const int l = (int)(e / m);
+    T2 v = cz<T2>();
+    if (l < r && i < pa) {
+      const int j = s_idx[l];
+      v = tr ? cscale(cconj(V[i + (int64_t)j * q]), sig[j]) : X[i + (int64_t)j * p];
+    }
+    stA(Ao + e, v);
+  }
+  for (int64_t e = threadIdx.x; e < n * kc; e += HX_THREADS) {
+    const int64_t i = e % n;
+    const int l = (int)(e / n);
+    T2 v = cz<T2>();
+    if (l < r && i < pb) {
+      const int j = s_idx[l];
+      v = tr ? cscale(X[i + (int64_t)j * p], R(1) / sig[j]) : cconj(V[i + (int64_t)j * q]);
+    }
+    stA(Bo + e, v);
+  }
+  __syncthreads();
+  house_apply(SA, m, pa, hA, Ao, m, r, true, red);
+  house_apply(SB, n, pb, hB, Bo, n, r, true, red);
+}
+
+// ---------------------------------------------------------------- the executor
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_relaxed(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// waits until *f != 0; false when the error word is set or the wait ran out
+__device__ bool wait_flag(const int* f, int* ctrl, int64_t limit) {
+  if (ld_acquire(f)) return true;
+  const long long t0 = clock64();
+  unsigned ns = 32;
+  for (;;) {
+    __nanosleep(ns);
+    if (ns < 1024) ns <<= 1;
+    if (ld_acquire(f)) return true;
+    if (ld_relaxed(ctrl + 1)) return false;
+    if (clock64() - t0 > limit) {
+      atomicCAS(ctrl + 1, 0, 1);  // 1: a dependency wait ran out of time
+      return false;
+    }
+  }
+}
+
+template <typename T2>
+__global__ void __launch_bounds__(HX_THREADS) hlu_exec_kernel(HluExecArgs a) {
+  extern __shared__ __align__(16) unsigned char hx_smem[];
+  T2* sm = reinterpret_cast<T2*>(hx_smem);
+  __shared__ int s_task, s_go;
+  T2* arena = reinterpret_cast<T2*>(a.arena);
+  T2* slot = reinterpret_cast<T2*>(a.scratch) + (int64_t)blockIdx.x * a.scratch_per_cta;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      int t = -1, go = 0;
+      if (ld_relaxed(a.ctrl + 1) == 0) t = atomicAdd(a.ctrl, 1);
+      if (t >= 0 && t < a.ntasks) {
+        go = 1;
+        if (a.trace) a.trace[3 * (int64_t)t] = globaltimer();
+        const int d1 = __ldg(a.dep_off + t + 1);
+        for (int i = __ldg(a.dep_off + t); i < d1; i++)
+          if (!wait_flag(a.done + __ldg(a.deps + i), a.ctrl, a.wait_cycles)) {
+            go = 0;
+            break;
+          }
+      }
+      s_task = t;
+      s_go = go;
+      if (go && a.trace) a.trace[3 * (int64_t)t + 1] = globaltimer();
+    }
+    __syncthreads();
+    if (!s_go) break;
+    const int ti = s_task;
+    const HluTask t = a.tasks[ti];
+    switch (t.type) {
+      case HT_GEMM: task_gemm<T2>(t, arena, sm); break;
+      case HT_LMUL: task_lmul<T2>(t, arena, sm); break;
+      case HT_RMUL: task_rmul<T2>(t, arena, sm); break;
+      case HT_QR: task_qr<T2>(t, a, arena, sm); break;
+      case HT_TRUNC: task_trunc<T2>(t, a, arena, slot, sm); break;
+      case HT_COPY: task_copy<T2>(t, arena, reinterpret_cast<const T2*>(a.F)); break;
+      case HT_ZERO: task_zero<T2>(t, arena); break;
+      default: break;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      if (a.trace) a.trace[3 * (int64_t)ti + 2] = globaltimer();
+      __threadfence();
+      st_release(a.done + ti, 1);
+    }
+  }
+}
+
+template <typename T2>
+int smem_bytes() {
+  return Cx<T2>::SMEM * (int)sizeof(T2);
+}
+
+template <typename T2>
+int occupancy() {
+  static int occ = -1;
+  if (occ >= 0) return occ;
+  cudaFuncSetAttribute(hlu_exec_kernel<T2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       smem_bytes<T2>());
+  int o = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, hlu_exec_kernel<T2>, HX_THREADS,
+                                                    smem_bytes<T2>()) != cudaSuccess)
+    o = 0;
+  occ = o;
+  return occ;
+}
+
+}  // namespace
+
+int hlu_exec_occupancy(int precision) {
+  return precision == 0 ? occupancy<double2>() : occupancy<float2>();
+}
+
+int launch_hlu_exec(const HluExecArgs& a, int grid, cudaStream_t s) {
+  HluExecArgs args = a;
+  void* p[] = {&args};
+  cudaError_t e;
+  if (a.precision == 0) {
+    occupancy<double2>();
+    e = cudaLaunchCooperativeKernel((const void*)hlu_exec_kernel<double2>, grid, HX_THREADS, p,
+                                    smem_bytes<double2>(), s);
+  } else {
+    occupancy<float2>();
+    e = cudaLaunchCooperativeKernel((const void*)hlu_exec_kernel<float2>, grid, HX_THREADS, p,
+                                    smem_bytes<float2>(), s);
+  }
+  if (e != cudaSuccess) return -1;
+  return 1;
+}
+
+}  // namespace bemgpu
+
+namespace bemgpu {
+namespace {
+template <typename T2>
+__global__ void finite_check_kernel(const T2* p, int64_t n, int* flag) {
+  int bad = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const T2 v = p[i];
+    if (!isfinite(v.x) || !isfinite(v.y)) bad = 1;
+  }
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+}  // namespace
+
+void launch_hlu_finite_check(const void* arena, int64_t n, int precision, int* flag, int nsm,
+                             cudaStream_t s) {
+  if (n <= 0) return;
+  if (precision == 0)
+    finite_check_kernel<double2><<<nsm * 4, 256, 0, s>>>(reinterpret_cast<const double2*>(arena), n, flag);
+  else
+    finite_check_kernel<float2><<<nsm * 4, 256, 0, s>>>(reinterpret_cast<const float2*>(arena), n, flag);
+}
+
+}  // namespace bemgpu

@@ -79,6 +79,10 @@ typedef struct bem_config {
                               (frequency sweeps; GMRES still converges to the
                               solution of the current matrix); <= 1: factors
                               rebuilt for every solve, as the reference does */
+  int32_t hlu_device;      /* 1: the H-LU factorization runs on the GPU (task
+                              program of hlu_gpu.h; needs precond_rank 1..64
+                              and leaf_size <= 49, else the host factorization
+                              is used); 0: on the host */
 } bem_config;
 
 typedef struct bem_solve_info {
@@ -120,6 +124,18 @@ bem_status bem_get_partition(const bem_handle* h, int64_t* nblocks, int64_t* inf
  * (perm: n entries; info: 5 per block, NULL to query *nblocks). */
 bem_status bem_plan_mesh(const bem_config* cfg, const double* tri, int64_t n, int64_t* perm,
                          int64_t* nblocks, int64_t* info);
+
+/* Host-only planning of the GPU H-LU factorization (no GPU needed): the task
+ * program bem_hlu_build runs on the device for this mesh and configuration
+ * (cfg->precond_rank = the rank of every low-rank factor block). stats
+ * (nstats <= 24 values): tasks, arena (complex elements), truncation scratch
+ * per CTA (complex elements), longest dependency chain (tasks), model cost of
+ * the critical path and of all tasks (microseconds), widest truncation,
+ * dataflow sweeps usable (1 / 0), tasks per type (GEMM, LMUL, RMUL, QR,
+ * TRUNC, COPY, ZERO), dependency entries, scratch of the large truncations
+ * (complex elements), tasks per type on the model's critical path. */
+bem_status bem_hlu_plan(const bem_config* cfg, const double* tri, int64_t n, double* stats,
+                        int64_t nstats);
 
 /* Robin coefficients a, b per element, caller order
  * (calculateBoundaryConditionAndSourceTermVector, :3386-3429). */

@@ -74,6 +74,16 @@ def lib():
                                 F64P, ct.c_int64, ct.c_double, ct.c_int64, ct.c_double,
                                 ct.c_int64, ct.c_int64, ct.c_uint64, ct.c_int, F64P, F64P,
                                 F64P, F64P]
+        L.orc_solve_precond.restype = ct.c_int
+        L.orc_solve_precond.argtypes = [vp, ct.c_double, ct.c_double, ct.c_double, ct.c_int, F64P,
+                                        F64P, F64P, ct.c_int64, ct.c_double, ct.c_int64,
+                                        ct.c_double, ct.c_int64, ct.c_int64, ct.c_uint64, ct.c_int,
+                                        ct.c_int64, ct.c_double, F64P, F64P, F64P, F64P]
+        L.orc_hlu_factor.restype = vp
+        L.orc_hlu_factor.argtypes = [vp, vp, ct.c_int64, ct.c_double]
+        L.orc_hlu_sizes.argtypes = [vp, I64P]
+        L.orc_hlu_get.argtypes = [vp, I64P, F64P, I64P, F64P]
+        L.orc_hlu_free.argtypes = [vp]
         L.orc_dense.argtypes = [vp, ct.c_double, ct.c_int, F64P, F64P, F64P, F64P, ct.c_int]
         L.orc_triangle_rule.restype = ct.c_int64
         L.orc_triangle_rule.argtypes = [ct.c_int64, F64P]
@@ -195,8 +205,10 @@ class Problem:
         return HMatrix(h, self.n, self.n, self.blocks())
 
     def solve(self, freq, c, rho, coupling, a, b, g, aca_tol, gmres_tol, max_rank=0,
-              restart=300, maxit=1000, seed=1234, nthreads=0):
-        """Whole frequency solve; a, b, g in caller order; g is N x R."""
+              restart=300, maxit=1000, seed=1234, nthreads=0, precond_rank=0, precond_tol=0.0):
+        """Whole frequency solve; a, b, g in caller order; g is N x R. With
+        precond_rank >= 1 GMRES runs on the H-LU preconditioned system (the
+        reference's usePreconditioner)."""
         n = self.n
         g = np.asfortranarray(np.asarray(g, np.complex128).reshape(n, -1))
         R = g.shape[1]
@@ -204,13 +216,30 @@ class Problem:
         phi = np.zeros((n, R), np.complex128, order="F")
         dphi = np.zeros((n, R), np.complex128, order="F")
         p = np.zeros((n, R), np.complex128, order="F")
-        st = np.zeros(8)
-        lib().orc_solve(self._h, freq, c, rho, coupling, _f(a), _f(b), _f(g), R, aca_tol,
-                        max_rank, gmres_tol, restart, maxit, seed, nthreads, _f(phi),
-                        _f(dphi), _f(p), _f(st))
+        st = np.zeros(9)
+        lib().orc_solve_precond(self._h, freq, c, rho, coupling, _f(a), _f(b), _f(g), R, aca_tol,
+                                max_rank, gmres_tol, restart, maxit, seed, nthreads, precond_rank,
+                                precond_tol, _f(phi), _f(dphi), _f(p), _f(st))
         keys = ["t_assemble_phi", "t_rhs", "t_assemble_dphi", "t_gmres", "iters",
-                "rel_resid", "t_total", "max_rank"]
+                "rel_resid", "t_total", "max_rank", "t_factor"]
         return phi, dphi, p, dict(zip(keys, st.tolist()))
+
+    def hlu(self, hmat, rank, tol=0.0):
+        """H-LU factors of an assembled H-matrix of this problem: (L leaves,
+        L data, U leaves, U data), leaves as rows r0, m, c0, n, kind, rank,
+        offset (the format of bem_hlu_export)."""
+        f = lib().orc_hlu_factor(self._h, hmat._h, rank, tol)
+        try:
+            sz = np.zeros(4, np.int64)
+            lib().orc_hlu_sizes(f, _i(sz))
+            Ll = np.zeros((sz[0], 7), np.int64)
+            Ld = np.zeros(sz[1], np.complex128)
+            Ul = np.zeros((sz[2], 7), np.int64)
+            Ud = np.zeros(sz[3], np.complex128)
+            lib().orc_hlu_get(f, _i(Ll), _f(Ld), _i(Ul), _f(Ud))
+        finally:
+            lib().orc_hlu_free(f)
+        return Ll, Ld, Ul, Ud
 
 
 class HMatrix:

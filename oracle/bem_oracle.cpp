@@ -483,14 +483,65 @@ void orc_upper_solve(int64_t n, int64_t nblk, const int64_t* blocks, const doubl
   }
 }
 
-// hMatrixSolve (boundaryelementsolver.cpp:526-744) without the preconditioner
-// branch: phi H-matrix by ACA, rhs = phi * g, dPhi H-matrix by ACAextra,
-// GMRES, BC back-substitution (:729-740), p = i rho omega phi (:2251-2261).
+// H-LU factors of an assembled H-matrix (hlu.cpp): flat leaf lists of L and U
+// in the format of orc_lower_solve / orc_upper_solve.
+struct orc_hlu {
+  std::vector<int64_t> Ll, Ul;
+  std::vector<cd> Ld, Ud;
+};
+
+orc_hlu* orc_hlu_factor(const orc_problem* p, const orc_hmatrix* h, int64_t rank, double tol) {
+  auto* f = new orc_hlu();
+  hlu_factor_blocks(p->tree, h->blk, rank, tol, f->Ll, f->Ld, f->Ul, f->Ud);
+  return f;
+}
+
+void orc_hlu_sizes(const orc_hlu* f, int64_t* out) {
+  out[0] = (int64_t)f->Ll.size() / 7;
+  out[1] = (int64_t)f->Ld.size();
+  out[2] = (int64_t)f->Ul.size() / 7;
+  out[3] = (int64_t)f->Ud.size();
+}
+
+void orc_hlu_get(const orc_hlu* f, int64_t* Ll, double* Ld, int64_t* Ul, double* Ud) {
+  if (Ll) std::memcpy(Ll, f->Ll.data(), f->Ll.size() * sizeof(int64_t));
+  if (Ld) std::memcpy(Ld, f->Ld.data(), f->Ld.size() * sizeof(cd));
+  if (Ul) std::memcpy(Ul, f->Ul.data(), f->Ul.size() * sizeof(int64_t));
+  if (Ud) std::memcpy(Ud, f->Ud.data(), f->Ud.size() * sizeof(cd));
+}
+
+void orc_hlu_free(orc_hlu* f) { delete f; }
+
+// hMatrixSolve (boundaryelementsolver.cpp:526-744): phi H-matrix by ACA,
+// rhs = phi * g, dPhi H-matrix by ACAextra, GMRES (with precond_rank >= 1:
+// the H-LU preconditioner of the dPhi matrix truncated to that rank, initial
+// guess (LU)^{-1} rhs and GMRES on (LU)^{-1} A x = (LU)^{-1} rhs,
+// :657-700 and GMRES::gmresLUPreconditionedSolve, gmres.h:191-207), BC
+// back-substitution (:729-740), p = i rho omega phi (:2251-2261).
+int orc_solve_precond(const orc_problem* p, double freq, double c, double rho, int coupling,
+                      const double* a_in, const double* b_in, const double* g_in, int64_t R,
+                      double aca_tol, int64_t max_rank, double gmres_tol, int64_t restart,
+                      int64_t maxit, uint64_t seed, int nthreads, int64_t precond_rank,
+                      double precond_tol, double* phi_out, double* dphi_out, double* p_out,
+                      double* stats);
+
+// The unpreconditioned solve.
 int orc_solve(const orc_problem* p, double freq, double c, double rho, int coupling,
               const double* a_in, const double* b_in, const double* g_in, int64_t R,
               double aca_tol, int64_t max_rank, double gmres_tol, int64_t restart,
               int64_t maxit, uint64_t seed, int nthreads, double* phi_out, double* dphi_out,
               double* p_out, double* stats) {
+  return orc_solve_precond(p, freq, c, rho, coupling, a_in, b_in, g_in, R, aca_tol, max_rank,
+                           gmres_tol, restart, maxit, seed, nthreads, 0, 0.0, phi_out, dphi_out,
+                           p_out, stats);
+}
+
+int orc_solve_precond(const orc_problem* p, double freq, double c, double rho, int coupling,
+                      const double* a_in, const double* b_in, const double* g_in, int64_t R,
+                      double aca_tol, int64_t max_rank, double gmres_tol, int64_t restart,
+                      int64_t maxit, uint64_t seed, int nthreads, int64_t precond_rank,
+                      double precond_tol, double* phi_out, double* dphi_out, double* p_out,
+                      double* stats) {
   using clk = std::chrono::steady_clock;
   auto t0 = clk::now();
   if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -540,11 +591,42 @@ int orc_solve(const orc_problem* p, double freq, double c, double rho, int coupl
   int64_t itmax = 0;
   double resmax = 0;
   std::vector<cd> x(N * R, 0.0);
-  for (int64_t r = 0; r < R; r++) {
-    double res = 0;
-    int64_t it = orc_gmres(hd, (double*)&rhs[r * N], (double*)&x[r * N], gmres_tol, restart, maxit, &res);
-    itmax = std::max(itmax, it);
-    resmax = std::max(resmax, res);
+  double t_factor = 0;
+  if (precond_rank >= 1) {
+    auto tf = clk::now();
+    orc_hlu* f = orc_hlu_factor(p, hd, precond_rank, precond_tol);
+    t_factor = secs(tf, clk::now());
+    const int64_t nl = (int64_t)f->Ll.size() / 7, nu = (int64_t)f->Ul.size() / 7;
+    auto prec = [&](const std::vector<cd>& in, std::vector<cd>& out) {  // out = (LU)^{-1} in
+      std::vector<cd> y(N);
+      orc_lower_solve(N, nl, f->Ll.data(), (const double*)f->Ld.data(), (const double*)in.data(),
+                      (double*)y.data());
+      orc_upper_solve(N, nu, f->Ul.data(), (const double*)f->Ud.data(), (const double*)y.data(),
+                      (double*)out.data());
+    };
+    MatVec A = [&](const std::vector<cd>& in, std::vector<cd>& out) {
+      std::vector<cd> w(N, 0.0);
+      orc_hmatvec(hd, reinterpret_cast<const double*>(in.data()), reinterpret_cast<double*>(w.data()));
+      prec(w, out);
+    };
+    for (int64_t r = 0; r < R; r++) {
+      std::vector<cd> b(rhs.begin() + r * N, rhs.begin() + (r + 1) * N), bp(N), xr(N);
+      prec(b, bp);
+      xr = bp;  // initial guess (LU)^{-1} rhs
+      double res = 0;
+      const int64_t it = gmres_core(N, A, bp, xr, gmres_tol, restart, maxit, &res);
+      std::copy(xr.begin(), xr.end(), x.begin() + r * N);
+      itmax = std::max(itmax, it);
+      resmax = std::max(resmax, res);
+    }
+    orc_hlu_free(f);
+  } else {
+    for (int64_t r = 0; r < R; r++) {
+      double res = 0;
+      int64_t it = orc_gmres(hd, (double*)&rhs[r * N], (double*)&x[r * N], gmres_tol, restart, maxit, &res);
+      itmax = std::max(itmax, it);
+      resmax = std::max(resmax, res);
+    }
   }
   int64_t maxrank = 0;
   for (auto& bl : hd->blk)
@@ -578,6 +660,7 @@ int orc_solve(const orc_problem* p, double freq, double c, double rho, int coupl
     stats[5] = resmax;
     stats[6] = secs(t0, t6);
     stats[7] = (double)maxrank;
+    if (precond_rank >= 1) stats[8] = t_factor;  // the caller passes 9 values
   }
   return 0;
 }

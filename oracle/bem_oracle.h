@@ -135,6 +135,25 @@ void orc_lower_solve(int64_t n, int64_t nblk, const int64_t* blocks,
 void orc_upper_solve(int64_t n, int64_t nblk, const int64_t* blocks,
                      const double* data, const double* y, double* x);
 
+/* H-LU factors of an assembled H-matrix (HMatrix(const HMatrix&, rank, tol)
+ * + HArithm::LUDecomposition, harithm.cpp:1192-1296; hlu.cpp): flat leaf
+ * lists for orc_lower_solve / orc_upper_solve. sizes: L leaves, L data
+ * (complex), U leaves, U data. */
+typedef struct orc_hlu orc_hlu;
+orc_hlu* orc_hlu_factor(const orc_problem* p, const orc_hmatrix* h, int64_t rank, double tol);
+void orc_hlu_sizes(const orc_hlu* f, int64_t* sizes4);
+void orc_hlu_get(const orc_hlu* f, int64_t* Ll, double* Ld, int64_t* Ul, double* Ud);
+void orc_hlu_free(orc_hlu* f);
+
+/* Whole frequency solve with the H-LU preconditioner of rank precond_rank
+ * (>= 1; 0 = none): stats gets 9 values, the 9th the factorization time. */
+int orc_solve_precond(const orc_problem* p, double freq, double c, double rho, int coupling,
+                      const double* a, const double* b, const double* g, int64_t R,
+                      double aca_tol, int64_t max_rank, double gmres_tol, int64_t restart,
+                      int64_t maxit, uint64_t seed, int nthreads, int64_t precond_rank,
+                      double precond_tol, double* phi, double* dphi, double* p_out,
+                      double* stats);
+
 /* Whole frequency solve (reference hMatrixSolve, unpreconditioned GMRES).
  * g: N x R complex (column-major, caller order), outputs in caller order.
  * stats: [t_assemble_phi, t_rhs, t_assemble_dphi, t_gmres, iters_max,

@@ -158,6 +158,12 @@ std::vector<std::pair<int64_t, int64_t>> normal_filtered_pivots(
     const Mesh& mesh, const BlockInfo& b, double filter_angle, uint64_t seed,
     uint64_t block_id);
 void recompress_block(HBlock& blk, int64_t rank, double tol);
+// H-LU factorization (hlu.cpp) of an H-matrix given by its blocks in
+// partition order: flat leaf lists of L and U (r0, m, c0, n, kind, rank,
+// offset; kinds 0 full, 1 low rank, 2 diagonal Q, 3 diagonal R).
+void hlu_factor_blocks(const ClusterTree& t, const std::vector<HBlock>& blk, int64_t rank,
+                       double tol, std::vector<int64_t>& Ll, std::vector<cd>& Ld,
+                       std::vector<int64_t>& Ul, std::vector<cd>& Ud);
 
 // dense complex helpers
 void householder_qr(int64_t m, int64_t k, std::vector<cd>& A, std::vector<cd>& Q,

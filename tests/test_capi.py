@@ -61,3 +61,24 @@ def test_plan_rejects_bad_input(bem):
     L = bem.lib()
     nb = ct.c_int64()
     assert L.bem_plan_mesh(None, None, 0, None, ct.byref(nb), None) == bem.BEM_EINVAL
+
+
+def test_hlu_plan_program(bem, meshes):
+    """The GPU H-LU task program is built on the host alone: every task type
+    appears, dependencies are fewer than a handful per task, the sweeps'
+    dataflow form applies to its factors, and the program refuses what the
+    executor cannot hold (rank above 64, diagonal leaves above 48 rows)."""
+    tri = meshes.icosphere(3)
+    st = bem.hlu_plan(tri, bem.default_config(precond_rank=2))
+    assert st["tasks"] > 1000 and st["dataflow_sweeps"] == 1.0
+    for k in ("gemm", "lmul", "qr", "trunc", "copy", "zero"):
+        assert st[k] > 0, k
+    assert st["qr"] == 55  # one per leaf cluster (diagonal leaf)
+    assert st["levels"] < st["tasks"] and st["dep_entries"] < 4 * st["tasks"]
+    assert st["cost_path_us"] < st["cost_total_us"]
+    big = bem.hlu_plan(tri, bem.default_config(precond_rank=64))
+    assert big["tasks"] == st["tasks"] and big["arena_elems"] > st["arena_elems"]
+    with pytest.raises(bem.BemError):
+        bem.hlu_plan(tri, bem.default_config(precond_rank=65))
+    with pytest.raises(bem.BemError):
+        bem.hlu_plan(tri, bem.default_config(precond_rank=2, leaf_size=64))

@@ -218,3 +218,81 @@ def test_factor_reuse_over_a_sweep(bem, meshes):
     assert all(i["status"] == 0 and i["true_residual"] < 1e-9 for i in i0 + i1)
     assert rel(p1, p0) < 1e-7
 
+
+
+# ---- H-LU factorization on the GPU (task program, hlu_gpu.h) ----
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_device_factors_match_host_and_oracle(bem, meshes, orc, precision):
+    """Rank-2 factors from the GPU task program against the host
+    factorization of the same matrix and the oracle's restatement
+    (HArithm::LUDecomposition, harithm.cpp:1192-1296) of the oracle's own
+    assembly: the three approximate A equally well and differ by less than
+    the truncation error."""
+    tri = meshes.icosphere(3, 1.0)
+    n = tri.shape[0]
+    prods, errs = {}, {}
+    for dev in (1, 0):
+        _, s = setup(bem, meshes, 3, precision=precision, precond_rank=2, hlu_device=dev)
+        s.assemble(FREQ)
+        s.hlu_build()
+        Ll, Ld, Ls = s.hlu_export(0)
+        Ul, Ud, Us = s.hlu_export(1)
+        if precision == 0:  # Q unitary to FP64 rounding
+            check_structure(n, Ll, Ld, Ls, True)
+            check_structure(n, Ul, Ud, Us, False)
+        A = s.dense(1)
+        prods[dev] = dense_factor(n, Ll, Ld) @ dense_factor(n, Ul, Ud)
+        errs[dev] = rel(prods[dev], A)
+        s.close()
+    P = orc.Problem(tri, 32, 2.0)
+    k = 2 * np.pi * FREQ / 343.0
+    H = P.hassemble(k, 2, np.zeros(n), np.ones(n), 1, 1e-6)
+    Ll, Ld, Ul, Ud = P.hlu(H, 2)
+    Ao = H.dense()
+    LUo = dense_factor(n, Ll, Ld) @ dense_factor(n, Ul, Ud)
+    err_o = rel(LUo, Ao)
+    for e in (errs[0], errs[1], err_o):
+        assert 1e-4 < e < 5e-3, (errs, err_o)
+    assert errs[1] < 1.1 * errs[0] and errs[1] < 1.1 * err_o
+    assert rel(prods[1], prods[0]) < 1e-3
+    # the oracle's cluster order is the library's (same tree), so the
+    # factor products compare entry by entry
+    assert rel(prods[1], LUo) < 1e-3
+
+
+@pytest.mark.parametrize("sub", [2, 3])
+def test_device_factors_exact_at_full_rank(bem, meshes, orc, sub):
+    """At rank 64 with a 1e-14 truncation the GPU factors reproduce the
+    matrix (L U = A to 1e-9), as the oracle's do."""
+    tri, s = setup(bem, meshes, sub, precond_rank=64, precond_tol=1e-14)
+    n = tri.shape[0]
+    s.assemble(FREQ)
+    s.hlu_build()
+    Ll, Ld, Ls = s.hlu_export(0)
+    Ul, Ud, Us = s.hlu_export(1)
+    check_structure(n, Ll, Ld, Ls, True)
+    check_structure(n, Ul, Ud, Us, False)
+    A = s.dense(1)
+    assert rel(dense_factor(n, Ll, Ld) @ dense_factor(n, Ul, Ud), A) < 1e-9
+    rng = np.random.default_rng(sub)
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    assert rel(s.hlu_solve(s.hmatvec(1, x)), x) < 1e-7
+
+
+def test_device_factorization_wait_limit(bem, meshes, monkeypatch):
+    """A dependency wait of the factorization kernel that runs out (a limit
+    of a few nanoseconds, which the dependencies cannot meet) ends the launch
+    with BEM_ETIMEOUT; no task is left running and the handle stays usable."""
+    tri, s = setup(bem, meshes, 3, precond_rank=2)
+    s.assemble(FREQ)
+    monkeypatch.setenv("BEM_HLU_WAIT_US", "0.001")
+    with pytest.raises(bem.BemError) as ei:
+        s.hlu_build()
+    assert ei.value.status == bem.BEM_ETIMEOUT
+    monkeypatch.delenv("BEM_HLU_WAIT_US")
+    s.hlu_build()
+    n = tri.shape[0]
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    assert rel(s.hlu_solve(s.hmatvec(1, x)), x) < 1e-2
