@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <complex>
@@ -56,6 +57,18 @@ void require(bool ok, bem_status st, const char* msg) {
   if (!ok) throw BemError{st, msg};
 }
 
+// Device bytes held by the library's buffers. BEM_DEVICE_MEM_CAP (bytes, read
+// once) turns any allocation beyond it into the BEM_ENOMEM a failing
+// cudaMalloc gives, without taking the GPU's memory (tests of that path).
+std::atomic<int64_t> g_device_bytes{0};
+int64_t device_mem_cap() {
+  static const int64_t cap = [] {
+    const char* e = std::getenv("BEM_DEVICE_MEM_CAP");
+    return e ? (int64_t)std::atoll(e) : (int64_t)0;
+  }();
+  return cap;
+}
+
 template <typename T>
 struct DBuf {
   T* p = nullptr;
@@ -65,7 +78,10 @@ struct DBuf {
   DBuf& operator=(const DBuf&) = delete;
   ~DBuf() { release(); }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      cudaFree(p);
+      g_device_bytes -= (int64_t)(n * sizeof(T));
+    }
     p = nullptr;
     n = 0;
   }
@@ -73,8 +89,12 @@ struct DBuf {
     if (cnt <= n && p) return;
     release();
     size_t c = std::max<size_t>(cnt, 1);
+    const int64_t cap = device_mem_cap();
+    if (cap > 0 && g_device_bytes + (int64_t)(c * sizeof(T)) > cap)
+      throw BemError{BEM_ENOMEM, "device allocation beyond BEM_DEVICE_MEM_CAP"};
     CK(cudaMalloc((void**)&p, c * sizeof(T)));
     n = c;
+    g_device_bytes += (int64_t)(c * sizeof(T));
   }
   void upload(const std::vector<T>& v, cudaStream_t s) {
     ensure(v.size());
@@ -1021,12 +1041,19 @@ void hlu_trace_summary(const HluProgram& P, const DBuf<unsigned long long>& tr, 
     fin[i] = best + d;
     if (fin[i] > fin[last]) last = (int64_t)i;
   }
-  int64_t path_cnt[8] = {};
-  double path_t[8] = {};
+  int64_t path_cnt[8] = {}, path_loads = 0;
+  double path_t[8] = {}, path_load_t = 0;
+  std::vector<int64_t> chain;
   for (int64_t i = last; i >= 0; i = pred[i]) {
     const int ty = P.tasks[i].type & 7;
+    const double d = 1e-3 * (double)(t[3 * i + 2] - t[3 * i + 1]);
     path_cnt[ty]++;
-    path_t[ty] += 1e-3 * (double)(t[3 * i + 2] - t[3 * i + 1]);
+    path_t[ty] += d;
+    chain.push_back(i);
+    if (ty == HT_TRUNC && P.tasks[i].x1 == 1 && P.pairs[P.tasks[i].x0].rank_idx >= 0) {
+      path_loads++;
+      path_load_t += d;
+    }
   }
   FILE* f = std::fopen(path, "w");
   if (!f) return;
@@ -1037,6 +1064,15 @@ void hlu_trace_summary(const HluProgram& P, const DBuf<unsigned long long>& tr, 
     std::fprintf(f, "%-6s n %9lld busy_us %12.1f avg_us %8.2f max_us %9.1f wait_us %12.1f "
                  "path_n %6lld path_us %10.1f\n", nm[k], (long long)cnt[k], busy[k],
                  cnt[k] ? busy[k] / cnt[k] : 0.0, mx[k], wait[k], (long long)path_cnt[k], path_t[k]);
+  std::fprintf(f, "path loads n %lld us %.1f\n", (long long)path_loads, path_load_t);
+  std::sort(chain.begin(), chain.end(), [&](int64_t a, int64_t b) {
+    return t[3 * a + 2] - t[3 * a + 1] > t[3 * b + 2] - t[3 * b + 1];
+  });
+  for (size_t r = 0; r < std::min<size_t>(15, chain.size()); r++) {
+    const HluTask& k = P.tasks[chain[r]];
+    std::fprintf(f, "path %s m %d n %d q %d pairs %d us %.1f\n", nm[k.type & 7], k.m, k.n, k.q,
+                 k.x1, 1e-3 * (double)(t[3 * chain[r] + 2] - t[3 * chain[r] + 1]));
+  }
   // the slowest tasks
   std::vector<size_t> ord(nt);
   std::iota(ord.begin(), ord.end(), 0);

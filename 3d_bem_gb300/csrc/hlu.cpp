@@ -102,6 +102,12 @@ void jacobi_svd(int64_t p, int64_t q, const cd* C, std::vector<double>& s, std::
     return t;
   };
   for (int64_t j = 0; j < q; j++) nrm[j] = colnorm(j);
+  // columns below 1e-30 of the squared Frobenius norm (rotations keep it) are
+  // rounding noise: their relative test never settles, so they take no
+  // rotations
+  double fro = 0;
+  for (int64_t j = 0; j < q; j++) fro += nrm[j];
+  const double floor2 = 1e-30 * fro;
   // rotate columns x, y (length len) of a split array by (c, s, e)
   auto rot = [](double* xr, double* xi, double* yr, double* yi, int64_t len, double c, double sn,
                 double er, double ei) {
@@ -120,7 +126,7 @@ void jacobi_svd(int64_t p, int64_t q, const cd* C, std::vector<double>& s, std::
     for (int64_t a = 0; a < q - 1; a++)
       for (int64_t b = a + 1; b < q; b++) {
         const double na = nrm[a], nb = nrm[b];
-        if (na == 0.0 || nb == 0.0) continue;
+        if (!(na > floor2) || !(nb > floor2)) continue;
         const double *xr = &ar[a * p], *xi = &ai[a * p], *yr = &ar[b * p], *yi = &ai[b * p];
         double gr = 0, gi = 0;  // g = <x, y> = sum conj(x) y
         for (int64_t i = 0; i < p; i++) {

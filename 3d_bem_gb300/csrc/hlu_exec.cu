@@ -32,6 +32,9 @@ struct Cx<float2> {
   __device__ static float2 mk(float a, float b) { return make_float2(a, b); }
   __device__ static float sq(float x) { return sqrtf(x); }
   __device__ static float jacobi_thr() { return 1e-6f; }
+  // columns below this fraction of the squared Frobenius norm are rounding
+  // noise: they take no rotations (their relative test never settles)
+  __device__ static float jacobi_floor() { return 1e-14f; }
   static constexpr int JACOBI_SWEEPS = 30;
 };
 template <>
@@ -41,6 +44,7 @@ struct Cx<double2> {
   __device__ static double2 mk(double a, double b) { return make_double2(a, b); }
   __device__ static double sq(double x) { return sqrt(x); }
   __device__ static double jacobi_thr() { return 1e-15; }
+  __device__ static double jacobi_floor() { return 1e-30; }
   static constexpr int JACOBI_SWEEPS = 60;
 };
 
@@ -373,88 +377,142 @@ __device__ void task_qr(const HluTask& t, const HluExecArgs& a, T2* arena, T2* s
 // ---------------------------------------------------------------- truncation
 // Householder QR of X (rows x cols, column-major, ld = rows) in place: R in
 // the upper triangle, reflector j (unit norm) as head[j] at row j and X rows
-// below the diagonal; p = min(rows, cols) reflectors.
+// below the diagonal; p = min(rows, cols) reflectors. Every pass runs over the
+// rows with all threads and carries up to HQ_G columns in registers, so a
+// tall panel is streamed a few times per column instead of once per column
+// pair by a single warp.
+constexpr int HQ_G = 8;
+
+// CTA-wide sums of nv values per thread (nv <= 2 HQ_G); thread t < nv gets
+// sum t in out[t] (shared), the rest unchanged; ends with a barrier
+template <typename R>
+__device__ void block_sums(R* v, int nv, R (*part)[2 * HQ_G], R* out) {
+  const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  for (int q = 0; q < nv; q++) {
+    const R x = warp_sum(v[q]);
+    if (ln == 0) part[w][q] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < nv) {
+    R x = 0;
+    for (int q = 0; q < HX_WARPS; q++) x += part[q][threadIdx.x];
+    out[threadIdx.x] = x;
+  }
+  __syncthreads();
+}
+
 template <typename T2>
-__device__ void house_qr(T2* X, int64_t rows, int cols, T2* head, typename Cx<T2>::R* red) {
+__device__ void house_qr(T2* X, int64_t rows, int cols, T2* head) {
   using R = typename Cx<T2>::R;
   const int p = (int)(rows < cols ? rows : (int64_t)cols);
-  const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
-  __shared__ T2 s_v0, s_ph;
+  __shared__ R part[HX_WARPS][2 * HQ_G];
+  __shared__ R sums[2 * HQ_G];
+  __shared__ T2 s_v0, s_ph, s_c[HQ_G];
   __shared__ R s_inv, s_xn;
   for (int j = 0; j < p; j++) {
     T2* x = X + (int64_t)j * rows;
-    R part = 0;
-    for (int64_t i = j + threadIdx.x; i < rows; i += HX_THREADS) part += cabs2(x[i]);
-    const R xn2 = block_sum(part, red);
+    R nrm = 0;
+    for (int64_t i = j + threadIdx.x; i < rows; i += HX_THREADS) nrm += cabs2(x[i]);
+    block_sums(&nrm, 1, part, sums);
     if (threadIdx.x == 0) {
+      const R xn2 = sums[0];
       const R xn = Cx<T2>::sq(xn2);
       const T2 x0 = x[j];
       const R ax0 = Cx<T2>::sq(cabs2(x0));
       const T2 ph = ax0 > 0 ? cscale(x0, R(1) / ax0) : Cx<T2>::mk(1, 0);
       const T2 v0 = cadd(x0, cscale(ph, xn));
       const R vn2 = xn2 - cabs2(x0) + cabs2(v0);
-      const R inv = vn2 > 0 ? R(1) / Cx<T2>::sq(vn2) : R(0);
-      s_inv = inv;
-      s_v0 = cscale(v0, inv);
-      head[j] = s_v0;
-      s_xn = -xn;  // R(j, j) = -ph xn, set after the updates
+      s_inv = vn2 > 0 ? R(1) / Cx<T2>::sq(vn2) : R(0);
+      s_v0 = v0;
       s_ph = ph;
+      s_xn = -xn;
     }
     __syncthreads();
     const R inv = s_inv;
-    for (int64_t i = j + 1 + threadIdx.x; i < rows; i += HX_THREADS) x[i] = cscale(x[i], inv);
-    __syncthreads();
-    const T2 v0 = s_v0;
-    for (int c = j + 1 + w; c < cols; c += HX_WARPS) {
-      T2* y = X + (int64_t)c * rows;
-      R dr = 0, di = 0;
-      if (ln == 0) {
-        const T2 pp = cmulc(v0, y[j]);
-        dr = pp.x;
-        di = pp.y;
+    const T2 v0 = cscale(s_v0, inv);  // the unit reflector is v = inv (v0, x_{j+1}, ...)
+    // columns j + 1 .. in groups: c_g = 2 v^H y, y -= c_g v
+    for (int c0 = j + 1; c0 < cols; c0 += HQ_G) {
+      const int nc = min(HQ_G, cols - c0);
+      R acc[2 * HQ_G];
+#pragma unroll
+      for (int g = 0; g < 2 * HQ_G; g++) acc[g] = 0;
+      for (int64_t i = j + 1 + threadIdx.x; i < rows; i += HX_THREADS) {
+        const T2 xi = cscale(x[i], inv);
+#pragma unroll
+        for (int g = 0; g < HQ_G; g++)
+          if (g < nc) {
+            const T2 pr = cmulc(xi, X[i + (int64_t)(c0 + g) * rows]);
+            acc[2 * g] += pr.x;
+            acc[2 * g + 1] += pr.y;
+          }
       }
-      for (int64_t i = j + 1 + ln; i < rows; i += 32) {
-        const T2 pp = cmulc(x[i], y[i]);
-        dr += pp.x;
-        di += pp.y;
+      block_sums(acc, 2 * nc, part, sums);
+      if (threadIdx.x < nc) {
+        const T2 yj = X[j + (int64_t)(c0 + threadIdx.x) * rows];
+        const T2 d = cadd(cmulc(v0, yj), Cx<T2>::mk(sums[2 * threadIdx.x], sums[2 * threadIdx.x + 1]));
+        s_c[threadIdx.x] = cscale(d, R(2));
       }
-      dr = warp_sum(dr);
-      di = warp_sum(di);
-      const T2 d2 = Cx<T2>::mk(2 * dr, 2 * di);
-      if (ln == 0) y[j] = csub(y[j], cmul(v0, d2));
-      for (int64_t i = j + 1 + ln; i < rows; i += 32) y[i] = csub(y[i], cmul(x[i], d2));
+      __syncthreads();
+      for (int64_t i = j + threadIdx.x; i < rows; i += HX_THREADS) {
+        const T2 vi = i == j ? v0 : cscale(x[i], inv);
+#pragma unroll
+        for (int g = 0; g < HQ_G; g++)
+          if (g < nc) {
+            T2* y = X + i + (int64_t)(c0 + g) * rows;
+            *y = csub(*y, cmul(s_c[g], vi));
+          }
+      }
+      __syncthreads();
     }
-    __syncthreads();
-    if (threadIdx.x == 0) x[j] = cscale(s_ph, s_xn);
+    // normalise the reflector below the diagonal, R(j, j) on the diagonal
+    for (int64_t i = j + 1 + threadIdx.x; i < rows; i += HX_THREADS) x[i] = cscale(x[i], inv);
+    if (threadIdx.x == 0) {
+      head[j] = v0;
+      x[j] = cscale(s_ph, s_xn);
+    }
     __syncthreads();
   }
 }
 
-// Y (rows x nc, column-major, ld) := H_0 .. H_{p-1} Y with the reflectors of house_qr
+// Y (rows x nc, column-major, ld, in the arena) := H_0 .. H_{p-1} Y with the
+// reflectors of house_qr
 template <typename T2>
 __device__ void house_apply(const T2* X, int64_t rows, int p, const T2* head, T2* Y, int64_t ld,
-                            int nc, bool to_arena, typename Cx<T2>::R* red) {
+                            int nc) {
   using R = typename Cx<T2>::R;
+  __shared__ R part[HX_WARPS][2 * HQ_G];
+  __shared__ R sums[2 * HQ_G];
+  __shared__ T2 s_c[HQ_G];
   for (int j = p - 1; j >= 0; j--) {
     const T2* x = X + (int64_t)j * rows;
     const T2 v0 = head[j];
-    for (int c = 0; c < nc; c++) {
-      T2* y = Y + (int64_t)c * ld;
-      R dr = 0, di = 0;
+    for (int c0 = 0; c0 < nc; c0 += HQ_G) {
+      const int ng = min(HQ_G, nc - c0);
+      R acc[2 * HQ_G];
+#pragma unroll
+      for (int g = 0; g < 2 * HQ_G; g++) acc[g] = 0;
       for (int64_t i = j + threadIdx.x; i < rows; i += HX_THREADS) {
-        const T2 yi = to_arena ? ldA(y + i) : y[i];
-        const T2 pp = cmulc(i == j ? v0 : x[i], yi);
-        dr += pp.x;
-        di += pp.y;
+        const T2 vi = i == j ? v0 : x[i];
+#pragma unroll
+        for (int g = 0; g < HQ_G; g++)
+          if (g < ng) {
+            const T2 pr = cmulc(vi, ldA(Y + i + (int64_t)(c0 + g) * ld));
+            acc[2 * g] += pr.x;
+            acc[2 * g + 1] += pr.y;
+          }
       }
-      dr = block_sum(dr, red);
-      di = block_sum(di, red);
-      const T2 d2 = Cx<T2>::mk(2 * dr, 2 * di);
+      block_sums(acc, 2 * ng, part, sums);
+      if (threadIdx.x < ng)
+        s_c[threadIdx.x] = Cx<T2>::mk(2 * sums[2 * threadIdx.x], 2 * sums[2 * threadIdx.x + 1]);
+      __syncthreads();
       for (int64_t i = j + threadIdx.x; i < rows; i += HX_THREADS) {
-        const T2 yi = to_arena ? ldA(y + i) : y[i];
-        const T2 v = csub(yi, cmul(i == j ? v0 : x[i], d2));
-        if (to_arena) stA(y + i, v);
-        else y[i] = v;
+        const T2 vi = i == j ? v0 : x[i];
+#pragma unroll
+        for (int g = 0; g < HQ_G; g++)
+          if (g < ng) {
+            T2* y = Y + i + (int64_t)(c0 + g) * ld;
+            stA(y, csub(ldA(y), cmul(vi, s_c[g])));
+          }
       }
       __syncthreads();
     }
@@ -484,7 +542,6 @@ __device__ void task_trunc(const HluTask& t, const HluExecArgs& a, T2* arena, T2
   __shared__ unsigned s_off;
   const int64_t m = t.m, n = t.n;
   const int kc = a.kc;
-  T2* S = t.a >= 0 ? reinterpret_cast<T2*>(a.big_scratch) + t.a : slot;
   const HluTruncPair* P = a.pairs + t.x0;
   const int np = t.x1;
   if (threadIdx.x == 0) {
@@ -499,14 +556,22 @@ __device__ void task_trunc(const HluTask& t, const HluExecArgs& a, T2* arena, T2
   }
   __syncthreads();
   const int kt = s_cb[np];
+  // Small targets (both sides <= 32, the common leaf-level update) work in
+  // shared memory on the dense m x n sum itself: its SVD is the core's, no
+  // QR of the two sides is needed. Others gather into scratch and reduce the
+  // sides by Householder QR first.
+  const int K2 = kt > 32 ? kt : 32;
+  const bool small = m <= 32 && n <= 32 &&
+                     (m + n) * kt + m * n + 32 * 32 + 4 * K2 <= Cx<T2>::SMEM;
+  T2* S = small ? sm : (t.a >= 0 ? reinterpret_cast<T2*>(a.big_scratch) + t.a : slot);
   T2* SA = S;
   T2* SB = S + m * kt;
-  T2* C = SB + n * kt;          // pa x pb core, then the Jacobi matrix X (p x q)
-  T2* V = C + (int64_t)kt * kt;  // q x q
-  T2* hA = V + (int64_t)kt * kt;
-  T2* hB = hA + kt;
-  R* sig = reinterpret_cast<R*>(hB + kt);  // kt singular values, then kt marks
-  R* mark = sig + kt;
+  T2* C = SB + n * kt;  // the Jacobi matrix X (p x q): the core, or the dense sum
+  T2* V = C + (small ? m * n : (int64_t)kt * kt);  // q x q
+  T2* hA = V + (small ? 32 * 32 : (int64_t)kt * kt);
+  T2* hB = hA + K2;
+  R* sig = reinterpret_cast<R*>(hB + K2);  // K2 singular values, then K2 marks
+  R* mark = sig + K2;
   T2* Ao = arena + t.c;
   T2* Bo = arena + t.b;
   if (kt == 0 || m == 0 || n == 0) {
@@ -545,23 +610,33 @@ __device__ void task_trunc(const HluTask& t, const HluExecArgs& a, T2* arena, T2
     }
   }
   __syncthreads();
-  house_qr(SA, m, kt, hA, red);
-  house_qr(SB, n, kt, hB, red);
-  const int pa = (int)(m < kt ? m : (int64_t)kt), pb = (int)(n < kt ? n : (int64_t)kt);
-  // core = R_A R_B^T (pa x pb); R entries (r, l) with r <= l
+  if (!small) {
+    house_qr(SA, m, kt, hA);
+    house_qr(SB, n, kt, hB);
+  }
+  // core = R_A R_B^T (pa x pb; R entries (r, l) with r <= l), or for small
+  // targets the whole sum A B^T (m x n)
+  const int pa = small ? (int)m : (int)(m < kt ? m : (int64_t)kt);
+  const int pb = small ? (int)n : (int)(n < kt ? n : (int64_t)kt);
   const bool tr = pa < pb;  // Jacobi on the orientation with fewer columns
   const int p = tr ? pb : pa, q = tr ? pa : pb;
   T2* X = C;  // p x q
   for (int e = threadIdx.x; e < pa * pb; e += HX_THREADS) {
     const int r = e % pa, c = e / pa;
     T2 acc = cz<T2>();
-    for (int l = max(r, c); l < kt; l++) acc = cadd(acc, cmul(SA[r + (int64_t)l * m], SB[c + (int64_t)l * n]));
+    for (int l = small ? 0 : max(r, c); l < kt; l++)
+      acc = cadd(acc, cmul(SA[r + (int64_t)l * m], SB[c + (int64_t)l * n]));
     if (tr) X[c + r * p] = acc;  // X = core^T
     else X[r + c * p] = acc;
   }
   for (int e = threadIdx.x; e < q * q; e += HX_THREADS) V[e] = (e % q == e / q) ? Cx<T2>::mk(1, 0) : cz<T2>();
   __syncthreads();
-  // one-sided Jacobi on the q columns of X: X V = U diag(s)
+  // one-sided Jacobi on the q columns of X: X V = U diag(s). Rotations keep
+  // the Frobenius norm, so one floor for the whole run decides which columns
+  // are noise.
+  R fro = 0;
+  for (int e = threadIdx.x; e < p * q; e += HX_THREADS) fro += cabs2(X[e]);
+  const R floor2 = block_sum(fro, red) * Cx<T2>::jacobi_floor();
   const int qq = q + (q & 1);
   const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
   for (int sweep = 0; sweep < Cx<T2>::JACOBI_SWEEPS && q > 1; sweep++) {
@@ -597,9 +672,9 @@ __device__ void task_trunc(const HluTask& t, const HluExecArgs& a, T2* arena, T2
         nb = warp_sum(nb);
         gr = warp_sum(gr);
         gi = warp_sum(gi);
-        if (na == R(0) || nb == R(0)) continue;
+        if (!(na > floor2) || !(nb > floor2)) continue;
         const R ga = Cx<T2>::sq(gr * gr + gi * gi);
-        const R rel = ga / Cx<T2>::sq(na * nb);
+        const R rel = ga / (Cx<T2>::sq(na) * Cx<T2>::sq(nb));
         if (ga == R(0) || !(rel > Cx<T2>::jacobi_thr())) continue;
         if (ln == 0) atomicMax(&s_off, __float_as_uint((float)rel));
         const R er = gr / ga, ei = gi / ga;
@@ -681,8 +756,10 @@ __device__ void task_trunc(const HluTask& t, const HluExecArgs& a, T2* arena, T2
     stA(Bo + e, v);
   }
   __syncthreads();
-  house_apply(SA, m, pa, hA, Ao, m, r, true, red);
-  house_apply(SB, n, pb, hB, Bo, n, r, true, red);
+  if (!small) {
+    house_apply(SA, m, pa, hA, Ao, m, r);
+    house_apply(SB, n, pb, hB, Bo, n, r);
+  }
 }
 
 // ---------------------------------------------------------------- the executor
@@ -724,7 +801,7 @@ __device__ bool wait_flag(const int* f, int* ctrl, int64_t limit) {
 }
 
 template <typename T2>
-__global__ void __launch_bounds__(HX_THREADS) hlu_exec_kernel(HluExecArgs a) {
+__global__ void __launch_bounds__(HX_THREADS, sizeof(T2) == 8 ? 4 : 2) hlu_exec_kernel(HluExecArgs a) {
   extern __shared__ __align__(16) unsigned char hx_smem[];
   T2* sm = reinterpret_cast<T2*>(hx_smem);
   __shared__ int s_task, s_go;

@@ -1,39 +1,51 @@
 #!/usr/bin/env python
-"""Benchmark of the Helmholtz H-matrix BEM solve on one GB300.
+"""Benchmark of the Helmholtz H-matrix BEM hot path on one GB300.
 
-Workload (the configuration the headline metric is quoted on): pulsating
-sphere, radius 1 m, icosphere with 20,480 flat triangles, uniform normal
-velocity (a = 0, b = 1, g = 1), c = 343 m/s, rho = 1.2, f = 1.5 kHz, leaf 32,
-eta = 2, ACA tol 1e-5, GMRES tol 1e-10, Kirkup coupling.
+Headline workload (the large frequency sweep): pencil body -- cylinder of
+radius 4 mm and length 0.2 m with a 10 mm conical tip and a flat back cap --
+with exactly 81,920 flat triangles, Robin impedance walls (a = i k rho c / Z_e
+with Z_e seeded log-uniform in [0.5, 50] rho c, b = 1), 8 right-hand sides
+(g = 1 on the back-cap ring, and 7 seeded random-velocity patches on ~5 % of
+the elements), 64 log-spaced frequencies 200 Hz - 8 kHz, c = 343 m/s,
+rho = 1.2, leaf 32, eta = 2, ACA tol 1e-5, GMRES tol 1e-10 with the rank-2
+H-LU preconditioner, Kirkup coupling.
 
-A step is one complete frequency solve: near-field quadrature, ACA assembly of
-both H-matrices, right-hand side, GMRES, BC back-substitution and pressure.
-Consecutive steps use distinct frequencies 1500 (1 + 1e-4 i) Hz so nothing is
-reused between steps; every step's working set (the H-matrices, GBs) is far
-larger than the 129 MB L2, so no explicit flush is needed.
+A step is one frequency of that sweep solved completely for all 8
+right-hand sides: near field, ACA assembly of both H-matrices, H-LU
+factorization of the truncated system matrix (GPU task program), right-hand
+sides, preconditioned GMRES inside FP64 iterative refinement, BC
+back-substitution and pressure. The K timed steps are K of the 64
+frequencies spread evenly over the band (all 64 when K >= 64); the W warm-up
+solves use frequencies between them. Every step's working set (the
+H-matrices and factors, GBs) is far larger than the 129 MB L2, so no explicit
+flush is needed.
 
 Two arms of the same method run on the GPU:
   mixed (headline) -- FP32 regular quadrature with FP64-formed centroid
       differences, FP64 singular/near-singular rules, complex-FP32 storage,
-      FP32-arithmetic inner GMRES inside FP64 iterative refinement, and the
-      learned rule table for the ACA entries (--no-aca-rules: 16 points);
-      --selector adds the learned per-pair order of the near field;
-  plain            -- complex FP64 throughout.
-The line reports the mixed arm; the plain arm's rate and the relative surface-
-pressure difference between the two ride along.
+      FP32 H-LU factors (GPU task program), FP32-arithmetic inner GMRES inside
+      FP64 iterative refinement, and the learned rule table for the ACA
+      entries (--no-aca-rules: 16 points);
+  plain            -- complex FP64 throughout (FP64 H-LU on the GPU too),
+      timed on 2 of the K frequencies (the lowest and the highest).
 
   value : freq-solves/s with g resident in GPU memory (bem_solve_device)
-  e2e   : freq-solves/s through bem_solve with host buffers (g copied in, p
-          copied out inside the timed region)
+  e2e   : freq-solves/s through bem_solve with host buffers (g copied in and
+          p copied out inside the timed region, every step)
 
-Legs riding along in the same line (single GPU): the plain complex-FP64 arm,
-the field at 20,480 observation points (``field_eval``), the same sphere above
-a rigid plane (``half_space``), the 64-frequency box sweep (``box_sweep``) and
-the CPU baseline; ``--no-plain``, ``--no-field``, ``--no-half-space``,
-``--no-sweep``, ``--no-cpu-baseline`` skip them.
+Legs riding along in the same line: the plain arm (``plain_fp64``), the
+accuracy of the mixed arm against the FP64 oracle on the same body with 5,120
+triangles (``accuracy_vs_oracle``), the 20,480-triangle pulsating sphere at
+1.5 kHz (``sphere20k``: its own freq-solves/s, the plain arm and the oracle's
+solve), the field at 20,480 observation points, the sphere above a rigid plane
+and the 64-frequency box sweep; ``--no-plain``, ``--no-accuracy``,
+``--no-sphere``, ``--no-field``, ``--no-half-space``, ``--no-sweep``,
+``--no-cpu-baseline`` skip them. The CPU baseline is the oracle (FP64
+C++/OpenMP restatement of the reference path, H-LU preconditioned) on all host
+cores, one frequency of the headline workload.
 
-``--impl reference`` times the CPU restatement of the reference path (the
-oracle: FP64 C++/OpenMP, all host cores) on the same workload.
+``--impl reference`` times that CPU restatement alone on the headline
+workload (full frequency solves within a time budget).
 """
 from __future__ import annotations
 
@@ -55,29 +67,17 @@ sys.path.insert(0, ROOT)
 FREQ = 1500.0
 C0, RHO = 343.0, 1.2
 ACA_TOL, GMRES_TOL = 1e-5, 1e-10
+PENCIL_N, PENCIL_F = 81920, (200.0, 8000.0, 64)
 WORKLOADS = {
     # name: (icosphere subdivisions, description)
     "sphere20k": (5, "pulsating sphere r=1 m, icosphere 20,480 triangles, f=1.5 kHz"),
     "sphere5k": (4, "pulsating sphere r=1 m, icosphere 5,120 triangles, f=1.5 kHz (profiling case)"),
 }
-# DRAM traffic of the FP32 H-matvec per algorithmic byte, from one ncu
-# capture of hmv32_vpass + hmv32_upass at 5,120 elements (126.08 MB read +
-# write against 129.02 MB algorithmic), scaled to the benchmark operator by
-# its algorithmic bytes.
-HMV32_TRAFFIC_PER_BYTE = (57592832 + 169728 + 68490496 + 13568) / 129017600
+PENCIL_DESC = ("pencil r=4 mm L=0.2 m + 10 mm conical tip, 81,920 triangles, impedance walls "
+               "Z in [0.5, 50] rho c, 8 RHS, 64 log-spaced f 200 Hz-8 kHz, H-LU preconditioner "
+               "rank 2")
 METRIC = "freq-solves/sec (H-matrix Helmholtz BEM solve, <=1e-5 rel. surface-pressure error)"
 UNIT = "freq-solves/s"
-
-
-def workload_config(name, extra=None):
-    sub, desc = WORKLOADS[name]
-    cfg = {"workload": desc, "n_elements": 20 * 4 ** sub, "freq_hz": FREQ, "aca_tol": ACA_TOL,
-           "gmres_tol": GMRES_TOL, "leaf_size": 32, "eta": 2.0, "coupling": "Kirkup",
-           "bc": "Neumann v=1", "nrhs": 1,
-           "l2": "working set (H-matrix, GBs) >> 129 MB L2; no flush needed"}
-    if extra:
-        cfg.update(extra)
-    return cfg
 
 
 def freqs(count, offset=0):
@@ -176,46 +176,20 @@ def make_solver(pkg, meshes, sub, precision, **extra):
     return s, n
 
 
-def timed_arm(torch, pkg, s, n, args, ws):
-    """W warm-up solves, then K timed solves bracketed by barrier + sync;
-    returns (ms, infos, p of the last solve, launches)."""
-    stream = torch.cuda.ExternalStream(pkg.lib().bem_stream(s._h))
-    g = torch.ones(n, dtype=torch.complex128, device="cuda")
-    p = torch.zeros(n, dtype=torch.complex128, device="cuda")
-    for f in freqs(args.warmup, -args.warmup - 1):
-        s.solve_device(f, g.data_ptr(), 1, 0, 0, p.data_ptr())
-    torch.cuda.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    l0 = s.launch_count()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    infos = []
-    e0.record(stream)
-    for f in freqs(args.steps, 0):
-        infos.append(s.solve_device(f, g.data_ptr(), 1, 0, 0, p.data_ptr()))
-    e1.record(stream)
-    torch.cuda.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
-    ms = max_over_ranks(torch, e0.elapsed_time(e1), ws)
-    return ms, infos, p.cpu().numpy(), s.launch_count() - l0
-
-
-def time_matvec(torch, pkg, s, n, reps=50):
-    """Average duration of one system-matrix H-matvec as the inner GMRES runs
-    it (complex-FP32 storage, FP32 arithmetic: vector conversion, pass V,
-    pass U), with CUDA events on the library's stream."""
+def time_matvec(torch, pkg, s, n, reps=50, R=1):
+    """Average duration of one system-matrix H-matvec of R vectors as the
+    inner GMRES runs it (complex-FP32 storage, FP32 arithmetic: vector
+    conversion, pass V, pass U), with CUDA events on the library's stream."""
     L = pkg.lib()
     stream = torch.cuda.ExternalStream(L.bem_stream(s._h))
-    x = torch.randn(n, dtype=torch.complex128, device="cuda")
-    y = torch.zeros(n, dtype=torch.complex128, device="cuda")
+    x = torch.randn(n * R, dtype=torch.complex128, device="cuda")
+    y = torch.zeros(n * R, dtype=torch.complex128, device="cuda")
     for _ in range(3):
-        L.bem_hmatvec_device_ex(s._h, 1, x.data_ptr(), y.data_ptr(), 1, 0, pkg.BEM_ARITH_FP32)
+        L.bem_hmatvec_device_ex(s._h, 1, x.data_ptr(), y.data_ptr(), R, 0, pkg.BEM_ARITH_FP32)
     h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     h0.record(stream)
     for _ in range(reps):
-        L.bem_hmatvec_device_ex(s._h, 1, x.data_ptr(), y.data_ptr(), 1, 0, pkg.BEM_ARITH_FP32)
+        L.bem_hmatvec_device_ex(s._h, 1, x.data_ptr(), y.data_ptr(), R, 0, pkg.BEM_ARITH_FP32)
     h1.record(stream)
     torch.cuda.synchronize()
     return h0.elapsed_time(h1) / reps
@@ -225,7 +199,7 @@ def box_sweep(pkg, meshes, torch):
     """The batched sweep on the closed box with a piston: 5,120-triangle
     surface, 64 log-spaced frequencies 50-2000 Hz x 4 right-hand sides (piston
     + 3 random patches), mixed precision; sequential vs autotuned workers."""
-    tri = meshes.box(n_target=5120)
+    tri = meshes.box(n_target=5120, exact=True)
     n = tri.shape[0]
     g = meshes.box_piston_rhs(tri)
     freqs = meshes.log_frequencies(64, 50.0, 2000.0)
@@ -257,65 +231,6 @@ def box_sweep(pkg, meshes, torch):
             out["rel_diff_batched_vs_sequential"] = float(np.linalg.norm(p - p_seq)
                                                           / np.linalg.norm(p_seq))
         s.close()
-    return out
-
-
-def pencil_sweep(pkg, meshes, torch, every=8, plain_freqs=2):
-    """The large-body sweep: pencil (cylinder r = 4 mm, L = 0.2 m, conical tip),
-    81,760 triangles, impedance walls Z log-uniform in [0.5, 50] rho c,
-    8 right-hand sides (back-cap ring + 7 random patches), 64 log-spaced
-    frequencies 200 Hz - 8 kHz. Both arms use the H-LU preconditioner (rank 2,
-    rebuilt for every frequency as in the reference; unpreconditioned GMRES
-    does not reach 1e-10 on this body in 1000 steps). The mixed arm (learned
-    ACA rules) solves every `every`-th frequency; the plain complex-FP64 arm
-    solves `plain_freqs` of those; the 64-frequency times are extrapolated from
-    the per-frequency means. The host-side factorization (the same code in both
-    arms) is reported apart from the GPU work."""
-    tri = meshes.pencil()
-    n = tri.shape[0]
-    g = meshes.pencil_rhs(tri)
-    beta = meshes.wall_admittance(n)
-    freqs = meshes.log_frequencies(64, 200.0, 8000.0)
-    sub = freqs[::every]
-    out = {"workload": f"pencil r=4 mm L=0.2 m + conical tip, {n} triangles, impedance walls "
-                       "Z in [0.5, 50] rho c, 8 RHS, 64 log-spaced f 200 Hz-8 kHz, "
-                       "H-LU preconditioner rank 2",
-           "nrhs": int(g.shape[1]), "freqs_total": 64}
-
-    def solver(precision, **extra):
-        s = pkg.Solver(aca_tol=ACA_TOL, gmres_tol=GMRES_TOL, wave_speed=C0, density=RHO,
-                       precision=precision, use_preconditioner=1, precond_rank=2,
-                       gmres_maxit=1000, sweep_workers=1, **extra)
-        s.set_mesh(tri)
-        s.set_bc_impedance(beta)
-        return s
-
-    def arm(s, fr):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        p, info = s.sweep(fr, g)
-        dt = time.perf_counter() - t0
-        tp = sum(i["t_precond"] for i in info)
-        return p, info, {"freqs_solved": int(len(fr)), "seconds": round(dt, 3),
-                         "s_per_freq": round(dt / len(fr), 4),
-                         "host_factor_s_per_freq": round(tp / len(fr), 4),
-                         "gpu_s_per_freq": round((dt - tp) / len(fr), 4),
-                         "sweep_64_s_extrapolated": round(64 * dt / len(fr), 2),
-                         "max_iterations": int(max(i["iterations"] for i in info)),
-                         "all_converged": bool(all(i["status"] == 0 for i in info))}
-
-    s = solver(1, selector=2)
-    pm, im, out["mixed"] = arm(s, sub)
-    s.close()
-    pick = np.arange(0, len(sub), max(1, len(sub) // plain_freqs))[:plain_freqs]
-    s64 = solver(0)
-    pp, ip, out["plain_fp64"] = arm(s64, sub[pick])
-    s64.close()
-    errs = [float(np.linalg.norm(pm[:, r, f] - pp[:, r, j]) / np.linalg.norm(pp[:, r, j]))
-            for j, f in enumerate(pick) for r in range(g.shape[1])]
-    out["max_rel_err_mixed_vs_fp64"] = max(errs)
-    out["speedup_mixed_vs_fp64"] = round(out["plain_fp64"]["s_per_freq"] / out["mixed"]["s_per_freq"], 2)
-    out["speedup_gpu_work"] = round(out["plain_fp64"]["gpu_s_per_freq"] / out["mixed"]["gpu_s_per_freq"], 2)
     return out
 
 
@@ -432,6 +347,285 @@ def half_space(pkg, meshes, torch, reps=3):
     return out
 
 
+def pencil_problem(meshes, n_target=PENCIL_N):
+    """The pencil body, its 8 right-hand sides and wall admittances."""
+    tri = meshes.pencil(n_target=n_target)
+    return tri, meshes.pencil_rhs(tri), meshes.wall_admittance(tri.shape[0])
+
+
+def pencil_solver(pkg, tri, beta, precision, **extra):
+    s = pkg.Solver(aca_tol=ACA_TOL, gmres_tol=GMRES_TOL, wave_speed=C0, density=RHO,
+                   precision=precision, use_preconditioner=1, precond_rank=2, gmres_maxit=1000,
+                   sweep_workers=1, **extra)
+    s.set_mesh(tri)
+    s.set_bc_impedance(beta)
+    return s
+
+
+def sweep_frequencies(meshes, steps, warmup):
+    """K of the 64 log-spaced frequencies spread evenly over the band (all 64
+    for K >= 64) and W warm-up frequencies at geometric midpoints of the
+    first intervals (none of them timed)."""
+    f = meshes.log_frequencies(PENCIL_F[2], PENCIL_F[0], PENCIL_F[1])
+    k = min(max(steps, 1), len(f))
+    idx = np.unique(np.round(np.linspace(0, len(f) - 1, k)).astype(int))
+    warm = [float(np.sqrt(f[i] * f[i + 1])) for i in range(min(warmup, len(f) - 1))]
+    return [float(x) for x in f[idx]], warm
+
+
+def timed_solves(torch, pkg, s, n, R, fr_timed, fr_warm, ws, g=None):
+    """Warm-up solves, then the timed ones bracketed by barrier + sync, with
+    the right-hand sides resident in GPU memory (bem_solve_device); per-step
+    device times from events between the steps. Returns (ms, per-step ms,
+    infos, p per step (steps x n x R), launches)."""
+    stream = torch.cuda.ExternalStream(pkg.lib().bem_stream(s._h))
+    if g is None:
+        g = torch.ones(n * R, dtype=torch.complex128, device="cuda")
+    p = torch.zeros((len(fr_timed), R, n), dtype=torch.complex128, device="cuda")
+    for f in fr_warm:
+        s.solve_device(f, g.data_ptr(), R, 0, 0, p[0].data_ptr())
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    l0 = s.launch_count()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(fr_timed) + 1)]
+    infos = []
+    ev[0].record(stream)
+    for i, f in enumerate(fr_timed):
+        infos.append(s.solve_device(f, g.data_ptr(), R, 0, 0, p[i].data_ptr()))
+        ev[i + 1].record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    ms = max_over_ranks(torch, ev[0].elapsed_time(ev[-1]), ws)
+    per = [ev[i].elapsed_time(ev[i + 1]) for i in range(len(fr_timed))]
+    pn = p.cpu().numpy().transpose(0, 2, 1)  # steps x n x R
+    return ms, per, infos, pn, s.launch_count() - l0
+
+
+def rel_err_cols(p, ref):
+    """Largest relative 2-norm difference over the columns (right-hand sides)."""
+    return float(max(np.linalg.norm(p[:, r] - ref[:, r]) / np.linalg.norm(ref[:, r])
+                     for r in range(ref.shape[1])))
+
+
+def accuracy_vs_oracle(pkg, meshes, n_target=5120, fr=(1000.0, 8000.0)):
+    """The mixed and plain GPU arms against the FP64 oracle (H-LU
+    preconditioned, all host cores) on the same pencil body with 5,120
+    triangles: the oracle at the workload's tolerances (same approximation)
+    and at ACA 1e-8 / GMRES 1e-12 (the converged reference)."""
+    import oracle
+    tri, g, beta = pencil_problem(meshes, n_target)
+    n = tri.shape[0]
+    cores = os.cpu_count() or 1
+    P = oracle.Problem(tri, 32, 2.0)
+    out = {"workload": f"pencil as the headline with {n} triangles, 8 RHS, f = "
+                       + ", ".join(f"{f:g}" for f in fr) + " Hz"}
+    arms = {}
+    for name, prec, extra in (("mixed", 1, {"selector": 2}), ("plain", 0, {})):
+        s = pencil_solver(pkg, tri, beta, prec, **extra)
+        arms[name] = [s.solve(f, g, want=("p",))[2] for f in fr]
+        s.close()
+    t0 = time.perf_counter()
+    refs = {}
+    for key, aca, gt in (("same_tol", ACA_TOL, GMRES_TOL), ("converged", 1e-8, 1e-12)):
+        refs[key] = []
+        for f in fr:
+            k = 2 * np.pi * f / C0
+            _, _, p, _ = P.solve(f, C0, RHO, 2, 1j * k * beta, np.ones(n), g, aca, gt,
+                                 nthreads=cores, precond_rank=2)
+            refs[key].append(p)
+    out["oracle_s"] = round(time.perf_counter() - t0, 2)
+    for name, ps in arms.items():
+        for key, rs in refs.items():
+            out[f"{name}_vs_oracle_{key}"] = max(rel_err_cols(a, b) for a, b in zip(ps, rs))
+    return out
+
+
+def sphere_leg(torch, pkg, meshes, args, ws):
+    """The 20,480-triangle pulsating sphere at 1.5 kHz (ACA 1e-5, GMRES 1e-10,
+    no preconditioner, as the reference's default): mixed freq-solves/s, the
+    plain arm, the oracle's solve of the same workload and the errors of the
+    GPU arms against it, the field, the half-space and the box sweep legs."""
+    sub = WORKLOADS["sphere20k"][0]
+    steps = max(1, min(args.steps, 8))
+    fr_t = freqs(steps, 0)
+    fr_w = freqs(args.warmup, -args.warmup - 1)
+    out = {"workload": WORKLOADS["sphere20k"][1] + ", ACA 1e-5, GMRES 1e-10, 1 RHS"}
+    s, n = make_solver(pkg, meshes, sub, 1, selector=0 if args.no_aca_rules else 2)
+    ms, _, infos, pm, _ = timed_solves(torch, pkg, s, n, 1, fr_t, fr_w, ws)
+    out["mixed"] = {"freq_solves_per_s": round(steps / (ms / 1e3), 3),
+                    "ms_per_solve": round(ms / steps, 3),
+                    "gmres_iterations": int(max(i["iterations"] for i in infos))}
+    if not args.no_plain:
+        s64, _ = make_solver(pkg, meshes, sub, 0)
+        ms64, _, _, p64, _ = timed_solves(torch, pkg, s64, n, 1, fr_t[:2], fr_w[:1], ws)
+        s64.close()
+        out["plain_fp64"] = {"freq_solves_per_s": round(2 / (ms64 / 1e3), 3),
+                             "ms_per_solve": round(ms64 / 2, 2)}
+        out["rel_err_mixed_vs_plain"] = max(rel_err_cols(pm[i], p64[i]) for i in range(2))
+    k = 2 * np.pi * fr_t[-1] / C0
+    pa = RHO * C0 * (1j * k) / (1j * k - 1)
+    out["analytic_rel_err"] = round(float(np.abs(pm[-1] - pa).max() / abs(pa)), 5)
+    if not args.no_cpu_baseline:
+        import oracle
+        tri = meshes.icosphere(sub, 1.0)
+        cores = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        _, _, po, st = oracle.Problem(tri, 32, 2.0).solve(
+            fr_t[-1], C0, RHO, 2, np.zeros(n), np.ones(n), np.ones(n), ACA_TOL, GMRES_TOL,
+            nthreads=cores)
+        dt = time.perf_counter() - t0
+        out["cpu_oracle"] = {"freq_solves_per_s": round(1.0 / dt, 5), "cores": cores,
+                             "kind": "port", "gmres_iterations": int(st["iters"])}
+        out["rel_err_mixed_vs_oracle"] = rel_err_cols(pm[-1], po)
+        if "plain_fp64" in out:
+            s64, _ = make_solver(pkg, meshes, sub, 0)
+            _, _, p64l, _ = s64.solve(fr_t[-1], np.ones(n), want=("p",))
+            s64.close()
+            out["rel_err_plain_vs_oracle"] = rel_err_cols(p64l, po)
+    if not args.no_field:
+        out["field_eval"] = field_eval(pkg, meshes, torch, s, n, sub, cpu=not args.no_cpu_baseline)
+    s.close()
+    if not args.no_half_space:
+        out["half_space"] = half_space(pkg, meshes, torch)
+    if not args.no_sweep:
+        out["box_sweep"] = box_sweep(pkg, meshes, torch)
+    return out
+
+
+def cpu_pencil_solve(f, nthreads, n_target=PENCIL_N):
+    """One frequency of the headline workload on the host cores with the
+    oracle (FP64, H-LU preconditioned GMRES, 8 right-hand sides)."""
+    import oracle
+    meshes = importlib.import_module("3d_bem_gb300.meshes")
+    oracle.build()
+    tri, g, beta = pencil_problem(meshes, n_target)
+    n = tri.shape[0]
+    P = oracle.Problem(tri, 32, 2.0)
+    k = 2 * np.pi * f / C0
+    t0 = time.perf_counter()
+    _, _, p, st = P.solve(f, C0, RHO, 2, 1j * k * beta, np.ones(n), g, ACA_TOL, GMRES_TOL,
+                          nthreads=nthreads, precond_rank=2, maxit=1000)
+    return time.perf_counter() - t0, st, p
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    pkg = importlib.import_module("3d_bem_gb300")
+    meshes = importlib.import_module("3d_bem_gb300.meshes")
+    pkg.build()
+    tri, g_host, beta = pencil_problem(meshes)
+    n, R = tri.shape[0], g_host.shape[1]
+    fr_t, fr_w = sweep_frequencies(meshes, args.steps, max(args.warmup, 1))
+    g_dev = torch.from_numpy(np.ascontiguousarray(g_host.T)).reshape(-1).to("cuda")
+    learned = (1 if args.selector else 0) | (0 if args.no_aca_rules else 2)
+    extra = {"selector": learned} if learned else {}
+
+    s = pencil_solver(pkg, tri, beta, 1, **extra)
+    clk = Clocks(local)
+    clk.start()
+    ms, per, infos, pm, launches = timed_solves(torch, pkg, s, n, R, fr_t, fr_w, ws, g_dev)
+    clocks = clk.stop()
+    K = len(fr_t)
+    value = ws * K / (ms / 1e3)
+
+    # end to end through bem_solve: pinned host g in, host p out, every step
+    gh = torch.from_numpy(np.asfortranarray(g_host)).pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for f in fr_t:
+        s.solve(f, gh.numpy(), want=("p",))
+    torch.cuda.synchronize()
+    e2e = ws * K / (time.perf_counter() - t0)
+
+    # roofline of the inner-GMRES H-matvec (complex-FP32 storage, FP32
+    # arithmetic, the 8 right-hand sides of a product; matrix bytes read once)
+    info_part = s.partition()
+    ranks = s.ranks(1)
+    B = matvec_bytes(info_part, ranks, n, elem=8, R=R)
+    mv_ms = time_matvec(torch, pkg, s, n, R=R)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = B / (mv_ms * 1e-3) / 1e9
+    phase = {key: round(float(np.mean([i[key] for i in infos])), 5)
+             for key in ("t_nearfield", "t_aca", "t_rhs", "t_precond", "t_gmres", "t_total")}
+    line = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws,
+        "steps": K, "warmup": len(fr_w), "ms_per_step": round(ms / K, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64 storage + fp32 quadrature/H-LU, fp64 refinement/Arnoldi/singular rules",
+        "data": "synthetic (seeded pencil mesh, wall impedances and velocity patches)",
+        "config": {"workload": PENCIL_DESC, "n_elements": n, "nrhs": R,
+                   "frequencies_timed_hz": [round(f, 2) for f in fr_t],
+                   "aca_tol": ACA_TOL, "gmres_tol": GMRES_TOL, "leaf_size": 32, "eta": 2.0,
+                   "coupling": "Kirkup", "bc": "Robin impedance walls a = i k rho c / Z",
+                   "precision": "mixed", "hlu_preconditioner": "rank 2, factorized on the GPU",
+                   "learned_selector": bool(args.selector),
+                   "learned_aca_rules": not args.no_aca_rules,
+                   "parallelism": f"replicas{ws}" if ws > 1 else "single-gpu",
+                   "l2": "working set (H-matrices and factors, GBs) >> 129 MB L2; no flush"},
+        "e2e": {"value": round(e2e, 4), "unit": UNIT, "h2d_bytes_per_step": n * R * 16,
+                "d2h_bytes_per_step": n * R * 16},
+        "roofline": {"kernel": "hmatvec FP32 (hmv32_vpass + hmv32_upass), c64 storage, 8 RHS",
+                     "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(achieved / hbm, 4), "traffic": None,
+                     "bytes_per_launch": B, "ms_per_launch": round(mv_ms, 4),
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
+        "gpu_launches": int(launches),
+        "phases_s": phase,
+        "ms_per_frequency": [round(x, 1) for x in per],
+        "gmres_iterations": int(max(i["iterations"] for i in infos)),
+        "true_residual": float(max(i["true_residual"] for i in infos)),
+        "all_converged": bool(all(i["status"] == 0 for i in infos)),
+        "max_rank": int(max(i["max_rank"] for i in infos)),
+        "clocks": clocks,
+    }
+    s.close()
+    if not args.no_plain and ws == 1:
+        s64 = pencil_solver(pkg, tri, beta, 0)
+        pick = [fr_t[0], fr_t[-1]] if K > 1 else [fr_t[0]]
+        ms64, per64, i64, p64, _ = timed_solves(torch, pkg, s64, n, R, pick, fr_w[:1], ws, g_dev)
+        s64.close()
+        mixed_same = [per[fr_t.index(f)] for f in pick]
+        line["plain_fp64"] = {
+            "frequencies_hz": [round(f, 2) for f in pick],
+            "ms_per_frequency": [round(x, 1) for x in per64],
+            "mixed_ms_same_frequencies": [round(x, 1) for x in mixed_same],
+            "speedup_mixed_vs_plain": round(sum(per64) / sum(mixed_same), 2),
+            "phases_s": {key: round(float(np.mean([i[key] for i in i64])), 4)
+                         for key in ("t_nearfield", "t_aca", "t_precond", "t_gmres", "t_total")},
+            "rel_err_mixed_vs_plain": max(rel_err_cols(pm[fr_t.index(f)], p64[j])
+                                          for j, f in enumerate(pick))}
+    if not args.no_accuracy and ws == 1:
+        line["accuracy_vs_oracle"] = accuracy_vs_oracle(pkg, meshes)
+    if not args.no_sphere and ws == 1:
+        line["sphere20k"] = sphere_leg(torch, pkg, meshes, args, ws)
+    if not args.no_cpu_baseline and rank == 0 and ws == 1:
+        cores = os.cpu_count() or 1
+        f = fr_t[len(fr_t) // 2]
+        dt, st, _ = cpu_pencil_solve(f, cores)
+        line["cpu_baseline"] = {"value": round(1.0 / dt, 5), "unit": UNIT, "cores": cores,
+                                "kind": "port",
+                                "sample": f"one frequency ({f:.0f} Hz) of the workload, 8 RHS, "
+                                          f"{dt:.1f} s (assembly, H-LU {st['t_factor']:.1f} s, "
+                                          f"GMRES {int(st['iters'])} iterations)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
 def run_field_only(args):
     """The field leg alone on one GPU (for profiling its kernels)."""
     import torch
@@ -445,173 +639,30 @@ def run_field_only(args):
     s.close()
 
 
-def run_ours(args):
-    import torch
-    ws, rank, local = dist_env()
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    torch.cuda.set_device(local)
-    pkg = importlib.import_module("3d_bem_gb300")
-    meshes = importlib.import_module("3d_bem_gb300.meshes")
-    pkg.build()
-    sub = WORKLOADS[args.workload][0]
-
-    # plain complex-FP64 arm (comparison), then the mixed arm (headline)
-    plain = None
-    if not args.no_plain:
-        s64, n = make_solver(pkg, meshes, sub, 0)
-        ms64, infos64, p64, _ = timed_arm(torch, pkg, s64, n, args, ws)
-        plain = {"value": round(ws * args.steps / (ms64 / 1e3), 4),
-                 "ms_per_step": round(ms64 / args.steps, 3),
-                 "phases_s": {k: round(float(np.mean([i[k] for i in infos64])), 5)
-                              for k in ("t_nearfield", "t_aca", "t_rhs", "t_gmres")}}
-        s64.close()
-    extra = {}
-    if args.recompress > 0:
-        extra["recompress_tol"] = args.recompress
-    if args.precond:
-        extra.update(use_preconditioner=1, precond_rank=2)
-    learned = (1 if args.selector else 0) | (0 if args.no_aca_rules else 2)
-    if learned:
-        extra["selector"] = learned
-    s, n = make_solver(pkg, meshes, sub, 1, **extra)
-    clk = Clocks(local)
-    clk.start()
-    ms, infos, pm, launches = timed_arm(torch, pkg, s, n, args, ws)
-    clocks = clk.stop()
-    value = ws * args.steps / (ms / 1e3)
-
-    k = 2 * np.pi * freqs(args.steps, 0)[-1] / C0
-    pa = RHO * C0 * (1j * k) / (1j * k - 1)
-    analytic_err = float(np.abs(pm - pa).max() / abs(pa))
-    mixed_vs_fp64 = None
-    if plain is not None:
-        mixed_vs_fp64 = float(np.linalg.norm(pm - p64) / np.linalg.norm(p64))
-
-    # end-to-end through the host-buffer API (pinned host memory)
-    gh = torch.ones(n, dtype=torch.complex128).pin_memory()
-    K2 = max(1, args.steps // 2)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for f in freqs(K2, 200):
-        s.solve(f, gh.numpy(), want=("p",))
-    torch.cuda.synchronize()
-    e2e = K2 / (time.perf_counter() - t0)
-
-    # roofline of the inner-GMRES H-matvec (complex-FP32 storage, FP32
-    # arithmetic; the bytes are those of the stored matrix, read once)
-    info_part = s.partition()
-    ranks = s.ranks(1)
-    B = matvec_bytes(info_part, ranks, n, elem=8)
-    mv_ms = time_matvec(torch, pkg, s, n)
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except (OSError, ValueError):
-        pass
-    hbm = float(peaks.get("hbm_gbs", 6800.0))
-    achieved = B / (mv_ms * 1e-3) / 1e9
-
-    phase = {key: float(np.mean([i[key] for i in infos]))
-             for key in ("t_nearfield", "t_aca", "t_rhs", "t_gmres", "t_precond", "t_total")}
-    line = {
-        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None,
-        "dtype": "c64 storage + fp32 quadrature, fp64 refinement/Arnoldi/singular rules",
-        "data": "synthetic (seeded icosphere; analytic monopole as accuracy check)",
-        "config": workload_config(args.workload, {
-            "precision": "mixed", "parallelism": f"replicas{ws}" if ws > 1 else "single-gpu",
-            "recompress_tol": args.recompress, "hlu_preconditioner": bool(args.precond),
-            "learned_selector": bool(args.selector),
-            "learned_aca_rules": not args.no_aca_rules}),
-        "e2e": {"value": round(e2e, 4), "unit": UNIT, "h2d_bytes_per_step": n * 16,
-                "d2h_bytes_per_step": n * 16},
-        "roofline": {"kernel": "hmatvec FP32 (hmv32_vpass + hmv32_upass), c64 storage",
-                     "bound": "hbm",
-                     "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                     "frac": round(achieved / hbm, 4),
-                     "traffic": int(HMV32_TRAFFIC_PER_BYTE * B),
-                     "traffic_source": "ncu dram bytes at 5,120 elements, scaled by bytes",
-                     "bytes_per_launch": B, "ms_per_launch": round(mv_ms, 4),
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
-        "gpu_launches": int(launches),
-        "phases_s": {k2: round(v, 5) for k2, v in phase.items()},
-        "gmres_iterations": int(max(i["iterations"] for i in infos)),
-        "true_residual": float(max(i["true_residual"] for i in infos)),
-        "max_rank": int(max(i["max_rank"] for i in infos)),
-        "rel_err_vs_plain_fp64": mixed_vs_fp64,
-        "analytic_rel_err": round(analytic_err, 5),
-        "plain_fp64": plain,
-        "clocks": clocks,
-    }
-    if args.selector:
-        line["selector_stats"] = s.sel_stats()
-    if not args.no_field and ws == 1:
-        line["field_eval"] = field_eval(pkg, meshes, torch, s, n, sub,
-                                        cpu=not args.no_cpu_baseline and rank == 0)
-    if not args.no_half_space and ws == 1:
-        line["half_space"] = half_space(pkg, meshes, torch)
-    if not args.no_sweep and ws == 1:
-        line["box_sweep"] = box_sweep(pkg, meshes, torch)
-    if args.pencil and ws == 1:
-        line["pencil_sweep"] = pencil_sweep(pkg, meshes, torch)
-    if not args.no_cpu_baseline and rank == 0 and ws == 1:
-        line["cpu_baseline"] = cpu_baseline_sample(args)
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    s.close()
-    if ws > 1:
-        torch.distributed.destroy_process_group()
-
-
-def cpu_solve_once(tri, f, nthreads):
-    import oracle
-    oracle.build()
-    P = oracle.Problem(tri, 32, 2.0)
-    n = tri.shape[0]
-    t0 = time.perf_counter()
-    _, _, p, st = P.solve(f, C0, RHO, 2, np.zeros(n), np.ones(n), np.ones(n), ACA_TOL,
-                          GMRES_TOL, nthreads=nthreads)
-    return time.perf_counter() - t0, st
-
-
-def cpu_baseline_sample(args):
-    """The oracle (FP64 C++/OpenMP restatement of the reference path) on all
-    host cores, one full frequency solve of the same workload."""
-    meshes = importlib.import_module("3d_bem_gb300.meshes")
-    tri = meshes.icosphere(WORKLOADS[args.workload][0], 1.0)
-    cores = os.cpu_count() or 1
-    dt, st = cpu_solve_once(tri, FREQ, cores)
-    return {"value": round(1.0 / dt, 5), "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"one full frequency solve of the same workload ({dt:.1f} s; "
-                      f"GMRES iterations {int(st['iters'])})"}
-
-
 def run_reference(args):
+    """The oracle (the reference path restated on the CPU: FP64, H-LU
+    preconditioned GMRES, all host cores) on the headline workload: each step
+    one full frequency solve with 8 right-hand sides; warm-up and steps stop
+    once the next solve would pass the time budget (the counts are reported)."""
     ws, rank, local = dist_env()
     if rank != 0:
         return
     meshes = importlib.import_module("3d_bem_gb300.meshes")
-    tri = meshes.icosphere(WORKLOADS[args.workload][0], 1.0)
     cores = os.cpu_count() or 1
-    # each warm-up and each step is one full frequency solve (distinct
-    # frequencies); the whole run is bounded to a few minutes: once the next
-    # solve would pass the budget, fewer steps are timed (and reported)
-    budget = float(os.environ.get("BEM_REF_BUDGET_S", "240"))
+    budget = float(os.environ.get("BEM_REF_BUDGET_S", "300"))
+    fr_t, fr_w = sweep_frequencies(meshes, args.steps, max(args.warmup, 1))
     t_start = time.perf_counter()
     warm = 0
-    for f in freqs(args.warmup, -args.warmup - 1):
-        dt, _ = cpu_solve_once(tri, f, cores)
+    for f in fr_w:
+        dt, _, _ = cpu_pencil_solve(f, cores)
         warm += 1
         if time.perf_counter() - t_start + 2 * dt > budget:
             break
-    times = []
-    for f in freqs(args.steps):
-        dt, st = cpu_solve_once(tri, f, cores)
+    times, iters = [], []
+    for f in fr_t:
+        dt, st, _ = cpu_pencil_solve(f, cores)
         times.append(dt)
+        iters.append(int(st["iters"]))
         if time.perf_counter() - t_start + dt > budget:
             break
     value = len(times) / sum(times)
@@ -620,14 +671,18 @@ def run_reference(args):
         "steps": len(times), "warmup": warm,
         "ms_per_step": round(1e3 * sum(times) / len(times), 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "c128 (fp64)", "data": "synthetic (seeded icosphere)",
-        "config": workload_config(args.workload, {"precision": "fp64",
-                                                  "parallelism": "cpu-openmp"}),
+        "dtype": "c128 (fp64)", "data": "synthetic (seeded pencil mesh)",
+        "config": {"workload": PENCIL_DESC, "n_elements": PENCIL_N, "nrhs": 8,
+                   "frequencies_timed_hz": [round(f, 2) for f in fr_t[:len(times)]],
+                   "aca_tol": ACA_TOL, "gmres_tol": GMRES_TOL, "leaf_size": 32, "eta": 2.0,
+                   "coupling": "Kirkup", "precision": "fp64",
+                   "hlu_preconditioner": "rank 2 (host)", "parallelism": "cpu-openmp"},
         "impl": "reference",
         "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{len(times)} full frequency solve(s) of the workload; "
-                                   "the reference itself needs Qt 6 + Eigen and cannot be "
-                                   "built here, so its CPU path is the oracle restatement"},
+                         "sample": f"{len(times)} full frequency solve(s) of the workload "
+                                   f"(GMRES iterations {iters}); the reference itself needs Qt 6 "
+                                   "+ Eigen and cannot be built here, so its CPU path is the "
+                                   "oracle restatement"},
         "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -637,18 +692,19 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--steps", type=int, default=8,
+                    help="frequencies of the 64-frequency sweep timed (spread over the band)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="sphere20k", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="sphere20k", choices=sorted(WORKLOADS),
+                    help="workload of --field-only")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-plain", action="store_true", help="skip the complex-FP64 arm")
-    ap.add_argument("--recompress", type=float, default=0.0,
-                    help="mixed arm: truncating SVD recompression tolerance after ACA (0: off)")
-    ap.add_argument("--precond", action="store_true",
-                    help="mixed arm: H-LU preconditioned GMRES (rank 2)")
-    ap.add_argument("--pencil", action="store_true",
-                    help="also measure the 81,760-triangle pencil sweep (minutes)")
+    ap.add_argument("--no-plain", action="store_true", help="skip the complex-FP64 arms")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the accuracy leg against the oracle (5,120-triangle pencil)")
+    ap.add_argument("--no-sphere", action="store_true",
+                    help="skip the 20,480-triangle sphere leg (and its field, half-space and "
+                         "box-sweep legs)")
     ap.add_argument("--no-field", action="store_true",
                     help="skip the field evaluation at 20,480 observation points")
     ap.add_argument("--no-half-space", action="store_true",

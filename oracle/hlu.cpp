@@ -14,8 +14,8 @@
 // left-preconditioned GMRES of GMRES::gmresLUPreconditionedSolve
 // (gmres.h:191-207) on them.
 //
-// Written for clarity: every operation is sequential dense arithmetic on the
-// blocks, in the reference's order.
+// Written for clarity: dense arithmetic on the blocks in the reference's
+// order; independent sub-blocks run as OpenMP tasks, as in the reference.
 #include <chrono>
 #include <cstring>
 #include <memory>
@@ -39,7 +39,30 @@ struct HNode {
   std::vector<cd> U, W;
   int64_t k = 0;
   std::unique_ptr<HNode> ch[4];
+  const HBlock* src = nullptr;  // the assembled block of a low-rank leaf, until loaded
 };
+
+// compressAdmissibleBlock of one assembled block into a low-rank leaf
+void load_lowrank(HNode& nd, int64_t rank, double tol) {
+  HBlock c = *nd.src;
+  recompress_block(c, rank, tol);
+  nd.k = c.rank;
+  nd.U.assign(nd.m * nd.k, 0.0);
+  nd.W.assign(nd.n * nd.k, 0.0);
+  for (int64_t l = 0; l < nd.k; l++) {
+    for (int64_t i = 0; i < nd.m; i++) nd.U[l * nd.m + i] = c.U[l * nd.m + i] * c.s[l];
+    for (int64_t j = 0; j < nd.n; j++) nd.W[l * nd.n + j] = c.V[l * nd.n + j];
+  }
+  nd.src = nullptr;
+}
+
+void lowrank_leaves(HNode& nd, std::vector<HNode*>& out) {
+  if (nd.kind == NK::Split) {
+    for (auto& q : nd.ch) lowrank_leaves(*q, out);
+  } else if (nd.kind == NK::LowRank && nd.src) {
+    out.push_back(&nd);
+  }
+}
 
 struct Ctx {
   const ClusterTree* t;
@@ -107,17 +130,9 @@ std::unique_ptr<HNode> build(const Ctx& cx, const std::vector<HBlock>& blk, size
     // a partition leaf at this node (the partition lists the blocks in the
     // same depth-first order)
     next++;
-    if (b.info.adm) {
-      HBlock c = b;
-      recompress_block(c, cx.rank, cx.tol);
+    if (b.info.adm) {  // truncated to the rank afterwards (load_lowrank)
       nd->kind = NK::LowRank;
-      nd->k = c.rank;
-      nd->U.assign(nd->m * nd->k, 0.0);
-      nd->W.assign(nd->n * nd->k, 0.0);
-      for (int64_t l = 0; l < nd->k; l++) {
-        for (int64_t i = 0; i < nd->m; i++) nd->U[l * nd->m + i] = c.U[l * nd->m + i] * c.s[l];
-        for (int64_t j = 0; j < nd->n; j++) nd->W[l * nd->n + j] = c.V[l * nd->n + j];
-      }
+      nd->src = &b;
     } else {
       nd->kind = NK::Dense;
       nd->D = b.full;
@@ -378,13 +393,21 @@ void subtract(HNode& C, const Prod& P, int64_t ro, int64_t co, const Ctx& cx) {
   C.W = std::move(acc.W);
 }
 
+// sub-problems of at least this many entries run as OpenMP tasks (they write
+// disjoint blocks and read finished ones)
+constexpr int64_t TASK_ENTRIES = 128 * 128;
+
 // C -= A B
 void mul_subtract(HNode& C, const HNode& A, const HNode& B, const Ctx& cx) {
   if (A.kind == NK::Zero || B.kind == NK::Zero) return;
   if (C.kind == NK::Split && A.kind == NK::Split && B.kind == NK::Split) {
     for (int i = 0; i < 2; i++)
-      for (int j = 0; j < 2; j++)
-        for (int l = 0; l < 2; l++) mul_subtract(*C.ch[2 * i + j], *A.ch[2 * i + l], *B.ch[2 * l + j], cx);
+      for (int j = 0; j < 2; j++) {
+        HNode& Cq = *C.ch[2 * i + j];
+#pragma omp task default(shared) firstprivate(i, j) if (Cq.m * Cq.n >= TASK_ENTRIES)
+        for (int l = 0; l < 2; l++) mul_subtract(Cq, *A.ch[2 * i + l], *B.ch[2 * l + j], cx);
+      }
+#pragma omp taskwait
     return;
   }
   subtract(C, product(A, B, cx), 0, 0, cx);
@@ -397,11 +420,15 @@ void left_solve(const HNode& L, HNode& X, const Ctx& cx) {
     case NK::Dense: lsolve(L, X.D.data(), X.m, X.n); return;
     case NK::LowRank: lsolve(L, X.U.data(), X.m, X.k); return;
     case NK::Split:
-      for (int j = 0; j < 2; j++) {
-        left_solve(*L.ch[0], *X.ch[j], cx);
-        mul_subtract(*X.ch[2 + j], *L.ch[2], *X.ch[j], cx);
-        left_solve(*L.ch[3], *X.ch[2 + j], cx);
+      for (int j = 0; j < 2; j++) {  // the block columns are independent
+#pragma omp task default(shared) firstprivate(j) if (X.m * X.n >= 2 * TASK_ENTRIES)
+        {
+          left_solve(*L.ch[0], *X.ch[j], cx);
+          mul_subtract(*X.ch[2 + j], *L.ch[2], *X.ch[j], cx);
+          left_solve(*L.ch[3], *X.ch[2 + j], cx);
+        }
       }
+#pragma omp taskwait
   }
 }
 
@@ -420,11 +447,15 @@ void right_solve(HNode& X, const HNode& U, const Ctx& cx) {
     }
     case NK::LowRank: utsolve(U, X.W.data(), X.n, X.k); return;
     case NK::Split:
-      for (int i = 0; i < 2; i++) {
-        right_solve(*X.ch[2 * i], *U.ch[0], cx);
-        mul_subtract(*X.ch[2 * i + 1], *X.ch[2 * i], *U.ch[1], cx);
-        right_solve(*X.ch[2 * i + 1], *U.ch[3], cx);
+      for (int i = 0; i < 2; i++) {  // the block rows are independent
+#pragma omp task default(shared) firstprivate(i) if (X.m * X.n >= 2 * TASK_ENTRIES)
+        {
+          right_solve(*X.ch[2 * i], *U.ch[0], cx);
+          mul_subtract(*X.ch[2 * i + 1], *X.ch[2 * i], *U.ch[1], cx);
+          right_solve(*X.ch[2 * i + 1], *U.ch[3], cx);
+        }
       }
+#pragma omp taskwait
   }
 }
 
@@ -447,8 +478,10 @@ void factor(HNode& A, HNode& L, HNode& U, const Ctx& cx) {
   U.ch[2] = node(cx, R.son2, C.son1);
   U.ch[3] = node(cx, R.son2, C.son2);
   factor(*A.ch[0], *L.ch[0], *U.ch[0], cx);
+#pragma omp task default(shared) if (A.m * A.n >= 4 * TASK_ENTRIES)
   left_solve(*L.ch[0], *A.ch[1], cx);
   right_solve(*A.ch[2], *U.ch[0], cx);
+#pragma omp taskwait
   U.ch[1] = std::move(A.ch[1]);
   L.ch[2] = std::move(A.ch[2]);
   mul_subtract(*A.ch[3], *L.ch[2], *U.ch[1], cx);
@@ -487,6 +520,12 @@ void hlu_factor_blocks(const ClusterTree& t, const std::vector<HBlock>& blk, int
   Ctx cx{&t, rank, tol};
   size_t next = 0;
   auto A = build(cx, blk, next, 0, 0);
+  // the truncated copy HMatrix(const HMatrix&, rank, relError): blocks
+  // recompressed independently
+  std::vector<HNode*> lr;
+  lowrank_leaves(*A, lr);
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int64_t i = 0; i < (int64_t)lr.size(); i++) load_lowrank(*lr[i], rank, tol);
   HNode L, U;
   L.r0 = U.r0 = A->r0;
   L.m = U.m = A->m;
@@ -494,6 +533,8 @@ void hlu_factor_blocks(const ClusterTree& t, const std::vector<HBlock>& blk, int
   L.n = U.n = A->n;
   L.rc = U.rc = A->rc;
   L.cc = U.cc = A->cc;
+#pragma omp parallel
+#pragma omp single
   factor(*A, L, U, cx);
   Ll.clear();
   Ld.clear();

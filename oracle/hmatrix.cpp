@@ -439,6 +439,12 @@ void jacobi_svd(int64_t n, std::vector<cd>& A, std::vector<double>& sigma,
   // A: n x n col-major -> A = U diag(sigma) V^H, sigma descending.
   V.assign(n * n, 0.0);
   for (int64_t i = 0; i < n; i++) V[i * n + i] = 1.0;
+  // columns below 1e-30 of the squared Frobenius norm (kept by the rotations)
+  // are rounding noise and take no rotations: the relative test between two
+  // of them never settles
+  double fro = 0;
+  for (int64_t i = 0; i < n * n; i++) fro += std::norm(A[i]);
+  const double floor2 = 1e-30 * fro;
   for (int sweep = 0; sweep < 60; sweep++) {
     double off = 0;
     for (int64_t p = 0; p < n - 1; p++)
@@ -451,6 +457,7 @@ void jacobi_svd(int64_t n, std::vector<cd>& A, std::vector<double>& sigma,
           ga += std::conj(A[p * n + i]) * A[q * n + i];
         }
         double g = std::abs(ga);
+        if (!(al > floor2) || !(be > floor2)) continue;
         if (g == 0.0 || g <= 1e-15 * std::sqrt(al * be)) continue;
         off = std::max(off, g / std::sqrt(al * be));
         cd e = ga / g;  // e^{i phi}
