@@ -273,6 +273,7 @@ class Solver:
             raise BemError(st, "bem_create failed (is a CUDA device visible?)")
         self._h = h
         self.n = 0
+        self.rows = 0
         if self.config.selector:
             self.set_selector()
 
@@ -295,6 +296,7 @@ class Solver:
         tri = np.ascontiguousarray(tri, dtype=np.float64).reshape(-1, 9)
         self._check(lib().bem_set_mesh(self._h, _ptr(tri), tri.shape[0]), "bem_set_mesh")
         self.n = tri.shape[0]
+        self.rows = self.n  # rows of the assembled matrices
 
     @property
     def permutation(self) -> np.ndarray:
@@ -334,9 +336,13 @@ class Solver:
     def hmatvec(self, which: int, x, y=None, accumulate: bool = False) -> np.ndarray:
         x = _c128(x)
         R = 1 if x.ndim == 1 else x.shape[1]
-        nrows = x.shape[0] if y is None else np.asarray(y).shape[0]
-        out = np.zeros(x.shape if y is None else np.asarray(y).shape, np.complex128,
-                       order="F") if y is None else _c128(y).copy(order="F")
+        rows = self.rows or x.shape[0]
+        if y is None:  # one row per row of the matrix (point clouds: rectangular)
+            out = np.zeros((rows,) if x.ndim == 1 else (rows, R), np.complex128, order="F")
+        else:
+            out = _c128(y).copy(order="F")
+            if out.shape[0] != rows:
+                raise BemError(BEM_EINVAL, "hmatvec: y needs one row per matrix row")
         self._check(lib().bem_hmatvec(self._h, which, _ptr(x), _ptr(out), R, int(accumulate)),
                     "bem_hmatvec")
         return out
@@ -547,6 +553,7 @@ class Solver:
         self._check(lib().bem_points_assemble(self._h, _ptr(rowpts), rowpts.shape[0],
                                               _ptr(colpts), colpts.shape[0], k, _ptr(rp),
                                               _ptr(cp)), "bem_points_assemble")
+        self.rows = rowpts.shape[0]
         return rp, cp
 
     def launch_count(self) -> int:

@@ -31,11 +31,13 @@ struct Cx<float2> {
   static constexpr int SMEM = 6144;  // complex elements of dynamic shared memory
   __device__ static float2 mk(float a, float b) { return make_float2(a, b); }
   __device__ static float sq(float x) { return sqrtf(x); }
-  __device__ static float jacobi_thr() { return 1e-6f; }
+  // orthogonality target of the FP32 rotations: one decade above FP32
+  // rounding, where the relative test would otherwise oscillate
+  __device__ static float jacobi_thr() { return 1e-5f; }
   // columns below this fraction of the squared Frobenius norm are rounding
   // noise: they take no rotations (their relative test never settles)
   __device__ static float jacobi_floor() { return 1e-14f; }
-  static constexpr int JACOBI_SWEEPS = 30;
+  static constexpr int JACOBI_SWEEPS = 15;
 };
 template <>
 struct Cx<double2> {
@@ -476,7 +478,7 @@ __device__ void house_qr(T2* X, int64_t rows, int cols, T2* head) {
 
 // Y (rows x nc, column-major, ld, in the arena) := H_0 .. H_{p-1} Y with the
 // reflectors of house_qr
-template <typename T2>
+template <typename T2, bool ARENA = true>
 __device__ void house_apply(const T2* X, int64_t rows, int p, const T2* head, T2* Y, int64_t ld,
                             int nc) {
   using R = typename Cx<T2>::R;
@@ -496,7 +498,8 @@ __device__ void house_apply(const T2* X, int64_t rows, int p, const T2* head, T2
 #pragma unroll
         for (int g = 0; g < HQ_G; g++)
           if (g < ng) {
-            const T2 pr = cmulc(vi, ldA(Y + i + (int64_t)(c0 + g) * ld));
+            const T2* yp = Y + i + (int64_t)(c0 + g) * ld;
+            const T2 pr = cmulc(vi, ARENA ? ldA(yp) : *yp);
             acc[2 * g] += pr.x;
             acc[2 * g + 1] += pr.y;
           }
@@ -511,7 +514,8 @@ __device__ void house_apply(const T2* X, int64_t rows, int p, const T2* head, T2
         for (int g = 0; g < HQ_G; g++)
           if (g < ng) {
             T2* y = Y + i + (int64_t)(c0 + g) * ld;
-            stA(y, csub(ldA(y), cmul(vi, s_c[g])));
+            if (ARENA) stA(y, csub(ldA(y), cmul(vi, s_c[g])));
+            else *y = csub(*y, cmul(vi, s_c[g]));
           }
       }
       __syncthreads();
@@ -532,108 +536,17 @@ __device__ __forceinline__ T2 piece_get(const HluExecArgs& a, int kind, int64_t 
   return __ldg(reinterpret_cast<const T2*>(a.V) + off + r * rs + (int64_t)l * cs);
 }
 
+// One-sided Jacobi on the q columns of X (p x q, column-major): X V = U diag(s),
+// V (q x q) accumulates the rotations (set to I here). Round-robin pairs, a
+// warp per pair. Rotations keep the Frobenius norm, so one floor decides
+// which columns are rounding noise: those take no rotations (between two of
+// them the relative test never settles).
 template <typename T2>
-__device__ void task_trunc(const HluTask& t, const HluExecArgs& a, T2* arena, T2* slot, T2* sm) {
+__device__ void jacobi_cols(T2* X, int p, int q, T2* V, typename Cx<T2>::R* red) {
   using R = typename Cx<T2>::R;
-  __shared__ int s_cb[HX_MAX_PAIRS + 1];
-  __shared__ R red[HX_WARPS + 8];
-  __shared__ int s_idx[64];
-  __shared__ int s_r;
   __shared__ unsigned s_off;
-  const int64_t m = t.m, n = t.n;
-  const int kc = a.kc;
-  const HluTruncPair* P = a.pairs + t.x0;
-  const int np = t.x1;
-  if (threadIdx.x == 0) {
-    int c = 0;
-    for (int p = 0; p < np; p++) {
-      s_cb[p] = c;
-      int w = P[p].cols;
-      if (P[p].rank_idx >= 0) w = min(w, max(0, __ldg(a.rank + P[p].rank_idx)));
-      c += w;
-    }
-    s_cb[np] = c;
-  }
-  __syncthreads();
-  const int kt = s_cb[np];
-  // Small targets (both sides <= 32, the common leaf-level update) work in
-  // shared memory on the dense m x n sum itself: its SVD is the core's, no
-  // QR of the two sides is needed. Others gather into scratch and reduce the
-  // sides by Householder QR first.
-  const int K2 = kt > 32 ? kt : 32;
-  const bool small = m <= 32 && n <= 32 &&
-                     (m + n) * kt + m * n + 32 * 32 + 4 * K2 <= Cx<T2>::SMEM;
-  T2* S = small ? sm : (t.a >= 0 ? reinterpret_cast<T2*>(a.big_scratch) + t.a : slot);
-  T2* SA = S;
-  T2* SB = S + m * kt;
-  T2* C = SB + n * kt;  // the Jacobi matrix X (p x q): the core, or the dense sum
-  T2* V = C + (small ? m * n : (int64_t)kt * kt);  // q x q
-  T2* hA = V + (small ? 32 * 32 : (int64_t)kt * kt);
-  T2* hB = hA + K2;
-  R* sig = reinterpret_cast<R*>(hB + K2);  // K2 singular values, then K2 marks
-  R* mark = sig + K2;
-  T2* Ao = arena + t.c;
-  T2* Bo = arena + t.b;
-  if (kt == 0 || m == 0 || n == 0) {
-    for (int64_t e = threadIdx.x; e < m * kc; e += HX_THREADS) stA(Ao + e, cz<T2>());
-    for (int64_t e = threadIdx.x; e < n * kc; e += HX_THREADS) stA(Bo + e, cz<T2>());
-    return;
-  }
-  // gather both sides (placements, zeros elsewhere)
-  for (int p = 0; p < np; p++) {
-    const HluTruncPair pp = P[p];
-    const int c0 = s_cb[p], w = s_cb[p + 1] - c0;
-    const bool na = pp.neg & 1, nb = pp.neg & 2;
-    for (int64_t e = threadIdx.x; e < m * w; e += HX_THREADS) {
-      const int64_t r = e % m;
-      const int l = (int)(e / m);
-      T2 v = cz<T2>();
-      const int64_t rr = r - pp.ra;
-      if (rr >= 0 && rr < pp.ma) {
-        if (pp.akind == 1) v = rr == l ? Cx<T2>::mk(1, 0) : cz<T2>();
-        else v = piece_get<T2>(a, pp.akind, pp.aoff, pp.soff, pp.ars, pp.acs, rr, l);
-        if (na) v = cneg(v);
-      }
-      SA[r + (int64_t)(c0 + l) * m] = v;
-    }
-    for (int64_t e = threadIdx.x; e < n * w; e += HX_THREADS) {
-      const int64_t r = e % n;
-      const int l = (int)(e / n);
-      T2 v = cz<T2>();
-      const int64_t rr = r - pp.rb;
-      if (rr >= 0 && rr < pp.mb) {
-        if (pp.bkind == 1) v = rr == l ? Cx<T2>::mk(1, 0) : cz<T2>();
-        else v = piece_get<T2>(a, pp.bkind, pp.boff, 0, pp.brs, pp.bcs, rr, l);
-        if (nb) v = cneg(v);
-      }
-      SB[r + (int64_t)(c0 + l) * n] = v;
-    }
-  }
-  __syncthreads();
-  if (!small) {
-    house_qr(SA, m, kt, hA);
-    house_qr(SB, n, kt, hB);
-  }
-  // core = R_A R_B^T (pa x pb; R entries (r, l) with r <= l), or for small
-  // targets the whole sum A B^T (m x n)
-  const int pa = small ? (int)m : (int)(m < kt ? m : (int64_t)kt);
-  const int pb = small ? (int)n : (int)(n < kt ? n : (int64_t)kt);
-  const bool tr = pa < pb;  // Jacobi on the orientation with fewer columns
-  const int p = tr ? pb : pa, q = tr ? pa : pb;
-  T2* X = C;  // p x q
-  for (int e = threadIdx.x; e < pa * pb; e += HX_THREADS) {
-    const int r = e % pa, c = e / pa;
-    T2 acc = cz<T2>();
-    for (int l = small ? 0 : max(r, c); l < kt; l++)
-      acc = cadd(acc, cmul(SA[r + (int64_t)l * m], SB[c + (int64_t)l * n]));
-    if (tr) X[c + r * p] = acc;  // X = core^T
-    else X[r + c * p] = acc;
-  }
-  for (int e = threadIdx.x; e < q * q; e += HX_THREADS) V[e] = (e % q == e / q) ? Cx<T2>::mk(1, 0) : cz<T2>();
-  __syncthreads();
-  // one-sided Jacobi on the q columns of X: X V = U diag(s). Rotations keep
-  // the Frobenius norm, so one floor for the whole run decides which columns
-  // are noise.
+  for (int e = threadIdx.x; e < q * q; e += HX_THREADS)
+    V[e] = (e % q == e / q) ? Cx<T2>::mk(1, 0) : cz<T2>();
   R fro = 0;
   for (int e = threadIdx.x; e < p * q; e += HX_THREADS) fro += cabs2(X[e]);
   const R floor2 = block_sum(fro, red) * Cx<T2>::jacobi_floor();
@@ -703,7 +616,17 @@ __device__ void task_trunc(const HluTask& t, const HluExecArgs& a, T2* arena, T2
     __syncthreads();
     if (done) break;
   }
-  // singular values, the rank of the truncation (minRankforError with a cap)
+}
+
+// Singular values of the rotated columns (sig, q values) and the kept ones,
+// largest first (idx, returned count): minRankforError with the cap kc and,
+// for tol > 0, the tail relative to the sum of the squared singular values
+template <typename T2>
+__device__ int pick_rank(const T2* X, int p, int q, typename Cx<T2>::R* sig,
+                         typename Cx<T2>::R* mark, int kc, double tol, int* idx) {
+  using R = typename Cx<T2>::R;
+  __shared__ int s_r;
+  const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
   for (int j = w; j < q; j += HX_WARPS) {
     R s2 = 0;
     for (int i = ln; i < p; i += 32) s2 += cabs2(X[i + (int64_t)j * p]);
@@ -720,20 +643,240 @@ __device__ void task_trunc(const HluTask& t, const HluExecArgs& a, T2* arena, T2
     const int rmax = min(kc, q);
     int r = 0;
     R kept = 0;
-    while (r < rmax) {  // largest first
+    while (r < rmax) {
       int bj = -1;
       for (int j = 0; j < q; j++)
         if (mark[j] == R(0) && (bj < 0 || sig[j] > sig[bj])) bj = j;
       if (bj < 0 || !(sig[bj] > 0)) break;
       mark[bj] = 1;
-      s_idx[r++] = bj;
+      idx[r++] = bj;
       kept += sig[bj] * sig[bj];
-      if (a.tol > 0 && full > 0 && (full - kept) / full < R(a.tol * a.tol)) break;
+      if (tol > 0 && full > 0 && (full - kept) / full < R(tol * tol)) break;
     }
     s_r = r;
   }
   __syncthreads();
   const int r = s_r;
+  __syncthreads();
+  return r;
+}
+
+// seeded value in [-1, 1] of the randomized range finder's test matrix
+__device__ __forceinline__ float rnd_pm1(int64_t j, int c) {
+  const uint64_t h = pivot_hash(0x5DEECE66Dull, (uint64_t)j, (uint64_t)c);
+  return (float)((double)(h >> 11) * (2.0 / 9007199254740992.0) - 1.0);
+}
+
+// T (kt x L) = op(S)^T Y with S (rows x kt), Y (rows x L) in scratch
+// (column-major); conj_s: conj(S); omega: Y is the seeded test matrix. A warp
+// per entry, lanes over the rows.
+template <typename T2>
+__device__ void mm_ty(const T2* S, int64_t rows, int kt, const T2* Y, int L, T2* T, bool conj_s,
+                      bool omega) {
+  using R = typename Cx<T2>::R;
+  const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  for (int o = w; o < kt * L; o += HX_WARPS) {
+    const int l = o % kt, c = o / kt;
+    const T2* sc = S + (int64_t)l * rows;
+    R sr = 0, si = 0;
+    for (int64_t i = ln; i < rows; i += 32) {
+      const T2 sv = conj_s ? cconj(sc[i]) : sc[i];
+      const T2 yv = omega ? Cx<T2>::mk((R)rnd_pm1(i, c), 0) : Y[i + (int64_t)c * rows];
+      const T2 pr = cmul(sv, yv);
+      sr += pr.x;
+      si += pr.y;
+    }
+    sr = warp_sum(sr);
+    si = warp_sum(si);
+    if (ln == 0) T[l + (int64_t)c * kt] = Cx<T2>::mk(sr, si);
+  }
+  __syncthreads();
+}
+// Y (rows x L) = op(S) T with S (rows x kt), T (kt x L)
+template <typename T2>
+__device__ void mm_st(const T2* S, int64_t rows, int kt, const T2* T, int L, T2* Y, bool conj_s) {
+  for (int64_t e = threadIdx.x; e < rows * L; e += HX_THREADS) {
+    const int64_t i = e % rows;
+    const int c = (int)(e / rows);
+    T2 acc = cz<T2>();
+    for (int l = 0; l < kt; l++) {
+      const T2 sv = S[i + (int64_t)l * rows];
+      acc = cadd(acc, cmul(conj_s ? cconj(sv) : sv, T[l + (int64_t)c * kt]));
+    }
+    Y[e] = acc;
+  }
+  __syncthreads();
+}
+// Q (rows x L) := orthonormal basis of the columns of Y (Householder; Y is
+// overwritten by the reflectors)
+template <typename T2>
+__device__ void orth(T2* Y, int64_t rows, int L, T2* head, T2* Q) {
+  house_qr(Y, rows, L, head);
+  for (int64_t e = threadIdx.x; e < rows * L; e += HX_THREADS)
+    Q[e] = (e % rows == e / rows) ? Cx<T2>::mk(1, 0) : cz<T2>();
+  __syncthreads();
+  house_apply<T2, false>(Y, rows, L, head, Q, rows, L);
+}
+
+template <typename T2>
+__device__ void task_trunc(const HluTask& t, const HluExecArgs& a, T2* arena, T2* slot, T2* sm) {
+  using R = typename Cx<T2>::R;
+  __shared__ int s_cb[HX_MAX_PAIRS + 1];
+  __shared__ R red[HX_WARPS + 8];
+  __shared__ int s_idx[64];
+  const int64_t m = t.m, n = t.n;
+  const int kc = a.kc;
+  const HluTruncPair* P = a.pairs + t.x0;
+  const int np = t.x1;
+  if (threadIdx.x == 0) {
+    int c = 0;
+    for (int p = 0; p < np; p++) {
+      s_cb[p] = c;
+      int w = P[p].cols;
+      if (P[p].rank_idx >= 0) w = min(w, max(0, __ldg(a.rank + P[p].rank_idx)));
+      c += w;
+    }
+    s_cb[np] = c;
+  }
+  __syncthreads();
+  const int kt = s_cb[np];
+  T2* Ao = arena + t.c;
+  T2* Bo = arena + t.b;
+  if (kt == 0 || m == 0 || n == 0) {
+    for (int64_t e = threadIdx.x; e < m * kc; e += HX_THREADS) stA(Ao + e, cz<T2>());
+    for (int64_t e = threadIdx.x; e < n * kc; e += HX_THREADS) stA(Bo + e, cz<T2>());
+    return;
+  }
+  // Three ways to the truncated SVD of A B^T (A = [A_1 ..], B = [B_1 ..]):
+  //  small  -- both sides <= 32 (the common leaf-level update): the dense
+  //            m x n sum in shared memory, Jacobi on it directly;
+  //  range  -- a small rank (kc <= 8, no tolerance) of a wide sum: a seeded
+  //            randomized range finder with one power iteration on L = kc + 6
+  //            columns (Halko, Martinsson, Tropp 2011), then the SVD of the
+  //            L x n projection;
+  //  qr     -- otherwise: Householder QR of both sides, Jacobi on the core
+  //            R_A R_B^T, the reflectors applied to the kept vectors.
+  const int K2 = kt > 32 ? kt : 32;
+  const bool small = m <= 32 && n <= 32 &&
+                     (m + n) * kt + m * n + 32 * 32 + 4 * K2 <= Cx<T2>::SMEM;
+  const int L = kc + 6;
+  const bool range = !small && kc <= 8 && !(a.tol > 0) && kt > L && m > L && n > L;
+  T2* S = small ? sm : (t.a >= 0 ? reinterpret_cast<T2*>(a.big_scratch) + t.a : slot);
+  T2* SA = S;
+  T2* SB = S + m * kt;
+  T2* W = SB + n * kt;  // work area of the chosen path
+  // gather both sides (placements, zeros elsewhere)
+  for (int p = 0; p < np; p++) {
+    const HluTruncPair pp = P[p];
+    const int c0 = s_cb[p], w = s_cb[p + 1] - c0;
+    const bool na = pp.neg & 1, nb = pp.neg & 2;
+    for (int64_t e = threadIdx.x; e < m * w; e += HX_THREADS) {
+      const int64_t r = e % m;
+      const int l = (int)(e / m);
+      T2 v = cz<T2>();
+      const int64_t rr = r - pp.ra;
+      if (rr >= 0 && rr < pp.ma) {
+        if (pp.akind == 1) v = rr == l ? Cx<T2>::mk(1, 0) : cz<T2>();
+        else v = piece_get<T2>(a, pp.akind, pp.aoff, pp.soff, pp.ars, pp.acs, rr, l);
+        if (na) v = cneg(v);
+      }
+      SA[r + (int64_t)(c0 + l) * m] = v;
+    }
+    for (int64_t e = threadIdx.x; e < n * w; e += HX_THREADS) {
+      const int64_t r = e % n;
+      const int l = (int)(e / n);
+      T2 v = cz<T2>();
+      const int64_t rr = r - pp.rb;
+      if (rr >= 0 && rr < pp.mb) {
+        if (pp.bkind == 1) v = rr == l ? Cx<T2>::mk(1, 0) : cz<T2>();
+        else v = piece_get<T2>(a, pp.bkind, pp.boff, 0, pp.brs, pp.bcs, rr, l);
+        if (nb) v = cneg(v);
+      }
+      SB[r + (int64_t)(c0 + l) * n] = v;
+    }
+  }
+  __syncthreads();
+
+  if (range) {
+    T2* Y = W;            // m x L
+    T2* Q = Y + m * L;    // m x L
+    T2* Z = Q + m * L;    // n x L
+    T2* Zq = Z + n * L;   // n x L
+    T2* T = Zq + n * L;   // kt x L
+    T2* V = T + (int64_t)kt * L;  // L x L
+    T2* hd = V + L * L;   // L
+    R* sig = reinterpret_cast<R*>(hd + L);
+    R* mark = sig + L;
+    // Y = M Omega with M = A B^T, then one power iteration Y = M M^H Y
+    mm_ty(SB, n, kt, (const T2*)nullptr, L, T, false, true);  // T = B^T Omega
+    mm_st(SA, m, kt, T, L, Y, false);                         // Y = A T
+    orth(Y, m, L, hd, Q);
+    mm_ty(SA, m, kt, Q, L, T, true, false);                   // T = A^H Q
+    mm_st(SB, n, kt, T, L, Z, true);                          // Z = conj(B) T = M^H Q
+    orth(Z, n, L, hd, Zq);
+    mm_ty(SB, n, kt, Zq, L, T, false, false);                 // T = B^T Zq
+    mm_st(SA, m, kt, T, L, Y, false);                         // Y = M Zq
+    orth(Y, m, L, hd, Q);
+    // the projection's transpose (Q^H M)^T = M^T conj(Q) = B conj(A^H Q)
+    // (n x L); its SVD Z V = U S gives M ~ Q conj(V) S U^T
+    mm_ty(SA, m, kt, Q, L, T, true, false);
+    for (int o = threadIdx.x; o < kt * L; o += HX_THREADS) T[o] = cconj(T[o]);
+    __syncthreads();
+    mm_st(SB, n, kt, T, L, Z, false);
+    jacobi_cols(Z, (int)n, L, V, red);
+    const int r = pick_rank(Z, (int)n, L, sig, mark, kc, 0.0, s_idx);
+    for (int64_t e = threadIdx.x; e < m * kc; e += HX_THREADS) {  // A' = Q conj(V) S
+      const int64_t i = e % m;
+      const int l = (int)(e / m);
+      T2 v = cz<T2>();
+      if (l < r) {
+        const int j = s_idx[l];
+        for (int c = 0; c < L; c++) v = cadd(v, cmul(Q[i + (int64_t)c * m], cconj(V[c + j * L])));
+        v = cscale(v, sig[j]);
+      }
+      stA(Ao + e, v);
+    }
+    for (int64_t e = threadIdx.x; e < n * kc; e += HX_THREADS) {  // B' = U
+      const int64_t i = e % n;
+      const int l = (int)(e / n);
+      T2 v = cz<T2>();
+      if (l < r) {
+        const int j = s_idx[l];
+        v = cscale(Z[i + (int64_t)j * n], R(1) / sig[j]);
+      }
+      stA(Bo + e, v);
+    }
+    return;
+  }
+
+  T2* hA = W;
+  T2* hB = hA + K2;
+  R* sig = reinterpret_cast<R*>(hB + K2);  // K2 singular values, then K2 marks
+  R* mark = sig + K2;
+  T2* C = hB + 2 * K2;  // the Jacobi matrix X (p x q): the core, or the dense sum
+  T2* V = C + (small ? m * n : (int64_t)kt * kt);  // q x q
+  if (!small) {
+    house_qr(SA, m, kt, hA);
+    house_qr(SB, n, kt, hB);
+  }
+  // core = R_A R_B^T (pa x pb; R entries (r, l) with r <= l), or for small
+  // targets the whole sum A B^T (m x n)
+  const int pa = small ? (int)m : (int)(m < kt ? m : (int64_t)kt);
+  const int pb = small ? (int)n : (int)(n < kt ? n : (int64_t)kt);
+  const bool tr = pa < pb;  // Jacobi on the orientation with fewer columns
+  const int p = tr ? pb : pa, q = tr ? pa : pb;
+  T2* X = C;  // p x q
+  for (int e = threadIdx.x; e < pa * pb; e += HX_THREADS) {
+    const int r = e % pa, c = e / pa;
+    T2 acc = cz<T2>();
+    for (int l = small ? 0 : max(r, c); l < kt; l++)
+      acc = cadd(acc, cmul(SA[r + (int64_t)l * m], SB[c + (int64_t)l * n]));
+    if (tr) X[c + r * p] = acc;  // X = core^T
+    else X[r + c * p] = acc;
+  }
+  __syncthreads();
+  jacobi_cols(X, p, q, V, red);
+  const int r = pick_rank(X, p, q, sig, mark, kc, a.tol, s_idx);
   // top rows of the outputs: A' = [W S; 0], B' = [conj(Z); 0] (hlu rk_truncate)
   for (int64_t e = threadIdx.x; e < m * kc; e += HX_THREADS) {
     const int64_t i = e % m;

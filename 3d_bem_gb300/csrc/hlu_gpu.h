@@ -58,10 +58,14 @@ constexpr int HOP_N = 0, HOP_T = 1, HOP_C = 2;
 constexpr int HF_ACC = 16, HF_NEG = 32;
 constexpr int HF_SRC_SHIFT = 8;
 
-// A truncation's scratch: A and B gathered (m x kt, n x kt), the core and the
-// Jacobi rotations (kt x kt each), reflector heads and singular values.
+// A truncation's scratch: A and B gathered (m x kt, n x kt), then either the
+// QR path's reflector heads, singular values, core and Jacobi rotations, or
+// the range finder's panels (m x L and n x L twice, kt x L, L x L; L <= 14).
 inline int64_t trunc_scratch(int64_t m, int64_t n, int64_t kt) {
-  return (m + n) * kt + 2 * kt * kt + 4 * kt + 64;
+  const int64_t k2 = kt > 32 ? kt : 32, L = 14;
+  const int64_t qr = 3 * k2 + 2 * kt * kt;
+  const int64_t rng = 2 * (m + n) * L + kt * L + L * L + 2 * L;
+  return (m + n) * kt + (qr > rng ? qr : rng) + 64;
 }
 // truncations up to this many complex elements of scratch use their CTA's slot
 constexpr int64_t HLU_CTA_SCRATCH = int64_t(1) << 16;

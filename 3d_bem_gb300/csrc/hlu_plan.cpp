@@ -237,7 +237,7 @@ class Planner {
     t.c = C.off;
     t.ldc = C.ld;
     emit(t, {acc(A, 1), acc(B, 1), acc(C, accumulate ? 3 : 2)},
-         1.0 + (double)m * n * q / 4096.0);
+         6.0 + (double)m * n * q / 2048.0);
   }
   void zero(const View& C) {
     if (C.rows == 0 || C.cols == 0) return;
@@ -247,7 +247,7 @@ class Planner {
     t.n = (int32_t)C.cols;
     t.c = C.off;
     t.ldc = C.ld;
-    emit(t, {acc(C, 2)}, 0.5 + (double)C.rows * C.cols / 65536.0);
+    emit(t, {acc(C, 2)}, 1.0 + (double)C.rows * C.cols / 65536.0);
   }
   // X (rows x p) := op(M) X, M = rows x rows (in place)
   void lmul(const View& X, const View& M, int op) {
@@ -262,7 +262,7 @@ class Planner {
     t.lda = M.ld;
     t.c = X.off;
     t.ldc = X.ld;
-    emit(t, {acc(M, 1), acc(X, 3)}, 1.0 + (double)X.rows * X.rows * X.cols / 4096.0);
+    emit(t, {acc(M, 1), acc(X, 3)}, 2.5 + (double)X.rows * X.rows * X.cols / 4096.0);
   }
   // X (p x cols) := X op(M), M = cols x cols (in place)
   void rmul(const View& X, const View& M, int op) {
@@ -277,7 +277,7 @@ class Planner {
     t.lda = M.ld;
     t.c = X.off;
     t.ldc = X.ld;
-    emit(t, {acc(M, 1), acc(X, 3)}, 1.0 + (double)X.rows * X.cols * X.cols / 4096.0);
+    emit(t, {acc(M, 1), acc(X, 3)}, 2.5 + (double)X.rows * X.cols * X.cols / 4096.0);
   }
 
   // ---- structure ----
@@ -369,7 +369,7 @@ class Planner {
     t.lda = (int32_t)nd.m;
     t.c = nd.F.off;
     t.ldc = nd.F.ld;
-    emit(t, {acc(nd.F, 2)}, 0.5 + (double)nd.m * nd.n / 65536.0);
+    emit(t, {acc(nd.F, 2)}, 2.5 + (double)nd.m * nd.n / 65536.0);
   }
   void load_far(size_t bi, SNode& nd) {
     near_index(bi);
@@ -393,6 +393,17 @@ class Planner {
     p.cols = fb.kcap;
     p.rank_idx = (int32_t)fi;
     trunc_out(nd.A, nd.B, nd.m, nd.n, {p}, {}, fb.kcap);
+  }
+
+  // model cost (microseconds) of a truncation, by the executor's path: the
+  // dense sum of a small target, the range finder for a small rank of a wide
+  // sum, Householder QR otherwise (fitted to traced factorizations; it only
+  // orders the claims)
+  double trunc_cost(int64_t m, int64_t n, int64_t kt) const {
+    if (m <= 32 && n <= 32) return 60.0 + 0.2 * (double)kt * (m < n ? m : n);
+    if (kc_ <= 8 && kt > kc_ + 6 && m > kc_ + 6 && n > kc_ + 6)
+      return 150.0 + (double)(m + n) * kt / 50.0;
+    return 100.0 + (double)(m + n) * kt * kt / 4096.0;
   }
 
   // TRUNC task writing A' (m x kc at Ao), B' (n x kc at Bo)
@@ -424,7 +435,7 @@ class Planner {
       t.a = P_.big_scratch;
       P_.big_scratch += (sc + 31) / 32 * 32;
     }
-    emit_v(t, a, 4.0 + (double)(m + n) * kt * kt / 2048.0 + (double)kt * kt * kt / 512.0);
+    emit_v(t, a, trunc_cost(m, n, kt));
   }
 
   // ---- H-matrix times panel ----
@@ -672,7 +683,7 @@ class Planner {
           t.lda = d.ld;
           t.c = C.F.off;
           t.ldc = C.F.ld;
-          emit(t, {acc(d, 1), acc(C.F, 3)}, 0.5 + (double)C.m * C.n / 65536.0);
+          emit(t, {acc(d, 1), acc(C.F, 3)}, 2.5 + (double)C.m * C.n / 65536.0);
         } else {
           for (const Piece& pc : P.pieces)
             gemm(C.F, pc.a.sub(ro, 0, C.m, pc.width), HOP_N, pc.b.sub(co, 0, C.n, pc.width),
@@ -785,7 +796,7 @@ class Planner {
       t.a = A.F.off;
       t.lda = A.F.ld;
       P_.qr.push_back(q);
-      emit(t, {acc(A.F, 1), acc(L.F, 2), acc(U.F, 2), acc(ri, 2)}, 6.0 + A.m * 0.2);
+      emit(t, {acc(A.F, 1), acc(L.F, 2), acc(U.F, 2), acc(ri, 2)}, 60.0);
       return;
     }
     const HCluster &R = t_.c[A.rc], &C = t_.c[A.cc];

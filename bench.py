@@ -537,11 +537,13 @@ def run_ours(args):
     value = ws * K / (ms / 1e3)
 
     # end to end through bem_solve: pinned host g in, host p out, every step
-    gh = torch.from_numpy(np.asfortranarray(g_host)).pin_memory()
+    # pinned (R x n) rows = the n x R column-major layout bem_solve reads
+    gh = torch.from_numpy(np.ascontiguousarray(g_host.T)).pin_memory()
+    gpin = gh.numpy().T
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for f in fr_t:
-        s.solve(f, gh.numpy(), want=("p",))
+        s.solve(f, gpin, want=("p",))
     torch.cuda.synchronize()
     e2e = ws * K / (time.perf_counter() - t0)
 

@@ -67,9 +67,10 @@ print("SMALL", info["status"], bool(np.isfinite(p).all()))
 
 def test_aca_vanishing_residual(bem):
     """Column points within 1e-9 of one location: every admissible block has
-    numerical rank 2 at most, the next ACA step finds a residual at rounding
-    level and stops (no division by a vanishing pivot); the H-matvec equals
-    the dense product."""
+    numerical rank 4 at most (the point and the first-order terms of the
+    three jitter directions), so the next ACA step finds a residual at
+    rounding level and stops there (no division by a vanishing pivot); the
+    H-matvec equals the dense product."""
     rng = np.random.default_rng(3)
     rows = rng.uniform(-1, 1, (300, 3))
     cols = np.tile(np.array([[5.0, 0.3, -0.2]]), (200, 1)) + 1e-9 * rng.standard_normal((200, 3))
@@ -79,7 +80,7 @@ def test_aca_vanishing_residual(bem):
     ranks = s.ranks(0)
     info = s.partition()
     far = info[:, 4] == 1
-    assert far.any() and ranks[far].max() <= 3
+    assert far.any() and ranks[far].max() <= 4
     x = rng.standard_normal(200) + 1j * rng.standard_normal(200)
     y = s.hmatvec(0, x)
     R = rows[rp][:, None, :] - cols[cp][None, :, :]
