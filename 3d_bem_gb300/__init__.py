@@ -65,7 +65,8 @@ class Config(ct.Structure):
                 ("precond_rank", ct.c_int64), ("precond_tol", ct.c_double),
                 ("recompress_tol", ct.c_double), ("selector_guard", ct.c_double),
                 ("sweep_workers", ct.c_int64), ("aca_big_mn", ct.c_int64),
-                ("precond_reuse", ct.c_double), ("hlu_device", ct.c_int32)]
+                ("precond_reuse", ct.c_double), ("hlu_device", ct.c_int32),
+                ("near_fp64", ct.c_int32)]
 
 
 class SolveInfo(ct.Structure):

@@ -147,9 +147,14 @@ struct HmvArgs {
   const int2* vwork;
   int64_t nvwork;
   HmvGate gate;  // null f: always run
+  // two-float products only: remainders of the near-field entries (F + Flo
+  // = the FP64 entries), null when the pool holds FP32-computed entries
+  const void* Flo = nullptr;
 };
 
 void nearfield_upload_rules(const QuadRules& r, cudaStream_t s);
+// hi = (float) v, lo = (float) (v - hi) for n complex values
+void launch_split_twofloat(const double2* v, float2* hi, float2* lo, int64_t n, cudaStream_t s);
 void aca_upload_rules(const QuadRules& r, cudaStream_t s);
 void launch_nearfield(const NearfieldArgs& a, cudaStream_t s);
 void launch_operators(const Elem* E, const int64_t* rows, const int64_t* cols, int64_t count,

@@ -106,6 +106,8 @@ struct DBuf {
 // complex FP64 (16 bytes) or complex FP32 (8 bytes) per the precision mode.
 struct DevHM {
   DBuf<unsigned char> F, U, V, S;
+  DBuf<float2> Flo;      // near_fp64: remainders of the FP64 near-field entries
+  bool has_lo = false;
   DBuf<int32_t> rank, flags;
   std::vector<int32_t> h_rank, h_flags;
   DBuf<int2> vwork;  // H-matvec pass-V work items (block, first row)
@@ -206,6 +208,7 @@ struct bem_handle {
   DBuf<unsigned char> dfPre, dfFin;
   DBuf<int> dfCtrl, dfErr;
   DBuf<int> dBad;
+  DBuf<double2> dNear64[2];  // near_fp64: FP64 near field before the split
   // GPU H-LU factorization (hlu_gpu.h): the task program of the current
   // layout and rank, its device tables, the arena holding the factors, and
   // the truncation scratch
@@ -593,7 +596,17 @@ void assemble(bem_handle* h, double freq, double* t_near, double* t_aca) {
   CK(cudaStreamWaitEvent(ns, h->ev[0], 0));
   // the learned near-field orders were trained on free-space pairs: with an
   // impedance plane the near field keeps the 16-point rule
-  const bool learned = (h->cfg.selector & 1) && na.precision == 1 && !h->have_plane;
+  const bool fp64_near = na.precision == 1 && h->cfg.near_fp64;
+  const bool learned = (h->cfg.selector & 1) && na.precision == 1 && !h->have_plane && !fp64_near;
+  for (auto& m : h->hm) m.has_lo = false;
+  if (fp64_near) {  // FP64 quadrature into temporaries, split into hi + lo below
+    h->dNear64[0].ensure(std::max<int64_t>(h->L.near_entries, 1));
+    h->dNear64[1].ensure(std::max<int64_t>(h->L.near_entries, 1));
+    for (auto& m : h->hm) m.Flo.ensure(std::max<int64_t>(h->L.near_entries, 1));
+    na.precision = 0;
+    na.phi = h->dNear64[0].p;
+    na.dphi = h->dNear64[1].p;
+  }
   if (learned) {
     require(h->have_selector, BEM_EINVAL, "selector weights not set (bem_set_selector)");
     h->dCls.ensure(h->L.near_entries);
@@ -631,6 +644,14 @@ void assemble(bem_handle* h, double freq, double* t_near, double* t_aca) {
   }
   launch_nearfield(na, ns);
   h->launches += (na.ntiles > 0) + (na.nspecial > 0);
+  if (fp64_near) {
+    for (int q = 0; q < 2; q++) {
+      launch_split_twofloat(h->dNear64[q].p, (float2*)h->hm[q].F.p, h->hm[q].Flo.p,
+                            h->L.near_entries, ns);
+      h->hm[q].has_lo = true;
+    }
+    h->launches += 2 * (h->L.near_entries > 0);
+  }
   if (learned)
     CK(cudaMemcpyAsync(h->sel_stats, h->dSelCnt.p, 3 * sizeof(unsigned long long),
                        cudaMemcpyDeviceToHost, ns));
@@ -719,6 +740,7 @@ void hmatvec_dev(bem_handle* h, int which, const double2* x, double2* y, int64_t
     a.tf = h->dTf.p;
     a.vwork = m.vwork.p;
     a.nvwork = m.nvwork;
+    a.Flo = (arith == ARITH_TWOFLOAT && m.has_lo) ? m.Flo.p : nullptr;
     if (gate_flags) a.gate = HmvGate{gate_flags + r0 * GATE_STRIDE, GATE_STRIDE, (int)a.nrhs};
     h->launches += launch_hmatvec(a, h->stream);
   }
@@ -1754,6 +1776,7 @@ void bem_config_default(bem_config* c) {
   c->aca_big_mn = 0;
   c->precond_reuse = 0.0;
   c->hlu_device = 1;
+  c->near_fp64 = 0;
 }
 
 bem_status bem_create(const bem_config* cfg, bem_handle** out) {
@@ -1782,6 +1805,8 @@ bem_status bem_create(const bem_config* cfg, bem_handle** out) {
             "precond_reuse must be finite and >= 0");
     require(h->cfg.hlu_device == 0 || h->cfg.hlu_device == 1, BEM_EINVAL,
             "hlu_device must be 0 or 1");
+    require(h->cfg.near_fp64 == 0 || h->cfg.near_fp64 == 1, BEM_EINVAL,
+            "near_fp64 must be 0 or 1");
     CK(cudaGetDevice(&h->device));
     CK(cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->device));
     // the near-field stream at the highest priority: its short, FP64-bound
@@ -2712,6 +2737,7 @@ bem_status bem_points_assemble(bem_handle* h, const double* rowpts, int64_t nr,
     h->have_mesh = false;
     h->N = nr;
     h->k = k;
+    for (auto& q : h->hm) q.has_lo = false;  // point clouds: FP64 storage, no remainders
     DevHM& m = h->hm[0];
     alloc_hm(h, m);
     launch_points_nearfield(h->dNear.p, (int64_t)h->L.near.size(), h->dTiles.p,

@@ -572,9 +572,9 @@ __global__ void __launch_bounds__(UT) hmvdf_upass(
     const LeafRows* __restrict__ leaves, const int32_t* __restrict__ list_off,
     const int32_t* __restrict__ list, const FarBlock* __restrict__ far,
     const int32_t* __restrict__ rank, const NearBlock* __restrict__ nearb,
-    const float2* __restrict__ Up, const float2* __restrict__ F, const float4* __restrict__ x,
-    int64_t ldx, const float4* __restrict__ t, int64_t ldt, double2* __restrict__ y,
-    int64_t ldy, int accumulate) {
+    const float2* __restrict__ Up, const float2* __restrict__ F, const float2* __restrict__ Flo,
+    const float4* __restrict__ x, int64_t ldx, const float4* __restrict__ t, int64_t ldt,
+    double2* __restrict__ y, int64_t ldy, int accumulate) {
   __shared__ float4 part[UT / 32][32];
   const LeafRows lf = leaves[blockIdx.x];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -600,11 +600,24 @@ __global__ void __launch_bounds__(UT) hmvdf_upass(
       } else {
         const NearBlock nb = nearb[-code - 1];
         const float2* Fb = F + nb.off + (grow - nb.r0);
-#pragma unroll 2
-        for (int j = 0; j < nb.n; j++) {
-          const float2 f = __ldg(Fb + (int64_t)j * nb.m);
+        if (Flo) {  // FP64 entries as hi + lo
+          const float2* Lb = Flo + nb.off + (grow - nb.r0);
+          for (int j = 0; j < nb.n; j++) {
+            const float2 f = __ldg(Fb + (int64_t)j * nb.m), fl = __ldg(Lb + (int64_t)j * nb.m);
 #pragma unroll
-          for (int r = 0; r < R; r++) acc[r].fma(f, __ldg(x + r * ldx + nb.c0 + j));
+            for (int r = 0; r < R; r++) {
+              const float4 xv = __ldg(x + r * ldx + nb.c0 + j);
+              acc[r].fma(f, xv);
+              acc[r].fma(fl, xv);
+            }
+          }
+        } else {
+#pragma unroll 2
+          for (int j = 0; j < nb.n; j++) {
+            const float2 f = __ldg(Fb + (int64_t)j * nb.m);
+#pragma unroll
+            for (int r = 0; r < R; r++) acc[r].fma(f, __ldg(x + r * ldx + nb.c0 + j));
+          }
         }
       }
     }
@@ -643,7 +656,7 @@ void launchdf_r(const HmvArgs& a, cudaStream_t s) {
   if (a.nleaves > 0)
     hmvdf_upass<R><<<(unsigned)a.nleaves, UT, 0, s>>>(
         a.leaves, a.list_off, a.list, a.far, a.rank, a.nearb, (const float2*)a.U,
-        (const float2*)a.F, xd, a.ldx, td, a.ldt, a.y, a.ldy, a.accumulate);
+        (const float2*)a.F, (const float2*)a.Flo, xd, a.ldx, td, a.ldt, a.y, a.ldy, a.accumulate);
 }
 
 void launchdf(const HmvArgs& a, cudaStream_t s) {

@@ -157,6 +157,23 @@ void launch_points_nearfield(const NearBlock* blocks, int64_t nblocks, const Nea
   if (ntiles > 0) points_nearfield_kernel<<<(unsigned)ntiles, 256, 0, s>>>(blocks, tiles, rp, cp, k, F);
 }
 
+namespace {
+__global__ void split_twofloat_kernel(const double2* __restrict__ v, float2* __restrict__ hi,
+                                      float2* __restrict__ lo, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double2 x = v[i];
+  const float rh = (float)x.x, ih = (float)x.y;
+  hi[i] = make_float2(rh, ih);
+  lo[i] = make_float2((float)(x.x - (double)rh), (float)(x.y - (double)ih));
+}
+}  // namespace
+
+void launch_split_twofloat(const double2* v, float2* hi, float2* lo, int64_t n, cudaStream_t s) {
+  if (n <= 0) return;
+  split_twofloat_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(v, hi, lo, n);
+}
+
 void launch_nearfield(const NearfieldArgs& a, cudaStream_t s) {
   const unsigned g = (unsigned)((a.nspecial + 127) / 128);
   if (a.precision == 0) {

@@ -83,6 +83,13 @@ typedef struct bem_config {
                               program of hlu_gpu.h; needs precond_rank 1..64
                               and leaf_size <= 49, else the host factorization
                               is used); 0: on the host */
+  int32_t near_fp64;       /* mixed precision (precision 1) only: 1 = the near
+                              field is integrated in FP64 and kept as two
+                              floats, the complex-FP32 pool plus its remainder;
+                              the inner FP32 GMRES reads the first, the FP64
+                              refinement residual both (FP64-accurate near
+                              field, for bodies whose hypersingular near field
+                              cancels strongly, e.g. fine meshes at low kh) */
 } bem_config;
 
 typedef struct bem_solve_info {
