@@ -22,6 +22,8 @@
 #include <string>
 #include <thread>
 #include <vector>
+#include <map>
+#include <array>
 
 #include "../../include/bemgpu.h"
 #include "bem_kernels.h"
@@ -1033,7 +1035,7 @@ void upload_df_plans_device(bem_handle* h) {
 // the measured critical path (longest chain of start-to-end times along the
 // dependencies) and the time tasks waited for their dependencies.
 void hlu_trace_summary(const HluProgram& P, const DBuf<unsigned long long>& tr, int grid,
-                       const char* path) {
+                       double tol, const char* path) {
   const size_t nt = P.tasks.size();
   std::vector<unsigned long long> t(3 * nt);
   CK(cudaMemcpy(t.data(), tr.p, t.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
@@ -1087,6 +1089,57 @@ void hlu_trace_summary(const HluProgram& P, const DBuf<unsigned long long>& tr, 
                  "path_n %6lld path_us %10.1f\n", nm[k], (long long)cnt[k], busy[k],
                  cnt[k] ? busy[k] / cnt[k] : 0.0, mx[k], wait[k], (long long)path_cnt[k], path_t[k]);
   std::fprintf(f, "path loads n %lld us %.1f\n", (long long)path_loads, path_load_t);
+  // truncations by the executor's path (column bound q for kt): subspace with
+  // the sides in shared memory / in scratch, dense small, range finder, QR
+  {
+    const char* cn[5] = {"sub_smem", "sub_glob", "small", "range", "qr"};
+    int64_t cc[5] = {}, cp[5] = {};
+    double cb[5] = {}, cpt[5] = {};
+    std::vector<char> on_path(nt, 0);
+    for (int64_t i : chain) on_path[i] = 1;
+    for (size_t i = 0; i < nt; i++) {
+      const HluTask& k = P.tasks[i];
+      if ((k.type & 7) != HT_TRUNC) continue;
+      const int64_t m = k.m, n = k.n, kt = k.q, kc = P.kc;
+      const int64_t subb = hlu_sub_buffers(m, n, kt);
+      int c;
+      if (kc <= 2 && !(tol > 0) && subb <= HLU_SMEM_ELEMS)
+        c = subb + (m + n) * kt <= HLU_SMEM_ELEMS ? 0 : 1;
+      else if (m <= 32 && n <= 32)
+        c = 2;
+      else if (kc <= 8 && !(tol > 0) && kt > kc + 6 && m > kc + 6 && n > kc + 6)
+        c = 3;
+      else
+        c = 4;
+      const double d = 1e-3 * (double)(t[3 * i + 2] - t[3 * i + 1]);
+      cc[c]++;
+      cb[c] += d;
+      if (on_path[i]) {
+        cp[c]++;
+        cpt[c] += d;
+      }
+    }
+    for (int c = 0; c < 5; c++)
+      std::fprintf(f, "trunc %-8s n %9lld busy_us %12.1f avg_us %8.2f path_n %6lld path_us %10.1f\n",
+                   cn[c], (long long)cc[c], cb[c], cc[c] ? cb[c] / cc[c] : 0.0, (long long)cp[c],
+                   cpt[c]);
+  }
+  {  // the most frequent GEMM shapes (m, n, q, ops) with their mean time
+    std::map<std::array<int, 4>, std::pair<int64_t, double>> shp;
+    for (size_t i = 0; i < nt; i++) {
+      const HluTask& k = P.tasks[i];
+      if ((k.type & 7) != HT_GEMM) continue;
+      auto& e = shp[{k.m, k.n, k.q, k.flags & 15}];
+      e.first++;
+      e.second += 1e-3 * (double)(t[3 * i + 2] - t[3 * i + 1]);
+    }
+    std::vector<std::pair<std::array<int, 4>, std::pair<int64_t, double>>> v(shp.begin(), shp.end());
+    std::sort(v.begin(), v.end(), [](const auto& a, const auto& b) { return a.second.second > b.second.second; });
+    for (size_t r = 0; r < std::min<size_t>(12, v.size()); r++)
+      std::fprintf(f, "gemm m %d n %d q %d ops %d n %lld busy_us %.1f avg_us %.2f\n", v[r].first[0],
+                   v[r].first[1], v[r].first[2], v[r].first[3], (long long)v[r].second.first,
+                   v[r].second.second, v[r].second.second / v[r].second.first);
+  }
   std::sort(chain.begin(), chain.end(), [&](int64_t a, int64_t b) {
     return t[3 * a + 2] - t[3 * a + 1] > t[3 * b + 2] - t[3 * b + 1];
   });
@@ -1139,6 +1192,10 @@ bool build_hlu_device(bem_handle* h) {
   a.kc = P.kc;
   a.tol = h->cfg.precond_tol;
   a.wait_cycles = hlu_wait_cycles();
+  {  // power iterations of the truncations' range finder (default 1)
+    const char* e = std::getenv("BEM_HLU_RANGE_POWER");
+    a.range_power = e && *e ? (std::atoi(e) > 0 ? 1 : 0) : 1;
+  }
   // BEM_HLU_TRACE=<file>: per-task timestamps, summarised into the file
   const char* trace_path = std::getenv("BEM_HLU_TRACE");
   DBuf<unsigned long long> trace;
@@ -1156,7 +1213,7 @@ bool build_hlu_device(bem_handle* h) {
   int ctrl[4] = {0, 0, 0, 0};
   CK(cudaMemcpyAsync(ctrl, h->dHCtrl.p, sizeof(ctrl), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
-  if (a.trace) hlu_trace_summary(P, trace, h->hp_grid, trace_path);
+  if (a.trace) hlu_trace_summary(P, trace, h->hp_grid, h->cfg.precond_tol, trace_path);
   if (ctrl[1])
     throw BemError{BEM_ETIMEOUT, "H-LU factorization: a task dependency wait ran out of time"};
   if (ctrl[2] || ctrl[3]) return false;

@@ -31,6 +31,8 @@ struct Cx<float2> {
   static constexpr int SMEM = 6144;  // complex elements of dynamic shared memory
   __device__ static float2 mk(float a, float b) { return make_float2(a, b); }
   __device__ static float sq(float x) { return sqrtf(x); }
+  __device__ static float rsq(float x) { return rsqrtf(x); }
+  __device__ static float div(float a, float b) { return __fdividef(a, b); }
   // orthogonality target of the FP32 rotations: one decade above FP32
   // rounding, where the relative test would otherwise oscillate
   __device__ static float jacobi_thr() { return 1e-5f; }
@@ -45,6 +47,8 @@ struct Cx<double2> {
   static constexpr int SMEM = 6144;
   __device__ static double2 mk(double a, double b) { return make_double2(a, b); }
   __device__ static double sq(double x) { return sqrt(x); }
+  __device__ static double rsq(double x) { return rsqrt(x); }
+  __device__ static double div(double a, double b) { return a / b; }
   __device__ static double jacobi_thr() { return 1e-15; }
   __device__ static double jacobi_floor() { return 1e-30; }
   static constexpr int JACOBI_SWEEPS = 60;
@@ -159,6 +163,41 @@ __device__ void task_gemm(const HluTask& t, T2* arena, T2* sm) {
         T2* c = C + i + (int64_t)j * t.ldc;
         if (accu) v = cadd(ldA(c), v);
         stA(c, v);
+      }
+    }
+    return;
+  }
+  const int ldb_s = q | 1;  // odd: threads on different columns of B hit distinct banks
+  if (m * n <= 4 * HX_THREADS && (int64_t)m * q + (int64_t)ldb_s * n <= Cx<T2>::SMEM) {
+    // small product: both operands staged whole (one round of loads, C's
+    // old values fetched alongside), then up to four outputs per thread
+    T2* sa = sm;          // m x q
+    T2* sb = sm + m * q;  // q x n, leading dimension ldb_s
+    for (int e = tid; e < m * q; e += HX_THREADS) sa[e] = opget(A, opa, e % m, e / m, t.lda);
+    for (int e = tid; e < q * n; e += HX_THREADS) {
+      const int l = e % q, j = e / q;
+      sb[l + j * ldb_s] = opget(B, opb, l, j, t.ldb);
+    }
+    T2 cv[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int o = tid + k * HX_THREADS;
+      cv[k] = (accu && o < m * n) ? ldA(C + o % m + (int64_t)(o / m) * t.ldc) : cz<T2>();
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int o = tid + k * HX_THREADS;
+      if (o < m * n) {
+        const int i = o % m, j = o / m;
+        R ar = 0, ai = 0;
+        for (int l = 0; l < q; l++) {
+          const T2 av = sa[i + l * m], bv = sb[l + j * ldb_s];
+          ar += av.x * bv.x - av.y * bv.y;
+          ai += av.x * bv.y + av.y * bv.x;
+        }
+        const T2 v = Cx<T2>::mk(neg ? cv[k].x - ar : cv[k].x + ar, neg ? cv[k].y - ai : cv[k].y + ai);
+        stA(C + i + (int64_t)j * t.ldc, v);
       }
     }
     return;
@@ -296,81 +335,110 @@ __device__ void task_zero(const HluTask& t, T2* arena) {
 template <typename T2>
 __device__ void task_qr(const HluTask& t, const HluExecArgs& a, T2* arena, T2* sm) {
   using R = typename Cx<T2>::R;
-  const int m = t.m;
-  T2* sA = sm;              // m x m
-  T2* sW = sm + m * m;      // m x m
-  T2* sv = sm + 2 * m * m;  // current reflector, m
+  const int m = t.m, ld = m + 1;  // odd leading dimension
+  T2* sA = sm;               // m x m
+  T2* sW = sA + m * ld;      // m x m
+  T2* sv = sW + m * ld;      // reflectors of steps j (even / odd), 2 x m
+  T2* sd = sv + 2 * m;       // 1 / R(r, r), m
   __shared__ R s_r[4];
   for (int e = threadIdx.x; e < m * m; e += HX_THREADS) {
-    sA[e] = ldA(arena + t.a + (e % m) + (int64_t)(e / m) * t.lda);
-    sW[e] = (e % m == e / m) ? Cx<T2>::mk(1, 0) : cz<T2>();
+    const int i = e % m, j = e / m;
+    sA[i + j * ld] = ldA(arena + t.a + i + (int64_t)j * t.lda);
+    sW[i + j * ld] = i == j ? Cx<T2>::mk(1, 0) : cz<T2>();
   }
+  if (threadIdx.x == 0) s_r[0] = 0;
   __syncthreads();
-  const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  // tpc threads per column (consecutive lanes): rows i = j + sub, j + sub + tpc, ..
+  const int tpc = m <= 32 ? 4 : 2;
+  const int c = threadIdx.x / tpc, sub = threadIdx.x % tpc;
+  const unsigned gmask = ((1u << tpc) - 1u) << ((threadIdx.x & 31) & ~(tpc - 1));  // the group's lanes
+  // reflector of column j from the group holding it (only its lanes call):
+  // v = (x + ph |x| e_j) / |.|
+  auto reflector = [&](int j) {
+    const T2* x = sA + j * ld;
+    R xn2 = 0;
+    for (int i = j + sub; i < m; i += tpc) xn2 += cabs2(x[i]);
+    for (int o = tpc / 2; o > 0; o >>= 1) xn2 += __shfl_xor_sync(gmask, xn2, o, tpc);
+    const T2 x0 = x[j];
+    const R ax2 = cabs2(x0);
+    const R xn = Cx<T2>::sq(xn2);
+    const T2 ph = ax2 > 0 ? cscale(x0, Cx<T2>::rsq(ax2)) : Cx<T2>::mk(1, 0);
+    const T2 v0 = cadd(x0, cscale(ph, xn));
+    const R vn2 = xn2 - ax2 + cabs2(v0);
+    const R inv = vn2 > 0 ? Cx<T2>::rsq(vn2) : R(0);
+    T2* v = sv + (j & 1) * m;
+    for (int i = j + sub; i < m; i += tpc) v[i] = cscale(i == j ? v0 : x[i], inv);
+  };
+  if (c == 0) reflector(0);
+  __syncthreads();
   for (int j = 0; j < m; j++) {
-    if (w == 0) {
-      R xn2 = 0;
-      for (int i = j + ln; i < m; i += 32) xn2 += cabs2(sA[i + j * m]);
-      xn2 = warp_sum(xn2);
-      const R xn = Cx<T2>::sq(xn2);
-      const T2 x0 = sA[j + j * m];
-      const R ax0 = Cx<T2>::sq(cabs2(x0));
-      const T2 ph = ax0 > 0 ? cscale(x0, R(1) / ax0) : Cx<T2>::mk(1, 0);
-      const T2 v0 = cadd(x0, cscale(ph, xn));
-      const R vn2 = xn2 - cabs2(x0) + cabs2(v0);
-      const R inv = vn2 > 0 ? R(1) / Cx<T2>::sq(vn2) : R(0);
-      for (int i = j + ln; i < m; i += 32) sv[i] = cscale(i == j ? v0 : sA[i + j * m], inv);
-    }
-    __syncthreads();
-    // apply H_j to columns j.. of A and to all columns of W (rows j..m-1)
-    for (int c = w; c < 2 * m - j; c += HX_WARPS) {
-      T2* y = c < m - j ? sA + (j + c) * m : sW + (c - (m - j)) * m;
-      R dr = 0, di = 0;
-      for (int i = j + ln; i < m; i += 32) {
-        const T2 p = cmulc(sv[i], y[i]);
+    // H_j = I - 2 v v^H on columns j.. of A and all columns of W (rows j..);
+    // the group of A's column j + 1 then forms the next reflector
+    const T2* v = sv + (j & 1) * m;
+    const bool act = c < 2 * m - j;
+    T2* y = c < m - j ? sA + (j + c) * ld : sW + (c - (m - j)) * ld;
+    R dr = 0, di = 0;
+    if (act)
+      for (int i = j + sub; i < m; i += tpc) {
+        const T2 p = cmulc(v[i], y[i]);
         dr += p.x;
         di += p.y;
       }
-      dr = warp_sum(dr);
-      di = warp_sum(di);
-      const T2 d2 = Cx<T2>::mk(2 * dr, 2 * di);
-      for (int i = j + ln; i < m; i += 32) y[i] = csub(y[i], cmul(sv[i], d2));
+    for (int o = tpc / 2; o > 0; o >>= 1) {
+      dr += __shfl_xor_sync(0xffffffffu, dr, o, tpc);
+      di += __shfl_xor_sync(0xffffffffu, di, o, tpc);
     }
+    if (act) {
+      const T2 d2 = Cx<T2>::mk(2 * dr, 2 * di);
+      for (int i = j + sub; i < m; i += tpc) y[i] = csub(y[i], cmul(v[i], d2));
+    }
+    __syncwarp();
+    if (c == 1 && j + 1 < m) reflector(j + 1);
     __syncthreads();
   }
   const HluQrOut o = a.qr[t.x0];
   // Q = W^H, Q^H row-major = W column-major read by rows: Qh[r m + c] = W(r, c)
   for (int e = threadIdx.x; e < m * m; e += HX_THREADS) {
     const int i = e % m, j = e / m;
-    stA(arena + o.q + e, cconj(sW[j + i * m]));         // Q(i, j) = conj(W(j, i))
-    stA(arena + o.qh + (int64_t)i * m + j, sW[i + j * m]);  // Q^H(i, j) = W(i, j)
-    stA(arena + o.r + e, i <= j ? sA[e] : cz<T2>());
+    stA(arena + o.q + e, cconj(sW[j + i * ld]));          // Q(i, j) = conj(W(j, i))
+    stA(arena + o.qh + (int64_t)i * m + j, sW[i + j * ld]);  // Q^H(i, j) = W(i, j)
+    stA(arena + o.r + e, i <= j ? sA[i + j * ld] : cz<T2>());
   }
-  // R^{-1} row-major, one thread per column t: R y = e_t
-  if (threadIdx.x == 0) s_r[0] = 0;
-  __syncthreads();
-  if (threadIdx.x < m) {
-    const int tc = threadIdx.x;
-    T2* y = sW + tc * m;  // W no longer needed: column tc as scratch
-    bool bad = false;
-    for (int r = m - 1; r >= 0; r--) {
-      if (r > tc) {
-        y[r] = cz<T2>();
-        continue;
-      }
-      T2 acc = r == tc ? Cx<T2>::mk(1, 0) : cz<T2>();
-      for (int q2 = r + 1; q2 <= tc; q2++) acc = csub(acc, cmul(sA[r + q2 * m], y[q2]));
-      const T2 d = sA[r + r * m];
-      const R dd = cabs2(d);
-      if (!(dd > 0) || !isfinite(dd)) {
-        bad = true;
-        y[r] = cz<T2>();
-        continue;
-      }
-      y[r] = cscale(cmulc(d, acc), R(1) / dd);  // acc / d
+  if (threadIdx.x < m) {  // 1 / R(r, r); a zero or non-finite pivot is flagged
+    const int r = threadIdx.x;
+    const T2 d = sA[r + r * ld];
+    const R dd = cabs2(d);
+    if (!(dd > 0) || !isfinite(dd)) {
+      s_r[0] = 1;
+      sd[r] = cz<T2>();
+    } else {
+      sd[r] = cscale(cconj(d), Cx<T2>::div(R(1), dd));
     }
-    if (bad) s_r[0] = 1;
-    for (int r = 0; r < m; r++) stA(arena + o.rinv + (int64_t)r * m + tc, y[r]);
+  }
+  __syncthreads();
+  // R^{-1} row-major, a warp per column tc (lanes over rows, two rows a lane
+  // up to 64): y = R^{-1} e_tc by column-oriented back substitution
+  {
+    const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
+    for (int tc = w; tc < m; tc += HX_WARPS) {
+      T2 acc0 = ln == tc ? Cx<T2>::mk(1, 0) : cz<T2>();
+      T2 acc1 = ln + 32 == tc ? Cx<T2>::mk(1, 0) : cz<T2>();
+      for (int r = tc; r >= 0; r--) {
+        // y_r = acc_r / R(r, r) from the lane holding row r, to every lane
+        const T2 mine = r < 32 ? acc0 : acc1;
+        T2 yr = cmul(mine, sd[r]);
+        yr.x = __shfl_sync(0xffffffffu, yr.x, r & 31);
+        yr.y = __shfl_sync(0xffffffffu, yr.y, r & 31);
+        if (ln == (r & 31)) {
+          if (r < 32) acc0 = yr;
+          else acc1 = yr;
+        }
+        if (ln < r) acc0 = csub(acc0, cmul(sA[ln + r * ld], yr));
+        if (ln + 32 < r) acc1 = csub(acc1, cmul(sA[ln + 32 + r * ld], yr));
+      }
+      if (ln < m) stA(arena + o.rinv + (int64_t)ln * m + tc, ln <= tc ? acc0 : cz<T2>());
+      if (ln + 32 < m) stA(arena + o.rinv + (int64_t)(ln + 32) * m + tc, ln + 32 <= tc ? acc1 : cz<T2>());
+    }
   }
   __syncthreads();
   if (threadIdx.x == 0 && s_r[0] != 0) atomicAdd(&a.ctrl[2], 1);
@@ -586,14 +654,17 @@ __device__ void jacobi_cols(T2* X, int p, int q, T2* V, typename Cx<T2>::R* red)
         gr = warp_sum(gr);
         gi = warp_sum(gi);
         if (!(na > floor2) || !(nb > floor2)) continue;
-        const R ga = Cx<T2>::sq(gr * gr + gi * gi);
-        const R rel = ga / (Cx<T2>::sq(na) * Cx<T2>::sq(nb));
-        if (ga == R(0) || !(rel > Cx<T2>::jacobi_thr())) continue;
+        const R g2 = gr * gr + gi * gi;
+        if (g2 == R(0)) continue;
+        const R iga = Cx<T2>::rsq(g2);  // 1 / |g|
+        const R rel = g2 * iga * Cx<T2>::rsq(na * nb);
+        if (!(rel > Cx<T2>::jacobi_thr())) continue;
         if (ln == 0) atomicMax(&s_off, __float_as_uint((float)rel));
-        const R er = gr / ga, ei = gi / ga;
-        const R zeta = (nb - na) / (2 * ga);
-        const R tt = (zeta >= 0 ? R(1) : R(-1)) / (fabs(zeta) + Cx<T2>::sq(1 + zeta * zeta));
-        const R cs = R(1) / Cx<T2>::sq(1 + tt * tt), sn = cs * tt;
+        const R er = gr * iga, ei = gi * iga;
+        const R zeta = (nb - na) * (R(0.5) * iga);
+        const R tt = Cx<T2>::div(zeta >= 0 ? R(1) : R(-1),
+                                 fabs(zeta) + Cx<T2>::sq(1 + zeta * zeta));
+        const R cs = Cx<T2>::rsq(1 + tt * tt), sn = cs * tt;
         // x' = c x - s (y conj(e)), y' = s x + c (y conj(e))
         for (int i = ln; i < p; i += 32) {
           const T2 x = xa[i], y = xb[i];
@@ -718,6 +789,380 @@ __device__ void orth(T2* Y, int64_t rows, int L, T2* head, T2* Q) {
   house_apply<T2, false>(Y, rows, L, head, Q, rows, L);
 }
 
+// ---------------------------------------------------------------- subspace truncation
+// For ranks kc <= 2 without a tolerance (the preconditioner's default) every
+// truncation works through a basis of at most HS_L columns held in shared
+// memory: small matrices, a warp per long reduction, no CTA-wide sweeps over
+// L2-resident panels.
+constexpr int HS_L = HLU_SUB_L;
+static_assert(Cx<float2>::SMEM == HLU_SMEM_ELEMS && Cx<double2>::SMEM == HLU_SMEM_ELEMS,
+              "the planner's shared-memory size");
+
+// One side of a truncation (A: m x kt or B: n x kt, column-major, leading
+// dimension ld): in shared memory (odd ld: a warp reading one row of
+// consecutive columns hits distinct banks), or in the CTA's scratch, where
+// the products stage it in chunks of rows.
+template <typename T2>
+struct Side {
+  const T2* p;
+  int ld;
+  bool glob;
+};
+// Staging area of the products: up to rc rows of a side, leading dimension
+// rc | 1.
+template <typename T2>
+struct Stage {
+  T2* p;
+  int rc;
+};
+
+// rows i0 .. i0 + h of side S (all kt columns) as a shared-memory matrix
+// (returns its pointer and leading dimension)
+template <typename T2>
+__device__ const T2* stage_rows(const Side<T2>& S, int i0, int h, int kt, const Stage<T2>& st,
+                                int& ld) {
+  if (!S.glob) {
+    ld = S.ld;
+    return S.p + i0;
+  }
+  const int ldp = st.rc | 1;
+  __syncthreads();  // the previous chunk's readers are done
+  for (int e = threadIdx.x; e < h * kt; e += HX_THREADS)
+    st.p[e % h + (e / h) * ldp] = S.p[i0 + e % h + (int64_t)(e / h) * S.ld];
+  __syncthreads();
+  ld = ldp;
+  return st.p;
+}
+
+// T (kt x lq, shared) = op(S)^T Y, Y (rows x lq, shared); a thread per entry
+// of T, summed chunk by chunk
+template <typename T2>
+__device__ void sub_mm_ty(const Side<T2>& S, int rows, int kt, const T2* Y, int lq, T2* T,
+                          bool conj_s, bool conj_out, const Stage<T2>& st) {
+  using R = typename Cx<T2>::R;
+  const int nout = kt * lq;
+  for (int o = threadIdx.x; o < nout; o += HX_THREADS) T[o] = cz<T2>();
+  const int rc = S.glob ? st.rc : rows;
+  for (int i0 = 0; i0 < rows; i0 += rc) {
+    const int h = min(rc, rows - i0);
+    int ld;
+    const T2* Sc = stage_rows(S, i0, h, kt, st, ld);
+    for (int o = threadIdx.x; o < nout; o += HX_THREADS) {
+      const int l = o % kt, c = o / kt;
+      const T2* sc = Sc + l * ld;
+      const T2* yc = Y + i0 + c * rows;
+      R ar = 0, ai = 0;
+#pragma unroll 4
+      for (int i = 0; i < h; i++) {
+        T2 sv = sc[i];
+        if (conj_s) sv.y = -sv.y;
+        const T2 y = yc[i];
+        ar += sv.x * y.x - sv.y * y.y;
+        ai += sv.x * y.y + sv.y * y.x;
+      }
+      const T2 t0 = T[o];
+      T[o] = Cx<T2>::mk(t0.x + ar, t0.y + ai);
+    }
+  }
+  if (conj_out) {
+    __syncthreads();
+    for (int o = threadIdx.x; o < nout; o += HX_THREADS) T[o] = cconj(T[o]);
+  }
+  __syncthreads();
+}
+
+// Y (rows x lq, shared) = op(S) T, T (kt x lq, shared); a thread per entry of
+// Y, chunk by chunk
+template <typename T2>
+__device__ void sub_mm_st(const Side<T2>& S, int rows, int kt, const T2* T, int lq, T2* Y,
+                          bool conj_s, const Stage<T2>& st) {
+  using R = typename Cx<T2>::R;
+  const int rc = S.glob ? st.rc : rows;
+  for (int i0 = 0; i0 < rows; i0 += rc) {
+    const int h = min(rc, rows - i0);
+    int ld;
+    const T2* Sc = stage_rows(S, i0, h, kt, st, ld);
+    for (int o = threadIdx.x; o < h * lq; o += HX_THREADS) {
+      const int i = o % h, c = o / h;
+      const T2* tc = T + c * kt;
+      R ar = 0, ai = 0;
+#pragma unroll 4
+      for (int l = 0; l < kt; l++) {
+        T2 sv = Sc[i + l * ld];
+        if (conj_s) sv.y = -sv.y;
+        const T2 tv = tc[l];
+        ar += sv.x * tv.x - sv.y * tv.y;
+        ai += sv.x * tv.y + sv.y * tv.x;
+      }
+      Y[i0 + i + c * rows] = Cx<T2>::mk(ar, ai);
+    }
+  }
+  __syncthreads();
+}
+
+// Orthonormal columns of Y (rows x lq, shared) in place by modified
+// Gram-Schmidt with a second pass (one warp, lanes over the rows). A column
+// whose remainder falls below drop x its own norm lies in the span of the
+// earlier ones (rank deficiency) and becomes zero: it adds no direction, and
+// a zero column of the basis carries no singular value.
+template <typename T2>
+__device__ void sub_orth(T2* Y, int rows, int lq, T2* Rz = nullptr) {
+  using R = typename Cx<T2>::R;
+  const R drop = sizeof(R) == 4 ? R(1e-10) : R(1e-26);
+  if (threadIdx.x < 32) {
+    const int ln = threadIdx.x;
+    if (Rz) {
+      for (int e = ln; e < HS_L * HS_L; e += 32) Rz[e] = cz<T2>();
+      __syncwarp();
+    }
+    R n0 = 0;  // |y_j|^2 before the projections
+    for (int i = ln; i < rows; i += 32) n0 += cabs2(Y[i]);
+    for (int j = 0; j < lq; j++) {
+      T2* y = Y + j * rows;
+      R nn = 0;
+      for (int pass = 0; pass < 2; pass++) {
+        // d_k = q_k^H y (k < j) and, in the first pass, |y|^2: one butterfly
+        // over all the sums at once
+        R d[2 * HS_L + 1];
+#pragma unroll
+        for (int k = 0; k < 2 * HS_L + 1; k++) d[k] = 0;
+        if (j > 0) {
+          for (int i = ln; i < rows; i += 32) {
+            const T2 yi = y[i];
+#pragma unroll
+            for (int k = 0; k < HS_L; k++)
+              if (k < j) {
+                const T2 q = Y[i + k * rows];  // conj(q) y
+                d[2 * k] += q.x * yi.x + q.y * yi.y;
+                d[2 * k + 1] += q.x * yi.y - q.y * yi.x;
+              }
+          }
+        }
+        if (pass == 0) d[2 * HS_L] = n0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+          for (int k = 0; k < 2 * HS_L + 1; k++) d[k] += __shfl_xor_sync(0xffffffffu, d[k], o);
+        }
+        if (pass == 0) n0 = d[2 * HS_L];
+        if (Rz && ln < j) {  // R(k, j) = the two passes' coefficients
+#pragma unroll
+          for (int k = 0; k < HS_L; k++)
+            if (k == ln) {
+              const T2 o = Rz[k + j * HS_L];
+              Rz[k + j * HS_L] = Cx<T2>::mk(o.x + d[2 * k], o.y + d[2 * k + 1]);
+            }
+        }
+        // y -= sum_k d_k q_k, and the new |y|^2
+        R part = 0;
+        for (int i = ln; i < rows; i += 32) {
+          T2 yi = y[i];
+#pragma unroll
+          for (int k = 0; k < HS_L; k++)
+            if (k < j) {
+              const T2 q = Y[i + k * rows];
+              yi.x -= q.x * d[2 * k] - q.y * d[2 * k + 1];
+              yi.y -= q.x * d[2 * k + 1] + q.y * d[2 * k];
+            }
+          y[i] = yi;
+          part += cabs2(yi);
+        }
+        nn = warp_sum(part);
+        __syncwarp();
+        if (j == 0) break;  // nothing to project on
+      }
+      const R s = (nn > 0 && nn > drop * n0) ? Cx<T2>::rsq(nn) : R(0);
+      if (Rz && ln == 0) Rz[j + j * HS_L] = Cx<T2>::mk(s > 0 ? nn * s : R(0), 0);
+      R nx = 0;  // |y_{j+1}|^2 for the next column
+      for (int i = ln; i < rows; i += 32) {
+        y[i] = cscale(y[i], s);
+        if (j + 1 < lq) nx += cabs2(y[i + rows]);
+      }
+      n0 = nx;  // reduced with the next column's first pass
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+}
+
+// One-sided Jacobi on X (q x q, q <= 8, column-major, leading dimension 8,
+// shared) by one warp: X V = U diag(s), V (q x q, leading dimension 8)
+// accumulates the rotations. Lane = 8 x pair + row: the four pairs of a
+// round rotate at once, each reduced over its 8 lanes; the same noise floor
+// and threshold as jacobi_cols.
+template <typename T2>
+__device__ void jacobi_small(T2* X, int q, T2* V) {
+  using R = typename Cx<T2>::R;
+  if (threadIdx.x < 32) {
+    const int ln = threadIdx.x, g = ln >> 3, r = ln & 7;
+    for (int e = ln; e < HS_L * HS_L; e += 32)
+      V[e] = (e % HS_L == e / HS_L && e % HS_L < q) ? Cx<T2>::mk(1, 0) : cz<T2>();
+    R fro = 0;
+    if (g == 0 && r < q)
+      for (int c = 0; c < q; c++) fro += cabs2(X[r + c * HS_L]);
+    const R floor2 = warp_sum(fro) * Cx<T2>::jacobi_floor();
+    __syncwarp();
+    const int qq = q + (q & 1);
+    for (int sweep = 0; sweep < Cx<T2>::JACOBI_SWEEPS && q > 1; sweep++) {
+      unsigned off = 0u;
+      for (int rd = 0; rd < qq - 1; rd++) {
+        int i1, i2;
+        if (g == 0) {
+          i1 = rd;
+          i2 = qq - 1;
+        } else {
+          i1 = (rd + g) % (qq - 1);
+          i2 = (rd - g + (qq - 1)) % (qq - 1);
+        }
+        if (i1 > i2) {
+          const int tt = i1;
+          i1 = i2;
+          i2 = tt;
+        }
+        const bool pair = g < qq / 2 && i2 < q;
+        T2 xa = cz<T2>(), xb = cz<T2>();
+        if (pair && r < q) {
+          xa = X[r + i1 * HS_L];
+          xb = X[r + i2 * HS_L];
+        }
+        R na = cabs2(xa), nb = cabs2(xb);
+        const T2 gp = cmulc(xa, xb);
+        R gr = gp.x, gi = gp.y;
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) {
+          na += __shfl_xor_sync(0xffffffffu, na, o, 8);
+          nb += __shfl_xor_sync(0xffffffffu, nb, o, 8);
+          gr += __shfl_xor_sync(0xffffffffu, gr, o, 8);
+          gi += __shfl_xor_sync(0xffffffffu, gi, o, 8);
+        }
+        const R g2 = gr * gr + gi * gi;
+        bool rot = pair && na > floor2 && nb > floor2 && g2 > R(0);
+        R rel = 0, iga = 0;
+        if (rot) {
+          iga = Cx<T2>::rsq(g2);
+          rel = g2 * iga * Cx<T2>::rsq(na * nb);
+          rot = rel > Cx<T2>::jacobi_thr();
+        }
+        if (rot) {
+          const unsigned rb = __float_as_uint((float)rel);
+          off = rb > off ? rb : off;
+          const R er = gr * iga, ei = gi * iga;
+          const R zeta = (nb - na) * (R(0.5) * iga);
+          const R tt = Cx<T2>::div(zeta >= 0 ? R(1) : R(-1),
+                                   fabs(zeta) + Cx<T2>::sq(1 + zeta * zeta));
+          const R cs = Cx<T2>::rsq(1 + tt * tt), sn = cs * tt;
+          if (r < q) {
+            const T2 ye = Cx<T2>::mk(xb.x * er + xb.y * ei, xb.y * er - xb.x * ei);
+            X[r + i1 * HS_L] = Cx<T2>::mk(cs * xa.x - sn * ye.x, cs * xa.y - sn * ye.y);
+            X[r + i2 * HS_L] = Cx<T2>::mk(sn * xa.x + cs * ye.x, sn * xa.y + cs * ye.y);
+            const T2 va = V[r + i1 * HS_L], vb = V[r + i2 * HS_L];
+            const T2 we = Cx<T2>::mk(vb.x * er + vb.y * ei, vb.y * er - vb.x * ei);
+            V[r + i1 * HS_L] = Cx<T2>::mk(cs * va.x - sn * we.x, cs * va.y - sn * we.y);
+            V[r + i2 * HS_L] = Cx<T2>::mk(sn * va.x + cs * we.x, sn * va.y + cs * we.y);
+          }
+        }
+        __syncwarp();
+      }
+      if (__reduce_max_sync(0xffffffffu, off) == 0u) break;
+    }
+  }
+  __syncthreads();
+}
+
+// A' (m x kc) B'^T (n x kc) = the rank-kc truncated SVD of A B^T with
+// A = SA (m x kt), B = SB (n x kt); the buffers in shared memory at sm.
+template <typename T2>
+__device__ void trunc_subspace(const Side<T2>& SA, const Side<T2>& SB, int m, int n, int kt,
+                               int kc, int power, T2* sm, const Stage<T2>& st, T2* Ao, T2* Bo,
+                               int* s_idx) {
+  using R = typename Cx<T2>::R;
+  T2* Q = sm;               // m x lq
+  T2* Z = Q + m * HS_L;     // n x lq
+  T2* T = Z + n * HS_L;     // kt x lq
+  T2* V = T + kt * HS_L;    // lq x lq (leading dimension 8)
+  T2* Rz = V + HS_L * HS_L;  // lq x lq (leading dimension 8)
+  R* sig = reinterpret_cast<R*>(Rz + HS_L * HS_L);
+  R* mark = sig + HS_L;
+  const bool ident = m <= HS_L;  // Q = I_m
+  int lq;
+  if (ident) {
+    lq = m;
+  } else if (kt <= HS_L) {  // range(M) inside range(A): Q = orth(A), exact
+    lq = kt;
+    for (int e = threadIdx.x; e < m * kt; e += HX_THREADS)
+      Q[e] = SA.p[e % m + (int64_t)(e / m) * SA.ld];
+    __syncthreads();
+    sub_orth(Q, m, lq);
+  } else if (n <= HS_L) {  // Q = orth(M), M = A B^T formed (m x n), exact
+    lq = n;
+    for (int e = threadIdx.x; e < kt * n; e += HX_THREADS) {
+      const int l = e % kt, c = e / kt;
+      T[e] = SB.p[c + (int64_t)l * SB.ld];  // T = B^T
+    }
+    __syncthreads();
+    sub_mm_st(SA, m, kt, T, lq, Q, false, st);
+    sub_orth(Q, m, lq);
+  } else {
+    // seeded randomized range finder with power iterations q = power (0 or
+    // 1; Halko, Martinsson, Tropp, SIAM Review 53(2), 2011: algorithm 4.4)
+    lq = kc + 6 < HS_L ? kc + 6 : HS_L;
+    for (int e = threadIdx.x; e < n * lq; e += HX_THREADS)
+      Z[e] = Cx<T2>::mk((R)rnd_pm1(e % n, e / n), 0);
+    __syncthreads();
+    sub_mm_ty(SB, n, kt, Z, lq, T, false, false, st);  // T = B^T Omega
+    sub_mm_st(SA, m, kt, T, lq, Q, false, st);         // Q = A T = M Omega
+    sub_orth(Q, m, lq);
+    if (power) {
+      sub_mm_ty(SA, m, kt, Q, lq, T, true, false, st);   // T = A^H Q
+      sub_mm_st(SB, n, kt, T, lq, Z, true, st);          // Z = conj(B) T = M^H Q
+      sub_orth(Z, n, lq);
+      sub_mm_ty(SB, n, kt, Z, lq, T, false, false, st);  // T = B^T Z
+      sub_mm_st(SA, m, kt, T, lq, Q, false, st);         // Q = M Z
+      sub_orth(Q, m, lq);
+    }
+  }
+  // the projection's transpose (Q^H M)^T = B conj(A^H Q) (n x lq); its SVD
+  // Z V = U S gives M ~ Q conj(V) S U^T
+  if (ident) {
+    for (int e = threadIdx.x; e < kt * m; e += HX_THREADS) {
+      const int l = e % kt, c = e / kt;
+      T[e] = SA.p[c + (int64_t)l * SA.ld];  // conj(A^H I) = A^T
+    }
+    __syncthreads();
+  } else {
+    sub_mm_ty(SA, m, kt, Q, lq, T, true, true, st);
+  }
+  sub_mm_st(SB, n, kt, T, lq, Z, false, st);
+  // Z = Qz Rz, then Rz V = Ur S (Jacobi on the small factor): Z V = Qz Ur S
+  sub_orth(Z, n, lq, Rz);
+  jacobi_small(Rz, lq, V);
+  const int r = pick_rank(Rz, HS_L, lq, sig, mark, kc, 0.0, s_idx);
+  for (int e = threadIdx.x; e < m * kc; e += HX_THREADS) {  // A' = Q conj(V) S
+    const int i = e % m, l = e / m;
+    T2 v = cz<T2>();
+    if (l < r) {
+      const int j = s_idx[l];
+      if (ident) {
+        v = cconj(V[i + j * HS_L]);
+      } else {
+        for (int c = 0; c < lq; c++) v = cadd(v, cmul(Q[i + c * m], cconj(V[c + j * HS_L])));
+      }
+      v = cscale(v, sig[j]);
+    }
+    stA(Ao + e, v);
+  }
+  for (int e = threadIdx.x; e < n * kc; e += HX_THREADS) {  // B' = U = Qz Ur
+    const int i = e % n, l = e / n;
+    T2 v = cz<T2>();
+    if (l < r) {
+      const int j = s_idx[l];
+      for (int c = 0; c < lq; c++) v = cadd(v, cmul(Z[i + c * n], Rz[c + j * HS_L]));
+      v = cscale(v, Cx<T2>::div(R(1), sig[j]));
+    }
+    stA(Bo + e, v);
+  }
+}
+
 template <typename T2>
 __device__ void task_trunc(const HluTask& t, const HluExecArgs& a, T2* arena, T2* slot, T2* sm) {
   using R = typename Cx<T2>::R;
@@ -757,46 +1202,72 @@ __device__ void task_trunc(const HluTask& t, const HluExecArgs& a, T2* arena, T2
   //  qr     -- otherwise: Householder QR of both sides, Jacobi on the core
   //            R_A R_B^T, the reflectors applied to the kept vectors.
   const int K2 = kt > 32 ? kt : 32;
-  const bool small = m <= 32 && n <= 32 &&
+  // subspace path (kc <= 2, no tolerance) when its buffers and a staging
+  // area of at least 8 rows fit in shared memory; the two sides go there too
+  // when they fit beside the buffers (odd leading dimensions)
+  const int64_t subb = hlu_sub_buffers(m, n, kt);
+  const int64_t mp = m | 1, np1 = n | 1;
+  const bool sub = kc <= 2 && !(a.tol > 0) && subb + 9 * kt <= Cx<T2>::SMEM;
+  const bool sub_sides = sub && subb + (mp + np1) * kt <= Cx<T2>::SMEM;
+  const bool small = !sub && m <= 32 && n <= 32 &&
                      (m + n) * kt + m * n + 32 * 32 + 4 * K2 <= Cx<T2>::SMEM;
   const int L = kc + 6;
-  const bool range = !small && kc <= 8 && !(a.tol > 0) && kt > L && m > L && n > L;
-  T2* S = small ? sm : (t.a >= 0 ? reinterpret_cast<T2*>(a.big_scratch) + t.a : slot);
+  const bool range = !sub && !small && kc <= 8 && !(a.tol > 0) && kt > L && m > L && n > L;
+  T2* S = small ? sm
+                : (sub_sides ? sm + subb
+                             : (t.a >= 0 ? reinterpret_cast<T2*>(a.big_scratch) + t.a : slot));
+  const int lda = (int)(sub_sides ? mp : m), ldb = (int)(sub_sides ? np1 : n);
   T2* SA = S;
-  T2* SB = S + m * kt;
-  T2* W = SB + n * kt;  // work area of the chosen path
-  // gather both sides (placements, zeros elsewhere)
+  T2* SB = S + (int64_t)lda * kt;
+  T2* W = SB + (int64_t)ldb * kt;  // work area of the chosen path
+  // gather both sides (placements, zeros elsewhere), four loads in flight
+  // per thread
   for (int p = 0; p < np; p++) {
     const HluTruncPair pp = P[p];
     const int c0 = s_cb[p], w = s_cb[p + 1] - c0;
     const bool na = pp.neg & 1, nb = pp.neg & 2;
-    for (int64_t e = threadIdx.x; e < m * w; e += HX_THREADS) {
-      const int64_t r = e % m;
-      const int l = (int)(e / m);
-      T2 v = cz<T2>();
-      const int64_t rr = r - pp.ra;
-      if (rr >= 0 && rr < pp.ma) {
-        if (pp.akind == 1) v = rr == l ? Cx<T2>::mk(1, 0) : cz<T2>();
-        else v = piece_get<T2>(a, pp.akind, pp.aoff, pp.soff, pp.ars, pp.acs, rr, l);
-        if (na) v = cneg(v);
+    for (int side = 0; side < 2; side++) {
+      const int rows = (int)(side ? n : m), ld = side ? ldb : lda;
+      const int64_t r0 = side ? pp.rb : pp.ra, mr = side ? pp.mb : pp.ma;
+      const int kind = side ? pp.bkind : pp.akind;
+      const int64_t off = side ? pp.boff : pp.aoff, soff = side ? 0 : pp.soff;
+      const int rs = side ? pp.brs : pp.ars, cs = side ? pp.bcs : pp.acs;
+      const bool ng = side ? nb : na;
+      T2* D = side ? SB : SA;
+      for (int e0 = threadIdx.x; e0 < rows * w; e0 += 4 * HX_THREADS) {
+        T2 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int e = e0 + u * HX_THREADS;
+          v[u] = cz<T2>();
+          if (e < rows * w) {
+            const int r = e % rows, l = e / rows;
+            const int64_t rr = r - r0;
+            if (rr >= 0 && rr < mr) {
+              if (kind == 1) v[u] = rr == l ? Cx<T2>::mk(1, 0) : cz<T2>();
+              else v[u] = piece_get<T2>(a, kind, off, soff, rs, cs, rr, l);
+              if (ng) v[u] = cneg(v[u]);
+            }
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int e = e0 + u * HX_THREADS;
+          if (e < rows * w) D[e % rows + (int64_t)(c0 + e / rows) * ld] = v[u];
+        }
       }
-      SA[r + (int64_t)(c0 + l) * m] = v;
-    }
-    for (int64_t e = threadIdx.x; e < n * w; e += HX_THREADS) {
-      const int64_t r = e % n;
-      const int l = (int)(e / n);
-      T2 v = cz<T2>();
-      const int64_t rr = r - pp.rb;
-      if (rr >= 0 && rr < pp.mb) {
-        if (pp.bkind == 1) v = rr == l ? Cx<T2>::mk(1, 0) : cz<T2>();
-        else v = piece_get<T2>(a, pp.bkind, pp.boff, 0, pp.brs, pp.bcs, rr, l);
-        if (nb) v = cneg(v);
-      }
-      SB[r + (int64_t)(c0 + l) * n] = v;
     }
   }
   __syncthreads();
 
+  if (sub) {
+    const Side<T2> sa{SA, lda, !sub_sides}, sb{SB, ldb, !sub_sides};
+    int rc = (int)((Cx<T2>::SMEM - subb) / kt) - 1;  // (rc | 1) * kt elements fit
+    rc = rc > 256 ? 256 : rc;
+    const Stage<T2> st{sm + subb, rc};
+    trunc_subspace(sa, sb, (int)m, (int)n, kt, kc, a.range_power, sm, st, Ao, Bo, s_idx);
+    return;
+  }
   if (range) {
     T2* Y = W;            // m x L
     T2* Q = Y + m * L;    // m x L

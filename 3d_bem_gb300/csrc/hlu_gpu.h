@@ -69,6 +69,17 @@ inline int64_t trunc_scratch(int64_t m, int64_t n, int64_t kt) {
 }
 // truncations up to this many complex elements of scratch use their CTA's slot
 constexpr int64_t HLU_CTA_SCRATCH = int64_t(1) << 16;
+// complex elements of the executor's dynamic shared memory per CTA
+constexpr int64_t HLU_SMEM_ELEMS = 6144;
+// subspace truncation (rank <= 2, no tolerance): basis width and the shared
+// memory of its buffers (Q m x 8, Z n x 8, T kt x 8, V and R 8 x 8, 8 values)
+constexpr int HLU_SUB_L = 8;
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline int64_t hlu_sub_buffers(int64_t m, int64_t n, int64_t kt) {
+  return (m + n + kt) * HLU_SUB_L + 2 * HLU_SUB_L * HLU_SUB_L + HLU_SUB_L;
+}
 
 struct HluTask {
   int32_t type, flags;
@@ -157,6 +168,7 @@ struct HluExecArgs {
   void* big_scratch;             // regions of the large truncations (HluTask.a)
   int32_t kc;
   double tol;                    // truncation tolerance (0: rank kc)
+  int32_t range_power;           // power iterations of the randomized range finder (0 or 1)
   int64_t wait_cycles;           // bound of one dependency wait (clock64 cycles)
   unsigned long long* trace;     // optional: per task claim, start, end (ns)
 };

@@ -396,10 +396,12 @@ class Planner {
   }
 
   // model cost (microseconds) of a truncation, by the executor's path: the
-  // dense sum of a small target, the range finder for a small rank of a wide
-  // sum, Householder QR otherwise (fitted to traced factorizations; it only
-  // orders the claims)
+  // shared-memory subspace path for ranks <= 2, the dense sum of a small
+  // target, the range finder for a small rank of a wide sum, Householder QR
+  // otherwise (fitted to traced factorizations; it only orders the claims)
   double trunc_cost(int64_t m, int64_t n, int64_t kt) const {
+    if (kc_ <= 2 && hlu_sub_buffers(m, n, kt) <= HLU_SMEM_ELEMS)
+      return 10.0 + (double)(m + n) * kt / 400.0;
     if (m <= 32 && n <= 32) return 60.0 + 0.2 * (double)kt * (m < n ? m : n);
     if (kc_ <= 8 && kt > kc_ + 6 && m > kc_ + 6 && n > kc_ + 6)
       return 150.0 + (double)(m + n) * kt / 50.0;
