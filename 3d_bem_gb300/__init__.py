@@ -35,7 +35,8 @@ EXPORTS = [
     "bem_plan_mesh", "bem_hlu_plan",
     "bem_get_permutation", "bem_get_partition", "bem_set_bc", "bem_operators",
     "bem_assemble", "bem_hmatvec", "bem_hmatvec_device", "bem_get_block", "bem_get_ranks",
-    "bem_gmres", "bem_solve", "bem_solve_device", "bem_sweep", "bem_points_assemble",
+    "bem_gmres", "bem_solve", "bem_solve_device", "bem_sweep", "bem_sweep_device",
+    "bem_points_assemble",
     "bem_launch_count", "bem_stream", "bem_hmatvec_noalloc", "bem_hmatvec_device_ex",
     "bem_hlu_build", "bem_hlu_solve", "bem_hlu_export", "bem_hlu_sweep_kind", "bem_recompress",
     "bem_sel_nparam", "bem_sel_label", "bem_mlp_grad", "bem_mlp_adam", "bem_mlp_forward",
@@ -129,6 +130,7 @@ def lib():
     L.bem_solve.argtypes = [vp, dbl, vp, i64, vp, vp, vp, P(SolveInfo)]
     L.bem_solve_device.argtypes = [vp, dbl, vp, i64, vp, vp, vp, P(SolveInfo)]
     L.bem_sweep.argtypes = [vp, vp, i64, vp, i64, vp, vp]
+    L.bem_sweep_device.argtypes = [vp, vp, i64, vp, i64, vp, vp]
     L.bem_points_assemble.argtypes = [vp, vp, i64, vp, i64, dbl, vp, vp]
     L.bem_recompress.argtypes = [vp, i32, i64, dbl]
     L.bem_sel_nparam.argtypes = []
@@ -498,6 +500,18 @@ class Solver:
         if st not in (BEM_OK, BEM_EMAXIT):
             self._check(st, "bem_sweep")
         return p, [i.as_dict() for i in infos]
+
+    def sweep_device(self, freqs, g_ptr: int, R: int, p_ptr: int):
+        """bem_sweep with device pointers: g (n x R complex FP64, caller order)
+        and p (n x R per frequency, nf slices) in GPU memory. Returns the
+        per-frequency infos."""
+        freqs = np.ascontiguousarray(freqs, np.float64)
+        infos = (SolveInfo * freqs.size)()
+        st = lib().bem_sweep_device(self._h, _ptr(freqs), freqs.size, ct.c_void_p(g_ptr), R,
+                                    ct.c_void_p(p_ptr), infos)
+        if st not in (BEM_OK, BEM_EMAXIT):
+            self._check(st, "bem_sweep_device")
+        return [i.as_dict() for i in infos]
 
     def set_point_sources(self, sources=None):
         """Point sources of the right-hand side: rows (x, y, z, complex weight);

@@ -220,6 +220,10 @@ struct bem_handle {
   bool hp_ok = false;
   uint64_t hp_gen = ~0ull;
   int64_t hp_kc = -1;
+  // a sweep worker starts with its parent's program (same layout): valid
+  // while layout_gen still equals hp_inherit_gen
+  bool hp_inherited = false;
+  uint64_t hp_inherit_gen = 0;
   int hp_prec = -1, hp_grid = 0;
   std::string hp_why;
   DBuf<HluTask> dHT;
@@ -935,8 +939,11 @@ bool prepare_hlu_program(bem_handle* h) {
   h->hp_ok = false;
   h->hp_prec = -1;
   HluProgram& P = h->hp;
+  const bool inherit = h->hp_inherited && h->hp_inherit_gen == h->layout_gen &&
+                       h->hp_kc == h->cfg.precond_rank;
+  h->hp_inherited = false;
   std::string why;
-  if (!hlu_gpu_plan(h->rows, h->L, h->cfg.precond_rank, P, &why)) {
+  if (!inherit && !hlu_gpu_plan(h->rows, h->L, h->cfg.precond_rank, P, &why)) {
     h->hp_why = why;
     return false;
   }
@@ -964,7 +971,12 @@ void prepare_hlu_arena(bem_handle* h, int prec) {
   const size_t es = prec ? sizeof(float2) : sizeof(double2);
   const int occ = hlu_exec_occupancy(prec);
   require(occ >= 1, BEM_ECUDA, "H-LU executor: no co-resident CTA fits an SM");
-  h->hp_grid = h->nsm * std::min(occ, 4);
+  // CTAs per SM of the executor (all that fit, at most 4; BEM_HLU_CTAS_PER_SM
+  // caps it lower, leaving SM room to concurrent sweep workers' kernels)
+  int cap = 4;
+  if (const char* e = std::getenv("BEM_HLU_CTAS_PER_SM"))
+    if (std::atoi(e) >= 1) cap = std::min(4, std::atoi(e));
+  h->hp_grid = h->nsm * std::min(occ, cap);
   h->dArena.release();
   h->dHScr.release();
   h->dHBig.release();
@@ -1192,9 +1204,10 @@ bool build_hlu_device(bem_handle* h) {
   a.kc = P.kc;
   a.tol = h->cfg.precond_tol;
   a.wait_cycles = hlu_wait_cycles();
-  {  // power iterations of the truncations' range finder (default 1)
+  {  // power iterations of the truncations' range finder (default 0: on the
+     // pencil the factors precondition as well as with one iteration)
     const char* e = std::getenv("BEM_HLU_RANGE_POWER");
-    a.range_power = e && *e ? (std::atoi(e) > 0 ? 1 : 0) : 1;
+    a.range_power = e && *e ? (std::atoi(e) > 0 ? 1 : 0) : 0;
   }
   // BEM_HLU_TRACE=<file>: per-task timestamps, summarised into the file
   const char* trace_path = std::getenv("BEM_HLU_TRACE");
@@ -1342,6 +1355,29 @@ const void* hlu_data(const bem_handle* h, int which) {
   return which ? h->dUd.p : h->dLd.p;
 }
 
+// mean driver phase times of a traced lower sweep: wait for R(i), corner,
+// solve, hand-over to the next chunk (appended to path)
+void df_trace_summary(bem_handle* h, const DBuf<unsigned long long>& tr, int R, const char* path) {
+  const int D = h->dfL.view.D;
+  std::vector<unsigned long long> t(4 * (size_t)D);
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaMemcpy(t.data(), tr.p, t.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  double ph[4] = {};
+  for (int i = 0; i + 1 < D; i++) {
+    ph[0] += 1e-3 * (double)(t[4 * i + 1] - t[4 * i]);
+    ph[1] += 1e-3 * (double)(t[4 * i + 2] - t[4 * i + 1]);
+    ph[2] += 1e-3 * (double)(t[4 * i + 3] - t[4 * i + 2]);
+    ph[3] += 1e-3 * (double)(t[4 * (i + 1)] - t[4 * i + 3]);
+  }
+  FILE* f = std::fopen(path, "a");
+  if (!f) return;
+  const double n = D > 1 ? (double)(D - 1) : 1.0;
+  std::fprintf(f, "df L sweep: chunks %d R %d total_us %.1f per chunk us: wait %.3f corner %.3f "
+               "solve %.3f handover %.3f\n", D, R, 1e-3 * (double)(t[4 * (D - 1) + 3] - t[0]),
+               ph[0] / n, ph[1] / n, ph[2] / n, ph[3] / n);
+  std::fclose(f);
+}
+
 // w := U^{-1} L^{-1} w for R device vectors (LUPrecondidionedHMatrixWrapper's
 // two substitutions, gmres.h:134-147)
 void apply_precond(bem_handle* h, double2* w, int R, const int* gate_flags = nullptr) {
@@ -1351,6 +1387,14 @@ void apply_precond(bem_handle* h, double2* w, int R, const int* gate_flags = nul
     h->dP2.ensure((size_t)std::min(R, HLU_DF_MAX_R) * N);
     HluDfWork ws{h->dfXi.p, h->dfAcc.p, h->dfEacc.p, h->dfPre.p, h->dfFin.p, h->dfCtrl.p, h->dfErr.p};
     const int hp = df_helpers();
+    // BEM_DF_TRACE=<file>: the lower sweep's driver phases of this
+    // application, summarised into the file (profiling)
+    const char* trace_path = std::getenv("BEM_DF_TRACE");
+    DBuf<unsigned long long> trace;
+    if (trace_path && *trace_path) {
+      trace.ensure(4 * (size_t)h->dfL.view.D);
+      ws.trace = trace.p;
+    }
     for (int r0 = 0; r0 < R; r0 += HLU_DF_MAX_R) {
       const int rc = std::min(HLU_DF_MAX_R, R - r0);
       double2* wr = w + (size_t)r0 * N;
@@ -1358,9 +1402,12 @@ void apply_precond(bem_handle* h, double2* w, int R, const int* gate_flags = nul
                                       : HmvGate{nullptr, 0, 0};
       h->launches += launch_hlu_df(h->dfL.view, h->dLl.p, hlu_data(h, 0), h->hlu_prec, wr, h->dP2.p,
                                    N, rc, ws, hp, s, gate);
+      HluDfWork wu = ws;
+      wu.trace = nullptr;
       h->launches += launch_hlu_df(h->dfU.view, h->dUl.p, hlu_data(h, 1), h->hlu_prec, h->dP2.p, wr,
-                                   N, rc, ws, hp, s, gate);
+                                   N, rc, wu, hp, s, gate);
     }
+    if (ws.trace) df_trace_summary(h, trace, R, trace_path);
     return;
   }
   h->dP1.ensure((size_t)R * N);
@@ -1664,6 +1711,12 @@ void clone_state(bem_handle* c, bem_handle* p) {
                        c->stream));
     for (int i = 0; i < 4; i++) c->aca_axes[i] = p->aca_axes[i];
   }
+  if (p->hp_ok && p->hp_gen == p->layout_gen) {  // the parent's H-LU program fits this layout
+    c->hp = p->hp;
+    c->hp_kc = p->hp_kc;
+    c->hp_inherited = true;
+    c->hp_inherit_gen = c->layout_gen;
+  }
   c->have_selector = false;
   if (p->have_selector) {
     c->dSel.ensure(1);
@@ -1701,9 +1754,12 @@ void ensure_workers(bem_handle* h, int nw) {
 // Frequencies idx[0..n) of a sweep on W handles (h and W - 1 workers), one
 // host thread per handle, each on its own stream; frequency i goes to handle
 // i mod W (with H-LU factor reuse: contiguous blocks of ascending frequencies). p (caller order, n_freq slices) gets each frequency's pressure.
+// With device pointers (gd, pd non-null) instead of g / p: every worker reads
+// gd and writes its frequencies' slices of pd directly; the workers' streams
+// start after the work already on h's stream and h's stream waits for them.
 void run_sweep(bem_handle* h, int W, const double* freqs, const int64_t* idx, int64_t n,
                const double* g, int64_t nrhs, double* p, bem_solve_info* info,
-               bem_status& worst) {
+               bem_status& worst, const double2* gd = nullptr, double2* pd = nullptr) {
   require(h->have_mesh && h->have_bc && !h->points_mode, BEM_EINVAL,
           "mesh and boundary conditions must be set");
   W = (int)std::max<int64_t>(1, std::min<int64_t>(W, n));
@@ -1711,11 +1767,33 @@ void run_sweep(bem_handle* h, int W, const double* freqs, const int64_t* idx, in
   std::vector<bem_handle*> hs{h};
   for (int w = 0; w + 1 < W; w++) hs.push_back(h->workers[w]);
   const size_t cnt = (size_t)h->N * nrhs;
+  const bool dev = gd != nullptr;
+  cudaEvent_t e0 = nullptr;
+  std::vector<cudaEvent_t> ew(W, nullptr);
+  if (dev) {
+    CK(cudaEventCreateWithFlags(&e0, cudaEventDisableTiming));
+    for (auto& e : ew) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    CK(cudaEventRecord(e0, h->stream));
+  }
   std::vector<bem_status> st(W, BEM_OK), wst(W, BEM_OK);
   auto body = [&](int w) {
     bem_handle* x = hs[w];
     st[w] = guarded(x, [&] {
       CK(cudaSetDevice(h->device));
+      if (dev) {
+        CK(cudaStreamWaitEvent(x->stream, e0, 0));
+        const bool blocks = h->cfg.use_preconditioner && h->cfg.precond_reuse > 1.0;
+        const int64_t i0 = blocks ? n * w / W : w, i1 = blocks ? n * (w + 1) / W : n;
+        for (int64_t i = i0; i < i1; i += blocks ? 1 : W) {
+          const int64_t f = idx[i];
+          bem_solve_info loc{};
+          solve_dev(x, freqs[f], gd, nrhs, nullptr, nullptr, pd + cnt * f, &loc);
+          if (info) info[f] = loc;
+          if (loc.status != BEM_OK) wst[w] = loc.status;
+        }
+        CK(cudaEventRecord(ew[w], x->stream));
+        return;
+      }
       copy_in(x, x->dIn, g, cnt);
       x->dOut3.ensure(cnt);
       // with factor reuse, each handle takes a contiguous block of the
@@ -1740,6 +1818,12 @@ void run_sweep(bem_handle* h, int W, const double* freqs, const int64_t* idx, in
     for (int w = 1; w < W; w++) th.emplace_back(body, w);
     body(0);
     for (auto& t : th) t.join();
+  }
+  if (dev) {
+    for (int w = 0; w < W; w++)
+      if (st[w] == BEM_OK) CK(cudaStreamWaitEvent(h->stream, ew[w], 0));
+    CK(cudaEventDestroy(e0));
+    for (auto& e : ew) CK(cudaEventDestroy(e));
   }
   for (int w = 0; w < W; w++) {
     if (st[w] != BEM_OK) throw BemError{st[w], "sweep worker: " + hs[w]->err};
@@ -2771,6 +2855,27 @@ bem_status bem_sweep(bem_handle* h, const double* freqs, int64_t nf, const doubl
   return st != BEM_OK ? st : worst;
 }
 
+bem_status bem_sweep_device(bem_handle* h, const double* freqs, int64_t nf, const void* g,
+                            int64_t nrhs, void* p, bem_solve_info* info) {
+  if (!h) return BEM_EINVAL;
+  bem_status worst = BEM_OK;
+  bem_status st = guarded(h, [&] {
+    require(freqs && g && p && nf >= 1 && nrhs >= 1, BEM_EINVAL, "bad arguments");
+    for (int64_t f = 0; f < nf; f++)
+      require(freqs[f] > 0 && std::isfinite(freqs[f]), BEM_EINVAL, "frequencies must be positive");
+    int W = (int)h->cfg.sweep_workers;
+    if (W == 0) W = h->tuned_workers > 0 ? (int)h->tuned_workers : 1;
+    std::vector<int64_t> idx(nf);
+    for (int64_t i = 0; i < nf; i++) idx[i] = i;
+    if (h->cfg.use_preconditioner && h->cfg.precond_reuse > 1.0)
+      std::stable_sort(idx.begin(), idx.end(),
+                       [&](int64_t x, int64_t y) { return freqs[x] < freqs[y]; });
+    run_sweep(h, W, freqs, idx.data(), nf, nullptr, nrhs, nullptr, info, worst,
+              (const double2*)g, (double2*)p);
+  });
+  return st != BEM_OK ? st : worst;
+}
+
 bem_status bem_points_assemble(bem_handle* h, const double* rowpts, int64_t nr,
                                const double* colpts, int64_t nc, double k, int64_t* rowperm,
                                int64_t* colperm) {
@@ -2812,7 +2917,12 @@ bem_status bem_points_assemble(bem_handle* h, const double* rowpts, int64_t nr,
   });
 }
 
-int64_t bem_launch_count(const bem_handle* h) { return h ? h->launches : 0; }
+int64_t bem_launch_count(const bem_handle* h) {
+  if (!h) return 0;
+  int64_t c = h->launches;
+  for (const bem_handle* w : h->workers) c += w->launches;  // the sweep workers' kernels
+  return c;
+}
 
 void* bem_stream(const bem_handle* h) { return h ? (void*)h->stream : nullptr; }
 

@@ -361,6 +361,7 @@ struct DfArgs {
   int64_t N;
   int R;
   HmvGate gate;
+  unsigned long long* trace;  // optional: per chunk the driver's phase times (ns)
   __device__ int* flagR(int i) const { return ctrl + 4 + i; }
   __device__ int* flagC(int j) const { return ctrl + 4 + p.D + j; }
   __device__ int* flagE(int i) const { return ctrl + 4 + 2 * p.D + i; }
@@ -443,9 +444,11 @@ __device__ void df_driver(const DfArgs& a, unsigned char* sm) {
   cp_async_commit();
   double2 wn = make_double2(0.0, 0.0);
   if (row < ring[0].m && part == 0) wn = a.w[(int64_t)r * N + ring[0].r0 + row];
+  unsigned long long* tr = a.trace;
   for (int i = 0; i < D; i++) {
     cp_async_wait_all();
     __syncthreads();  // M(i), corner(i) and chunk i + 1 have landed
+    if (tr && tid == 0) tr[4 * (int64_t)i] = gtimer();
     const HluDfChunk& c = ring[i & 3];
     const int m = c.m;
     const bool act = row < m && lanes;  // this thread holds partial sums
@@ -467,6 +470,7 @@ __device__ void df_driver(const DfArgs& a, unsigned char* sm) {
       cp_async_wait_all();  // no copy in flight at exit
       return;
     }
+    if (tr && tid == 0) tr[4 * (int64_t)i + 1] = gtimer();
     T2 accv = mk<T2>(0, 0);
     if (i >= 1 && own) accv = ldv((const T2*)a.acc + (int64_t)r * N + c.r0 + row);
     T2 cs = mk<T2>(0, 0);  // this thread's part of the corner contribution
@@ -510,6 +514,7 @@ __device__ void df_driver(const DfArgs& a, unsigned char* sm) {
       if (act) red[(part * a.R + r) * 32 + row] = cs;
     }
     __syncthreads();  // corner partials complete; xs (chunk i - 1) no longer read
+    if (tr && tid == 0) tr[4 * (int64_t)i + 2] = gtimer();
     if (own) {
       if (c.corner >= 0) {
         cs = red[r * 32 + row];
@@ -542,6 +547,7 @@ __device__ void df_driver(const DfArgs& a, unsigned char* sm) {
       xi[(int64_t)r * N + c.r0 + row] = y;
       if ((void*)xi != (void*)a.x) a.x[(int64_t)r * N + c.r0 + row] = make_double2(y.x, y.y);
     }
+    if (tr && tid == 0) tr[4 * (int64_t)i + 3] = gtimer();
     df_publish(a.ctrl + 1, i + 1);
   }
   cp_async_wait_all();
@@ -930,6 +936,7 @@ int launch_hlu_df(const HluDfDev& p, const int64_t* leaves, const void* data, in
   a.N = N;
   a.R = R;
   a.gate = gate;
+  a.trace = ws.trace;
   void* args[] = {&a};
   const int cap = precision == 0 ? df_prepare<double2>() : df_prepare<float2>();
   const int grid = std::max(2, std::min(1 + std::max(1, helpers), cap));

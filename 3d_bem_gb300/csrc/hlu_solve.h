@@ -98,6 +98,7 @@ struct HluDfWork {
   void* fin = nullptr;
   int* ctrl = nullptr;
   int* err = nullptr;
+  unsigned long long* trace = nullptr;  // optional: 4 x D driver timestamps (ns)
 };
 
 // w (R x N) -> x (R x N) with one cooperative launch of 1 driver + `helpers`

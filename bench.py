@@ -355,9 +355,10 @@ def pencil_problem(meshes, n_target=PENCIL_N):
 
 def pencil_solver(pkg, tri, beta, precision, **extra):
     extra.setdefault("aca_tol", ACA_TOL)
+    extra.setdefault("sweep_workers", 1)
     s = pkg.Solver(gmres_tol=GMRES_TOL, wave_speed=C0, density=RHO,
                    precision=precision, use_preconditioner=1, precond_rank=2, gmres_maxit=1000,
-                   sweep_workers=1, **extra)
+                   **extra)
     s.set_mesh(tri)
     s.set_bc_impedance(beta)
     return s
@@ -535,22 +536,47 @@ def run_ours(args):
     extra = {"selector": learned} if learned else {}
     extra["near_fp64"] = 0 if args.fp32_near else 1
 
-    s = pencil_solver(pkg, tri, beta, 1, **extra)
+    # batched sweep: W concurrent frequency workers (each its own stream,
+    # buffers and H-LU factors), K frequencies; g and p resident in GPU memory
+    W = max(1, args.workers)
+    s = pencil_solver(pkg, tri, beta, 1, sweep_workers=W, **extra)
+    p_dev = torch.zeros((len(fr_t), R, n), dtype=torch.complex128, device="cuda")
+    stream = torch.cuda.ExternalStream(pkg.lib().bem_stream(s._h))
+    # warm-up: one solve plans the H-LU task program (the workers inherit
+    # it), then a sweep with every worker busy
+    warm = [fr_w[i % len(fr_w)] * (1.0 + 1e-3 * i) for i in range(max(W, len(fr_w)))]
+    p_warm = torch.zeros((len(warm), R, n), dtype=torch.complex128, device="cuda")
+    s.solve_device(warm[0], g_dev.data_ptr(), R, 0, 0, p_warm[0].data_ptr())
+    s.sweep_device(warm, g_dev.data_ptr(), R, p_warm.data_ptr())
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
     clk = Clocks(local)
     clk.start()
-    ms, per, infos, pm, launches = timed_solves(torch, pkg, s, n, R, fr_t, fr_w, ws, g_dev)
+    l0 = s.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    infos = s.sweep_device(fr_t, g_dev.data_ptr(), R, p_dev.data_ptr())
+    e1.record(stream)
+    torch.cuda.synchronize()
     clocks = clk.stop()
+    launches = s.launch_count() - l0  # the first handle's own kernels
+    if ws > 1:
+        torch.distributed.barrier()
+    ms = max_over_ranks(torch, e0.elapsed_time(e1), ws)
+    pm = p_dev.cpu().numpy().transpose(0, 2, 1)  # steps x n x R
     K = len(fr_t)
     value = ws * K / (ms / 1e3)
+    per = [1e3 * i["t_total"] for i in infos]
 
-    # end to end through bem_solve: pinned host g in, host p out, every step
-    # pinned (R x n) rows = the n x R column-major layout bem_solve reads
+    # end to end through bem_sweep: pinned host g in, host p out (every
+    # frequency's pressures copied back), the same workers
     gh = torch.from_numpy(np.ascontiguousarray(g_host.T)).pin_memory()
     gpin = gh.numpy().T
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for f in fr_t:
-        s.solve(f, gpin, want=("p",))
+    s.sweep(fr_t, gpin)
     torch.cuda.synchronize()
     e2e = ws * K / (time.perf_counter() - t0)
 
@@ -580,6 +606,7 @@ def run_ours(args):
                    "aca_tol": ACA_TOL, "gmres_tol": GMRES_TOL, "leaf_size": 32, "eta": 2.0,
                    "coupling": "Kirkup", "bc": "Robin impedance walls a = i k rho c / Z",
                    "precision": "mixed", "hlu_preconditioner": "rank 2, factorized on the GPU",
+                   "batching": f"{W} concurrent frequency workers x 8 RHS (bem_sweep_device)",
                    "learned_selector": bool(args.selector),
                    "learned_aca_rules": not args.no_aca_rules,
                    "near_field": "complex FP32 in GMRES; FP64 (two complex-FP32 parts) in the "
@@ -595,7 +622,7 @@ def run_ours(args):
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
         "gpu_launches": int(launches),
         "phases_s": phase,
-        "ms_per_frequency": [round(x, 1) for x in per],
+        "worker_ms_per_frequency": [round(x, 1) for x in per],
         "gmres_iterations": int(max(i["iterations"] for i in infos)),
         "true_residual": float(max(i["true_residual"] for i in infos)),
         "all_converged": bool(all(i["status"] == 0 for i in infos)),
@@ -604,16 +631,20 @@ def run_ours(args):
     }
     s.close()
     if not args.no_plain and ws == 1:
+        # the plain method: complex FP64 throughout, one frequency after the
+        # other (no concurrent workers), at the lowest, middle and highest
+        # timed frequencies (its cost per frequency falls with frequency, as
+        # the GMRES step counts do)
         s64 = pencil_solver(pkg, tri, beta, 0)
-        pick = [fr_t[0], fr_t[-1]] if K > 1 else [fr_t[0]]
+        pick = sorted({fr_t[0], fr_t[len(fr_t) // 2], fr_t[-1]})
         ms64, per64, i64, p64, _ = timed_solves(torch, pkg, s64, n, R, pick, fr_w[:1], ws, g_dev)
         s64.close()
-        mixed_same = [per[fr_t.index(f)] for f in pick]
         line["plain_fp64"] = {
             "frequencies_hz": [round(f, 2) for f in pick],
             "ms_per_frequency": [round(x, 1) for x in per64],
-            "mixed_ms_same_frequencies": [round(x, 1) for x in mixed_same],
-            "speedup_mixed_vs_plain": round(sum(per64) / sum(mixed_same), 2),
+            "mean_ms_per_frequency": round(float(np.mean(per64)), 1),
+            "mixed_sweep_ms_per_frequency": round(ms / K, 1),
+            "speedup_mixed_vs_plain": round(float(np.mean(per64)) / (ms / K), 2),
             "phases_s": {key: round(float(np.mean([i[key] for i in i64])), 4)
                          for key in ("t_nearfield", "t_aca", "t_precond", "t_gmres", "t_total")},
             "rel_err_mixed_vs_plain": max(rel_err_cols(pm[fr_t.index(f)], p64[j])
@@ -637,6 +668,27 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_hlu_only(args):
+    """One H-LU factorization of the pencil on the GPU, after a warm-up one
+    (for profiling the executor kernel): mixed precision, rank 2, 1 kHz,
+    args.pencil_n triangles."""
+    import torch
+    pkg = importlib.import_module("3d_bem_gb300")
+    meshes = importlib.import_module("3d_bem_gb300.meshes")
+    pkg.build()
+    tri, _, beta = pencil_problem(meshes, args.pencil_n)
+    s = pencil_solver(pkg, tri, beta, 1, selector=2, near_fp64=1)
+    s.assemble(1000.0)
+    s.hlu_build()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.hlu_build()
+    torch.cuda.synchronize()
+    print(json.dumps({"hlu_only": {"n_elements": int(tri.shape[0]),
+                                   "seconds": round(time.perf_counter() - t0, 4)}}), flush=True)
+    s.close()
 
 
 def run_field_only(args):
@@ -705,8 +757,10 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=8,
+    ap.add_argument("--steps", type=int, default=16,
                     help="frequencies of the 64-frequency sweep timed (spread over the band)")
+    ap.add_argument("--workers", type=int, default=4,
+                    help="concurrent frequency workers of the batched sweep (mixed arm)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="sphere20k", choices=sorted(WORKLOADS),
@@ -722,6 +776,11 @@ def main():
                     help="skip the field evaluation at 20,480 observation points")
     ap.add_argument("--no-half-space", action="store_true",
                     help="skip the sphere-above-a-rigid-plane solves")
+    ap.add_argument("--hlu-only", action="store_true",
+                    help="only one H-LU factorization of the pencil (after a warm-up one); "
+                         "profiling")
+    ap.add_argument("--pencil-n", type=int, default=PENCIL_N,
+                    help="triangles of the pencil for --hlu-only")
     ap.add_argument("--field-only", action="store_true",
                     help="only the field evaluation leg (one mixed solve first); profiling")
     ap.add_argument("--no-sweep", action="store_true",
@@ -735,7 +794,9 @@ def main():
                     help="mixed arm: the 16-point rule for the ACA entries instead of the "
                          "learned rule table")
     args = ap.parse_args()
-    if args.field_only:
+    if args.hlu_only:
+        run_hlu_only(args)
+    elif args.field_only:
         run_field_only(args)
     elif args.impl == "reference":
         run_reference(args)

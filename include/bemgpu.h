@@ -319,6 +319,13 @@ bem_status bem_autotune(bem_handle* h, double freq, int64_t nrhs, int64_t* tuned
  * info may be NULL or hold nf records. */
 bem_status bem_sweep(bem_handle* h, const double* freqs, int64_t nf, const double* g,
                      int64_t nrhs, double* p, bem_solve_info* info);
+/* Same with device pointers: g (n x nrhs complex FP64) and p (n x nrhs x nf)
+ * in GPU memory. The workers' work follows what the caller enqueued on the
+ * handle's stream (bem_stream) before the call, and the handle's stream
+ * waits for all of it before the call returns, so events recorded on that
+ * stream bracket the whole sweep. */
+bem_status bem_sweep_device(bem_handle* h, const double* freqs, int64_t nf, const void* g,
+                            int64_t nrhs, void* p, bem_solve_info* info);
 
 /* Point sources of the boundary solve (BoundaryElementSolver::pointSources):
  * nsrc rows x, y, z, Re w, Im w (nsrc = 0 clears; bem_set_mesh clears too).
@@ -434,7 +441,7 @@ bem_status bem_points_assemble(bem_handle* h, const double* rowpts, int64_t nr,
                                int64_t* colperm);
 
 /* Number of kernel launches issued by the library since the handle was
- * created (instrumentation for benchmarks). */
+ * created, its sweep workers' included (instrumentation for benchmarks). */
 int64_t bem_launch_count(const bem_handle* h);
 
 /* The CUDA stream (cudaStream_t) every kernel of this handle runs on, so a

@@ -102,3 +102,44 @@ def test_impedance_walls_match_robin_data(bem, meshes):
         r.set_bc(1j * k * beta, np.ones(n))
         _, _, pr, _ = r.solve(f, g)
         assert np.array_equal(p[:, :, q], pr)
+
+
+def test_device_sweep_with_preconditioner_matches_solves(bem, meshes):
+    """bem_sweep_device: concurrent workers with the GPU H-LU preconditioner
+    (each worker starts from the parent's task program) read g and write p in
+    GPU memory; the pressures equal single device solves bitwise, and events
+    on the handle's stream bracket the whole sweep."""
+    import torch
+    tri = meshes.pencil(n_target=1280)
+    n = tri.shape[0]
+    g = meshes.pencil_rhs(tri)[:, :3]
+    beta = meshes.wall_admittance(n)
+    cfg = dict(aca_tol=1e-5, gmres_tol=1e-10, wave_speed=343.0, density=1.2, precision=1,
+               use_preconditioner=1, precond_rank=2, near_fp64=1)
+    freqs = np.array([400.0, 900.0, 2500.0, 6000.0, 1500.0])
+    R = g.shape[1]
+    gd = torch.from_numpy(np.ascontiguousarray(g.T)).to("cuda")  # n x R column-major
+    s = bem.Solver(sweep_workers=3, **cfg)
+    s.set_mesh(tri)
+    s.set_bc_impedance(beta)
+    s.solve(700.0, g)  # the parent's task program, then inherited by the workers
+    p = torch.zeros((freqs.size, R, n), dtype=torch.complex128, device="cuda")
+    stream = torch.cuda.ExternalStream(bem.lib().bem_stream(s._h))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    infos = s.sweep_device(freqs, gd.data_ptr(), R, p.data_ptr())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    assert e0.elapsed_time(e1) > 0
+    assert all(i["status"] == 0 for i in infos)
+    ref = bem.Solver(sweep_workers=1, **cfg)
+    ref.set_mesh(tri)
+    ref.set_bc_impedance(beta)
+    for k, f in enumerate(freqs):
+        q = torch.zeros((R, n), dtype=torch.complex128, device="cuda")
+        ref.solve_device(float(f), gd.data_ptr(), R, 0, 0, q.data_ptr())
+        torch.cuda.synchronize()
+        assert torch.equal(q, p[k]), f
+    s.close()
+    ref.close()
