@@ -227,6 +227,71 @@ __device__ __forceinline__ T aca_entry(const AcaArgs& a, int64_t row, int64_t co
   }
 }
 
+// Lane q's share of the entry when Q lanes split it (Q a power of two): the
+// FP32 regular rule over the points q, q + Q, ..; entries on the FP64 path
+// (singular / near-singular pairs, the complex-FP64 method, the point-cloud
+// kernel) come whole from lane 0. The Q shares sum to the entry (the BC
+// substitution of regular entries is linear in the operators).
+template <int MODE, typename T>
+__device__ __forceinline__ T aca_entry_part(const AcaArgs& a, int64_t row, int64_t col, int q,
+                                            int Q) {
+  if constexpr ((MODE == 0 || MODE == 2) && sizeof(T) == sizeof(float2)) {
+    if (row != col && !near_pair32(a.EF, row, col, a.near_r2f)) {
+      const ElemF& P = a.EF[row];
+      const ElemF& Qe = a.EF[col];
+      OpsF o;
+      if (a.rule_tab) {
+        float dx, dy, dz;
+        centroid_diff(P, Qe, dx, dy, dz);
+        const float em = Qe.emax;
+        const float x = __logf(sqrtf(dx * dx + dy * dy + dz * dz) / em);
+        const float y = __logf(a.kf * em);
+        const int ix = min(max((int)floorf((x - a.tab_x0) / a.tab_dx), 0), ACA_TAB_N - 1);
+        const int iy = min(max((int)floorf((y - a.tab_y0) / a.tab_dy), 0), ACA_TAB_N - 1);
+        const int c = min((int)a.rule_tab[ix * ACA_TAB_N + iy], SEL_C - 1);
+        o = ops_pts32(P, Qe, a.kf, c_cls.x1, c_cls.x2, c_cls.w, c_cls.off[c] + q, c_cls.off[c + 1], Q);
+      } else {
+        o = ops_pts32(P, Qe, a.kf, c_rules.freg_x1, c_rules.freg_x2, c_rules.freg_w, q, 16, Q);
+      }
+      if constexpr (MODE == 2)
+        ops_add(o, ops_pts32(P, a.EFr[col], a.kf, c_rules.freg_x1, c_rules.freg_x2,
+                             c_rules.freg_w, q, 16, Q));
+      float2 p, d;
+      substitute32(o, a.bc[col], a.alphaf, p, d);
+      return a.which ? d : p;
+    }
+    return q == 0 ? entry64f(a, row, col) : T{0, 0};
+  } else {
+    return q == 0 ? aca_entry<MODE, T>(a, row, col) : T{0, 0};
+  }
+}
+
+// Lanes per entry of a residual row or column of cnt entries: the FP32 path
+// splits each entry's rule over 4-16 lanes when at most a quarter of the CTA
+// would be busy otherwise (a 32-entry column on 128 threads: 4 lanes each).
+// Two lanes per entry measured slower than one (sphere, 20,480 elements).
+template <int MODE, typename T, int NT>
+__device__ __forceinline__ int lanes_per_entry(int cnt) {
+  if constexpr (!((MODE == 0 || MODE == 2) && sizeof(T) == sizeof(float2))) return 1;
+  if (4 * cnt > NT) return 1;
+  int Q = 4;
+  while (Q < 16 && 2 * Q * cnt <= NT) Q *= 2;
+  return Q;
+}
+
+// sum over l = q, q + Q, .. < k of p[l * stride] * c[l]
+template <typename T>
+__device__ __forceinline__ T dot_strided_part(const T* p, int64_t stride, const T* c, int k, int q,
+                                              int Q) {
+  T acc{0, 0};
+  for (int l = q; l < k; l += Q) {
+    const T v = p[(int64_t)l * stride], cq = c[l];
+    acc.x += v.x * cq.x - v.y * cq.y;
+    acc.y += v.x * cq.y + v.y * cq.x;
+  }
+  return acc;
+}
+
 // sum_l p[l * stride] * c[l] with 4 independent loads in flight (the chain
 // of dependent loads was the ACA's latency bottleneck)
 template <typename T>
@@ -265,9 +330,21 @@ __device__ void residual_col(const AcaArgs& a, const FarBlock& fb, const T* U, c
                              const T* S, int k, int ci, T* dst, T* coef) {
   for (int l = threadIdx.x; l < k; l += NT) coef[l] = cx_mul(S[l], V[(int64_t)l * fb.n + ci]);
   __syncthreads();
-  for (int i = threadIdx.x; i < fb.m; i += NT) {
-    T v = aca_entry<MODE, T>(a, fb.r0 + i, fb.c0 + ci);
-    dst[i] = cx_sub(v, dot_strided(U + i, (int64_t)fb.m, coef, k));
+  // Q lanes per entry (consecutive lanes; every lane of a warp loops alike)
+  const int Q = lanes_per_entry<MODE, T, NT>(fb.m);
+  const int q = threadIdx.x & (Q - 1);
+  for (int base = 0; base < fb.m; base += NT / Q) {
+    const int i = base + threadIdx.x / Q;
+    T v{0, 0};
+    if (i < fb.m)
+      v = cx_sub(aca_entry_part<MODE, T>(a, fb.r0 + i, fb.c0 + ci, q, Q),
+                 Q == 1 ? dot_strided(U + i, (int64_t)fb.m, coef, k)
+                        : dot_strided_part(U + i, (int64_t)fb.m, coef, k, q, Q));
+    for (int o = Q / 2; o > 0; o >>= 1) {
+      v.x += __shfl_xor_sync(0xffffffffu, v.x, o, Q);
+      v.y += __shfl_xor_sync(0xffffffffu, v.y, o, Q);
+    }
+    if (q == 0 && i < fb.m) dst[i] = v;
   }
   __syncthreads();
 }
@@ -278,9 +355,20 @@ __device__ void residual_row(const AcaArgs& a, const FarBlock& fb, const T* U, c
                              const T* S, int k, int ri, T* dst, T* coef) {
   for (int l = threadIdx.x; l < k; l += NT) coef[l] = cx_mul(U[(int64_t)l * fb.m + ri], S[l]);
   __syncthreads();
-  for (int j = threadIdx.x; j < fb.n; j += NT) {
-    T v = aca_entry<MODE, T>(a, fb.r0 + ri, fb.c0 + j);
-    dst[j] = cx_sub(v, dot_strided(V + j, (int64_t)fb.n, coef, k));
+  const int Q = lanes_per_entry<MODE, T, NT>(fb.n);
+  const int q = threadIdx.x & (Q - 1);
+  for (int base = 0; base < fb.n; base += NT / Q) {
+    const int j = base + threadIdx.x / Q;
+    T v{0, 0};
+    if (j < fb.n)
+      v = cx_sub(aca_entry_part<MODE, T>(a, fb.r0 + ri, fb.c0 + j, q, Q),
+                 Q == 1 ? dot_strided(V + j, (int64_t)fb.n, coef, k)
+                        : dot_strided_part(V + j, (int64_t)fb.n, coef, k, q, Q));
+    for (int o = Q / 2; o > 0; o >>= 1) {
+      v.x += __shfl_xor_sync(0xffffffffu, v.x, o, Q);
+      v.y += __shfl_xor_sync(0xffffffffu, v.y, o, Q);
+    }
+    if (q == 0 && j < fb.n) dst[j] = v;
   }
   __syncthreads();
 }
@@ -430,7 +518,7 @@ __global__ void __launch_bounds__(NT, NT == 128 ? 8 : 2) aca_kernel(AcaArgs a) {
     const int npiv = a.piv_cnt[bi];
     for (int p = 0; p < npiv && k < kmax; p++) {
       int ri = piv[2 * p], ci = piv[2 * p + 1];
-      const T pivv = aca_entry<MODE, T>(a, fb.r0 + ri, fb.c0 + ci);
+      const T pivv = aca_entry_part<MODE, T>(a, fb.r0 + ri, fb.c0 + ci, 0, 1);
       const R pabs2 = mag2(pivv);
       if (sqrt(pabs2) < tiny) continue;
       // approximation already good at the seed?

@@ -882,6 +882,7 @@ void upload_df_plans(bem_handle* h) {
     d.view.erows = (const HluDfRow*)d.erows.p;
     d.view.cols = (const HluDfCol*)d.cols.p;
     d.view.slot = d.slot.p;
+    d.view.nslot = p.nslot;
     d.view.diag = d.diag.p;
     d.view.D = p.D();
     nslot = std::max(nslot, p.nslot);
@@ -890,9 +891,9 @@ void upload_df_plans(bem_handle* h) {
   h->dfXi.ensure((size_t)HLU_DF_MAX_R * h->N * cs);
   h->dfAcc.ensure((size_t)HLU_DF_MAX_R * h->N * cs);
   h->dfEacc.ensure((size_t)HLU_DF_MAX_R * h->N * cs);
-  h->dfPre.ensure((size_t)std::max<int64_t>(nslot, 1) * cs);
+  h->dfPre.ensure((size_t)std::max<int64_t>(2 * nslot, 1) * cs);  // pre and pre2
   h->dfFin.ensure((size_t)std::max<int64_t>(nslot, 1) * cs);
-  h->dfCtrl.ensure((size_t)(4 + 3 * D));
+  h->dfCtrl.ensure((size_t)(4 + 4 * D));
   h->dfErr.ensure(1);
   CK(cudaMemsetAsync(h->dfErr.p, 0, sizeof(int), s));
   h->df_ok = true;
@@ -1021,6 +1022,7 @@ void upload_df_plans_device(bem_handle* h) {
     d.view.erows = (const HluDfRow*)d.erows.p;
     d.view.cols = (const HluDfCol*)d.cols.p;
     d.view.slot = d.slot.p;
+    d.view.nslot = p.nslot;
     d.view.diag = h->dArena.p + (size_t)(q ? h->hp.rinv_base : h->hp.qh_base) * cs;
     d.view.D = p.D();
     nslot = std::max(nslot, p.nslot);
@@ -1029,9 +1031,9 @@ void upload_df_plans_device(bem_handle* h) {
   h->dfXi.ensure((size_t)HLU_DF_MAX_R * h->N * cs);
   h->dfAcc.ensure((size_t)HLU_DF_MAX_R * h->N * cs);
   h->dfEacc.ensure((size_t)HLU_DF_MAX_R * h->N * cs);
-  h->dfPre.ensure((size_t)std::max<int64_t>(nslot, 1) * cs);
+  h->dfPre.ensure((size_t)std::max<int64_t>(2 * nslot, 1) * cs);  // pre and pre2
   h->dfFin.ensure((size_t)std::max<int64_t>(nslot, 1) * cs);
-  h->dfCtrl.ensure((size_t)(4 + 3 * D));
+  h->dfCtrl.ensure((size_t)(4 + 4 * D));
   h->dfErr.ensure(1);
   CK(cudaMemsetAsync(h->dfErr.p, 0, sizeof(int), s));
   h->df_ok = true;
@@ -1375,6 +1377,24 @@ void df_trace_summary(bem_handle* h, const DBuf<unsigned long long>& tr, int R, 
   std::fprintf(f, "df L sweep: chunks %d R %d total_us %.1f per chunk us: wait %.3f corner %.3f "
                "solve %.3f handover %.3f\n", D, R, 1e-3 * (double)(t[4 * (D - 1) + 3] - t[0]),
                ph[0] / n, ph[1] / n, ph[2] / n, ph[3] / n);
+  // the wait by corner kind (device factors: the program's plan): none,
+  // full, low rank, low rank with a prefix (R(i) then waits for C(i - 2))
+  if (h->hlu_dev && (int)h->hpl.chunks.size() == D + 1) {
+    double wsum[4] = {}, late[4] = {};
+    int64_t cnt[4] = {};
+    for (int i = 1; i + 1 < D; i++) {
+      const HluDfChunk& c = h->hpl.chunks[i];
+      const int kind = c.corner < 0 ? 0 : (!(c.cflags & 1) ? 1 : ((c.cflags & 2) ? 3 : 2));
+      wsum[kind] += 1e-3 * (double)(t[4 * i + 1] - t[4 * i]);
+      late[kind] += (double)(h->hpl.chunks[i + 1].rbeg - c.rbeg);
+      cnt[kind]++;
+    }
+    const char* nm[4] = {"none", "full", "lowrank", "lowrank+pre"};
+    for (int k = 0; k < 4; k++)
+      if (cnt[k])
+        std::fprintf(f, "  corner %-11s chunks %6lld wait_us %.3f late_entries %.2f\n", nm[k],
+                     (long long)cnt[k], wsum[k] / cnt[k], late[k] / cnt[k]);
+  }
   std::fclose(f);
 }
 

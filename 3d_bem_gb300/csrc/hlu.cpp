@@ -879,7 +879,10 @@ bool df_plan_impl(const FlatFactor& f, int64_t N, int elem_bytes, HluDfPlan& p,
         ch[i].corner = o;
         ch[i].cro = ro;
         ch[i].cco = (int32_t)(cr0[i - 1] - L[2]);
-        ch[i].cflags = (lr ? 1 : 0) | (lr && ca < cb ? 2 : 0) | (!lr && ca == cb ? 4 : 0);
+        ch[i].cflags = (lr ? 1 : 0) | (lr && ca < cb ? 2 : 0) | (!lr && ca == cb ? 4 : 0) |
+                       (lr && ca + 1 < cb ? 8 : 0);
+        ch[i].cco2 = lr && ca < cb ? (int32_t)(cr0[i - 2] - L[2]) : 0;
+        ch[i].cw2 = lr && ca < cb ? (int32_t)cm[i - 2] : 0;
         ch[i].cm = (int32_t)L[1];
         ch[i].cn = (int32_t)L[3];
         ch[i].ck = (int32_t)k;
@@ -898,8 +901,10 @@ bool df_plan_impl(const FlatFactor& f, int64_t N, int elem_bytes, HluDfPlan& p,
       }
     }
     if (!lr) continue;
-    // the prefix over cols ca..cb-1 is read by the corner (rows cb + 1) and
-    // by mode 2 (rows cb + 2); fin by mode 1
+    // prefixes of t = V x: pre over cols ca..cb-2, read by the corner (rows
+    // cb + 1, which adds chunks cb - 1 and cb itself, so it waits on nothing
+    // solved after chunk cb - 2); pre2 over ca..cb-1, read by mode 2 (rows
+    // cb + 2) and by the last step into fin (mode 1)
     const bool uses_pre = ca < cb && ra <= cb + 2;
     if (!uses_pre && !uses_fin) continue;
     p.slot[o] = p.nslot;
@@ -907,8 +912,10 @@ bool df_plan_impl(const FlatFactor& f, int64_t N, int elem_bytes, HluDfPlan& p,
     for (int j = ca; j <= cb; j++) {
       const bool last = j == cb;
       if (last && !uses_fin) continue;
+      const int32_t fl = (j == ca ? 1 : 0) | (last ? 2 : 0) | (j == cb - 1 ? 4 : 0) |
+                         (last && ca < cb ? 8 : 0);
       for (int32_t l = 0; l < (int32_t)k; l++)
-        cl[j].push_back(HluDfCol{o, (int32_t)(cr0[j] - L[2]), (j == ca ? 1 : 0) | (last ? 2 : 0), l});
+        cl[j].push_back(HluDfCol{o, (int32_t)(cr0[j] - L[2]), fl, l});
     }
   }
   // CSR lists, apply matrices

@@ -204,19 +204,23 @@ int launch_hlu_sweep(const int32_t* sched, int nops, const int64_t* leaves, cons
 // order: s = w(i) - acc(i) - corner(i) x, x(i) = M(i) s with M = Q^H (L) or
 // R^{-1} (U), then publishes progress = i + 1. Its inputs for the next step
 // (M, the corner leaf's rows and the corner's already solved columns) are
-// copied to shared memory with cp.async while the current step runs.
+// copied to shared memory with cp.async while the current step runs. A
+// low-rank corner's t = V x takes the prefix over the columns before chunk
+// i - 2 (pre) and adds chunks i - 2 and i - 1 from the driver's own last two
+// results, so no item solved after x(i - 2) sits between two driver steps.
 // Blocks 1.. (helpers) claim items in a fixed order, three per level
 // L = 0, 1, ...: C(L - 1), E(L + LAG - 1), R(L + 1), where
-//   C(j): t partials of the low-rank leaves over cols(j) into pre / fin, one
-//         warp per (leaf, row of V), lanes over the columns; ready when x(j)
-//         is solved and C(j - 1) is done;
+//   C(j): t partials of the low-rank leaves over cols(j) into pre (through
+//         the third-to-last column chunk of a leaf), pre2 (through the
+//         second-to-last) or fin (complete), one warp per (leaf, row of V),
+//         lanes over the columns; ready when x(j) is solved and C(j - 1) is
+//         done;
 //   E(i): eacc(i), the contributions of the early leaves to rows(i), one warp
 //         per leaf; ready when x(i - LAG) is solved and C(i - LAG) is done,
 //         LAG - 2 steps before the driver needs it;
 //   R(i): acc(i) = eacc(i) + the late leaves (at most LAG - 2, one warp each,
 //         their constants staged in shared memory before the wait); ready
-//         when x(i - 2) is solved and C(i - 3) (C(i - 2) for a low-rank
-//         corner with a prefix) and E(i) are done.
+//         when x(i - 2) is solved and C(i - 3) and E(i) are done.
 // Every item waits only on progress up to its level and on items earlier in
 // the order, and the launch is cooperative (all blocks resident), so the
 // chain always advances. Each sum has one fixed order: results do not depend
@@ -237,7 +241,8 @@ constexpr int LAG = HLU_DF_LAG, NLATE = HLU_DF_NLATE;
 constexpr int PS = 4;  // column pairs per warp and round in C(j)
 constexpr unsigned long long DF_TIMEOUT_NS = 2000000000ull;
 constexpr int MS_ELEMS = DM * (DM + 1);  // apply matrix, rows padded
-constexpr int CS_ELEMS = 2 * DK * DM;    // corner: F (<= 64 cols x rows) or U rows + V cols
+constexpr int CS_ELEMS = 3 * DK * DM;    // corner: F (<= 64 cols x rows) or U rows + V over
+                                         // the columns of chunks i - 1 and i - 2
 constexpr int BUF_ELEMS = MS_ELEMS + CS_ELEMS;
 constexpr int WCOLS = 2 * DM;            // widest staged full leaf (corner, late entries)
 
@@ -273,7 +278,7 @@ template <typename T2> __device__ __forceinline__ void cmac(T2& s, T2 a, T2 b) {
 template <typename T2>
 constexpr size_t df_smem() {
   constexpr size_t drv = 2 * BUF_ELEMS * sizeof(T2) + 2 * WCOLS * DR * sizeof(T2) +
-                         2 * DM * DR * sizeof(T2) + DK * DR * sizeof(T2) + 4 * sizeof(HluDfChunk) +
+                         3 * DM * DR * sizeof(T2) + DK * DR * sizeof(T2) + 4 * sizeof(HluDfChunk) +
                          NW * 32 * sizeof(T2);
   constexpr size_t ei = NW * DR * 32 * sizeof(T2);
   constexpr size_t ri = NW * DR * 32 * sizeof(T2) + NLATE * WCOLS * DR * sizeof(T2) +
@@ -331,6 +336,10 @@ __device__ bool df_wait(const int* p, int v, int* err) {
   }
 }
 
+// thread 0 only: wait until chunks 0 .. v - 1 are solved
+struct DfArgs;
+__device__ bool df_wait_progress(const DfArgs& a, int v);
+
 // publish: every thread's global writes of this block, then the flag (the
 // barrier orders them before thread 0's release store)
 __device__ __forceinline__ void df_publish(int* p, int v) {
@@ -365,7 +374,15 @@ struct DfArgs {
   __device__ int* flagR(int i) const { return ctrl + 4 + i; }
   __device__ int* flagC(int j) const { return ctrl + 4 + p.D + j; }
   __device__ int* flagE(int i) const { return ctrl + 4 + 2 * p.D + i; }
+  // chunk i solved (x(i) published): one flag per chunk, so the items that
+  // wait for different chunks poll different lines instead of one counter
+  __device__ int* flagX(int i) const { return ctrl + 4 + 3 * p.D + i; }
 };
+
+__device__ bool df_wait_progress(const DfArgs& a, int v) {
+  return v <= 0 || df_wait(a.flagX(v - 1), 1, a.err);
+}
+
 
 // cp.async of step i's inputs: M(i) into Ms (row-major, padded rows); the
 // corner leaf's F[rows(i), :] as Cs[c * DM + row] (full, <= WCOLS columns)
@@ -408,6 +425,14 @@ __device__ void df_stage(const DfArgs& a, const HluDfChunk& c, const HluDfChunk&
       const int l = e / pw, cc = e % pw;
       cp_async(Cs + DK * DM + l * DM + cc, V + l * nL + cc);
     }
+    if (c.cflags & 2) {  // and over cols(i - 2)
+      const int w2 = c.cw2;
+      const T2* V2 = Dd + mL * k + c.cco2;
+      for (int e = tid; e < k * w2; e += DT) {
+        const int l = e / w2, cc = e % w2;
+        cp_async(Cs + 2 * DK * DM + l * DM + cc, V2 + l * nL + cc);
+      }
+    }
   }
 }
 
@@ -421,8 +446,8 @@ template <typename T2>
 __device__ void df_driver(const DfArgs& a, unsigned char* sm) {
   T2* bufs = (T2*)sm;
   T2* xcs = bufs + 2 * BUF_ELEMS;            // corner columns, 2 buffers [c][r]
-  T2* xs = xcs + 2 * WCOLS * DR;             // x of the last chunk, [c][r]
-  T2* ss = xs + DM * DR;                     // s, [t][r]
+  T2* xs2 = xcs + 2 * WCOLS * DR;            // x of the last two chunks, [chunk & 1][c][r]
+  T2* ss = xs2 + 2 * DM * DR;                // s, [t][r]
   T2* tks = ss + DM * DR;                    // corner t, [l][r]
   HluDfChunk* ring = (HluDfChunk*)(tks + DK * DR);  // chunks, slot = index & 3
   T2* red = (T2*)(ring + 4);                 // partial sums, [part][r][row]
@@ -474,6 +499,7 @@ __device__ void df_driver(const DfArgs& a, unsigned char* sm) {
     T2 accv = mk<T2>(0, 0);
     if (i >= 1 && own) accv = ldv((const T2*)a.acc + (int64_t)r * N + c.r0 + row);
     T2 cs = mk<T2>(0, 0);  // this thread's part of the corner contribution
+    const T2* xs = xs2 + ((i - 1) & 1) * DM * DR;  // x(i - 1)
     if (c.corner >= 0) {
       const int64_t mL = c.cm, nL = c.cn;
       const int k = c.ck;
@@ -492,15 +518,22 @@ __device__ void df_driver(const DfArgs& a, unsigned char* sm) {
               cmac(cs, HC<T2>::ld(fg + (int64_t)cc * mL), ldv(xr + cc));
           }
         }
-      } else {  // low rank: t = pre + V[:, cols(i - 1)] x(i - 1), then U[rows(i), :] t
-        // pre is complete: R(i) waited for C(i - 2) before publishing
+      } else {  // low rank: t = pre + V[:, cols(i - 2)] x(i - 2) + V[:, cols(i - 1)] x(i - 1),
+                // then U[rows(i), :] t; pre (the columns before chunk i - 2) is
+                // complete: R(i) waited for C(i - 3) before publishing
         const T2* pre = (const T2*)a.pre + (a.p.slot[c.corner] >= 0 ? a.p.slot[c.corner] : 0);
+        const T2* xp = xs2 + (i & 1) * DM * DR;  // x(i - 2)
+        const int w2 = c.cw2;
         for (int q = tid; q < k * a.R; q += DT) {
           const int l = q / a.R, rr = q % a.R;
           T2 t = mk<T2>(0, 0);
           const T2* v = Cs + DK * DM + l * DM;
           for (int cc = 0; cc < pw; cc++) cmac(t, v[cc], xs[cc * DR + rr]);
           if (c.cflags & 2) {
+            const T2* v2 = Cs + 2 * DK * DM + l * DM;
+            for (int cc = 0; cc < w2; cc++) cmac(t, v2[cc], xp[cc * DR + rr]);
+          }
+          if (c.cflags & 8) {
             const T2 p = ldv(pre + l * DR + rr);
             t.x = p.x + t.x;
             t.y = p.y + t.y;
@@ -513,7 +546,7 @@ __device__ void df_driver(const DfArgs& a, unsigned char* sm) {
       }
       if (act) red[(part * a.R + r) * 32 + row] = cs;
     }
-    __syncthreads();  // corner partials complete; xs (chunk i - 1) no longer read
+    __syncthreads();  // corner partials complete; x(i - 2) no longer read
     if (tr && tid == 0) tr[4 * (int64_t)i + 2] = gtimer();
     if (own) {
       if (c.corner >= 0) {
@@ -543,12 +576,13 @@ __device__ void df_driver(const DfArgs& a, unsigned char* sm) {
         y.x += v.x;
         y.y += v.y;
       }
-      xs[row * DR + r] = y;
+      xs2[(i & 1) * DM * DR + row * DR + r] = y;  // x(i), over x(i - 2)
       xi[(int64_t)r * N + c.r0 + row] = y;
       if ((void*)xi != (void*)a.x) a.x[(int64_t)r * N + c.r0 + row] = make_double2(y.x, y.y);
     }
     if (tr && tid == 0) tr[4 * (int64_t)i + 3] = gtimer();
     df_publish(a.ctrl + 1, i + 1);
+    if (tid == 0) st_release(a.flagX(i), 1);
   }
   cp_async_wait_all();
 }
@@ -565,7 +599,7 @@ __device__ bool df_early_item(const DfArgs& a, int i, unsigned char* sm) {
   const int e1 = a.p.chunks[i + 1].ebeg;
   bool ok = true;
   if (tid == 0) {
-    ok = df_wait(a.ctrl + 1, i - LAG + 1, a.err);
+    ok = df_wait_progress(a, i - LAG + 1);
     if (ok && i >= LAG) ok = df_wait(a.flagC(i - LAG), 1, a.err);
   }
   if (!__syncthreads_and(ok)) return false;
@@ -688,8 +722,8 @@ __device__ bool df_late_item(const DfArgs& a, int i, unsigned char* sm) {
   cp_async_commit();
   bool ok = true;
   if (tid == 0) {
-    ok = df_wait(a.ctrl + 1, i - 1, a.err);
-    const int cdep = (c.cflags & 3) == 3 ? i - 2 : i - 3;
+    ok = df_wait_progress(a, i - 1);
+    const int cdep = i - 3;  // pre (corner) and pre2 (mode 2) are complete after C(i - 3)
     if (ok && cdep >= 0) ok = df_wait(a.flagC(cdep), 1, a.err);
     if (ok && i >= LAG - 1) ok = df_wait(a.flagE(i), 1, a.err);
   }
@@ -714,7 +748,7 @@ __device__ bool df_late_item(const DfArgs& a, int i, unsigned char* sm) {
       if (lane < w2)
         for (int r = 0; r < RR; r++) cp_async(xs + lane * DR + r, xi + (int64_t)r * N + c02 + lane);
       if (en.mode == 2) {
-        const T2* pre = (const T2*)a.pre + so;
+        const T2* pre = (const T2*)a.pre + a.p.nslot + so;  // pre2
         for (int q = lane; q < k * DR; q += 32)
           if (q % DR < RR) cp_async(ts + q, pre + q);
       }
@@ -822,7 +856,7 @@ __device__ bool df_col_item(const DfArgs& a, int j) {
   load(0);
   bool ok = true;
   if (tid == 0) {
-    ok = df_wait(a.ctrl + 1, j + 1, a.err);
+    ok = df_wait_progress(a, j + 1);
     if (ok && j >= 1) ok = df_wait(a.flagC(j - 1), 1, a.err);
   }
   if (!__syncthreads_and(ok)) return false;
@@ -836,7 +870,8 @@ __device__ bool df_col_item(const DfArgs& a, int j) {
 #pragma unroll
     for (int s = 0; s < PS; s++) {
       pr[s] = mk<T2>(0, 0);
-      if (fl[s] >= 0 && !(fl[s] & 1) && lane < RR) pr[s] = ldv((const T2*)a.pre + so[s] + lane);
+      if (fl[s] >= 0 && !(fl[s] & 1) && lane < RR)
+        pr[s] = ldv((const T2*)a.pre + ((fl[s] & 8) ? a.p.nslot : 0) + so[s] + lane);
     }
 #pragma unroll
     for (int s = 0; s < PS; s++) {
@@ -852,7 +887,8 @@ __device__ bool df_col_item(const DfArgs& a, int j) {
       if (lane < RR) {
         res.x = pr[s].x + res.x;
         res.y = pr[s].y + res.y;
-        ((T2*)((fl[s] & 2) ? a.fin : a.pre))[so[s] + lane] = res;
+        T2* dst = (fl[s] & 2) ? (T2*)a.fin : (T2*)a.pre + ((fl[s] & 4) ? a.p.nslot : 0);
+        dst[so[s] + lane] = res;
       }
     }
   }
@@ -919,7 +955,7 @@ int launch_hlu_df(const HluDfDev& p, const int64_t* leaves, const void* data, in
                   cudaStream_t s, HmvGate gate) {
   if (p.D <= 0 || R <= 0) return 0;
   if (R > HLU_DF_MAX_R) throw std::runtime_error("launch_hlu_df: more than 8 right-hand sides");
-  CUDA_OK(cudaMemsetAsync(ws.ctrl, 0, (size_t)(4 + 3 * p.D) * sizeof(int), s));
+  CUDA_OK(cudaMemsetAsync(ws.ctrl, 0, (size_t)(4 + 4 * p.D) * sizeof(int), s));
   DfArgs a;
   a.p = p;
   a.lv = leaves;

@@ -44,24 +44,28 @@ struct HluDfChunk {
   int32_t corner;       // leaf index holding rows(i) x cols(i - 1), -1 if none
   int32_t cro;          // row offset of this chunk inside the corner leaf
   int32_t cco;          // column offset of chunk i - 1 inside the corner leaf
-  int32_t cflags;       // bit 0 low rank, bit 1 with earlier column chunks (pre),
-                        // bit 2 full leaf whose columns are exactly chunk i - 1
+  int32_t cflags;       // bit 0 low rank, bit 1 with earlier column chunks,
+                        // bit 2 full leaf whose columns are exactly chunk i - 1,
+                        // bit 3 low rank with columns before chunk i - 2 (their
+                        // prefix pre is complete once C(i - 3) is done)
   int32_t rbeg, ebeg;   // starts of the late and early row lists
   int32_t cbeg;         // start of the column pair list (ends: the next
                         // chunk's, a sentinel chunk closes them)
-  int32_t pad0;
+  int32_t cco2;         // low rank with bit 1: column offset of chunk i - 2 in the leaf
   int64_t moff;         // offset of the m x m apply matrix (row-major)
   int32_t cm, cn, ck;   // corner leaf: rows, columns, rank
   int32_t cc0;          // corner leaf: first column
   int64_t cdata;        // corner leaf: data offset
-  int64_t pad1;         // 80 bytes: five 16-byte copies
+  int32_t cw2;          // low rank with bit 1: columns of chunk i - 2 (its row count;
+                        // in the U sweep they follow chunk i - 1's in the leaf)
+  int32_t pad1;         // 80 bytes: five 16-byte copies
 };
 static_assert(sizeof(HluDfChunk) == 80, "HluDfChunk is copied in 16-byte pieces");
 
 // row list entry of chunk i: the contribution of one leaf to rows(i)
 struct HluDfRow {
   int32_t leaf, ro;  // leaf and the row offset of chunk i inside it
-  int32_t mode;      // 0 full; low rank: 1 t = fin, 2 t = pre + V x(i - 2), 3 t = V x(i - 2)
+  int32_t mode;      // 0 full; low rank: 1 t = fin, 2 t = pre2 + V x(i - 2), 3 t = V x(i - 2)
   int32_t co2;       // column offset of chunk i - 2 inside the leaf (modes 2, 3)
   int32_t soff;      // late entries: staging offset (factor elements), -1 = read from global
 };
@@ -69,7 +73,9 @@ struct HluDfRow {
 // column pair list of chunk j: row l of a low-rank leaf's V over cols(j)
 struct HluDfCol {
   int32_t leaf, co;  // leaf and the column offset of chunk j inside it
-  int32_t flags;     // bit 0 first chunk of the leaf (no pre yet), bit 1 last (write fin)
+  int32_t flags;     // bit 0 first chunk of the leaf (no prefix yet), bit 1 last (write
+                     // fin), bit 2 second to last (write pre2), bit 3 read pre2
+                     // (else pre)
   int32_t l;         // row of V (0 <= l < rank)
 };
 
@@ -80,6 +86,8 @@ struct HluDfDev {
   const HluDfRow* erows = nullptr;  // early
   const HluDfCol* cols = nullptr;
   const int64_t* slot = nullptr;  // per leaf: offset of its k x HLU_DF_MAX_R pre/fin slots
+  int64_t nslot = 0;              // pre2 of a leaf: pre + nslot (its prefix through the
+                                  // second-to-last column chunk)
   const void* diag = nullptr;     // apply matrices, factor precision
   int D = 0;
 };
@@ -87,7 +95,7 @@ struct HluDfDev {
 // Workspace shared by the sweeps of one handle, vectors in the factor type
 // (HLU_DF_MAX_R x N each): xi (the solution as the helpers read it; unused
 // for FP64 factors, where x itself is read), acc and eacc (all and early
-// contributions); pre and fin (nslot values each); ctrl (4 + 3 D ints,
+// contributions); pre and fin (nslot values each); ctrl (4 + 4 D ints,
 // cleared by every launch), err (sticky error word: nonzero after a wait ran
 // out of time).
 struct HluDfWork {

@@ -501,6 +501,59 @@ __device__ __forceinline__ OpsF ops_rule32_pts(const ElemF* __restrict__ EF, int
   return o;
 }
 
+// The same FP32 integrand over the points b, b + s, b + 2 s, .. < e of the
+// tables x1, x2, wt: one lane's share when s lanes split an entry's rule (the
+// operators are sums over the points, so the shares add up to the entry).
+__device__ __forceinline__ OpsF ops_pts32(const ElemF& P, const ElemF& Q, float k,
+                                          const float* x1, const float* x2, const float* wt,
+                                          int b, int e, int s) {
+  float dx, dy, dz;
+  centroid_diff(P, Q, dx, dy, dz);
+  const float npx = P.nrm[0], npy = P.nrm[1], npz = P.nrm[2];
+  const float nqx = Q.nrm[0], nqy = Q.nrm[1], nqz = Q.nrm[2];
+  const float upNq = npx * nqx + npy * nqy + npz * nqz;
+  const float inv4pi = 0.0795774715459476679f;
+  float Lx = 0, Ly = 0, Mx = 0, My = 0, Tx = 0, Ty = 0, Nx = 0, Ny = 0;
+  for (int i = b; i < e; i += s) {
+    const float a1 = x1[i], a2 = x2[i], a3 = 1.0f - a2 - a1, w = wt[i];
+    const float rx = dx - (a1 * Q.v[0] + a2 * Q.v[3] + a3 * Q.v[6]);
+    const float ry = dy - (a1 * Q.v[1] + a2 * Q.v[4] + a3 * Q.v[7]);
+    const float rz = dz - (a1 * Q.v[2] + a2 * Q.v[5] + a3 * Q.v[8]);
+    const float rr = rx * rx + ry * ry + rz * rz;
+    const float ir = rsqrtf(rr);
+    const float r = rr * ir;
+    const float rnq = -(rx * nqx + ry * nqy + rz * nqz) * ir;
+    const float rnp = (rx * npx + ry * npy + rz * npz) * ir;
+    const float kr = k * r;
+    float sn, cs;
+    sincosf(kr, &sn, &cs);
+    const float g0 = ir * inv4pi;
+    const float Gx = cs * g0, Gy = sn * g0;
+    const float Grx = Gx * ir, Gry = Gy * ir;
+    const float dGx = -Grx - kr * Gry, dGy = -Gry + kr * Grx;
+    const float Grrx = Grx * ir, Grry = Gry * ir;
+    const float a2c = 2.0f - kr * kr, b2c = -2.0f * kr;
+    const float d2Gx = Grrx * a2c - Grry * b2c, d2Gy = Grrx * b2c + Grry * a2c;
+    Lx += w * Gx;
+    Ly += w * Gy;
+    const float wm = w * rnq, wtt = w * rnp;
+    Mx += wm * dGx;
+    My += wm * dGy;
+    Tx += wtt * dGx;
+    Ty += wtt * dGy;
+    const float f1 = -(upNq + rnp * rnq) * ir, f2 = rnp * rnq;
+    Nx += w * (f1 * dGx + f2 * d2Gx);
+    Ny += w * (f1 * dGy + f2 * d2Gy);
+  }
+  const float A = Q.area;
+  OpsF o;
+  o.L = fmk(A * Lx, A * Ly);
+  o.M = fmk(A * Mx, A * My);
+  o.Mt = fmk(A * Tx, A * Ty);
+  o.N = fmk(A * Nx, A * Ny);
+  return o;
+}
+
 __device__ __forceinline__ void substitute32(const OpsF& o, const BcCoef& bc, float2 alpha,
                                              float2& phi, float2& dphi) {
   const float2 X = fadd(o.L, fmul(alpha, o.Mt));

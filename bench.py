@@ -366,12 +366,16 @@ def pencil_solver(pkg, tri, beta, precision, **extra):
 
 def sweep_frequencies(meshes, steps, warmup):
     """K of the 64 log-spaced frequencies spread evenly over the band (all 64
-    for K >= 64) and W warm-up frequencies at geometric midpoints of the
-    first intervals (none of them timed)."""
+    for K >= 64) and W warm-up frequencies at geometric midpoints of
+    intervals spread over the band (none of them timed; the highest one
+    first meets the largest ACA ranks, so any growth of the rank
+    reservation happens before the timed region)."""
     f = meshes.log_frequencies(PENCIL_F[2], PENCIL_F[0], PENCIL_F[1])
     k = min(max(steps, 1), len(f))
     idx = np.unique(np.round(np.linspace(0, len(f) - 1, k)).astype(int))
-    warm = [float(np.sqrt(f[i] * f[i + 1])) for i in range(min(warmup, len(f) - 1))]
+    nw = min(max(warmup, 1), len(f) - 1)
+    wi = np.unique(np.round(np.linspace(len(f) - 2, 0, nw)).astype(int))[::-1]
+    warm = [float(np.sqrt(f[i] * f[i + 1])) for i in wi]
     return [float(x) for x in f[idx]], warm
 
 
@@ -534,7 +538,7 @@ def run_ours(args):
     g_dev = torch.from_numpy(np.ascontiguousarray(g_host.T)).reshape(-1).to("cuda")
     learned = (1 if args.selector else 0) | (0 if args.no_aca_rules else 2)
     extra = {"selector": learned} if learned else {}
-    extra["near_fp64"] = 0 if args.fp32_near else 1
+    extra["near_fp64"] = 1 if args.near_fp64 else 0
 
     # batched sweep: W concurrent frequency workers (each its own stream,
     # buffers and H-LU factors), K frequencies; g and p resident in GPU memory
@@ -610,7 +614,7 @@ def run_ours(args):
                    "learned_selector": bool(args.selector),
                    "learned_aca_rules": not args.no_aca_rules,
                    "near_field": "complex FP32 in GMRES; FP64 (two complex-FP32 parts) in the "
-                                 "refinement residual" if not args.fp32_near else "complex FP32",
+                                 "refinement residual" if args.near_fp64 else "complex FP32",
                    "parallelism": f"replicas{ws}" if ws > 1 else "single-gpu",
                    "l2": "working set (H-matrices and factors, GBs) >> 129 MB L2; no flush"},
         "e2e": {"value": round(e2e, 4), "unit": UNIT, "h2d_bytes_per_step": n * R * 16,
@@ -688,6 +692,27 @@ def run_hlu_only(args):
     torch.cuda.synchronize()
     print(json.dumps({"hlu_only": {"n_elements": int(tri.shape[0]),
                                    "seconds": round(time.perf_counter() - t0, 4)}}), flush=True)
+    s.close()
+
+
+def run_hmatvec_only(args):
+    """The inner-GMRES H-matvec of the pencil (complex-FP32 storage, FP32
+    arithmetic, 8 right-hand sides) after one assembly at 1 kHz, args.pencil_n
+    triangles: its algorithmic bytes and event-timed duration (for profiling
+    the hmv32 kernels)."""
+    import torch
+    pkg = importlib.import_module("3d_bem_gb300")
+    meshes = importlib.import_module("3d_bem_gb300.meshes")
+    pkg.build()
+    tri, g, beta = pencil_problem(meshes, args.pencil_n)
+    n, R = tri.shape[0], g.shape[1]
+    s = pencil_solver(pkg, tri, beta, 1, selector=2)
+    s.assemble(1000.0)
+    B = matvec_bytes(s.partition(), s.ranks(1), n, elem=8, R=R)
+    ms = time_matvec(torch, pkg, s, n, reps=10, R=R)
+    print(json.dumps({"hmatvec_only": {"n_elements": int(n), "nrhs": R, "bytes": int(B),
+                                       "ms": round(ms, 4),
+                                       "gbs": round(B / (ms * 1e-3) / 1e9, 1)}}), flush=True)
     s.close()
 
 
@@ -779,23 +804,28 @@ def main():
     ap.add_argument("--hlu-only", action="store_true",
                     help="only one H-LU factorization of the pencil (after a warm-up one); "
                          "profiling")
+    ap.add_argument("--hmatvec-only", action="store_true",
+                    help="only the pencil's inner-GMRES H-matvec (8 RHS); profiling")
     ap.add_argument("--pencil-n", type=int, default=PENCIL_N,
-                    help="triangles of the pencil for --hlu-only")
+                    help="triangles of the pencil for --hlu-only / --hmatvec-only")
     ap.add_argument("--field-only", action="store_true",
                     help="only the field evaluation leg (one mixed solve first); profiling")
     ap.add_argument("--no-sweep", action="store_true",
                     help="skip the batched box sweep (64 frequencies x 4 RHS)")
     ap.add_argument("--selector", action="store_true",
                     help="mixed arm: learned quadrature order per near-field pair")
-    ap.add_argument("--fp32-near", action="store_true",
-                    help="mixed arm: the refinement residual reads the complex-FP32 near field "
-                         "(no FP64 low part)")
+    ap.add_argument("--near-fp64", action="store_true",
+                    help="mixed arm: the refinement residual reads the near field in FP64 (two "
+                         "complex-FP32 parts); on this body the difference to the FP64 arm is "
+                         "the ACA approximation's, so it is off by default")
     ap.add_argument("--no-aca-rules", action="store_true",
                     help="mixed arm: the 16-point rule for the ACA entries instead of the "
                          "learned rule table")
     args = ap.parse_args()
     if args.hlu_only:
         run_hlu_only(args)
+    elif args.hmatvec_only:
+        run_hmatvec_only(args)
     elif args.field_only:
         run_field_only(args)
     elif args.impl == "reference":
