@@ -76,6 +76,11 @@ WORKLOADS = {
 PENCIL_DESC = ("pencil r=4 mm L=0.2 m + 10 mm conical tip, 81,920 triangles, impedance walls "
                "Z in [0.5, 50] rho c, 8 RHS, 64 log-spaced f 200 Hz-8 kHz, H-LU preconditioner "
                "rank 2")
+# DRAM bytes per algorithmic byte of the 8-RHS FP32 H-matvec, measured with
+# ncu (dram__bytes_read.sum + dram__bytes_write.sum of hmv32_vpass<8> and
+# hmv32_upass<8,256,6>) on the 20,480-triangle pencil: 592 MB for 521 MB; the
+# traffic grows with the stored entries, so it scales to the headline size
+HMV32_R8_TRAFFIC_PER_BYTE = 592.2 / 521.4
 METRIC = "freq-solves/sec (H-matrix Helmholtz BEM solve, <=1e-5 rel. surface-pressure error)"
 UNIT = "freq-solves/s"
 
@@ -621,7 +626,10 @@ def run_ours(args):
                 "d2h_bytes_per_step": n * R * 16},
         "roofline": {"kernel": "hmatvec FP32 (hmv32_vpass + hmv32_upass), c64 storage, 8 RHS",
                      "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                     "frac": round(achieved / hbm, 4), "traffic": None,
+                     "frac": round(achieved / hbm, 4),
+                     "traffic": int(B * HMV32_R8_TRAFFIC_PER_BYTE),
+                     "traffic_source": "ncu DRAM bytes per algorithmic byte on the 20,480-"
+                                       "triangle pencil, scaled by the algorithmic bytes",
                      "bytes_per_launch": B, "ms_per_launch": round(mv_ms, 4),
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
         "gpu_launches": int(launches),
