@@ -227,10 +227,12 @@ struct bem_handle {
   int hp_prec = -1, hp_grid = 0;
   std::string hp_why;
   DBuf<HluTask> dHT;
-  DBuf<int32_t> dHDepOff, dHDeps;
+  DBuf<int32_t> dHSuccOff, dHSucc;
+  DBuf<int32_t> dHPendInit, dHQueueInit, dHCtrlInit;  // the executor's state at launch
+  DBuf<int32_t> dHPend, dHQueue;
   DBuf<HluTruncPair> dHPairs;
   DBuf<HluQrOut> dHQr;
-  DBuf<int> dHDone, dHCtrl;
+  DBuf<int> dHCtrl;
   DBuf<unsigned char> dArena, dHScr, dHBig;
   HluDfPlan hpl, hpu;       // sweep plans of the program's factors (structure)
   // impedance plane (bem_set_impedance_plane): point, unit normal and the
@@ -951,12 +953,20 @@ bool prepare_hlu_program(bem_handle* h) {
   require(P.tasks.size() < (size_t)INT32_MAX, BEM_EINVAL, "H-LU program too large");
   cudaStream_t s = h->stream;
   h->dHT.upload(P.tasks, s);
-  h->dHDepOff.upload(P.dep_off, s);
-  h->dHDeps.upload(P.deps, s);
+  h->dHSuccOff.upload(P.succ_off, s);
+  h->dHSucc.upload(P.succ.empty() ? std::vector<int32_t>{0} : P.succ, s);
+  {
+    std::vector<int32_t> pend(P.tasks.size());
+    for (size_t i = 0; i < P.tasks.size(); i++) pend[i] = P.dep_off[i + 1] - P.dep_off[i];
+    h->dHPendInit.upload(pend, s);
+  }
+  h->dHQueueInit.upload(P.queue_init, s);
+  h->dHCtrlInit.upload(std::vector<int32_t>{0, 0, 0, 0, P.nready0, 0, 0, 0}, s);
+  h->dHPend.ensure(P.tasks.size());
+  h->dHQueue.ensure(P.tasks.size());
   h->dHPairs.upload(P.pairs, s);
   h->dHQr.upload(P.qr, s);
-  h->dHDone.ensure(P.tasks.size());
-  h->dHCtrl.ensure(4);
+  h->dHCtrl.ensure(8);
   sync(h);
   h->hp_gen = h->layout_gen;
   h->hp_kc = h->cfg.precond_rank;
@@ -1182,8 +1192,10 @@ bool build_hlu_device(bem_handle* h) {
   const HluProgram& P = h->hp;
   prepare_hlu_arena(h, m.prec);
   cudaStream_t s = h->stream;
-  CK(cudaMemsetAsync(h->dHDone.p, 0, P.tasks.size() * sizeof(int), s));
-  CK(cudaMemsetAsync(h->dHCtrl.p, 0, 4 * sizeof(int), s));
+  const size_t nt = P.tasks.size();
+  CK(cudaMemcpyAsync(h->dHPend.p, h->dHPendInit.p, nt * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(h->dHQueue.p, h->dHQueueInit.p, nt * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(h->dHCtrl.p, h->dHCtrlInit.p, 8 * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
   HluExecArgs a{};
   a.precision = m.prec;
   a.arena = h->dArena.p;
@@ -1194,11 +1206,12 @@ bool build_hlu_device(bem_handle* h) {
   a.rank = m.rank.p;
   a.tasks = h->dHT.p;
   a.ntasks = (int32_t)P.tasks.size();
-  a.dep_off = h->dHDepOff.p;
-  a.deps = h->dHDeps.p;
+  a.succ_off = h->dHSuccOff.p;
+  a.succ = h->dHSucc.p;
   a.pairs = h->dHPairs.p;
   a.qr = h->dHQr.p;
-  a.done = h->dHDone.p;
+  a.pending = h->dHPend.p;
+  a.queue = h->dHQueue.p;
   a.ctrl = h->dHCtrl.p;
   a.scratch = h->dHScr.p;
   a.scratch_per_cta = P.scratch;

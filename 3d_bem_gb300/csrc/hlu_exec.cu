@@ -1397,51 +1397,65 @@ __device__ __forceinline__ unsigned long long globaltimer() {
   return t;
 }
 
-// waits until *f != 0; false when the error word is set or the wait ran out
-__device__ bool wait_flag(const int* f, int* ctrl, int64_t limit) {
-  if (ld_acquire(f)) return true;
+// the ready task in queue slot q (-1 until pushed); -1 when the error word is
+// set or the wait ran out (a bounded wait)
+__device__ int wait_slot(const int* q, int* ctrl, int64_t limit) {
+  int v = ld_acquire(q);
+  if (v >= 0) return v;
   const long long t0 = clock64();
   unsigned ns = 32;
   for (;;) {
     __nanosleep(ns);
-    if (ns < 1024) ns <<= 1;
-    if (ld_acquire(f)) return true;
-    if (ld_relaxed(ctrl + 1)) return false;
+    if (ns < 512) ns <<= 1;
+    v = ld_acquire(q);
+    if (v >= 0) return v;
+    if (ld_relaxed(ctrl + 1)) return -1;
     if (clock64() - t0 > limit) {
-      atomicCAS(ctrl + 1, 0, 1);  // 1: a dependency wait ran out of time
-      return false;
+      atomicCAS(ctrl + 1, 0, 1);  // 1: a wait ran out of time
+      return -1;
     }
   }
 }
 
+// *p -= 1 with acquire-release ordering (the last predecessor to finish
+// sees every earlier one's results); returns the old value
+__device__ __forceinline__ int dec_acq_rel(int* p) {
+  int old;
+  asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], -1;" : "=r"(old) : "l"(p) : "memory");
+  return old;
+}
+
+// The executor pops ready tasks in the order they became ready: thread 0
+// takes the next queue slot and waits (bounded) until a task is pushed into
+// it; the CTA runs the task; then its threads release the successors, each
+// decrementing a successor's pending count, and the one that reaches zero
+// pushes it. Every task is pushed once, so the queue has one slot per task.
 template <typename T2>
 __global__ void __launch_bounds__(HX_THREADS, sizeof(T2) == 8 ? 4 : 2) hlu_exec_kernel(HluExecArgs a) {
   extern __shared__ __align__(16) unsigned char hx_smem[];
   T2* sm = reinterpret_cast<T2*>(hx_smem);
-  __shared__ int s_task, s_go;
+  __shared__ int s_task;
   T2* arena = reinterpret_cast<T2*>(a.arena);
   T2* slot = reinterpret_cast<T2*>(a.scratch) + (int64_t)blockIdx.x * a.scratch_per_cta;
   for (;;) {
     if (threadIdx.x == 0) {
-      int t = -1, go = 0;
-      if (ld_relaxed(a.ctrl + 1) == 0) t = atomicAdd(a.ctrl, 1);
-      if (t >= 0 && t < a.ntasks) {
-        go = 1;
-        if (a.trace) a.trace[3 * (int64_t)t] = globaltimer();
-        const int d1 = __ldg(a.dep_off + t + 1);
-        for (int i = __ldg(a.dep_off + t); i < d1; i++)
-          if (!wait_flag(a.done + __ldg(a.deps + i), a.ctrl, a.wait_cycles)) {
-            go = 0;
-            break;
+      int t = -1;
+      if (ld_relaxed(a.ctrl + 1) == 0) {
+        const int h = atomicAdd(a.ctrl, 1);
+        if (h < a.ntasks) {
+          const unsigned long long tc = a.trace ? globaltimer() : 0ull;
+          t = wait_slot(a.queue + h, a.ctrl, a.wait_cycles);
+          if (t >= 0 && a.trace) {
+            a.trace[3 * (int64_t)t] = tc;
+            a.trace[3 * (int64_t)t + 1] = globaltimer();
           }
+        }
       }
       s_task = t;
-      s_go = go;
-      if (go && a.trace) a.trace[3 * (int64_t)t + 1] = globaltimer();
     }
     __syncthreads();
-    if (!s_go) break;
     const int ti = s_task;
+    if (ti < 0) break;
     const HluTask t = a.tasks[ti];
     switch (t.type) {
       case HT_GEMM: task_gemm<T2>(t, arena, sm); break;
@@ -1453,11 +1467,16 @@ __global__ void __launch_bounds__(HX_THREADS, sizeof(T2) == 8 ? 4 : 2) hlu_exec_
       case HT_ZERO: task_zero<T2>(t, arena); break;
       default: break;
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      if (a.trace) a.trace[3 * (int64_t)ti + 2] = globaltimer();
+    __syncthreads();  // the task's writes are done (and ordered before the releases below)
+    if (threadIdx.x == 0 && a.trace) a.trace[3 * (int64_t)ti + 2] = globaltimer();
+    const int s1 = __ldg(a.succ_off + ti + 1);
+    for (int k = __ldg(a.succ_off + ti) + threadIdx.x; k < s1; k += HX_THREADS) {
+      const int sc = __ldg(a.succ + k);
       __threadfence();
-      st_release(a.done + ti, 1);
+      if (dec_acq_rel(a.pending + sc) == 1) {
+        const int pos = atomicAdd(a.ctrl + 4, 1);
+        st_release(a.queue + pos, sc);
+      }
     }
   }
 }

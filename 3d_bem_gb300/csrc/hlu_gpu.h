@@ -120,6 +120,10 @@ struct HluQrOut {
 struct HluProgram {
   std::vector<HluTask> tasks;
   std::vector<int32_t> dep_off, deps;  // CSR, topological: deps[i] < i
+  std::vector<int32_t> succ_off, succ;  // the reverse CSR (successors), ascending
+  std::vector<int32_t> queue_init;     // ready queue at launch: tasks without
+                                       // dependencies, then -1
+  int32_t nready0 = 0;                 // their count
   std::vector<HluTruncPair> pairs;
   std::vector<HluQrOut> qr;
   int64_t arena = 0;                   // complex elements
@@ -157,12 +161,15 @@ struct HluExecArgs {
   const int32_t* rank;           // its ACA ranks
   const HluTask* tasks;
   int32_t ntasks;
-  const int32_t* dep_off;
-  const int32_t* deps;
+  const int32_t* succ_off;       // CSR of the successors (the dependency graph reversed)
+  const int32_t* succ;
   const HluTruncPair* pairs;
   const HluQrOut* qr;
-  int* done;                     // ntasks flags, cleared before the launch
-  int* ctrl;                     // [0] claim counter, [1] error word, [2] bad pivots
+  int* pending;                  // per task: dependencies not yet done (indegree at launch)
+  int* queue;                    // ntasks slots of ready tasks: the tasks without
+                                 // dependencies first, -1 in the others at launch
+  int* ctrl;                     // [0] pop counter, [1] error word, [2] bad pivots,
+                                 // [3] non-finite flag, [4] push counter (initial ready count)
   void* scratch;                 // grid x scratch_per_cta complex elements
   int64_t scratch_per_cta;
   void* big_scratch;             // regions of the large truncations (HluTask.a)

@@ -237,7 +237,7 @@ class Planner {
     t.c = C.off;
     t.ldc = C.ld;
     emit(t, {acc(A, 1), acc(B, 1), acc(C, accumulate ? 3 : 2)},
-         6.0 + (double)m * n * q / 2048.0);
+         2.0 + (double)m * n * q / 4096.0);
   }
   void zero(const View& C) {
     if (C.rows == 0 || C.cols == 0) return;
@@ -401,7 +401,7 @@ class Planner {
   // otherwise (fitted to traced factorizations; it only orders the claims)
   double trunc_cost(int64_t m, int64_t n, int64_t kt) const {
     if (kc_ <= 2 && hlu_sub_buffers(m, n, kt) <= HLU_SMEM_ELEMS)
-      return 10.0 + (double)(m + n) * kt / 400.0;
+      return 30.0 + (double)(m + n) * kt / 80.0;
     if (m <= 32 && n <= 32) return 60.0 + 0.2 * (double)kt * (m < n ? m : n);
     if (kc_ <= 8 && kt > kc_ + 6 && m > kc_ + 6 && n > kc_ + 6)
       return 150.0 + (double)(m + n) * kt / 50.0;
@@ -798,7 +798,7 @@ class Planner {
       t.a = A.F.off;
       t.lda = A.F.ld;
       P_.qr.push_back(q);
-      emit(t, {acc(A.F, 1), acc(L.F, 2), acc(U.F, 2), acc(ri, 2)}, 60.0);
+      emit(t, {acc(A.F, 1), acc(L.F, 2), acc(U.F, 2), acc(ri, 2)}, 25.0);
       return;
     }
     const HCluster &R = t_.c[A.rc], &C = t_.c[A.cc];
@@ -967,12 +967,29 @@ class Planner {
       std::vector<int32_t> d;
       for (int32_t x : tdeps_[o]) d.push_back(pos[x]);
       std::sort(d.begin(), d.end());
+      d.erase(std::unique(d.begin(), d.end()), d.end());
       for (int32_t x : d)
         if (x >= i) throw std::runtime_error("claim order is not topological");
       P_.deps.insert(P_.deps.end(), d.begin(), d.end());
       P_.dep_off[i + 1] = (int32_t)P_.deps.size();
     }
     P_.tasks = std::move(tasks);
+    // successors (the reverse CSR) and the ready queue at launch: the
+    // executor pops ready tasks, and the task that completes a successor's
+    // last dependency pushes it
+    std::vector<int32_t> cnt(nt + 1, 0);
+    for (int32_t x : P_.deps) cnt[x + 1]++;
+    P_.succ_off.assign(nt + 1, 0);
+    for (int64_t i = 0; i < nt; i++) P_.succ_off[i + 1] = P_.succ_off[i] + cnt[i + 1];
+    P_.succ.assign(P_.deps.size(), 0);
+    std::vector<int32_t> fill(P_.succ_off.begin(), P_.succ_off.end() - 1);
+    for (int64_t i = 0; i < nt; i++)
+      for (int32_t k = P_.dep_off[i]; k < P_.dep_off[i + 1]; k++)
+        P_.succ[fill[P_.deps[k]]++] = (int32_t)i;
+    P_.queue_init.assign(nt, -1);
+    P_.nready0 = 0;
+    for (int64_t i = 0; i < nt; i++)
+      if (P_.dep_off[i + 1] == P_.dep_off[i]) P_.queue_init[P_.nready0++] = (int32_t)i;
     validate();
   }
 

@@ -379,8 +379,11 @@ def sweep_frequencies(meshes, steps, warmup):
     k = min(max(steps, 1), len(f))
     idx = np.unique(np.round(np.linspace(0, len(f) - 1, k)).astype(int))
     nw = min(max(warmup, 1), len(f) - 1)
+    # the first warm-up lies 2 % above the band: its ACA ranks are the
+    # largest, so the rank reservation grows there once (a new layout means a
+    # new H-LU task program) and not inside the timed sweep
     wi = np.unique(np.round(np.linspace(len(f) - 2, 0, nw)).astype(int))[::-1]
-    warm = [float(np.sqrt(f[i] * f[i + 1])) for i in wi]
+    warm = [float(f[-1] * 1.02)] + [float(np.sqrt(f[i] * f[i + 1])) for i in wi[1:]]
     return [float(x) for x in f[idx]], warm
 
 
@@ -425,9 +428,9 @@ def accuracy_vs_oracle(pkg, meshes, n_target=5120, fr=(200.0, 1000.0, 8000.0)):
     """The GPU arms against the FP64 oracle (H-LU preconditioned, all host
     cores) on the same pencil body with 5,120 triangles: the oracle at the
     workload's tolerances (the same approximation) and at ACA 1e-7 / GMRES
-    1e-12 (the converged reference). Arms: the headline's mixed arm (FP64
-    near field in the refinement residual), the same with the complex-FP32
-    near field, mixed at ACA 1e-6 and the plain complex-FP64 arm."""
+    1e-12 (the converged reference). Arms: the headline's mixed arm, the
+    same with the FP64 near field in the refinement residual, the latter at
+    ACA 1e-6, and the plain complex-FP64 arm."""
     import oracle
     tri, g, beta = pencil_problem(meshes, n_target)
     n = tri.shape[0]
@@ -436,9 +439,9 @@ def accuracy_vs_oracle(pkg, meshes, n_target=5120, fr=(200.0, 1000.0, 8000.0)):
     out = {"workload": f"pencil as the headline with {n} triangles, 8 RHS, f = "
                        + ", ".join(f"{f:g}" for f in fr) + " Hz"}
     arms = {}
-    for name, prec, extra in (("mixed", 1, {"selector": 2, "near_fp64": 1}),
-                              ("mixed_fp32_near", 1, {"selector": 2}),
-                              ("mixed_aca1e-6", 1, {"near_fp64": 1, "aca_tol": 1e-6}),
+    for name, prec, extra in (("mixed", 1, {"selector": 2}),
+                              ("mixed_fp64_near", 1, {"selector": 2, "near_fp64": 1}),
+                              ("mixed_aca1e-6_fp64_near", 1, {"near_fp64": 1, "aca_tol": 1e-6}),
                               ("plain", 0, {})):
         s = pencil_solver(pkg, tri, beta, prec, **extra)
         arms[name] = [s.solve(f, g, want=("p",))[2] for f in fr]
