@@ -1638,6 +1638,7 @@ void solve_dev(bem_handle* h, double freq, const double2* g_caller, int64_t R, d
   auto t0 = std::chrono::steady_clock::now();
   bem_solve_info loc{};
   assemble(h, freq, &loc.t_nearfield, &loc.t_aca);
+  const auto t_asm = std::chrono::steady_clock::now();
   if (h->cfg.use_preconditioner) {
     const double r = h->hlu_freq > 0 ? std::max(freq / h->hlu_freq, h->hlu_freq / freq) : 0.0;
     if (h->have_hlu && h->cfg.precond_reuse > 1.0 && r > 0 && r <= h->cfg.precond_reuse) {
@@ -1686,6 +1687,10 @@ void solve_dev(bem_handle* h, double freq, const double2* g_caller, int64_t R, d
   loc.t_rhs = elapsed(h->ev[3], h->ev[4]);
   loc.t_gmres = elapsed(h->ev[4], h->ev[5]);
   loc.t_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (std::getenv("BEM_SOLVE_TRACE"))  // host wall time of the assembly step (profiling)
+    std::fprintf(stderr, "solve f %.2f assemble_wall %.4f t_nearfield %.4f t_aca %.4f total %.4f\n",
+                 freq, std::chrono::duration<double>(t_asm - t0).count(), loc.t_nearfield,
+                 loc.t_aca, loc.t_total);
   fill_rank_info(h, &loc);
   if (bad) loc.status = BEM_ENONFINITE;
   if (info) *info = loc;

@@ -34,6 +34,7 @@ constexpr int UT = 512;  // threads of a pass-U CTA (16 warps split a leaf's blo
 // 0.030 against 0.038 ms.
 constexpr int UT32_NARROW = 256, UT32_NARROW_MIN_CTAS = 6;
 constexpr int UT32_NARROW_LEAVES_PER_SM = 4;
+constexpr int UT32_WIDE_R = 256, UT32_WIDE_R_MIN_CTAS = 2;  // R >= 4: up to 128 registers
 constexpr int VROWS = 16;  // rows of V per pass-V work item (4 warps x 4 rows)
 
 template <typename T, bool F32> struct Acc;
@@ -420,7 +421,12 @@ void launch32_r(const HmvArgs& a, cudaStream_t s) {
                                                (const float2*)a.S, a.xf, a.ldx, a.tf, a.ldt,
                                                a.vwork, a.gate);
   if (a.nleaves > 0) {
-    if (a.nleaves >= (int64_t)UT32_NARROW_LEAVES_PER_SM * sm_count())
+    if (R >= 4)  // many right-hand sides: their accumulators need the registers
+                 // (the 40-register narrow shape spilled ~0.9 KB a thread at R = 8)
+      hmv32_upass<R, UT32_WIDE_R, UT32_WIDE_R_MIN_CTAS><<<(unsigned)a.nleaves, UT32_WIDE_R, 0, s>>>(
+          a.leaves, a.list_off, a.list, a.far, a.rank, a.nearb, (const float2*)a.U,
+          (const float2*)a.F, a.xf, a.ldx, a.tf, a.ldt, a.y, a.ldy, a.accumulate, a.gate);
+    else if (a.nleaves >= (int64_t)UT32_NARROW_LEAVES_PER_SM * sm_count())
       hmv32_upass<R, UT32_NARROW, UT32_NARROW_MIN_CTAS><<<(unsigned)a.nleaves, UT32_NARROW, 0, s>>>(
           a.leaves, a.list_off, a.list, a.far, a.rank, a.nearb, (const float2*)a.U,
           (const float2*)a.F, a.xf, a.ldx, a.tf, a.ldt, a.y, a.ldy, a.accumulate, a.gate);
