@@ -16,6 +16,8 @@ present, every call raises :class:`BemError`.
 from __future__ import annotations
 
 import ctypes as ct
+import hashlib
+import json
 import os
 from dataclasses import dataclass, field
 
@@ -36,6 +38,7 @@ EXPORTS = [
     "bem_get_permutation", "bem_get_partition", "bem_set_bc", "bem_operators",
     "bem_assemble", "bem_hmatvec", "bem_hmatvec_device", "bem_get_block", "bem_get_ranks",
     "bem_gmres", "bem_solve", "bem_solve_device", "bem_sweep", "bem_sweep_device",
+    "bem_sweep_resume",
     "bem_points_assemble",
     "bem_launch_count", "bem_stream", "bem_hmatvec_noalloc", "bem_hmatvec_device_ex",
     "bem_hlu_build", "bem_hlu_solve", "bem_hlu_export", "bem_hlu_sweep_kind", "bem_recompress",
@@ -70,6 +73,28 @@ class Config(ct.Structure):
                 ("near_fp64", ct.c_int32)]
 
 
+# bem_freq_done_fn: int (*)(int64_t f, void* user)
+FREQ_DONE_FN = ct.CFUNCTYPE(ct.c_int, ct.c_int64, ct.c_void_p)
+
+
+def _write_atomic(path, data: bytes):
+    """Write a file under a temporary name, then rename it into place, so a
+    reader sees either nothing or the whole file."""
+    tmp = f"{path}.tmp{os.getpid()}"
+    with open(tmp, "wb") as fh:
+        fh.write(data)
+        fh.flush()
+        os.fsync(fh.fileno())
+    os.replace(tmp, path)
+
+
+def _npz_bytes(**arrays) -> bytes:
+    import io
+    b = io.BytesIO()
+    np.savez(b, **arrays)
+    return b.getvalue()
+
+
 class SolveInfo(ct.Structure):
     _fields_ = [("iterations", ct.c_int64), ("rel_residual", ct.c_double),
                 ("true_residual", ct.c_double), ("max_rank", ct.c_int64),
@@ -80,6 +105,52 @@ class SolveInfo(ct.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# ---- sweep checkpoints (per-frequency files of a resumable sweep) ----
+def checkpoint_open(path: str, manifest: dict) -> list[str]:
+    """Create the checkpoint directory of a sweep, or check that it belongs
+    to the same sweep (ValueError otherwise). Returns the per-frequency file
+    names."""
+    os.makedirs(path, exist_ok=True)
+    mpath = os.path.join(path, "manifest.json")
+    if os.path.exists(mpath):
+        with open(mpath) as fh:
+            if json.load(fh) != manifest:
+                raise ValueError(f"{path} holds a checkpoint of a different sweep")
+    else:
+        _write_atomic(mpath, json.dumps(manifest).encode())
+    return [f"freq_{i:05d}.npz" for i in range(len(manifest["freqs"]))]
+
+
+def _info_record(info: SolveInfo) -> np.ndarray:
+    return np.array(tuple(getattr(info, k) for k, _ in SolveInfo._fields_),
+                    dtype=[(k, np.dtype(t)) for k, t in SolveInfo._fields_])
+
+
+def checkpoint_write(path: str, name: str, p_slice, freq: float, info: SolveInfo):
+    """One completed frequency: its pressures (n x R) and info record."""
+    _write_atomic(os.path.join(path, name),
+                  _npz_bytes(p=np.ascontiguousarray(p_slice), freq=np.float64(freq),
+                             info=_info_record(info)))
+
+
+def checkpoint_load(path: str, names, p, infos) -> np.ndarray:
+    """The completed frequencies of a checkpoint into p[:, :, i] and
+    infos[i]; returns the solved flags (uint8 per frequency)."""
+    solved = np.zeros(len(names), np.uint8)
+    for i, name in enumerate(names):
+        f = os.path.join(path, name)
+        if not os.path.exists(f):
+            continue
+        with np.load(f) as z:
+            p[:, :, i] = z["p"]
+            rec = z["info"][()]
+            for k, _ in SolveInfo._fields_:
+                setattr(infos[i], k, rec[k].item())
+        solved[i] = 1
+    return solved
+
 
 
 _lib = None
@@ -131,6 +202,7 @@ def lib():
     L.bem_solve_device.argtypes = [vp, dbl, vp, i64, vp, vp, vp, P(SolveInfo)]
     L.bem_sweep.argtypes = [vp, vp, i64, vp, i64, vp, vp]
     L.bem_sweep_device.argtypes = [vp, vp, i64, vp, i64, vp, vp]
+    L.bem_sweep_resume.argtypes = [vp, vp, i64, vp, i64, vp, vp, vp, FREQ_DONE_FN, vp]
     L.bem_points_assemble.argtypes = [vp, vp, i64, vp, i64, dbl, vp, vp]
     L.bem_recompress.argtypes = [vp, i32, i64, dbl]
     L.bem_sel_nparam.argtypes = []
@@ -277,6 +349,7 @@ class Solver:
         self._h = h
         self.n = 0
         self.rows = 0
+        self._inputs = {}  # digests of what was set, for sweep checkpoints
         if self.config.selector:
             self.set_selector()
 
@@ -288,6 +361,22 @@ class Solver:
     def __del__(self):
         self.close()
 
+    def _note(self, key, *arrays):
+        d = hashlib.sha256()
+        for x in arrays:
+            x = np.ascontiguousarray(x)
+            d.update(str((x.dtype.str, x.shape)).encode())
+            d.update(x.tobytes())
+        self._inputs[key] = d.hexdigest()
+
+    def fingerprint(self) -> str:
+        """Digest of the configuration and of every input set on this
+        handle (mesh, boundary conditions, sources, plane, selector)."""
+        d = hashlib.sha256(bytes(self.config))
+        for k in sorted(self._inputs):
+            d.update(f"{k}={self._inputs[k]};".encode())
+        return d.hexdigest()
+
     def _check(self, st, what=""):
         if st != BEM_OK:
             msg = lib().bem_last_error(self._h)
@@ -298,6 +387,10 @@ class Solver:
     def set_mesh(self, tri: np.ndarray):
         tri = np.ascontiguousarray(tri, dtype=np.float64).reshape(-1, 9)
         self._check(lib().bem_set_mesh(self._h, _ptr(tri), tri.shape[0]), "bem_set_mesh")
+        # a new mesh drops the boundary conditions, sources and plane
+        for k in ("bc", "sources", "plane"):
+            self._inputs.pop(k, None)
+        self._note("mesh", tri)
         self.n = tri.shape[0]
         self.rows = self.n  # rows of the assembled matrices
 
@@ -318,11 +411,13 @@ class Solver:
         """Impedance walls: a = i k beta (beta = rho c / Z per element), b = 1."""
         beta = np.ascontiguousarray(np.asarray(beta, np.complex128).ravel())
         self._check(lib().bem_set_bc_impedance(self._h, _ptr(beta)), "bem_set_bc_impedance")
+        self._note("bc", np.array([1]), beta)
 
     def set_bc(self, a, b):
         a = _c128(a)
         b = _c128(b)
         self._check(lib().bem_set_bc(self._h, _ptr(a), _ptr(b)), "bem_set_bc")
+        self._note("bc", np.array([0]), a, b)
 
     # ---- operators / matrices ----
     def operators(self, k, rows, cols) -> np.ndarray:
@@ -359,11 +454,13 @@ class Solver:
         sg = np.ascontiguousarray(w["sigma"], np.float32)
         self._check(lib().bem_set_selector(self._h, _ptr(prm), _ptr(mu), _ptr(sg)),
                     "bem_set_selector")
+        self._note("selector", prm, mu, sg)
         if "aca_table" in w:
             tab = np.ascontiguousarray(w["aca_table"], np.uint8)
             axes = np.ascontiguousarray(w["aca_axes"], np.float32)
             self._check(lib().bem_set_aca_rules(self._h, _ptr(tab), _ptr(axes)),
                         "bem_set_aca_rules")
+            self._note("aca_rules", tab, axes)
 
     def sel_stats(self) -> dict:
         st = np.zeros(4, np.int64)
@@ -490,16 +587,58 @@ class Solver:
             self._check(st, "bem_solve_device")
         return info.as_dict()
 
-    def sweep(self, freqs, g):
+    def sweep(self, freqs, g, checkpoint: str | None = None):
+        """Frequency sweep: pressures n x R x nf (caller order) and the
+        per-frequency infos.
+
+        checkpoint: a directory. Each frequency is written there as it
+        completes (``freq_<index>.npz``: its pressures and info), beside a
+        manifest of the sweep (frequencies, right-hand sides and the handle's
+        :meth:`fingerprint`). A call with the same directory and the same
+        sweep loads the completed frequencies and solves only the others,
+        as the controller's per-frequency solved flags do
+        (bemsolvercontroller.cpp:61-69); a directory of a different sweep
+        raises ValueError."""
         freqs = np.ascontiguousarray(freqs, np.float64)
         g = np.asfortranarray(np.asarray(g, np.complex128).reshape(self.n, -1))
         R = g.shape[1]
         p = np.zeros((self.n, R, freqs.size), np.complex128, order="F")
         infos = (SolveInfo * freqs.size)()
-        st = lib().bem_sweep(self._h, _ptr(freqs), freqs.size, _ptr(g), R, _ptr(p), infos)
+        if checkpoint is None:
+            st = lib().bem_sweep(self._h, _ptr(freqs), freqs.size, _ptr(g), R, _ptr(p), infos)
+        else:
+            st = self._sweep_checkpointed(freqs, g, p, infos, checkpoint)
         if st not in (BEM_OK, BEM_EMAXIT):
             self._check(st, "bem_sweep")
         return p, [i.as_dict() for i in infos]
+
+    _stop_after = None  # tests: stop a checkpointed sweep after this many frequencies
+
+    def _sweep_checkpointed(self, freqs, g, p, infos, path):
+        key = hashlib.sha256()
+        for x in (freqs, g):
+            key.update(np.ascontiguousarray(x).tobytes())
+        key.update(self.fingerprint().encode())
+        names = checkpoint_open(path, {"n": self.n, "R": int(g.shape[1]),
+                                       "freqs": freqs.tolist(), "key": key.hexdigest()})
+        solved = checkpoint_load(path, names, p, infos)
+        count, failed = [0], []
+
+        def done(i, _user):
+            try:
+                checkpoint_write(path, names[i], p[:, :, i], freqs[i], infos[i])
+            except Exception as e:  # stop the sweep; raised below
+                failed.append(e)
+                return 1
+            count[0] += 1
+            return int(self._stop_after is not None and count[0] >= self._stop_after)
+
+        cb = FREQ_DONE_FN(done)
+        st = lib().bem_sweep_resume(self._h, _ptr(freqs), freqs.size, _ptr(g), g.shape[1],
+                                    _ptr(p), infos, _ptr(solved), cb, None)
+        if failed:
+            raise failed[0]
+        return st
 
     def sweep_device(self, freqs, g_ptr: int, R: int, p_ptr: int):
         """bem_sweep with device pointers: g (n x R complex FP64, caller order)
@@ -519,17 +658,20 @@ class Solver:
         src = _sources(sources)
         self._check(lib().bem_set_point_sources(self._h, _ptr(src) if src.shape[0] else None,
                                                 src.shape[0]), "bem_set_point_sources")
+        self._note("sources", src)
 
     def set_impedance_plane(self, point=None, normal=None):
         """One infinite rigid plane (impedance plane); None removes it."""
         if normal is None:
             self._check(lib().bem_set_impedance_plane(self._h, None, None),
                         "bem_set_impedance_plane")
+            self._inputs.pop("plane", None)
             return
         p = np.ascontiguousarray(point, np.float64).reshape(3)
         n = np.ascontiguousarray(normal, np.float64).reshape(3)
         self._check(lib().bem_set_impedance_plane(self._h, _ptr(p), _ptr(n)),
                     "bem_set_impedance_plane")
+        self._note("plane", p, n)
 
     def field(self, freq: float, pts, phi, dphi, sources=None):
         """Velocity potential and sound pressure (npts x R each) at the

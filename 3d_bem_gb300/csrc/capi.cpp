@@ -17,6 +17,7 @@
 #include <new>
 #include <numeric>
 #include <cstdio>
+#include <functional>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -1795,9 +1796,14 @@ void ensure_workers(bem_handle* h, int nw) {
 // With device pointers (gd, pd non-null) instead of g / p: every worker reads
 // gd and writes its frequencies' slices of pd directly; the workers' streams
 // start after the work already on h's stream and h's stream waits for them.
+// on_done (host buffers only; may be null) runs after each frequency's slice
+// of p and its info record are written, one call at a time across the
+// handles; a true return stops the sweep before the next frequency of every
+// handle (the ones running finish and are reported).
 void run_sweep(bem_handle* h, int W, const double* freqs, const int64_t* idx, int64_t n,
                const double* g, int64_t nrhs, double* p, bem_solve_info* info,
-               bem_status& worst, const double2* gd = nullptr, double2* pd = nullptr) {
+               bem_status& worst, const double2* gd = nullptr, double2* pd = nullptr,
+               const std::function<bool(int64_t)>* on_done = nullptr) {
   require(h->have_mesh && h->have_bc && !h->points_mode, BEM_EINVAL,
           "mesh and boundary conditions must be set");
   W = (int)std::max<int64_t>(1, std::min<int64_t>(W, n));
@@ -1814,6 +1820,8 @@ void run_sweep(bem_handle* h, int W, const double* freqs, const int64_t* idx, in
     CK(cudaEventRecord(e0, h->stream));
   }
   std::vector<bem_status> st(W, BEM_OK), wst(W, BEM_OK);
+  std::atomic<bool> stop{false};
+  std::mutex done_mu;
   auto body = [&](int w) {
     bem_handle* x = hs[w];
     st[w] = guarded(x, [&] {
@@ -1838,7 +1846,8 @@ void run_sweep(bem_handle* h, int W, const double* freqs, const int64_t* idx, in
       // (sorted) frequencies, so its consecutive solves are close
       const bool blocks = h->cfg.use_preconditioner && h->cfg.precond_reuse > 1.0;
       const int64_t i0 = blocks ? n * w / W : w, i1 = blocks ? n * (w + 1) / W : n;
-      for (int64_t i = i0; i < i1; i += blocks ? 1 : W) {
+      for (int64_t i = i0; i < i1 && !stop.load(std::memory_order_acquire);
+           i += blocks ? 1 : W) {
         const int64_t f = idx[i];
         bem_solve_info loc{};
         solve_dev(x, freqs[f], x->dIn.p, nrhs, nullptr, nullptr, x->dOut3.p, &loc);
@@ -1846,6 +1855,10 @@ void run_sweep(bem_handle* h, int W, const double* freqs, const int64_t* idx, in
         sync(x);
         if (info) info[f] = loc;
         if (loc.status != BEM_OK) wst[w] = loc.status;
+        if (on_done) {
+          std::lock_guard<std::mutex> lk(done_mu);
+          if ((*on_done)(f)) stop.store(true, std::memory_order_release);
+        }
       }
     });
   };
@@ -2864,33 +2877,59 @@ bem_status bem_autotune(bem_handle* h, double freq, int64_t nrhs, int64_t* tuned
   });
 }
 
-bem_status bem_sweep(bem_handle* h, const double* freqs, int64_t nf, const double* g, int64_t nrhs,
-                     double* p, bem_solve_info* info) {
+namespace {
+// bem_sweep / bem_sweep_resume: the frequencies whose solved flag is zero
+// (all of them without flags), sorted ascending under factor reuse.
+bem_status sweep_host(bem_handle* h, const double* freqs, int64_t nf, const double* g,
+                      int64_t nrhs, double* p, bem_solve_info* info, uint8_t* solved,
+                      bem_freq_done_fn done, void* user) {
   if (!h) return BEM_EINVAL;
   bem_status worst = BEM_OK;
   bem_status st = guarded(h, [&] {
     require(freqs && g && p && nf >= 1 && nrhs >= 1, BEM_EINVAL, "bad arguments");
     for (int64_t f = 0; f < nf; f++)
       require(freqs[f] > 0 && std::isfinite(freqs[f]), BEM_EINVAL, "frequencies must be positive");
+    std::vector<int64_t> idx;
+    for (int64_t i = 0; i < nf; i++)
+      if (!solved || !solved[i]) idx.push_back(i);
+    if (idx.empty()) return;
+    const int64_t n = (int64_t)idx.size();
     int W = (int)h->cfg.sweep_workers;
     if (W == 0) {  // autotuned once per handle, on long sweeps only
-      if (h->tuned_workers == 0 && nf >= 16) {
-        std::vector<double> sorted(freqs, freqs + nf);
+      if (h->tuned_workers == 0 && n >= 16) {
+        std::vector<double> sorted;
+        for (int64_t i : idx) sorted.push_back(freqs[i]);
         std::sort(sorted.begin(), sorted.end());
-        autotune(h, sorted[nf / 2], nrhs);
+        autotune(h, sorted[n / 2], nrhs);
       }
       W = h->tuned_workers > 0 ? (int)h->tuned_workers : 1;
     }
     // interleave cheap and expensive frequencies over the workers; with
     // factor reuse, frequencies go in ascending order
-    std::vector<int64_t> idx(nf);
-    for (int64_t i = 0; i < nf; i++) idx[i] = i;
     if (h->cfg.use_preconditioner && h->cfg.precond_reuse > 1.0)
       std::stable_sort(idx.begin(), idx.end(),
                        [&](int64_t x, int64_t y) { return freqs[x] < freqs[y]; });
-    run_sweep(h, W, freqs, idx.data(), nf, g, nrhs, p, info, worst);
+    std::function<bool(int64_t)> on_done = [&](int64_t f) {
+      solved[f] = 1;
+      return done != nullptr && done(f, user) != 0;
+    };
+    run_sweep(h, W, freqs, idx.data(), n, g, nrhs, p, info, worst, nullptr, nullptr,
+              solved ? &on_done : nullptr);
   });
   return st != BEM_OK ? st : worst;
+}
+}  // namespace
+
+bem_status bem_sweep(bem_handle* h, const double* freqs, int64_t nf, const double* g, int64_t nrhs,
+                     double* p, bem_solve_info* info) {
+  return sweep_host(h, freqs, nf, g, nrhs, p, info, nullptr, nullptr, nullptr);
+}
+
+bem_status bem_sweep_resume(bem_handle* h, const double* freqs, int64_t nf, const double* g,
+                            int64_t nrhs, double* p, bem_solve_info* info, uint8_t* solved,
+                            bem_freq_done_fn done, void* user) {
+  if (!solved) return BEM_EINVAL;
+  return sweep_host(h, freqs, nf, g, nrhs, p, info, solved, done, user);
 }
 
 bem_status bem_sweep_device(bem_handle* h, const double* freqs, int64_t nf, const void* g,

@@ -327,6 +327,24 @@ bem_status bem_sweep(bem_handle* h, const double* freqs, int64_t nf, const doubl
 bem_status bem_sweep_device(bem_handle* h, const double* freqs, int64_t nf, const void* g,
                             int64_t nrhs, void* p, bem_solve_info* info);
 
+/* Resumable frequency sweep: bem_sweep with the controller's per-frequency
+ * solved flags (boundariesSolvedAtFrequency, bemsolvercontroller.cpp:61-69,
+ * set as each frequency completes). solved (nf bytes, in and out, not NULL):
+ * a frequency whose flag is non-zero on entry is skipped, and its slice of p
+ * and its info record are left as they are. When a frequency completes, its
+ * slice of p and its info record are written, its flag is set to 1 and then
+ * done(f, user) runs (done may be NULL), one call at a time over the
+ * workers, on a worker's thread. A non-zero return from done stops the
+ * sweep: frequencies already running finish and are reported, no new one
+ * starts, and the call returns as bem_sweep would (the flags tell which
+ * frequencies are solved). A later call with the same flags solves the rest;
+ * a frequency's result does not depend on which others were solved with it
+ * unless precond_reuse > 1 (factors shared by neighbouring frequencies). */
+typedef int (*bem_freq_done_fn)(int64_t f, void* user);
+bem_status bem_sweep_resume(bem_handle* h, const double* freqs, int64_t nf, const double* g,
+                            int64_t nrhs, double* p, bem_solve_info* info, uint8_t* solved,
+                            bem_freq_done_fn done, void* user);
+
 /* Point sources of the boundary solve (BoundaryElementSolver::pointSources):
  * nsrc rows x, y, z, Re w, Im w (nsrc = 0 clears; bem_set_mesh clears too).
  * Every solve adds their source term at each collocation point to the

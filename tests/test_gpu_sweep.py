@@ -143,3 +143,40 @@ def test_device_sweep_with_preconditioner_matches_solves(bem, meshes):
         assert torch.equal(q, p[k]), f
     s.close()
     ref.close()
+
+
+def test_checkpointed_sweep_resumes(bem, meshes, tmp_path):
+    """Checkpoint / resume (the controller's per-frequency solved flags,
+    bemsolvercontroller.cpp:61-69): a checkpointed sweep stopped after 3 of 7
+    frequencies leaves those (and the one another worker was finishing) on
+    disk; a new handle over the same inputs loads them, solves only the rest
+    and gives the pressures of an uninterrupted sweep bitwise. A checkpoint
+    of a different sweep is refused."""
+    import os
+
+    tri, s = box_solver(bem, meshes, sweep_workers=2)
+    g = meshes.box_piston_rhs(tri, patches=1)
+    freqs = meshes.log_frequencies(7, 100.0, 1500.0)
+    ref, iref = s.sweep(freqs, g)
+    d = str(tmp_path / "ck")
+    s._stop_after = 3
+    s.sweep(freqs, g, checkpoint=d)
+    first = {f: os.stat(os.path.join(d, f)).st_mtime_ns
+             for f in os.listdir(d) if f.startswith("freq_")}
+    assert 3 <= len(first) <= 4, sorted(first)
+    s.close()
+    _, s2 = box_solver(bem, meshes, sweep_workers=2)
+    p, infos = s2.sweep(freqs, g, checkpoint=d)
+    assert np.array_equal(p, ref)
+    assert all(i["status"] == 0 and i["iterations"] == r["iterations"]
+               for i, r in zip(infos, iref))
+    files = {f: os.stat(os.path.join(d, f)).st_mtime_ns
+             for f in os.listdir(d) if f.startswith("freq_")}
+    assert len(files) == 7
+    assert all(files[f] == t for f, t in first.items())  # loaded, not solved again
+    # a finished checkpoint solves nothing and returns the same pressures
+    p2, _ = s2.sweep(freqs, g, checkpoint=d)
+    assert np.array_equal(p2, ref)
+    with pytest.raises(ValueError):
+        s2.sweep(freqs, 2.0 * g, checkpoint=d)
+    s2.close()
