@@ -1463,8 +1463,12 @@ struct GmresResult {
 
 // Restarted GMRES for R right-hand sides on the dPhi matrix (device b, x;
 // x holds the initial guess). f32 selects the FP32-arithmetic operator.
+// estimate_ok: stop when the Arnoldi residual estimates of all right-hand
+// sides meet tol, without the explicit residual of the updated x (one more
+// operator product and preconditioner application); for the inner solves of
+// the refinement, whose outer step measures the true residual in FP64.
 GmresResult gmres_core(bem_handle* h, const double2* b, double2* x, int R, double tol,
-                       int64_t maxit, bool f32, bool x_zero = false) {
+                       int64_t maxit, bool f32, bool x_zero = false, bool estimate_ok = false) {
   ensure_gmres(h, R);
   GmresWS& g = h->gw;
   const int64_t N = h->N;
@@ -1499,6 +1503,7 @@ GmresResult gmres_core(bem_handle* h, const double2* b, double2* x, int R, doubl
     // flags: the steps run past convergence before the next host check
     // (every 8 steps) do no work
     const int* done_flags = &g.st.p[0].done;
+    bool conv = false;
     for (int j = 0; j < g.m; j++) {
       hmatvec_dev(h, 1, g.Vb.p + (int64_t)j * R * N, g.w.p, R, 0, f32, done_flags);
       if (pc) apply_precond(h, g.w.p, R, done_flags);
@@ -1506,12 +1511,16 @@ GmresResult gmres_core(bem_handle* h, const double2* b, double2* x, int R, doubl
       total++;
       const bool last = (j == g.m - 1) || total >= maxit;
       if (((j + 1) % 8 == 0) || last) {
-        if (read_states(h)) break;
+        if (read_states(h)) {
+          conv = true;
+          break;
+        }
       }
       if (total >= maxit) break;
     }
     krylov_update(a, s);
     h->launches += 2;
+    if (conv && estimate_ok) break;
   }
   CK(cudaGetLastError());
   GmresResult res;
@@ -1596,7 +1605,7 @@ void gmres_dev(bem_handle* h, const double2* b, double2* x, int R, bem_solve_inf
       // products cap what one inner solve can deliver at about 1e-6
       const double inner_tol = std::max(1e-6, 0.3 * tol / rel);
       CK(cudaMemsetAsync(g.d.p, 0, (size_t)R * N * sizeof(double2), s));
-      GmresResult ir = gmres_core(h, g.r.p, g.d.p, R, inner_tol, maxit - total, true, true);
+      GmresResult ir = gmres_core(h, g.r.p, g.d.p, R, inner_tol, maxit - total, true, true, true);
       total += ir.iters;
       inner_res = ir.resid;
       krylov_axpy(x, g.d.p, (int64_t)R * N, s);

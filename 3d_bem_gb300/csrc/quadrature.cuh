@@ -501,6 +501,32 @@ __device__ __forceinline__ OpsF ops_rule32_pts(const ElemF* __restrict__ EF, int
   return o;
 }
 
+// sin and cos of 2 pi x for x >= 0 (x in turns): the quarter turn q =
+// rint(4 x) is split off exactly (x - q / 4 has no rounding, by Sterbenz'
+// lemma), the rest t = 2 pi (x - q / 4) lies in [-pi/4, pi/4], where the
+// Taylor series of sin to t^9 and of cos to t^8 are within 2.5e-8 of the
+// functions, and the quadrant rotates (sin t, cos t) by q quarter turns.
+// Maximum error 7.6e-8 (FP32 rounding of the result), relative accuracy near
+// zero, no slow path for large arguments. The ACA entries need this: the
+// hardware sin / cos (absolute error ~4e-7) moved the mixed solution of an
+// ill-conditioned body by ~4e-6 at ACA 1e-6.
+__device__ __forceinline__ void sincos_turns(float x, float& sn, float& cs) {
+  const int iq = __float2int_rn(4.0f * x);
+  const float t = 6.28318530717959f * fmaf(-0.25f, (float)iq, x);
+  const float t2 = t * t;
+  float ps = fmaf(t2, 2.75573192e-6f, -1.98412698e-4f);  // 1/9!, -1/7!
+  ps = fmaf(t2, ps, 8.33333333e-3f);                    // 1/5!
+  ps = fmaf(t2, ps, -0.166666667f);                     // -1/3!
+  const float st = fmaf(t * t2, ps, t);
+  float pc = fmaf(t2, 2.48015873e-5f, -1.38888889e-3f);  // 1/8!, -1/6!
+  pc = fmaf(t2, pc, 4.16666667e-2f);                    // 1/4!
+  pc = fmaf(t2, pc, -0.5f);                             // -1/2!
+  const float ct = fmaf(t2, pc, 1.0f);
+  const float a = (iq & 1) ? ct : st, b = (iq & 1) ? st : ct;
+  sn = (iq & 2) ? -a : a;
+  cs = ((iq ^ (iq >> 1)) & 1) ? -b : b;
+}
+
 // The same FP32 integrand over the points b, b + s, b + 2 s, .. < e of the
 // tables x1, x2, wt: one lane's share when s lanes split an entry's rule (the
 // operators are sums over the points, so the shares add up to the entry).
@@ -526,14 +552,8 @@ __device__ __forceinline__ OpsF ops_pts32(const ElemF& P, const ElemF& Q, float 
     const float rnq = -(rx * nqx + ry * nqy + rz * nqz) * ir;
     const float rnp = (rx * npx + ry * npy + rz * npz) * ir;
     const float kr = k * r;
-    // exp(ikr): x = k r / (2 pi) reduced exactly to [-1/2, 1/2] (x - rint(x)
-    // has no rounding), then the hardware sin / cos on 2 pi (x - rint(x))
-    // (absolute error ~4e-7 on [-pi, pi], relative to |G| the same size as
-    // the FP32 rounding of k r itself)
-    const float xph = kc * r;
-    const float xr = xph - rintf(xph);
     float sn, cs;
-    __sincosf(6.28318530717959f * xr, &sn, &cs);
+    sincos_turns(kc * r, sn, cs);
     const float g0 = ir * inv4pi;
     const float Gx = cs * g0, Gy = sn * g0;
     const float Grx = Gx * ir, Gry = Gy * ir;
