@@ -449,7 +449,13 @@ void fetch_ranks(bem_handle* h, DevHM& m) {
   }
   sync(h);
   // pass-V work items of the H-matvec: 16 rows of one block each, so the
-  // largest blocks spread over many CTAs
+  // largest blocks spread over many CTAs. The buffer holds the most items the
+  // rank reservations allow, so it is allocated once per layout: growing it
+  // with the ranks of a frequency would free the old one, and cudaFree waits
+  // for every stream of the device (all sweep workers' queued kernels).
+  int64_t most = 0;
+  for (const FarBlock& f : h->L.far) most += ((int64_t)f.kcap + 15) / 16;
+  m.vwork.ensure((size_t)std::max<int64_t>(most, 1));
   std::vector<int2> vw;
   for (size_t i = 0; i < nf; i++)
     for (int32_t l0 = 0; l0 < m.h_rank[i]; l0 += 16) vw.push_back(make_int2((int)i, l0));
@@ -1234,7 +1240,7 @@ bool build_hlu_device(bem_handle* h) {
     a.trace = trace.p;
   }
   const int nl = launch_hlu_exec(a, h->hp_grid, s);
-  require(nl > 0, BEM_ECUDA, "H-LU executor: cooperative launch refused");
+  require(nl > 0, BEM_ECUDA, "H-LU executor: launch refused");
   h->launches += nl;
   CK(cudaGetLastError());
   launch_hlu_finite_check(h->dArena.p, P.arena, m.prec, h->dHCtrl.p + 3, h->nsm, s);
@@ -1420,6 +1426,8 @@ void apply_precond(bem_handle* h, double2* w, int R, const int* gate_flags = nul
   if (h->df_ok) {  // dataflow sweeps: w -> dP2 -> w, up to 8 vectors per launch
     h->dP2.ensure((size_t)std::min(R, HLU_DF_MAX_R) * N);
     HluDfWork ws{h->dfXi.p, h->dfAcc.p, h->dfEacc.p, h->dfPre.p, h->dfFin.p, h->dfCtrl.p, h->dfErr.p};
+    if (const char* e = std::getenv("BEM_DF_WAIT_US"))  // tests of the timeout path
+      if (std::atof(e) > 0) ws.wait_ns = (unsigned long long)(std::atof(e) * 1000.0);
     const int hp = df_helpers();
     // BEM_DF_TRACE=<file>: the lower sweep's driver phases of this
     // application, summarised into the file (profiling)
@@ -1659,6 +1667,7 @@ void solve_dev(bem_handle* h, double freq, const double2* g_caller, int64_t R, d
       loc.t_precond = std::chrono::duration<double>(std::chrono::steady_clock::now() - tp).count();
     }
   }
+  const auto t_pc = std::chrono::steady_clock::now();
   h->dG.ensure((size_t)R * N);
   h->dRhs.ensure((size_t)R * N);
   h->dX.ensure((size_t)R * N);
@@ -1682,6 +1691,7 @@ void solve_dev(bem_handle* h, double freq, const double2* g_caller, int64_t R, d
     gmres_dev(h, h->dRhs.p, h->dX.p, (int)R, &loc, true);
   }
   CK(cudaEventRecord(h->ev[5], s));
+  const auto t_gm = std::chrono::steady_clock::now();
   const double omega = 2.0 * M_PI * freq;
   double2 pfac = make_double2(0.0, h->cfg.density * omega);
   launch_backsub(h->dX.p, h->dG.p, h->dA.p, h->dB.p, h->dBc.p, h->dPerm.p, N, (int)R, pfac, phi,
@@ -1697,10 +1707,16 @@ void solve_dev(bem_handle* h, double freq, const double2* g_caller, int64_t R, d
   loc.t_rhs = elapsed(h->ev[3], h->ev[4]);
   loc.t_gmres = elapsed(h->ev[4], h->ev[5]);
   loc.t_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-  if (std::getenv("BEM_SOLVE_TRACE"))  // host wall time of the assembly step (profiling)
-    std::fprintf(stderr, "solve f %.2f assemble_wall %.4f t_nearfield %.4f t_aca %.4f total %.4f\n",
-                 freq, std::chrono::duration<double>(t_asm - t0).count(), loc.t_nearfield,
-                 loc.t_aca, loc.t_total);
+  if (std::getenv("BEM_SOLVE_TRACE")) {  // host wall times of the steps (profiling)
+    auto sec = [&](std::chrono::steady_clock::time_point t) {
+      return std::chrono::duration<double>(t - t0).count();
+    };
+    std::fprintf(stderr,
+                 "solve h %p f %.2f wall: assembled %.4f precond %.4f gmres %.4f total %.4f | "
+                 "device: nearfield %.4f aca %.4f rhs %.4f gmres %.4f iters %lld\n",
+                 (void*)h, freq, sec(t_asm), sec(t_pc), sec(t_gm), loc.t_total, loc.t_nearfield,
+                 loc.t_aca, loc.t_rhs, loc.t_gmres, (long long)loc.iterations);
+  }
   fill_rank_info(h, &loc);
   if (bad) loc.status = BEM_ENONFINITE;
   if (info) *info = loc;
@@ -1800,8 +1816,12 @@ void ensure_workers(bem_handle* h, int nw) {
 }
 
 // Frequencies idx[0..n) of a sweep on W handles (h and W - 1 workers), one
-// host thread per handle, each on its own stream; frequency i goes to handle
-// i mod W (with H-LU factor reuse: contiguous blocks of ascending frequencies). p (caller order, n_freq slices) gets each frequency's pressure.
+// host thread per handle, each on its own stream; a handle that is free takes
+// the next frequency of idx (a shared counter: the sweep ends at most one
+// solve after the average load instead of with the heaviest share of a fixed
+// split; each frequency's result is the same on every handle). With H-LU
+// factor reuse each handle takes a fixed contiguous block of ascending
+// frequencies instead. p (caller order, n_freq slices) gets each frequency's pressure.
 // With device pointers (gd, pd non-null) instead of g / p: every worker reads
 // gd and writes its frequencies' slices of pd directly; the workers' streams
 // start after the work already on h's stream and h's stream waits for them.
@@ -1830,16 +1850,23 @@ void run_sweep(bem_handle* h, int W, const double* freqs, const int64_t* idx, in
   }
   std::vector<bem_status> st(W, BEM_OK), wst(W, BEM_OK);
   std::atomic<bool> stop{false};
+  std::atomic<int64_t> next{0};
   std::mutex done_mu;
+  const bool blocks = h->cfg.use_preconditioner && h->cfg.precond_reuse > 1.0;
+  // the k-th position of handle w's share of idx, or n when it has none left
+  auto claim = [&](int w, int64_t k) -> int64_t {
+    if (stop.load(std::memory_order_acquire)) return n;
+    if (!blocks) return std::min<int64_t>(n, next.fetch_add(1));
+    const int64_t i = n * w / W + k;
+    return i < n * (w + 1) / W ? i : n;
+  };
   auto body = [&](int w) {
     bem_handle* x = hs[w];
     st[w] = guarded(x, [&] {
       CK(cudaSetDevice(h->device));
       if (dev) {
         CK(cudaStreamWaitEvent(x->stream, e0, 0));
-        const bool blocks = h->cfg.use_preconditioner && h->cfg.precond_reuse > 1.0;
-        const int64_t i0 = blocks ? n * w / W : w, i1 = blocks ? n * (w + 1) / W : n;
-        for (int64_t i = i0; i < i1; i += blocks ? 1 : W) {
+        for (int64_t k = 0, i; (i = claim(w, k)) < n; k++) {
           const int64_t f = idx[i];
           bem_solve_info loc{};
           solve_dev(x, freqs[f], gd, nrhs, nullptr, nullptr, pd + cnt * f, &loc);
@@ -1853,10 +1880,7 @@ void run_sweep(bem_handle* h, int W, const double* freqs, const int64_t* idx, in
       x->dOut3.ensure(cnt);
       // with factor reuse, each handle takes a contiguous block of the
       // (sorted) frequencies, so its consecutive solves are close
-      const bool blocks = h->cfg.use_preconditioner && h->cfg.precond_reuse > 1.0;
-      const int64_t i0 = blocks ? n * w / W : w, i1 = blocks ? n * (w + 1) / W : n;
-      for (int64_t i = i0; i < i1 && !stop.load(std::memory_order_acquire);
-           i += blocks ? 1 : W) {
+      for (int64_t k = 0, i; (i = claim(w, k)) < n; k++) {
         const int64_t f = idx[i];
         bem_solve_info loc{};
         solve_dev(x, freqs[f], x->dIn.p, nrhs, nullptr, nullptr, x->dOut3.p, &loc);

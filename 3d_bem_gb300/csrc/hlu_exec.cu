@@ -1,16 +1,16 @@
 // hlu_exec.cu -- executor of the H-LU task program (hlu_gpu.h): one persistent
-// cooperative kernel. Every CTA claims the next task index (the program's
-// topological order), waits until the tasks it depends on have raised their
-// done flags (acquire loads, a bounded wait), runs the task with all its
-// threads and raises its own flag (release store). Claims in a topological
-// order with all CTAs co-resident cannot deadlock: the earliest unfinished
-// task has every dependency finished.
+// kernel over a ready queue. A CTA takes the next queue slot, waits (bounded)
+// until a task is pushed into it, runs the task with all its threads, then
+// releases the task's successors; the release that completes a successor's
+// dependencies pushes it. Only CTAs that are running hold slots and tasks, so
+// the queue advances with any number of resident CTAs: the launch needs no
+// co-residency and starts on the SMs that are free (beside other streams'
+// kernels) instead of waiting for a whole idle GPU.
 //
 // Data that other CTAs wrote during the launch is read through L2
 // (ld.global.cg) and written with st.global.cg, so no SM reads a stale L1
 // line of the arena. The arithmetic is the storage type's: complex FP32
 // factors are computed in FP32, complex FP64 factors in FP64.
-#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "hlu_gpu.h"
@@ -1512,12 +1512,12 @@ int launch_hlu_exec(const HluExecArgs& a, int grid, cudaStream_t s) {
   cudaError_t e;
   if (a.precision == 0) {
     occupancy<double2>();
-    e = cudaLaunchCooperativeKernel((const void*)hlu_exec_kernel<double2>, grid, HX_THREADS, p,
-                                    smem_bytes<double2>(), s);
+    e = cudaLaunchKernel((const void*)hlu_exec_kernel<double2>, grid, HX_THREADS, p,
+                         smem_bytes<double2>(), s);
   } else {
     occupancy<float2>();
-    e = cudaLaunchCooperativeKernel((const void*)hlu_exec_kernel<float2>, grid, HX_THREADS, p,
-                                    smem_bytes<float2>(), s);
+    e = cudaLaunchKernel((const void*)hlu_exec_kernel<float2>, grid, HX_THREADS, p,
+                         smem_bytes<float2>(), s);
   }
   if (e != cudaSuccess) return -1;
   return 1;

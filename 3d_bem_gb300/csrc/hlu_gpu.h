@@ -180,9 +180,9 @@ struct HluExecArgs {
   unsigned long long* trace;     // optional: per task claim, start, end (ns)
 };
 
-// One cooperative launch of `grid` CTAs (at most the co-resident count, and
-// the per-CTA scratch must hold grid slots); returns the kernels launched (1),
-// or -1 when the launch was refused.
+// One launch of `grid` CTAs (the per-CTA scratch must hold grid slots; any
+// number of them may be resident at a time); returns the kernels launched
+// (1), or -1 when the launch was refused.
 int launch_hlu_exec(const HluExecArgs& a, int grid, cudaStream_t s);
 // Largest co-resident CTA count per SM of the executor for a precision.
 int hlu_exec_occupancy(int precision);

@@ -222,10 +222,13 @@ int launch_hlu_sweep(const int32_t* sched, int nops, const int64_t* leaves, cons
 //         their constants staged in shared memory before the wait); ready
 //         when x(i - 2) is solved and C(i - 3) and E(i) are done.
 // Every item waits only on progress up to its level and on items earlier in
-// the order, and the launch is cooperative (all blocks resident), so the
-// chain always advances. Each sum has one fixed order: results do not depend
+// the order. Roles follow the order in which blocks start: the first one
+// drives, the others claim items in order, so every wait is on a block that
+// is already running and the chain advances with any number of resident
+// blocks; the launch needs no co-residency and starts on the SMs that are
+// free, beside other streams' kernels. Each sum has one fixed order: results do not depend
 // on which block ran an item or on the number of helpers. Every wait is
-// bounded: after DF_TIMEOUT_NS the block sets the sticky error word and
+// bounded: after DfArgs::wait_ns the block sets the sticky error word and
 // returns.
 // All arithmetic and every vector inside the sweep (x, acc, partial sums,
 // staging) is in the factor's type T2: complex FP32 for the mixed method,
@@ -239,7 +242,6 @@ constexpr int NW = DT / 32;
 constexpr int DM = HLU_DF_MAX_M, DR = HLU_DF_MAX_R, DK = HLU_DF_MAX_RANK;
 constexpr int LAG = HLU_DF_LAG, NLATE = HLU_DF_NLATE;
 constexpr int PS = 4;  // column pairs per warp and round in C(j)
-constexpr unsigned long long DF_TIMEOUT_NS = 2000000000ull;
 constexpr int MS_ELEMS = DM * (DM + 1);  // apply matrix, rows padded
 constexpr int CS_ELEMS = 3 * DK * DM;    // corner: F (<= 64 cols x rows) or U rows + V over
                                          // the columns of chunks i - 1 and i - 2
@@ -321,14 +323,14 @@ __device__ __forceinline__ double2 ldv(const double2* p) { return __ldcg(p); }
 
 // thread 0 only: wait until *p >= v; false (and the error word set) after the
 // time limit or when another block already gave up
-__device__ bool df_wait(const int* p, int v, int* err) {
+__device__ bool df_wait(const int* p, int v, int* err, unsigned long long lim) {
   if (ld_acquire(p) >= v) return true;
   const unsigned long long t0 = gtimer();
   for (unsigned it = 1;; it++) {
     if (ld_acquire(p) >= v) return true;
-    if ((it & 63) == 0) {
+    if ((it & 63) == 1) {  // after the first failed poll, then every 64
       if (ld_acquire(err)) return false;
-      if (gtimer() - t0 > DF_TIMEOUT_NS) {
+      if (gtimer() - t0 > lim) {
         atomicCAS(err, 0, 1);
         return false;
       }
@@ -365,8 +367,9 @@ struct DfArgs {
   void* eacc;
   void* pre;
   void* fin;
-  int* ctrl;  // [0] item counter, [1] progress, then R, C and E done (D each)
+  int* ctrl;  // [0] item counter, [1] progress, [2] arrival ticket, then R, C and E done (D each)
   int* err;
+  unsigned long long wait_ns;  // bound of one wait
   int64_t N;
   int R;
   HmvGate gate;
@@ -380,7 +383,7 @@ struct DfArgs {
 };
 
 __device__ bool df_wait_progress(const DfArgs& a, int v) {
-  return v <= 0 || df_wait(a.flagX(v - 1), 1, a.err);
+  return v <= 0 || df_wait(a.flagX(v - 1), 1, a.err, a.wait_ns);
 }
 
 
@@ -490,7 +493,7 @@ __device__ void df_driver(const DfArgs& a, unsigned char* sm) {
     const T2* Cs = Ms + MS_ELEMS;
     const T2* xc = xcs + (i & 1) * WCOLS * DR;
     bool ok = true;
-    if (tid == 0 && i >= 1) ok = df_wait(a.flagR(i), 1, a.err);
+    if (tid == 0 && i >= 1) ok = df_wait(a.flagR(i), 1, a.err, a.wait_ns);
     if (!__syncthreads_and(ok)) {
       cp_async_wait_all();  // no copy in flight at exit
       return;
@@ -600,7 +603,7 @@ __device__ bool df_early_item(const DfArgs& a, int i, unsigned char* sm) {
   bool ok = true;
   if (tid == 0) {
     ok = df_wait_progress(a, i - LAG + 1);
-    if (ok && i >= LAG) ok = df_wait(a.flagC(i - LAG), 1, a.err);
+    if (ok && i >= LAG) ok = df_wait(a.flagC(i - LAG), 1, a.err, a.wait_ns);
   }
   if (!__syncthreads_and(ok)) return false;
   const int m = c.m, RR = a.R;
@@ -724,8 +727,8 @@ __device__ bool df_late_item(const DfArgs& a, int i, unsigned char* sm) {
   if (tid == 0) {
     ok = df_wait_progress(a, i - 1);
     const int cdep = i - 3;  // pre (corner) and pre2 (mode 2) are complete after C(i - 3)
-    if (ok && cdep >= 0) ok = df_wait(a.flagC(cdep), 1, a.err);
-    if (ok && i >= LAG - 1) ok = df_wait(a.flagE(i), 1, a.err);
+    if (ok && cdep >= 0) ok = df_wait(a.flagC(cdep), 1, a.err, a.wait_ns);
+    if (ok && i >= LAG - 1) ok = df_wait(a.flagE(i), 1, a.err, a.wait_ns);
   }
   if (!__syncthreads_and(ok)) {
     cp_async_wait_all();
@@ -857,7 +860,7 @@ __device__ bool df_col_item(const DfArgs& a, int j) {
   bool ok = true;
   if (tid == 0) {
     ok = df_wait_progress(a, j + 1);
-    if (ok && j >= 1) ok = df_wait(a.flagC(j - 1), 1, a.err);
+    if (ok && j >= 1) ok = df_wait(a.flagC(j - 1), 1, a.err, a.wait_ns);
   }
   if (!__syncthreads_and(ok)) return false;
   T2 xr[DR];
@@ -926,7 +929,11 @@ __global__ void __launch_bounds__(DT, 1) hlu_df_kernel(DfArgs a) {
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ int sq;
   if (gate_closed(a.gate)) return;  // every block reads the same flags
-  if (blockIdx.x == 0)
+  if (threadIdx.x == 0) sq = atomicAdd(a.ctrl + 2, 1);  // arrival order
+  __syncthreads();
+  const bool driver = sq == 0;
+  __syncthreads();  // sq is the helpers' claim slot from here on
+  if (driver)
     df_driver<T2>(a, sm);
   else
     df_helper<T2>(a, sm, &sq);
@@ -973,15 +980,16 @@ int launch_hlu_df(const HluDfDev& p, const int64_t* leaves, const void* data, in
   a.R = R;
   a.gate = gate;
   a.trace = ws.trace;
+  a.wait_ns = ws.wait_ns;
   void* args[] = {&a};
   const int cap = precision == 0 ? df_prepare<double2>() : df_prepare<float2>();
   const int grid = std::max(2, std::min(1 + std::max(1, helpers), cap));
   if (precision == 0)
-    CUDA_OK(cudaLaunchCooperativeKernel((const void*)hlu_df_kernel<double2>, dim3(grid), dim3(DT),
-                                        args, df_smem<double2>(), s));
+    CUDA_OK(cudaLaunchKernel((const void*)hlu_df_kernel<double2>, dim3(grid), dim3(DT), args,
+                             df_smem<double2>(), s));
   else
-    CUDA_OK(cudaLaunchCooperativeKernel((const void*)hlu_df_kernel<float2>, dim3(grid), dim3(DT),
-                                        args, df_smem<float2>(), s));
+    CUDA_OK(cudaLaunchKernel((const void*)hlu_df_kernel<float2>, dim3(grid), dim3(DT), args,
+                             df_smem<float2>(), s));
   return 2;
 }
 

@@ -107,9 +107,12 @@ struct HluDfWork {
   int* ctrl = nullptr;
   int* err = nullptr;
   unsigned long long* trace = nullptr;  // optional: 4 x D driver timestamps (ns)
+  // bound of one wait (ns): a driver may wait for helpers that start only
+  // when other streams' kernels leave an SM free
+  unsigned long long wait_ns = 10000000000ull;
 };
 
-// w (R x N) -> x (R x N) with one cooperative launch of 1 driver + `helpers`
+// w (R x N) -> x (R x N) with one launch of 1 driver + `helpers`
 // CTAs (R <= HLU_DF_MAX_R; w is only read). Returns the kernels launched.
 // gate: optional early exit (bem_kernels.h HmvGate; all its flags set -> no work)
 int launch_hlu_df(const HluDfDev& p, const int64_t* leaves, const void* data, int precision,

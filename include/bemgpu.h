@@ -316,7 +316,10 @@ bem_status bem_autotune(bem_handle* h, double freq, int64_t nrhs, int64_t* tuned
 
 /* Frequency sweep (BemSolverController::run, bemsolvercontroller.cpp:49-109):
  * nf frequencies x nrhs right-hand sides; p is n x nrhs x nf (caller order).
- * info may be NULL or hold nf records. */
+ * info may be NULL or hold nf records. The cfg.sweep_workers handles take
+ * the frequencies in the order given, each the next one when it is free, so
+ * a sweep that lists its most expensive frequencies first ends most evenly;
+ * results do not depend on the order or on the worker count. */
 bem_status bem_sweep(bem_handle* h, const double* freqs, int64_t nf, const double* g,
                      int64_t nrhs, double* p, bem_solve_info* info);
 /* Same with device pointers: g (n x nrhs complex FP64) and p (n x nrhs x nf)

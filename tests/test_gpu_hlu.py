@@ -296,3 +296,24 @@ def test_device_factorization_wait_limit(bem, meshes, monkeypatch):
     rng = np.random.default_rng(2)
     x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
     assert rel(s.hlu_solve(s.hmatvec(1, x)), x) < 1e-2
+
+
+def test_dataflow_sweep_wait_limit(bem, meshes, monkeypatch):
+    """A wait of the dataflow sweep that runs out (a limit of a nanosecond,
+    which no dependency can meet) ends the launch: every block gives up and
+    returns, the call reports BEM_ETIMEOUT, and with the normal limit the same
+    handle gives the same solution as before, bitwise."""
+    tri, s = setup(bem, meshes, 3, precond_rank=2)
+    n = tri.shape[0]
+    s.assemble(FREQ)
+    s.hlu_build()
+    assert s.hlu_sweep_kind() == 1
+    rng = np.random.default_rng(5)
+    B = rng.standard_normal((n, 3)) + 1j * rng.standard_normal((n, 3))
+    X = s.hlu_solve(B)
+    monkeypatch.setenv("BEM_DF_WAIT_US", "0.001")
+    with pytest.raises(bem.BemError) as ei:
+        s.hlu_solve(B)
+    assert ei.value.status == bem.BEM_ETIMEOUT
+    monkeypatch.delenv("BEM_DF_WAIT_US")
+    assert np.array_equal(s.hlu_solve(B), X)
