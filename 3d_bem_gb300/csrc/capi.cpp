@@ -206,6 +206,7 @@ struct bem_handle {
     HluDfDev view;
   } dfL, dfU;
   bool df_ok = false;
+  int df_helpers = 32;  // helper CTAs per dataflow sweep (16 while concurrent sweep workers run)
   std::string df_why;
   DBuf<unsigned char> dfXi, dfAcc, dfEacc;  // factor-type vectors
   DBuf<unsigned char> dfPre, dfFin;
@@ -916,10 +917,10 @@ int64_t hlu_wait_cycles() {
   return us > 0 ? (int64_t)(us * 2000.0) : (int64_t)4000000000LL;
 }
 
-int df_helpers() {
+int df_helpers(const bem_handle* h) {
   const char* e = std::getenv("BEM_HLU_HELPERS");
   const int v = e ? std::atoi(e) : 0;
-  return v > 0 ? v : 32;
+  return v > 0 ? v : h->df_helpers;
 }
 
 // nonzero sticky error word of the dataflow sweeps: a wait ran out of time
@@ -1428,7 +1429,7 @@ void apply_precond(bem_handle* h, double2* w, int R, const int* gate_flags = nul
     HluDfWork ws{h->dfXi.p, h->dfAcc.p, h->dfEacc.p, h->dfPre.p, h->dfFin.p, h->dfCtrl.p, h->dfErr.p};
     if (const char* e = std::getenv("BEM_DF_WAIT_US"))  // tests of the timeout path
       if (std::atof(e) > 0) ws.wait_ns = (unsigned long long)(std::atof(e) * 1000.0);
-    const int hp = df_helpers();
+    const int hp = df_helpers(h);
     // BEM_DF_TRACE=<file>: the lower sweep's driver phases of this
     // application, summarised into the file (profiling)
     const char* trace_path = std::getenv("BEM_DF_TRACE");
@@ -1839,6 +1840,14 @@ void run_sweep(bem_handle* h, int W, const double* freqs, const int64_t* idx, in
   ensure_workers(h, W - 1);
   std::vector<bem_handle*> hs{h};
   for (int w = 0; w + 1 < W; w++) hs.push_back(h->workers[w]);
+  // a lone sweep is fastest with 32 helpers; concurrent ones share the SMs
+  // (each helper holds a whole SM's registers): 16 each measured 4-7 % faster
+  // at 5-7 workers on the 81,920-triangle pencil
+  for (bem_handle* x : hs) x->df_helpers = W > 1 ? 16 : 32;
+  struct Restore {
+    bem_handle* h;
+    ~Restore() { h->df_helpers = 32; }
+  } restore{h};
   const size_t cnt = (size_t)h->N * nrhs;
   const bool dev = gd != nullptr;
   cudaEvent_t e0 = nullptr;

@@ -795,9 +795,9 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=16,
                     help="frequencies of the 64-frequency sweep timed (spread over the band)")
-    ap.add_argument("--workers", type=int, default=5,
-                    help="concurrent frequency workers of the batched sweep (mixed arm; 3 / 4 "
-                         "/ 5 / 6 workers measured 0.71 / 0.67 / 0.61 / 0.63 s per frequency)")
+    ap.add_argument("--workers", type=int, default=6,
+                    help="concurrent frequency workers of the batched sweep (mixed arm; 5 / 6 "
+                         "/ 7 workers measured 0.49 / 0.47 / 0.48 s per frequency)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="sphere20k", choices=sorted(WORKLOADS),
