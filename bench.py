@@ -81,6 +81,10 @@ PENCIL_DESC = ("pencil r=4 mm L=0.2 m + 10 mm conical tip, 81,920 triangles, imp
 # hmv32_upass<8,256,6>) on the 20,480-triangle pencil: 592 MB for 521 MB; the
 # traffic grows with the stored entries, so it scales to the headline size
 HMV32_R8_TRAFFIC_PER_BYTE = 592.2 / 521.4
+# ncu --set full of aca_kernel<0,float2,128> (the 128-thread ACA launch of the
+# phi matrix) on the 20,480-triangle sphere at 1.5 kHz: FMA pipe active 40.6 %
+# of its peak, issue slots 64 %, warps active 50 %, L2 hit rate 66 %
+ACA_FMA_PIPE_NCU = 0.406
 METRIC = "freq-solves/sec (H-matrix Helmholtz BEM solve, <=1e-5 rel. surface-pressure error)"
 UNIT = "freq-solves/s"
 
@@ -477,6 +481,16 @@ def sphere_leg(torch, pkg, meshes, args, ws):
     out["mixed"] = {"freq_solves_per_s": round(steps / (ms / 1e3), 3),
                     "ms_per_solve": round(ms / steps, 3),
                     "gmres_iterations": int(max(i["iterations"] for i in infos))}
+    # the ACA phase of the last timed solve: entries evaluated per second
+    # (k (m + n) per block of rank k, both matrices) and the FMA-pipe share
+    part = s.partition()
+    E = aca_entries(part, s.ranks(0)) + aca_entries(part, s.ranks(1))
+    t_aca = infos[-1]["t_aca"]
+    out["aca"] = {"frequency_hz": fr_t[-1], "span_ms": round(1e3 * t_aca, 3), "entries": E,
+                  "entries_per_s": round(E / t_aca), "bound": "issue / FP32 pipes",
+                  "fma_pipe_active_ncu": ACA_FMA_PIPE_NCU,
+                  "fma_pipe_source": "ncu --set full of aca_kernel<0,float2,128>, this "
+                                     "workload at 1.5 kHz"}
     if not args.no_plain:
         s64, _ = make_solver(pkg, meshes, sub, 0)
         ms64, _, _, p64, _ = timed_solves(torch, pkg, s64, n, 1, fr_t[:2], fr_w[:1], ws)
@@ -727,6 +741,40 @@ def run_hmatvec_only(args):
     s.close()
 
 
+def aca_entries(partition, ranks):
+    """ACA entries of one matrix: a block of rank k (m x n) evaluates k rows and
+    k columns of itself, k (m + n) entries (the rejected last step not counted)."""
+    adm = partition[:, 4] != 0
+    m, n = partition[adm, 1], partition[adm, 3]
+    return int(np.sum(ranks[adm].astype(np.int64) * (m + n)))
+
+
+def run_aca_only(args):
+    """Assembly of the 20,480-triangle sphere at 1.5 kHz (mixed precision, ACA
+    1e-5, the learned ACA rule table), a warm-up one and three timed ones: the
+    ACA span and its entries per second (for profiling aca_kernel)."""
+    import torch
+    pkg = importlib.import_module("3d_bem_gb300")
+    meshes = importlib.import_module("3d_bem_gb300.meshes")
+    pkg.build()
+    s, n = make_solver(pkg, meshes, WORKLOADS["sphere20k"][0], 1, selector=2)
+    s.assemble(1500.0)
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        s.assemble(1500.0)
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    part = s.partition()
+    E = aca_entries(part, s.ranks(0)) + aca_entries(part, s.ranks(1))
+    t = min(ts)
+    print(json.dumps({"aca_only": {"n_elements": int(n), "assemble_ms": round(1e3 * t, 3),
+                                   "aca_entries": E,
+                                   "entries_per_s": round(E / t, 1)}}), flush=True)
+    s.close()
+
+
 def run_field_only(args):
     """The field leg alone on one GPU (for profiling its kernels)."""
     import torch
@@ -820,6 +868,9 @@ def main():
                     help="only the pencil's inner-GMRES H-matvec (8 RHS); profiling")
     ap.add_argument("--pencil-n", type=int, default=PENCIL_N,
                     help="triangles of the pencil for --hlu-only / --hmatvec-only")
+    ap.add_argument("--aca-only", action="store_true",
+                    help="only assemblies of the 20,480-triangle sphere (ACA span, entries/s); "
+                         "profiling")
     ap.add_argument("--field-only", action="store_true",
                     help="only the field evaluation leg (one mixed solve first); profiling")
     ap.add_argument("--no-sweep", action="store_true",
@@ -840,6 +891,8 @@ def main():
         run_hmatvec_only(args)
     elif args.field_only:
         run_field_only(args)
+    elif args.aca_only:
+        run_aca_only(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
