@@ -206,7 +206,7 @@ struct bem_handle {
     HluDfDev view;
   } dfL, dfU;
   bool df_ok = false;
-  int df_helpers = 32;  // helper CTAs per dataflow sweep (16 while concurrent sweep workers run)
+  int df_helpers = 32;  // helper CTAs per dataflow sweep (12 while concurrent sweep workers run)
   std::string df_why;
   DBuf<unsigned char> dfXi, dfAcc, dfEacc;  // factor-type vectors
   DBuf<unsigned char> dfPre, dfFin;
@@ -1841,9 +1841,10 @@ void run_sweep(bem_handle* h, int W, const double* freqs, const int64_t* idx, in
   std::vector<bem_handle*> hs{h};
   for (int w = 0; w + 1 < W; w++) hs.push_back(h->workers[w]);
   // a lone sweep is fastest with 32 helpers; concurrent ones share the SMs
-  // (each helper holds a whole SM's registers): 16 each measured 4-7 % faster
-  // at 5-7 workers on the 81,920-triangle pencil
-  for (bem_handle* x : hs) x->df_helpers = W > 1 ? 16 : 32;
+  // (each helper holds a whole SM's registers): on the 81,920-triangle pencil
+  // with 6 workers, 32 / 16 / 12 / 8 helpers each measured 0.51 / 0.48 /
+  // 0.46 / 0.47 s per frequency
+  for (bem_handle* x : hs) x->df_helpers = W > 1 ? 12 : 32;
   struct Restore {
     bem_handle* h;
     ~Restore() { h->df_helpers = 32; }
