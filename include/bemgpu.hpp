@@ -13,6 +13,9 @@
  *   BoundaryElementSolver            boundaryelementsolver.h
  *     ::calculateBoundarySolution()  -> hMatrixSolve() (:526-744)
  *     ::getPhiSolution() / getDPhiSolution() / getSoundPressure()
+ *   BemSolverController              bemsolvercontroller.cpp:49-109 (the
+ *     ::run() / requestStop()        frequency loop, per-frequency solved
+ *     ::isBoundarySolvedAtFreq(i)    flags; a stopped run resumes)
  *
  * Header-only; link libbemgpu.so. Every call that fails throws bemgpu::Error
  * with the status and the handle's message. Complex vectors are
@@ -22,7 +25,10 @@
 #ifndef BEMGPU_HPP
 #define BEMGPU_HPP
 
+#include <atomic>
 #include <complex>
+#include <exception>
+#include <functional>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -56,6 +62,7 @@ struct BemSolverParameters {
   long gmresRestart = 300;
   long gmresMaxIterations = 1000;
   bool mixedPrecision = false;  // complex-FP32 storage with FP64 refinement
+  long sweepWorkers = 1;        // frequencies solved concurrently by a sweep
 };
 
 namespace detail {
@@ -86,6 +93,7 @@ inline Handle make_handle(const BemSolverParameters& p, double c, double rho) {
   cfg.use_preconditioner = p.usePreconditioner ? 1 : 0;
   cfg.precond_rank = p.preconditionerRank;
   cfg.precond_tol = p.preconditionerRelError;
+  cfg.sweep_workers = p.sweepWorkers;
   bem_handle* h = nullptr;
   const bem_status st = bem_create(&cfg, &h);
   if (st != BEM_OK) throw Error(st, "bem_create failed");
@@ -215,6 +223,86 @@ class BoundaryElementSolver {
   double freq_;
   CVec g_, phi_, dphi_, p_;
   bem_solve_info info_{};
+};
+
+// BemSolverController (bemsolvercontroller.cpp:49-109): the frequency loop of
+// one mesh with the boundariesSolvedAtFrequency flags. run() solves every
+// frequency not flagged yet (sweepWorkers at a time), flags each one as it
+// completes and calls boundarySolvedForFreqIndex(i) (the reference's signal
+// of that name; a place to save the result). After requestStop() the run
+// ends once the frequencies in flight are done, in place of the reference's
+// QThread::terminate (:211-227); a later run() solves the rest.
+class BemSolverController {
+ public:
+  BemSolverController(const std::vector<double>& triangles, const CVec& a, const CVec& b,
+                      const CVec& g, const std::vector<double>& frequencies,
+                      const BemSolverParameters& params, double c = 343.0, double rho = 1.2)
+      : n_((int64_t)triangles.size() / 9), freqs_(frequencies) {
+    if ((int64_t)a.size() != n_ || (int64_t)b.size() != n_ || (int64_t)g.size() != n_)
+      throw Error(BEM_EINVAL, "BemSolverController: one a, b, g per triangle");
+    if (freqs_.empty()) throw Error(BEM_EINVAL, "BemSolverController: no frequencies");
+    h_ = make_handle(params, c, rho);
+    detail::check(bem_set_mesh(h_.get(), triangles.data(), n_), h_.get(), "bem_set_mesh");
+    std::vector<double> ad(2 * n_), bd(2 * n_);
+    g_.resize(2 * n_);
+    for (int64_t i = 0; i < n_; i++) {
+      ad[2 * i] = a[i].real();
+      ad[2 * i + 1] = a[i].imag();
+      bd[2 * i] = b[i].real();
+      bd[2 * i + 1] = b[i].imag();
+      g_[2 * i] = g[i].real();
+      g_[2 * i + 1] = g[i].imag();
+    }
+    detail::check(bem_set_bc(h_.get(), ad.data(), bd.data()), h_.get(), "bem_set_bc");
+    p_.assign(2 * n_ * freqs_.size(), 0.0);
+    solved_.assign(freqs_.size(), 0);
+    infos_.assign(freqs_.size(), bem_solve_info{});
+  }
+
+  void run() {
+    stop_ = false;
+    hook_error_ = nullptr;
+    const bem_status st =
+        bem_sweep_resume(h_.get(), freqs_.data(), (int64_t)freqs_.size(), g_.data(), 1,
+                         p_.data(), infos_.data(), solved_.data(), &on_done, this);
+    if (hook_error_) std::rethrow_exception(hook_error_);
+    if (st != BEM_OK && st != BEM_EMAXIT) detail::check(st, h_.get(), "bem_sweep_resume");
+  }
+  void requestStop() { stop_ = true; }
+
+  std::size_t numFrequencies() const { return freqs_.size(); }
+  bool isBoundarySolvedAtFreq(std::size_t i) const { return solved_.at(i) != 0; }
+  // sound pressure on the elements at frequency i (caller order)
+  CVec getSoundPressure(std::size_t i) const {
+    if (!isBoundarySolvedAtFreq(i)) throw Error(BEM_EINVAL, "frequency not solved yet");
+    const double* q = p_.data() + 2 * n_ * i;
+    CVec out(n_);
+    for (int64_t e = 0; e < n_; e++) out[e] = cplx(q[2 * e], q[2 * e + 1]);
+    return out;
+  }
+  const bem_solve_info& info(std::size_t i) const { return infos_.at(i); }
+
+  std::function<void(std::size_t)> boundarySolvedForFreqIndex;
+
+ private:
+  static int on_done(int64_t f, void* user) {  // one call at a time
+    auto* c = static_cast<BemSolverController*>(user);
+    try {
+      if (c->boundarySolvedForFreqIndex) c->boundarySolvedForFreqIndex((std::size_t)f);
+    } catch (...) {
+      c->hook_error_ = std::current_exception();
+      return 1;
+    }
+    return c->stop_.load() ? 1 : 0;
+  }
+
+  Handle h_;
+  int64_t n_;
+  std::vector<double> freqs_, g_, p_;
+  std::vector<uint8_t> solved_;
+  std::vector<bem_solve_info> infos_;
+  std::atomic<bool> stop_{false};
+  std::exception_ptr hook_error_;
 };
 
 }  // namespace bemgpu

@@ -35,6 +35,27 @@ int main(int argc, char** argv) {
     }
     par.acaRelativeError = 1e-6;
     par.gmresRelativeError = 1e-10;
+    if (mode == "sweep") {  // BemSolverController: stop after two frequencies, then resume
+      par.sweepWorkers = 2;
+      const bemgpu::CVec a(n, 0.0), b(n, 1.0), g(n, 1.0);
+      const std::vector<double> fr = {200.0, 300.0, 400.0, 500.0, 600.0};
+      bemgpu::BemSolverController c(tri, a, b, g, fr, par, 343.0, 1.2);
+      int done = 0;
+      c.boundarySolvedForFreqIndex = [&](std::size_t) {
+        if (++done == 2) c.requestStop();
+      };
+      c.run();
+      int first = 0;
+      for (std::size_t i = 0; i < fr.size(); i++) first += c.isBoundarySolvedAtFreq(i);
+      c.run();
+      std::printf("first_run %d second_run %d\n", first, done - first);
+      for (std::size_t i = 0; i < fr.size(); i++) {
+        double pn = 0;
+        for (const auto& v : c.getSoundPressure(i)) pn += std::norm(v);
+        std::printf("f%zu %.15e status%zu %d\n", i, std::sqrt(pn), i, c.info(i).status);
+      }
+      return 0;
+    }
     par.usePreconditioner = mode == "solve_precond";
     const bemgpu::CVec a(n, 0.0), b(n, 1.0), g(n, 1.0);
     bemgpu::BoundaryElementSolver s(tri, a, b, g, 300.0, par, 343.0, 1.2);

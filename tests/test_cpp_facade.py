@@ -67,3 +67,32 @@ def test_facade_solve_matches_python(bem, meshes, facade_bin, tmp_path, precond)
     assert abs(p0 - p[0, 0]) < 1e-9 * abs(p[0, 0])
     assert float(vals["gmres_rel_err"]) < 1e-6
     assert float(vals["hlu_rel_err"]) < 0.2  # rank-2 preconditioner, not a solver
+
+
+def test_facade_controller_compiles(facade_bin):
+    """BemSolverController is in the header the fixture compiled (-Wall
+    -Werror); the GPU test below runs it."""
+    assert os.path.exists(facade_bin)
+
+
+@pytest.mark.gpu
+def test_facade_controller_stops_and_resumes(bem, meshes, facade_bin, tmp_path):
+    """BemSolverController (bemsolvercontroller.cpp:49-109): a run stopped
+    after two completed frequencies (two workers, so two or three are
+    flagged), a second run that solves only the rest, and pressures equal to
+    the Python sweep of the same frequencies."""
+    tri = meshes.icosphere(2)
+    n = tri.shape[0]
+    out, vals = run(facade_bin, "sweep", tri, tmp_path)
+    first, second = int(vals["first_run"]), int(vals["second_run"])
+    assert 2 <= first <= 3 and first + second == 5, out
+    s = bem.Solver(leaf_size=32, eta=2.0, aca_tol=1e-6, gmres_tol=1e-10, wave_speed=343.0,
+                   density=1.2, sweep_workers=2)
+    s.set_mesh(tri)
+    s.set_bc(np.zeros(n), np.ones(n))
+    p, _ = s.sweep([200.0, 300.0, 400.0, 500.0, 600.0], np.ones(n))
+    s.close()
+    for i in range(5):
+        assert int(vals[f"status{i}"]) == 0, out
+        ref = np.linalg.norm(p[:, 0, i])
+        assert abs(float(vals[f"f{i}"]) - ref) < 1e-9 * ref, (i, out)
