@@ -983,13 +983,13 @@ bool prepare_hlu_program(bem_handle* h) {
 }
 
 // Arena (zeroed once, so padding never holds stale bits), per-CTA scratch for
-// the co-resident grid and the large truncations' regions, per precision.
+// the executor's grid and the large truncations' regions, per precision.
 void prepare_hlu_arena(bem_handle* h, int prec) {
   const HluProgram& P = h->hp;
   if (h->hp_prec == prec) return;
   const size_t es = prec ? sizeof(float2) : sizeof(double2);
   const int occ = hlu_exec_occupancy(prec);
-  require(occ >= 1, BEM_ECUDA, "H-LU executor: no co-resident CTA fits an SM");
+  require(occ >= 1, BEM_ECUDA, "H-LU executor: its CTA does not fit an SM");
   // CTAs per SM of the executor (all that fit, at most 4; BEM_HLU_CTAS_PER_SM
   // caps it lower, leaving SM room to concurrent sweep workers' kernels)
   int cap = 4;

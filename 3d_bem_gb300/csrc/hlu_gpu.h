@@ -184,7 +184,7 @@ struct HluExecArgs {
 // number of them may be resident at a time); returns the kernels launched
 // (1), or -1 when the launch was refused.
 int launch_hlu_exec(const HluExecArgs& a, int grid, cudaStream_t s);
-// Largest co-resident CTA count per SM of the executor for a precision.
+// Most CTAs of the executor an SM holds at once, for a precision (sizes the grid).
 int hlu_exec_occupancy(int precision);
 // flag |= 1 when the n arena values (complex, the precision's type) hold a NaN
 // or an Inf.
