@@ -207,6 +207,7 @@ struct bem_handle {
   } dfL, dfU;
   bool df_ok = false;
   int df_helpers = 32;  // helper CTAs per dataflow sweep (12 while concurrent sweep workers run)
+  int hlu_ctas_per_sm = 0;  // > 0: the executor's grid, per SM, below hp_grid (sweep workers)
   std::string df_why;
   DBuf<unsigned char> dfXi, dfAcc, dfEacc;  // factor-type vectors
   DBuf<unsigned char> dfPre, dfFin;
@@ -1240,7 +1241,9 @@ bool build_hlu_device(bem_handle* h) {
     CK(cudaMemsetAsync(trace.p, 0, 3 * P.tasks.size() * sizeof(unsigned long long), s));
     a.trace = trace.p;
   }
-  const int nl = launch_hlu_exec(a, h->hp_grid, s);
+  const int grid = h->hlu_ctas_per_sm > 0 ? std::min(h->hp_grid, h->nsm * h->hlu_ctas_per_sm)
+                                          : h->hp_grid;  // scratch holds hp_grid CTAs
+  const int nl = launch_hlu_exec(a, grid, s);
   require(nl > 0, BEM_ECUDA, "H-LU executor: launch refused");
   h->launches += nl;
   CK(cudaGetLastError());
@@ -1249,7 +1252,7 @@ bool build_hlu_device(bem_handle* h) {
   int ctrl[4] = {0, 0, 0, 0};
   CK(cudaMemcpyAsync(ctrl, h->dHCtrl.p, sizeof(ctrl), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
-  if (a.trace) hlu_trace_summary(P, trace, h->hp_grid, h->cfg.precond_tol, trace_path);
+  if (a.trace) hlu_trace_summary(P, trace, grid, h->cfg.precond_tol, trace_path);
   if (ctrl[1])
     throw BemError{BEM_ETIMEOUT, "H-LU factorization: a task dependency wait ran out of time"};
   if (ctrl[2] || ctrl[3]) return false;
@@ -1840,14 +1843,23 @@ void run_sweep(bem_handle* h, int W, const double* freqs, const int64_t* idx, in
   ensure_workers(h, W - 1);
   std::vector<bem_handle*> hs{h};
   for (int w = 0; w + 1 < W; w++) hs.push_back(h->workers[w]);
-  // a lone sweep is fastest with 32 helpers; concurrent ones share the SMs
-  // (each helper holds a whole SM's registers): on the 81,920-triangle pencil
-  // with 6 workers, 32 / 16 / 12 / 8 helpers each measured 0.51 / 0.48 /
-  // 0.46 / 0.47 s per frequency
-  for (bem_handle* x : hs) x->df_helpers = W > 1 ? 12 : 32;
+  // A lone solve is fastest with 32 helpers per dataflow sweep and the
+  // executor on every CTA an SM holds (4). Concurrent workers share the SMs
+  // (each helper holds a whole SM's registers; an executor grid of 4 per SM
+  // fills the GPU while its critical path leaves most CTAs waiting). On the
+  // 81,920-triangle pencil with 6 workers: 32 / 16 / 12 / 8 helpers measured
+  // 0.51 / 0.48 / 0.46 / 0.47 s per frequency (executor at 4 per SM); with
+  // 12 helpers, the executor at 4 / 2 / 1 per SM 0.465 / 0.397 / 0.390 s.
+  for (bem_handle* x : hs) {
+    x->df_helpers = W > 1 ? 12 : 32;
+    x->hlu_ctas_per_sm = W > 1 ? 1 : 0;
+  }
   struct Restore {
     bem_handle* h;
-    ~Restore() { h->df_helpers = 32; }
+    ~Restore() {
+      h->df_helpers = 32;
+      h->hlu_ctas_per_sm = 0;
+    }
   } restore{h};
   const size_t cnt = (size_t)h->N * nrhs;
   const bool dev = gd != nullptr;
