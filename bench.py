@@ -844,8 +844,8 @@ def main():
     ap.add_argument("--steps", type=int, default=16,
                     help="frequencies of the 64-frequency sweep timed (spread over the band)")
     ap.add_argument("--workers", type=int, default=6,
-                    help="concurrent frequency workers of the batched sweep (mixed arm; 5 / 6 "
-                         "/ 7 workers measured 0.49 / 0.47 / 0.48 s per frequency)")
+                    help="concurrent frequency workers of the batched sweep (mixed arm; six "
+                         "measured 0.39 s per frequency, one 0.9-1.3 s)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="sphere20k", choices=sorted(WORKLOADS),
