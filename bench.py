@@ -843,9 +843,9 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=16,
                     help="frequencies of the 64-frequency sweep timed (spread over the band)")
-    ap.add_argument("--workers", type=int, default=6,
-                    help="concurrent frequency workers of the batched sweep (mixed arm; six "
-                         "measured 0.39 s per frequency, one 0.9-1.3 s)")
+    ap.add_argument("--workers", type=int, default=8,
+                    help="concurrent frequency workers of the batched sweep (mixed arm; eight "
+                         "measured 2.70 freq-solves/s, six 2.45 on the same GPU, one 0.8-1.1)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="sphere20k", choices=sorted(WORKLOADS),
